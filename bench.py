@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Road designs valued per second at +-1% Monte Carlo standard error.
+
+Workload: one GA generation of 256 roads (8-64 control points) on a
+200 x 200 habitat grid with 5 habitat types (~300 patches per species) and
+3 species, 50 yearly steps (synthetic, seeded).  A "step" values every road
+of the generation: species-road model (patches, crossings, transition and
+survival matrices) plus the MTE population Monte Carlo at N* paths, where
+N* = ceil((sigma / (0.01 * mu))^2) comes from an untimed pilot at 2000 paths
+(the largest N* over roads and species is used for the batch).
+
+    value  - batched path, road inputs already resident in HBM
+    e2e    - same through the public C ABI with pinned host inputs, H2D and
+             D2H inside the timed region
+    plain  - the reference-style path: one road per call through the host
+             entry points (species model, then simulate MTE), for comparison
+    --impl reference - the CPU restatement of the reference (oracle/) on the
+             host cores, bounded sample of the same workload
+
+One JSON line on stdout (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "road designs valued/sec at ±1% MC error: batched/surrogate vs plain, 1 GB300"
+WORKLOAD = ("GA generation: 256 roads (8-64 control points), 200x200 grid, 5 habitat types, "
+            "~300 patches, 3 species, MTE valuation at N* paths, 50 years")
+N_ROADS = 256
+PILOT_PATHS = 2000
+YEARS = 50
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--roads", type=int, default=N_ROADS)
+    ap.add_argument("--plain-roads", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="one pilot + one step, for profiler launch lists")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------
+def clocks_start():
+    try:
+        f = open("/tmp/to_bench_clocks.csv", "w")
+        p = subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+            stdout=f, stderr=subprocess.DEVNULL)
+        return p, f
+    except Exception:
+        return None, None
+
+
+def clocks_stop(h, device_index=0):
+    p, f = h
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    f.close()
+    sm, mx, reasons = [], None, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open("/tmp/to_bench_clocks.csv"):
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9 or parts[0] != str(device_index):
+            continue
+        try:
+            sm.append(float(parts[1]))
+            mx = float(parts[2])
+        except ValueError:
+            continue
+        for n, v in zip(names, parts[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("bf16_tflops", 1900.0), d.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------
+def n_star(results, floor=64):
+    """Paths needed per road for a 1% relative standard error (max over species)."""
+    need = []
+    for r in range(results.shape[0]):
+        nr = 0
+        for s in range(results.shape[1]):
+            mean, se = results[r, s, 2], results[r, s, 4]
+            sigma = se * math.sqrt(PILOT_PATHS)
+            if mean > 0:
+                nr = max(nr, math.ceil((sigma / (0.01 * abs(mean))) ** 2))
+        need.append(max(floor, nr))
+    return need
+
+
+def cpu_baseline_port(scene, roads, P, seconds=20.0, threads=None):
+    """Oracle (CPU restatement of the reference) on all host cores: species
+    model + MTE for each species of as many roads as fit in `seconds`."""
+    from oracle import pyoracle as po
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    done = 0
+    for rd in roads:
+        for s, sp in enumerate(scene.species):
+            m = po.species_model(scene, sp, rd, sem=0, max_patches=1024)
+            po.simulate_mte(P, YEARS, m["N"], 1.0, sp.params, m["init_pops"], m["caps"],
+                            m["mmm"][-1], 0, done, s, 0, threads)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, threads, done
+
+
+# --------------------------------------------------------------------------
+def run_reference(args):
+    """--impl reference: the CPU port of the reference on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from transportoptimiser_gb300 import synth
+    from __graft_entry__ import build
+    from transportoptimiser_gb300 import build as b
+    b.build_oracle()
+    scene = synth.generation(0, n_roads=args.roads)
+    P = PILOT_PATHS
+    for _ in range(args.warmup):
+        cpu_baseline_port(scene, scene.roads[:1], 64, seconds=1.0)
+    vals = []
+    for k in range(args.steps):
+        v, cores, n = cpu_baseline_port(scene, scene.roads[k % len(scene.roads):], P,
+                                        seconds=8.0)
+        vals.append(v)
+    value = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "designs/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "paths": P, "note": "per step: roads valued "
+                       "in an 8 s sample"},
+            "cpu_baseline": {"value": value, "unit": "designs/s", "cores": cores,
+                             "kind": "port", "sample": "roads valued in 8 s per step, "
+                             "%d paths, all species" % P},
+            "e2e": {"value": value, "unit": "designs/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from transportoptimiser_gb300 import synth
+    from transportoptimiser_gb300._capi import MIG_SIMT_FP32, Context
+    from transportoptimiser_gb300.generation import Generation, pack_roads
+    from transportoptimiser_gb300 import simulate_gpu as sg
+
+    scene = synth.generation(0, n_roads=args.roads)
+    ctx = Context(local)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    gen = Generation(scene, max_roads=args.roads, max_patches=512, ctx=ctx)
+    packed = pack_roads(scene, scene.roads)
+    road0 = rank * 1_000_000
+
+    # pilot (untimed): N* per road
+    pilot = gen.evaluate(packed, gen.opts(PILOT_PATHS, YEARS, seed=1, road0=road0,
+                                          migration=MIG_SIMT_FP32))
+    need = n_star(pilot)
+    P = min(int(math.ceil(max(need) / 64.0) * 64), 16384)
+    opts = gen.opts(P, YEARS, seed=0, road0=road0, migration=MIG_SIMT_FP32)
+    Ns = pilot[:, :, 0].astype(int)
+
+    # device-resident inputs for `value`
+    dev = {k: torch.from_numpy(v).cuda() for k, v in packed.items()}
+    d_res = torch.zeros(args.roads * len(scene.species) * 8, dtype=torch.float64,
+                        device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_device():
+        gen.evaluate_device(args.roads, dev["cell_off"].data_ptr(), dev["cells"].data_ptr(),
+                            dev["seg_off"].data_ptr(), dev["segs"].data_ptr(), opts,
+                            d_res.data_ptr())
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step_device()
+            flush.zero_()
+        torch.cuda.synchronize()
+        if args.profile_only:
+            step_device()
+            torch.cuda.synchronize()
+            return 0
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        clk = clocks_start()
+        l0 = ctx.launches
+        ctx.profile(True)
+        evs = []
+        t_wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step_device()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+        launches = (ctx.launches - l0) // args.steps
+        mte_ms, mte_n = ctx.kernel_time("mte_simt")
+        sm_ms, sm_n = ctx.kernel_time("species_model")
+        ctx.profile(False)
+        clocks = clocks_stop(clk, local)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(step_ms) / len(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = args.roads * world / (ms / 1000.0)
+    res = d_res.cpu().numpy().reshape(args.roads, len(scene.species), 8)
+
+    # e2e: public host-pointer entry point, pinned inputs, copies inside
+    pinned = {k: torch.from_numpy(v).pin_memory() for k, v in packed.items()}
+    pnp = {k: v.numpy() for k, v in pinned.items()}
+    h2d = sum(v.nbytes for v in pnp.values())
+    d2h = args.roads * len(scene.species) * 8 * 8
+    gen.evaluate(pnp, opts)
+    torch.cuda.synchronize()
+    e2e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gen.evaluate(pnp, opts)
+        e2e_ms.append((time.perf_counter() - t0) * 1000.0)
+    e2e_value = args.roads * world / (statistics.mean(e2e_ms) / 1000.0)
+
+    # plain: one road per call through the host entry points (reference style)
+    plain_value = None
+    if rank == 0 and args.plain_roads > 0:
+        t0 = time.perf_counter()
+        for r in range(args.plain_roads):
+            rd = scene.roads[r]
+            hab = scene.hab_map(rd)
+            models = []
+            for s, sp in enumerate(scene.species):
+                models.append(sg.createSpeciesModel(
+                    hab, scene.pop_map(sp, hab), scene.W, scene.H, scene.res, sp.habitats,
+                    rd.colmajor(), rd.G, sp.hazard, sp.lambda_mean, sp.lambda_sd,
+                    sp.lambda_mult, sp.hab_pref_mult, sem=0, max_patches=512, ctx=ctx))
+            sg.simulateMTECUDA(models, [sp.params for sp in scene.species], P, YEARS,
+                               seed=0, road=road0 + r, migration=MIG_SIMT_FP32, ctx=ctx)
+        plain_value = args.plain_roads / (time.perf_counter() - t0)
+
+    # roofline of the dominant kernel (migration + growth, SIMT FP32)
+    Nsum2 = float((Ns.astype(np.float64) ** 2).sum())
+    flops_per_launch = 2.0 * P * Nsum2 * YEARS
+    mte_avg_s = (mte_ms / max(mte_n, 1)) / 1000.0
+    achieved_tf = flops_per_launch / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
+    bf16_peak, hbm_peak, peak_kind = measured_peaks()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        from transportoptimiser_gb300 import build as b
+        b.build_oracle()
+        v, cores, n = cpu_baseline_port(scene, scene.roads, P, seconds=20.0)
+        cpu = {"value": v, "unit": "designs/s", "cores": cores, "kind": "port",
+               "sample": "%d road(s) x 3 species, %d paths, 50 years (20 s budget)" % (n, P)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "designs/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded; no public dataset for this path)",
+            "config": {"workload": WORKLOAD, "roads": args.roads, "species": len(scene.species),
+                       "paths_per_road": P, "pilot_paths": PILOT_PATHS, "years": YEARS,
+                       "patches_min_max": [int(Ns.min()), int(Ns.max())],
+                       "migration": "simt_fp32", "l2": "flushed (256 MB write) between steps",
+                       "wall_s_timed": t_wall},
+            "e2e": {"value": e2e_value, "unit": "designs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "plain": {"value": plain_value, "unit": "designs/s",
+                      "roads": args.plain_roads, "note": "one road per call, host entry points"},
+            "roofline": {"kernel": "k_mte_simt", "bound": "tensor", "achieved": achieved_tf,
+                         "peak": bf16_peak, "unit": "TFLOP/s",
+                         "frac": achieved_tf / bf16_peak, "peak_kind": peak_kind + " bf16 dense",
+                         "traffic": None, "flops_per_launch": flops_per_launch,
+                         "kernel_ms": mte_ms / max(mte_n, 1),
+                         "species_model_ms": sm_ms / max(sm_n, 1)},
+            "cpu_baseline": cpu,
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    gen.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,268 @@
+/*
+ * transopt.h - C ABI of the GB300 (sm_103a) Monte Carlo road-evaluation
+ * engine.  It replaces the GPU entry points of TransportOptimiser's
+ * `namespace SimulateGPU` (include/gpuCode/SimulateGPU.h:34-482) and the
+ * vendored kNN (include/gpuCode/knn_cuda_with_indexes.h:4-47).
+ *
+ * Conventions
+ *   - Every entry point returns a to_status; nothing throws across the ABI
+ *     (the reference threw `const char*`, SimulateGPU.cu:14-26).
+ *   - Functions without a `_d` suffix take HOST pointers and do their own
+ *     host<->device copies, like the reference wrappers (which allocated,
+ *     copied, launched and synchronised inside every call).  `_d` variants
+ *     take DEVICE pointers and enqueue on the context's stream.
+ *   - Scratch memory comes from a per-context arena that grows on demand and
+ *     is reused between calls.
+ *   - Matrices keep the reference's layouts where a caller passes them in:
+ *     segment lists are G x 4 column-major (x1 | y1 | x2 | y2), grids are
+ *     column-major W x H (cell x + y*W), migration matrices are
+ *     destination-major (Eigen column-major of mmm(origin, destination)).
+ *   - `sem` selects TO_SEM_REFERENCE (reproduce the reference's arithmetic,
+ *     quirks included) or TO_SEM_CORRECTED.
+ *   - Random numbers are Philox4x32-10 streams addressed by (seed, road,
+ *     stream, path, year, lane); runs are reproducible for a given seed.
+ */
+#ifndef TRANSOPT_H
+#define TRANSOPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    TO_OK = 0,
+    TO_ERR_INVALID = 1,      /* bad argument or size                        */
+    TO_ERR_CUDA = 2,         /* CUDA runtime error (message via to_last_error) */
+    TO_ERR_ALLOC = 3,        /* device or host allocation failed            */
+    TO_ERR_NONFINITE = 4,    /* NaN/Inf found in an input                    */
+    TO_ERR_TIMEOUT = 5,      /* a bounded device wait gave up                */
+    TO_ERR_UNSUPPORTED = 6,  /* size or mode outside what is built          */
+    TO_ERR_NO_DEVICE = 7
+} to_status;
+
+typedef enum { TO_SEM_REFERENCE = 0, TO_SEM_CORRECTED = 1 } to_sem;
+
+typedef enum {
+    TO_MIG_AUTO = 0,         /* tensor cores where supported                 */
+    TO_MIG_SIMT_FP32 = 1,    /* CUDA-core FP32, bit-identical to the oracle  */
+    TO_MIG_TC_3XTF32 = 2     /* tcgen05 kind::tf32, 3 MMAs (hi/lo split)     */
+} to_migration;
+
+typedef struct to_ctx_s* to_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+/* SimulateGPU::deviceCount, SimulateGPU.h:44 */
+to_status to_device_count(int* count);
+to_status to_ctx_create(int device, to_ctx* ctx);
+to_status to_ctx_destroy(to_ctx ctx);
+/* enqueue `_d` work on a caller stream (cudaStream_t passed as void*) */
+to_status to_ctx_set_stream(to_ctx ctx, void* stream);
+to_status to_ctx_synchronize(to_ctx ctx);
+const char* to_status_string(to_status s);
+const char* to_last_error(to_ctx ctx);
+/* number of kernels this context has launched (for accounting) */
+uint64_t to_ctx_launch_count(to_ctx ctx);
+/* per-kernel CUDA-event timing: enable (clears the record), then read the
+ * summed milliseconds and launch count of one kernel by name */
+to_status to_ctx_profile(to_ctx ctx, int enable);
+to_status to_ctx_kernel_time(to_ctx ctx, const char* name, double* ms,
+                             int* launches);
+
+/* ---- habitat patches --------------------------------------------------- */
+/* LabelImage, include/utilities/labelmethod.cpp:34.  4-connected labels of
+ * input != 0 numbered 1.. in raster order of the first pixel (x + y*W).
+ * One CTA per image, union-find in shared memory (W*H <= 56000). */
+to_status to_label_image(to_ctx ctx, int W, int H, const int* input,
+                         int* output, int* n_regions);
+
+/* SimulateGPU::buildPatches, SimulateGPU.h:134-140 / SimulateGPU.cu:3573.
+ * For one habitat type with `labels` from to_label_image, appends the
+ * non-empty (coarse block x region) patches at index *n_patches in the
+ * reference order (by*xres + bx)*regions + region-1.  Outputs are host
+ * arrays of capacity max_patches; *init_pop accumulates the patch pops. */
+to_status to_build_patches(to_ctx ctx, int W, int H, int skpx, int skpy,
+                           int xres, int yres, int n_regions, double xspacing,
+                           double yspacing, double sub_patch_area,
+                           double max_pop, const int* labels,
+                           const double* pops, int max_patches, double* area,
+                           double* cap, double* pop, double* cx, double* cy,
+                           double* init_pop, int* n_patches);
+
+/* ---- road crossings ---------------------------------------------------- */
+/* SimulateGPU::lineSegmentIntersect, SimulateGPU.h:107-108 /
+ * SimulateGPU.cu:3478.  crossings[t] = number of segments of xy2 (G x 4)
+ * that line t of xy1 (T x 4) intersects; float predicate, exact. */
+to_status to_line_segment_intersect(to_ctx ctx, int T, const double* xy1,
+                                    int G, const double* xy2, int* crossings);
+
+/* ---- species-road model ------------------------------------------------ */
+typedef struct {
+    int type;                /* habitat code in hab_map                       */
+    double max_pop;          /* capacity per unit area                        */
+    double pref_mean;        /* habitat preference                            */
+    double pref_sd;
+} to_habitat;
+
+typedef struct {
+    int W, H, res;           /* grid cells; coarse patch resolution           */
+    double xspacing, yspacing;
+    int n_hab;
+    const to_habitat* habs;  /* host array                                    */
+    const int* hab_map;      /* W*H habitat codes, road cells already ROAD(4) */
+    const double* pop_map;   /* W*H animals                                   */
+    int G;                   /* visible road segments                         */
+    const double* road;      /* G x 4 column-major                            */
+    double lambda_mean, lambda_sd, lambda_mult, hab_pref_mult;
+    int n_controls;
+    const double* hazard;    /* per control Q_c (vehicle width + length)/(speed 3600) */
+    int sem;
+} to_species_in;
+
+typedef struct {
+    int max_patches;         /* capacity of every array below                 */
+    int n_patches;           /* out                                           */
+    int n_transitions;       /* out: patch pairs tested against the road      */
+    double *area, *cap, *pop, *cx, *cy;  /* [max_patches]                   */
+    int* type;               /* index into habs                               */
+    int* crossings;          /* N*N row-major (optional, may be NULL)         */
+    double* trans;           /* N*N row-major origin x destination (optional) */
+    double* surv;            /* C*N*N (optional)                              */
+    float* mmm;              /* C*N*N destination-major [c][k][l] (optional)  */
+} to_species_out;
+
+/* SpeciesRoadPatches::createSpeciesModel, SpeciesRoadPatches.cpp:12-451, on
+ * the device: labels, patches, distances, crossings, transition and
+ * survival probabilities, and the migration matrices mmm_c = trans o surv_c
+ * (float, entries <= 1e-5 set to zero as dense2Sparse drops them,
+ * SimulateGPU.cu:5973). */
+to_status to_species_model(to_ctx ctx, const to_species_in* in,
+                           to_species_out* out);
+
+/* ---- MTE --------------------------------------------------------------- */
+typedef struct {
+    int n_patches;           /* N                                              */
+    const float* params;     /* [8]: growth current, mean, sd, threshold,
+                                reversion, jump size, jump prob, local var.
+                                (SimulateGPU.cu:3694-3714)                    */
+    const float* init_pops;  /* [N]                                           */
+    const float* caps;       /* [N]                                           */
+    const float* mmm;        /* [N*N] destination-major, highest-flow control */
+} to_mte_species;
+
+typedef struct {
+    int n_species, n_paths, n_years;
+    float dt;
+    uint64_t seed;
+    int road;                /* stream id of the road                         */
+    int sem;
+    int migration;           /* to_migration                                  */
+    const to_mte_species* species;  /* host array [n_species]                */
+} to_mte_problem;
+
+typedef struct {
+    double mean, sd;         /* end population (Simulator.cpp:184-191 SD)     */
+    double se;               /* Monte Carlo standard error of the mean        */
+    double p_below;          /* P(end < 0.2 x initial population)             */
+    double init_total;
+} to_mte_stats;
+
+/* SimulateGPU::simulateMTECUDA, SimulateGPU.h:152-156 / SimulateGPU.cu:3650.
+ * end_pops (optional) is n_paths x n_species column-major (species-major),
+ * like the reference's endPops; stats (optional) is [n_species]. */
+to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
+                          double* end_pops, to_mte_stats* stats);
+
+/* ---- expected present value of an uncertain price ---------------------- */
+typedef struct {
+    float gr;                /* traffic growth x time step                     */
+    float mean;              /* long-run mean (x scenario multiplier)          */
+    float time_step;
+    float rrr;               /* discount rate                                  */
+    float current;
+    float reversion;         /* mean-reversion strength (x multiplier)         */
+    float jump_prob;
+    float noise_sd;          /* brownian sd (x time step x multiplier)         */
+    float jump_sd;           /* Poisson jump size (x multiplier)               */
+} to_exp_pv_params;
+
+/* SimulateGPU::expPV, SimulateGPU.h:53 / SimulateGPU.cu:3163.  values
+ * (optional) receives the per-path PV; mean and sd as the reference sets
+ * expPV / expPVSD (sem 0: sd = sqrt(sum of squared deviations)). */
+to_status to_exp_pv(to_ctx ctx, const to_exp_pv_params* prm, int n_paths,
+                     int n_years, uint64_t seed, int road, int sem,
+                     float* values, double* mean, double* sd);
+
+
+/* ---- batched GA generation ------------------------------------------------
+ * A scene (habitat map, species, initial-population maps) is uploaded once
+ * and stays resident in HBM; each GA generation then streams in only the
+ * road geometry (road cells and visible segments per road) and values every
+ * road in a few launches: one CTA per (road, species) builds the species
+ * model, one launch runs every road's Monte Carlo paths, one reduces them.
+ * This batches what RoadGA::evaluateGeneration / computeSurrogate
+ * (include/main/RoadGA.cpp:2040-2099, 1553-1748) do one road per call.
+ */
+typedef struct {
+    int n_hab;
+    const to_habitat* habs;  /* host [n_hab]                                  */
+    const double* pop_map;   /* host W*H animals                              */
+    const double* hazard;    /* host [n_controls]                             */
+    const float* params;     /* host [8] (SimulateGPU.cu:3694-3714 layout)    */
+    double lambda_mean, lambda_sd, lambda_mult, hab_pref_mult;
+} to_species_desc;
+
+typedef struct {
+    int W, H, res;
+    double xspacing, yspacing;
+    const int* base_map;     /* host W*H habitat codes without roads          */
+    int n_species;
+    const to_species_desc* species;
+    int n_controls;
+    int max_patches;         /* per (road, species) capacity                  */
+    int max_roads;           /* capacity of the per-generation buffers        */
+    int max_cells;           /* total road cells per generation               */
+    int max_segments;        /* total road segments per generation            */
+} to_scene;
+
+typedef struct to_gen_s* to_gen;
+
+typedef struct {
+    int mte_paths;           /* Monte Carlo paths per road                     */
+    int n_years;
+    float dt;
+    uint64_t seed;
+    int road0;               /* stream id of the first road                    */
+    int sem;
+    int migration;           /* to_migration                                   */
+} to_eval_opts;
+
+/* result block per (road, species), TO_RESULT_STRIDE doubles:
+ *   0 n_patches, 1 n_transitions, 2 mte mean, 3 mte sd, 4 mte se,
+ *   5 P(end < 0.2 init), 6 initial population, 7 reserved */
+#define TO_RESULT_STRIDE 8
+
+to_status to_scene_create(to_ctx ctx, const to_scene* scene, to_gen* gen);
+to_status to_scene_destroy(to_gen gen);
+
+/* Roads as CSR lists: road r owns cells [cell_off[r], cell_off[r+1]) of
+ * `cells` (index x + y*W, set to ROAD) and segments [seg_off[r], seg_off[r+1])
+ * of `segs` (4 doubles x1, y1, x2, y2 per segment).  Host pointers;
+ * results (host) is [n_roads][n_species][TO_RESULT_STRIDE]. */
+to_status to_evaluate_roads(to_ctx ctx, to_gen gen, int n_roads,
+                            const int* cell_off, const int* cells,
+                            const int* seg_off, const double* segs,
+                            const to_eval_opts* opts, double* results);
+/* Same with every array (inputs and results) in device memory; enqueued on
+ * the context stream without synchronising. */
+to_status to_evaluate_roads_d(to_ctx ctx, to_gen gen, int n_roads,
+                              const int* cell_off, const int* cells,
+                              const int* seg_off, const double* segs,
+                              const to_eval_opts* opts, double* results);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRANSOPT_H */

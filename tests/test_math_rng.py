@@ -1,0 +1,80 @@
+"""Philox4x32-10 known-answer vectors and the accuracy of the shared
+deterministic math (to_math.h) used by both the kernels and the oracle."""
+import ctypes as C
+import math
+
+import numpy as np
+
+from oracle import pyoracle as po
+
+# Known-answer vectors published with Random123 (Salmon et al., SC'11):
+# (counter, key) -> output for philox4x32 with 10 rounds.
+KAT = [
+    ((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
+    ((0xFFFFFFFF,) * 4, (0xFFFFFFFF,) * 2, (0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD)),
+    ((0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344), (0xA4093822, 0x299F31D0),
+     (0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1)),
+]
+
+HELPER = r"""
+#include <stdint.h>
+#include "to_math.h"
+void kat(const uint32_t* c, const uint32_t* k, uint32_t* o) {
+  to_u32x4 r = to_philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1]);
+  for (int i = 0; i < 4; ++i) o[i] = r.v[i];
+}
+void vlog(const float* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = to_logf(x[i]); }
+void vexp(const float* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = to_expf(x[i]); }
+void vsc(const float* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i) to_sincospif(x[i], &s[i], &c[i]); }
+"""
+
+
+def _helper(tmp_path_factory):
+    import subprocess
+    from transportoptimiser_gb300 import build
+    d = tmp_path_factory.mktemp("mathhelper")
+    src = d / "h.c"
+    src.write_text(HELPER)
+    so = d / "h.so"
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC",
+                    "-I", str(build.CSRC), str(src), "-o", str(so), "-lm"], check=True)
+    return C.CDLL(str(so))
+
+
+def test_philox_known_answers(tmp_path_factory):
+    h = _helper(tmp_path_factory)
+    for ctr, key, want in KAT:
+        c = (C.c_uint32 * 4)(*ctr)
+        k = (C.c_uint32 * 2)(*key)
+        o = (C.c_uint32 * 4)()
+        h.kat(c, k, o)
+        assert tuple(o) == want
+
+
+def test_math_accuracy(tmp_path_factory):
+    h = _helper(tmp_path_factory)
+    fp = C.POINTER(C.c_float)
+    x = np.linspace(1e-6, 1.0, 200001, dtype=np.float32)
+    y = np.zeros_like(x)
+    h.vlog(x.ctypes.data_as(fp), y.ctypes.data_as(fp), len(x))
+    ref = np.log(x.astype(np.float64))
+    assert np.max(np.abs(y - ref) / np.maximum(np.abs(ref), 1e-30)) < 4e-7
+    x = np.linspace(-87.0, 88.0, 200001, dtype=np.float32)
+    h.vexp(x.ctypes.data_as(fp), y.ctypes.data_as(fp), len(x))
+    ref = np.exp(x.astype(np.float64))
+    assert np.max(np.abs(y - ref) / ref) < 2.5e-7
+    x = np.linspace(0.0, 2.0, 200001, dtype=np.float32)
+    s = np.zeros_like(x); c = np.zeros_like(x)
+    h.vsc(x.ctypes.data_as(fp), s.ctypes.data_as(fp), c.ctypes.data_as(fp), len(x))
+    assert np.max(np.abs(s - np.sin(math.pi * x.astype(np.float64)))) < 2e-7
+    assert np.max(np.abs(c - np.cos(math.pi * x.astype(np.float64)))) < 2e-7
+
+
+def test_normal_stream_moments():
+    z = po.fill_stream(0, po.STREAM["GROWTH"], 0, 1, 200, 50, 40)
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1.0) < 0.01
+    u = po.fill_stream(0, po.STREAM["SP_JUMP"], 0, 0, 200, 50, 40)
+    assert u.min() >= 0.0 and u.max() < 1.0 and abs(u.mean() - 0.5) < 0.01
+    # distinct streams / roads are not the same numbers
+    z2 = po.fill_stream(0, po.STREAM["GROWTH"], 1, 1, 200, 50, 40)
+    assert abs(np.corrcoef(z, z2)[0, 1]) < 0.02

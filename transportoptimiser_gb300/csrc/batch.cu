@@ -1,0 +1,319 @@
+// batch.cu - a whole GA generation of roads valued in a handful of launches.
+//
+// RoadGA::evaluateGeneration (include/main/RoadGA.cpp:2040-2099) and the
+// surrogate sampling loop (RoadGA.cpp:1687-1748) call the species model and
+// SimulateGPU::simulateMTECUDA once per road from a host thread pool, with a
+// device allocation, copy and synchronisation inside every call.  Here the
+// scene is resident in HBM (to_scene_create) and a generation is:
+//   1. one launch, one CTA per (road, species): labels, patches, crossings,
+//      transition / survival probabilities, migration matrices;
+//   2. one read of the largest patch count (the only host round trip);
+//   3. one launch over (path tile, road*species): every road's Monte Carlo;
+//   4. one launch: FP64 statistics per (road, species).
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "to_internal.cuh"
+#include "to_model.cuh"
+#include "to_pop.cuh"
+
+struct to_gen_s {
+    to_ctx ctx = nullptr;
+    int W = 0, H = 0, S = 0, C = 0, NM = 0, NP = 0;
+    int max_roads = 0, max_cells = 0, max_segs = 0;
+    int skpx = 0, skpy = 0, xres = 0, yres = 0;
+    float xs = 1, ys = 1, spa = 1;
+    // resident scene
+    int* d_base = nullptr;
+    float* d_popmap = nullptr;           // [S][W*H]
+    to_model_species* d_species = nullptr;
+    float* d_params = nullptr;           // [S][8]
+    // per-generation buffers
+    char* buf = nullptr;
+    size_t buf_bytes = 0;
+    int *d_cell_off, *d_cells, *d_seg_off;
+    double* d_segs;
+    int *d_np, *d_nt;
+    double *d_area, *d_cap, *d_pop, *d_cx, *d_cy;
+    int* d_type;
+    int* d_cross;
+    double* d_tv;
+    float *d_mmm, *d_ip, *d_cp;
+    float* d_end = nullptr;              // grown on demand [RS][P]
+    size_t end_cap = 0;
+    double* d_stats;                     // [RS][5]
+    double* d_results;                   // [RS][8]
+};
+
+namespace {
+
+__global__ void k_pack_results(int n_rs, const int* __restrict__ np,
+                               const int* __restrict__ nt,
+                               const double* __restrict__ stats,
+                               double* __restrict__ out) {
+    int rs = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rs >= n_rs) return;
+    double* o = out + (size_t)rs * TO_RESULT_STRIDE;
+    o[0] = np[rs];
+    o[1] = nt[rs];
+    for (int q = 0; q < 5; ++q) o[2 + q] = stats[5 * (size_t)rs + q];
+    o[7] = 0.0;
+}
+
+__global__ void k_max_int(int n, const int* __restrict__ v, int* out) {
+    int m = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) m = max(m, v[i]);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ int s[32];
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = max(r, s[i]);
+        *out = r;
+    }
+}
+
+template <class T>
+T* carve(char*& p, size_t n) {
+    T* r = reinterpret_cast<T*>(p);
+    p += to_align256(n * sizeof(T));
+    return r;
+}
+
+to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
+                   const int* cells, const int* seg_off, const double* segs,
+                   const to_eval_opts* o, double* d_results_out) {
+    const int S = g->S, RS = R * S, NM = g->NM, NP = g->NP;
+    to_model_args a;
+    memset(&a, 0, sizeof(a));
+    a.W = g->W; a.H = g->H; a.S = S; a.C = g->C;
+    a.skpx = g->skpx; a.skpy = g->skpy; a.xres = g->xres; a.yres = g->yres;
+    a.xs = g->xs; a.ys = g->ys; a.spa = g->spa;
+    a.hab_map = g->d_base; a.cell_off = cell_off; a.cells = cells;
+    a.pop_map = g->d_popmap; a.species = g->d_species;
+    a.seg_off = seg_off; a.segs = segs;
+    a.sem = o->sem; a.max_patches = NM; a.npad = NP;
+    a.n_patches = g->d_np; a.n_transitions = g->d_nt;
+    a.area = g->d_area; a.cap = g->d_cap; a.pop = g->d_pop;
+    a.cx = g->d_cx; a.cy = g->d_cy; a.type = g->d_type;
+    a.crossings_scratch = g->d_cross; a.trans_scratch = g->d_tv;
+    a.mmm = g->d_mmm; a.init_pops = g->d_ip; a.caps = g->d_cp;
+    a.d_flags = ctx->d_flags;
+    TO_TRY(to_k::species_model(ctx, a, RS));
+
+    // the widest species model decides the tile shape of the path kernel
+    int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
+    k_max_int<<<1, 1024, 0, ctx->stream>>>(RS, g->d_np, d_max);
+    TO_LAUNCHED(ctx);
+    int maxN = 0;
+    TO_CUDA(ctx, cudaMemcpyAsync(&maxN, d_max, sizeof(int), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (maxN <= 0) maxN = 4;
+    int NE = (maxN + 3) & ~3;
+
+    const int P = o->mte_paths;
+    if ((size_t)RS * P > g->end_cap) {
+        if (g->d_end) TO_CUDA(ctx, cudaFree(g->d_end));
+        g->d_end = nullptr;
+        TO_CUDA(ctx, cudaMalloc(&g->d_end, (size_t)RS * P * sizeof(float)));
+        g->end_cap = (size_t)RS * P;
+    }
+    to_mte_args m;
+    memset(&m, 0, sizeof(m));
+    m.n_paths = P; m.n_years = o->n_years; m.S = S; m.C = g->C; m.c_use = g->C - 1;
+    m.dt = o->dt; m.seed = o->seed; m.sem = o->sem; m.road0 = o->road0;
+    m.npad = NP; m.npe = NE; m.n_patches = g->d_np; m.mmm = g->d_mmm;
+    m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
+    m.end_pops = g->d_end;
+    if (o->migration == TO_MIG_TC_3XTF32) {
+        TO_TRY(to_k::mte_tc(ctx, m, RS));
+    } else {
+        TO_TRY(to_k::mte_simt(ctx, m, RS));
+    }
+    TO_TRY(to_k::mte_stats(ctx, m, RS, g->d_stats));
+    k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(RS, g->d_np, g->d_nt,
+                                                             g->d_stats, d_results_out);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
+    if (!ctx || !sc || !out || sc->W <= 0 || sc->H <= 0 || sc->res <= 0 ||
+        !sc->base_map || sc->n_species <= 0 || !sc->species ||
+        sc->n_controls <= 0 || sc->n_controls > TO_MAX_CONTROLS ||
+        sc->max_patches <= 0 || sc->max_roads <= 0 || sc->max_cells < 0 ||
+        sc->max_segments <= 0)
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    to_gen g = new to_gen_s();
+    g->ctx = ctx;
+    g->W = sc->W; g->H = sc->H; g->S = sc->n_species; g->C = sc->n_controls;
+    g->NM = sc->max_patches; g->NP = (sc->max_patches + 3) & ~3;
+    g->max_roads = sc->max_roads; g->max_cells = sc->max_cells;
+    g->max_segs = sc->max_segments;
+    int res = sc->res;
+    g->xres = (g->W % res == 0) ? res : res + 1;
+    g->yres = (g->H % res == 0) ? res : res + 1;
+    g->skpx = (int)std::floor((double)(g->W - 1) / (double)res);
+    g->skpy = (int)std::floor((double)(g->H - 1) / (double)res);
+    g->xs = (float)sc->xspacing; g->ys = (float)sc->yspacing;
+    g->spa = (float)(sc->xspacing * sc->yspacing);
+    const size_t n = (size_t)g->W * g->H;
+    const int S = g->S, C = g->C, NM = g->NM, NP = g->NP;
+    std::vector<to_model_species> hs(S);
+    std::vector<float> pm((size_t)S * n), prm((size_t)S * 8);
+    for (int s = 0; s < S; ++s) {
+        const to_species_desc& d = sc->species[s];
+        if (d.n_hab <= 0 || d.n_hab > TO_MAX_HAB || !d.habs || !d.pop_map || !d.hazard ||
+            !d.params) { delete g; return TO_ERR_INVALID; }
+        memset(&hs[s], 0, sizeof(to_model_species));
+        hs[s].n_hab = d.n_hab;
+        for (int h = 0; h < d.n_hab; ++h) {
+            hs[s].hab_type[h] = d.habs[h].type;
+            hs[s].hab_max_pop[h] = d.habs[h].max_pop;
+            hs[s].hab_pref_mean[h] = d.habs[h].pref_mean;
+            hs[s].hab_pref_sd[h] = d.habs[h].pref_sd;
+        }
+        for (int c = 0; c < C; ++c) hs[s].hazard[c] = d.hazard[c];
+        hs[s].lambda_mean = d.lambda_mean; hs[s].lambda_sd = d.lambda_sd;
+        hs[s].lambda_mult = d.lambda_mult; hs[s].hab_pref_mult = d.hab_pref_mult;
+        for (size_t i = 0; i < n; ++i) pm[(size_t)s * n + i] = (float)d.pop_map[i];
+        for (int q = 0; q < 8; ++q) prm[(size_t)s * 8 + q] = d.params[q];
+    }
+    auto fail = [&](cudaError_t e) {
+        to_check_cuda(ctx, e, "to_scene_create");
+        to_scene_destroy(g);
+        return e == cudaErrorMemoryAllocation ? TO_ERR_ALLOC : TO_ERR_CUDA;
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&g->d_base, n * sizeof(int))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&g->d_popmap, pm.size() * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&g->d_species, S * sizeof(to_model_species))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&g->d_params, prm.size() * sizeof(float))) != cudaSuccess) return fail(e);
+    cudaMemcpy(g->d_base, sc->base_map, n * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(g->d_popmap, pm.data(), pm.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(g->d_species, hs.data(), S * sizeof(to_model_species), cudaMemcpyHostToDevice);
+    cudaMemcpy(g->d_params, prm.data(), prm.size() * sizeof(float), cudaMemcpyHostToDevice);
+
+    const size_t R = g->max_roads, RS = R * S;
+    size_t bytes = 0;
+    auto acc = [&](size_t b) { bytes += to_align256(b); };
+    acc((R + 1) * 4); acc((size_t)(g->max_cells > 0 ? g->max_cells : 1) * 4);
+    acc((R + 1) * 4); acc((size_t)g->max_segs * 32);
+    acc(RS * 4); acc(RS * 4);
+    for (int q = 0; q < 5; ++q) acc(RS * NM * 8);
+    acc(RS * NM * 4);
+    acc(RS * NM * NM * 4);
+    acc(RS * NM * NM * 8);
+    acc(RS * C * NP * NP * 4);
+    acc(RS * NP * 4); acc(RS * NP * 4);
+    acc(RS * 5 * 8);
+    acc((RS * TO_RESULT_STRIDE + 64) * 8);
+    if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
+    g->buf_bytes = bytes;
+    char* p = g->buf;
+    g->d_cell_off = carve<int>(p, R + 1);
+    g->d_cells = carve<int>(p, g->max_cells > 0 ? g->max_cells : 1);
+    g->d_seg_off = carve<int>(p, R + 1);
+    g->d_segs = carve<double>(p, (size_t)g->max_segs * 4);
+    g->d_np = carve<int>(p, RS);
+    g->d_nt = carve<int>(p, RS);
+    g->d_area = carve<double>(p, RS * NM);
+    g->d_cap = carve<double>(p, RS * NM);
+    g->d_pop = carve<double>(p, RS * NM);
+    g->d_cx = carve<double>(p, RS * NM);
+    g->d_cy = carve<double>(p, RS * NM);
+    g->d_type = carve<int>(p, RS * NM);
+    g->d_cross = carve<int>(p, RS * NM * NM);
+    g->d_tv = carve<double>(p, RS * NM * NM);
+    g->d_mmm = carve<float>(p, RS * C * NP * NP);
+    g->d_ip = carve<float>(p, RS * NP);
+    g->d_cp = carve<float>(p, RS * NP);
+    g->d_stats = carve<double>(p, RS * 5);
+    g->d_results = carve<double>(p, RS * TO_RESULT_STRIDE + 64);
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+    *out = g;
+    return TO_OK;
+}
+
+to_status to_scene_destroy(to_gen g) {
+    if (!g) return TO_OK;
+    if (g->ctx) cudaSetDevice(g->ctx->device);
+    cudaDeviceSynchronize();
+    cudaFree(g->d_base);
+    cudaFree(g->d_popmap);
+    cudaFree(g->d_species);
+    cudaFree(g->d_params);
+    cudaFree(g->buf);
+    cudaFree(g->d_end);
+    delete g;
+    return TO_OK;
+}
+
+static to_status check_eval(to_ctx ctx, to_gen g, int R, const to_eval_opts* o) {
+    if (!ctx || !g || !o || R <= 0 || R > g->max_roads || o->mte_paths <= 0 ||
+        o->n_years < 0)
+        return TO_ERR_INVALID;
+    return TO_OK;
+}
+
+to_status to_evaluate_roads(to_ctx ctx, to_gen g, int R, const int* cell_off,
+                            const int* cells, const int* seg_off,
+                            const double* segs, const to_eval_opts* o,
+                            double* results) {
+    TO_TRY(check_eval(ctx, g, R, o));
+    if (!cell_off || !seg_off || !segs || !results) return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    int ncell = cell_off[R] - cell_off[0], nseg = seg_off[R] - seg_off[0];
+    if (cell_off[0] != 0 || seg_off[0] != 0 || ncell > g->max_cells ||
+        nseg > g->max_segs || (ncell > 0 && !cells))
+        return TO_ERR_INVALID;
+    for (int r = 0; r < R; ++r)
+        if (cell_off[r + 1] < cell_off[r] || seg_off[r + 1] < seg_off[r])
+            return TO_ERR_INVALID;
+    for (int q = 0; q < ncell; ++q)
+        if (cells[q] < 0 || cells[q] >= g->W * g->H) return TO_ERR_INVALID;
+    for (int q = 0; q < 4 * nseg; ++q)
+        if (!std::isfinite(segs[q])) return to_set_error(ctx, TO_ERR_NONFINITE, "segment %d", q / 4);
+    TO_CUDA(ctx, cudaMemcpyAsync(g->d_cell_off, cell_off, (R + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    if (ncell > 0)
+        TO_CUDA(ctx, cudaMemcpyAsync(g->d_cells, cells, ncell * sizeof(int),
+                                     cudaMemcpyHostToDevice, ctx->stream));
+    TO_CUDA(ctx, cudaMemcpyAsync(g->d_seg_off, seg_off, (R + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    TO_CUDA(ctx, cudaMemcpyAsync(g->d_segs, segs, (size_t)nseg * 4 * sizeof(double),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    TO_TRY(evaluate(ctx, g, R, g->d_cell_off, g->d_cells, g->d_seg_off, g->d_segs, o,
+                    g->d_results));
+    TO_CUDA(ctx, cudaMemcpyAsync(results, g->d_results,
+                                 (size_t)R * g->S * TO_RESULT_STRIDE * sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int f = 0;
+    TO_TRY(to_read_device_flags(ctx, &f));
+    if (f != 0) {
+        cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream);
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "device check %d failed", f);
+    }
+    return TO_OK;
+}
+
+to_status to_evaluate_roads_d(to_ctx ctx, to_gen g, int R, const int* cell_off,
+                              const int* cells, const int* seg_off,
+                              const double* segs, const to_eval_opts* o,
+                              double* results) {
+    TO_TRY(check_eval(ctx, g, R, o));
+    if (!cell_off || !seg_off || !segs || !results) return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    return evaluate(ctx, g, R, cell_off, cells, seg_off, segs, o, results);
+}
+
+}  // extern "C"

@@ -1,0 +1,552 @@
+// patches.cu - habitat labelling, habitat patches, road crossings and the
+// species-road migration model on the device.
+//
+// Reference path (TransportOptimiser):
+//   LabelImage                       include/utilities/labelmethod.cpp:34-56
+//   SimulateGPU::buildPatches        include/gpuCode/SimulateGPU.cu:3573-3645
+//   patchComputation kernel          include/gpuCode/SimulateGPU.cu:498-573
+//   SimulateGPU::lineSegmentIntersect SimulateGPU.cu:3478-3568 (+454-493)
+//   SpeciesRoadPatches::createSpeciesModel include/road/SpeciesRoadPatches.cpp:12-451
+//   dense2Sparse threshold           include/gpuCode/SimulateGPU.cu:5973-5996
+//
+// GB300 layout: one CTA per (road, species) keeps the whole label image in
+// shared memory (W*H int32 <= 224 KB), labels it with a lock-free
+// union-find (atomicMin on shared memory), extracts the patches, and then
+// builds crossings, transition and survival probabilities and the
+// destination-major float migration matrices for every control.  Nothing
+// round-trips to the host between those steps.
+#include "to_internal.cuh"
+#include "to_model.cuh"
+
+namespace {
+
+constexpr int kMaxBlockRegions = 48;   // distinct regions per coarse block
+
+__device__ __forceinline__ int uf_find(volatile int* par, int x) {
+    int p = par[x];
+    int guard = 0;
+    while (p != x && guard < (1 << 20)) { x = p; p = par[x]; ++guard; }
+    return x;
+}
+
+// Playne & Hawick style lock-free union: roots only ever decrease, so the
+// loop makes progress on every failed attempt.
+__device__ __forceinline__ bool uf_union(int* par, int a, int b) {
+    volatile int* vp = par;
+    for (int it = 0; it < (1 << 20); ++it) {
+        a = uf_find(vp, a);
+        b = uf_find(vp, b);
+        if (a == b) return true;
+        if (a < b) {
+            int old = atomicMin(&par[b], a);
+            if (old == b) return true;
+            b = old;
+        } else {
+            int old = atomicMin(&par[a], b);
+            if (old == a) return true;
+            a = old;
+        }
+    }
+    return false;
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim.x <= 1024).
+__device__ int cta_exclusive_scan(int v, int* s_tmp, int* total) {
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int nw = (blockDim.x + 31) >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = (lane < nw) ? s_tmp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        s_tmp[lane] = w;   // inclusive over warps
+    }
+    __syncthreads();
+    int warp_base = (warp > 0) ? s_tmp[warp - 1] : 0;
+    int tot = s_tmp[nw - 1];
+    __syncthreads();
+    if (total) *total = tot;
+    return warp_base + x - v;
+}
+
+// Labels the foreground of a W*H image held as par[] in shared memory
+// (par[i] = i for foreground, -1 for background on entry).  On exit par[i]
+// holds the LabelImage number (1.. in raster order of first pixel) or 0.
+// Returns the number of regions.
+__device__ int cta_label(int n, int W, int* par, int* s_tmp, int* d_flags) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    bool ok = true;
+    for (int i = tid; i < n; i += nt) {
+        if (par[i] < 0) continue;
+        int x = i % W;
+        if (x > 0 && par[i - 1] >= 0) ok &= uf_union(par, i, i - 1);
+        if (i >= W && par[i - W] >= 0) ok &= uf_union(par, i, i - W);
+    }
+    if (!ok && d_flags) atomicExch(d_flags, TO_DEVERR_UNION);
+    __syncthreads();
+    for (int i = tid; i < n; i += nt)
+        if (par[i] >= 0) par[i] = uf_find(par, i);
+    __syncthreads();
+    // rank the roots (root = smallest raster index of its component)
+    int chunk = (n + nt - 1) / nt;
+    int lo = tid * chunk, hi = min(n, lo + chunk);
+    int cnt = 0;
+    for (int i = lo; i < hi; ++i) cnt += (par[i] == i);
+    int total = 0;
+    int base = cta_exclusive_scan(cnt, s_tmp, &total);
+    for (int i = lo; i < hi; ++i)
+        if (par[i] == i) par[i] = -(base++ + 2);
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        int v = par[i];
+        if (v >= 0) par[i] = -par[v] - 1;      // non-root: label of its root
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) {
+        int v = par[i];
+        if (v <= -2) par[i] = -v - 1;           // root
+        else if (v == -1) par[i] = 0;           // background
+    }
+    __syncthreads();
+    return total;
+}
+
+// Patch statistics of one coarse block, scanned in the reference's order
+// (x offset outer, y offset inner), one region list per block.  Writes up
+// to kMaxBlockRegions entries sorted by region number.
+struct BlockPatches {
+    int n;
+    int reg[kMaxBlockRegions];
+    int cnt[kMaxBlockRegions];
+    float pop[kMaxBlockRegions];
+    float sx[kMaxBlockRegions];
+    float sy[kMaxBlockRegions];
+};
+
+template <class LabelFn, class PopFn>
+__device__ bool scan_block(int bx, int by, int W, int H, int skpx, int skpy,
+                           LabelFn lab, PopFn popf, BlockPatches& bp) {
+    int bsx = ((bx + 1) * skpx <= H) ? skpx : H - bx * skpx;
+    int bsy = ((by + 1) * skpy <= W) ? skpy : W - by * skpy;
+    bp.n = 0;
+    bool ok = true;
+    for (int ii = 0; ii < bsx; ++ii)
+        for (int jj = 0; jj < bsy; ++jj) {
+            int xc = bx * skpx + ii, yc = by * skpy + jj;
+            int c = xc + yc * W;
+            int r = lab(c);
+            if (r <= 0) continue;
+            int q = 0;
+            while (q < bp.n && bp.reg[q] != r) ++q;
+            if (q == bp.n) {
+                if (bp.n == kMaxBlockRegions) { ok = false; continue; }
+                bp.reg[q] = r; bp.cnt[q] = 0; bp.pop[q] = 0.0f;
+                bp.sx[q] = 0.0f; bp.sy[q] = 0.0f;
+                bp.n++;
+            }
+            bp.cnt[q] += 1;
+            bp.pop[q] = bp.pop[q] + popf(c);
+            bp.sx[q] = bp.sx[q] + (float)ii;
+            bp.sy[q] = bp.sy[q] + (float)jj;
+        }
+    // insertion sort by region number
+    for (int a = 1; a < bp.n; ++a) {
+        int r = bp.reg[a], c = bp.cnt[a];
+        float p = bp.pop[a], x = bp.sx[a], y = bp.sy[a];
+        int b = a - 1;
+        while (b >= 0 && bp.reg[b] > r) {
+            bp.reg[b + 1] = bp.reg[b]; bp.cnt[b + 1] = bp.cnt[b];
+            bp.pop[b + 1] = bp.pop[b]; bp.sx[b + 1] = bp.sx[b];
+            bp.sy[b + 1] = bp.sy[b];
+            --b;
+        }
+        bp.reg[b + 1] = r; bp.cnt[b + 1] = c; bp.pop[b + 1] = p;
+        bp.sx[b + 1] = x; bp.sy[b + 1] = y;
+    }
+    return ok;
+}
+
+// Finishes one patch exactly as patchComputation (SimulateGPU.cu:560-563).
+__device__ __forceinline__ void finish_patch(const BlockPatches& bp, int q,
+        int bx, int by, int skpx, int skpy, float xs, float ys, float spa,
+        float maxpop, float out[5]) {
+    float area = (float)bp.cnt[q];
+    float cx = xs * (bp.sx[q] / area + (float)(bx * skpx));
+    float cy = ys * (bp.sy[q] / area + (float)(by * skpy));
+    area = area * spa;
+    out[0] = area;
+    out[1] = area * maxpop;
+    out[2] = bp.pop[q];
+    out[3] = cx;
+    out[4] = cy;
+}
+
+// All coarse blocks of one labelled image: block b is handled by thread b
+// (serial scan of its cells); a CTA scan orders the output.  Appends to
+// the patch list at *s_count (shared).  Returns false on overflow.
+template <class LabelFn, class PopFn, class Emit>
+__device__ bool cta_block_patches(int W, int H, int skpx, int skpy, int xres,
+                                  int yres, int max_out, int* s_count,
+                                  int* s_tmp, LabelFn lab, PopFn popf,
+                                  Emit emit) {
+    int nblocks = xres * yres;
+    bool ok = true;
+    for (int b0 = 0; b0 < nblocks; b0 += blockDim.x) {
+        int b = b0 + threadIdx.x;
+        BlockPatches bp;
+        bp.n = 0;
+        if (b < nblocks) {
+            int by = b / xres, bx = b - by * xres;
+            ok &= scan_block(bx, by, W, H, skpx, skpy, lab, popf, bp);
+        }
+        int total = 0;
+        int off = cta_exclusive_scan(bp.n, s_tmp, &total);
+        int base = *s_count;
+        if (b < nblocks) {
+            int by = b / xres, bx = b - by * xres;
+            for (int q = 0; q < bp.n; ++q) {
+                int o = base + off + q;
+                if (o < max_out) emit(o, bp, q, bx, by);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *s_count = base + total;
+        __syncthreads();
+    }
+    if (*s_count > max_out) ok = false;
+    return ok;
+}
+
+// ---- kernels ---------------------------------------------------------------
+
+__global__ void k_label_image(int W, int H, const int* __restrict__ in,
+                              int* __restrict__ out, int* n_regions,
+                              int* d_flags) {
+    extern __shared__ int smem[];
+    int n = W * H;
+    int* par = smem;
+    int* s_tmp = smem + n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) par[i] = in[i] ? i : -1;
+    __syncthreads();
+    int nr = cta_label(n, W, par, s_tmp, d_flags);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = par[i];
+    if (threadIdx.x == 0) *n_regions = nr;
+}
+
+// buildPatches on given labels: out5[5*o + {area,cap,pop,cx,cy}] (double)
+__global__ void k_build_patches(int W, int H, int skpx, int skpy, int xres,
+                                int yres, float xs, float ys, float spa,
+                                float maxpop, const int* __restrict__ labels,
+                                const float* __restrict__ pops, int max_out,
+                                double* __restrict__ out5, int* count,
+                                int* d_flags) {
+    __shared__ int s_tmp[33];
+    __shared__ int s_count;
+    if (threadIdx.x == 0) s_count = *count;
+    __syncthreads();
+    int start = s_count;
+    auto lab = [&](int c) { return labels[c]; };
+    auto popf = [&](int c) { return pops[c]; };
+    auto emit = [&](int o, const BlockPatches& bp, int q, int bx, int by) {
+        float v[5];
+        finish_patch(bp, q, bx, by, skpx, skpy, xs, ys, spa, maxpop, v);
+        for (int f = 0; f < 5; ++f) out5[5 * (size_t)o + f] = (double)v[f];
+    };
+    bool ok = cta_block_patches(W, H, skpx, skpy, xres, yres, max_out,
+                                &s_count, s_tmp, lab, popf, emit);
+    if (!ok && d_flags) atomicExch(d_flags, TO_DEVERR_PATCHES);
+    (void)start;
+    if (threadIdx.x == 0) *count = min(s_count, max_out);
+}
+
+// Segment-segment predicate in float without contraction
+// (pathAdjacencyKernel, SimulateGPU.cu:465-476).
+__device__ __forceinline__ int seg_cross(float x1, float y1, float x21,
+                                         float y21, float x3, float y3,
+                                         float x43, float y43) {
+    float y13 = __fsub_rn(y1, y3);
+    float x13 = __fsub_rn(x1, x3);
+    float numa = __fsub_rn(__fmul_rn(x43, y13), __fmul_rn(y43, x13));
+    float numb = __fsub_rn(__fmul_rn(x21, y13), __fmul_rn(y21, x13));
+    float deno = __fsub_rn(__fmul_rn(y43, x21), __fmul_rn(x43, y21));
+    float ua = __fdiv_rn(numa, deno);
+    float ub = __fdiv_rn(numb, deno);
+    return (ua >= 0.0f) && (ua <= 1.0f) && (ub >= 0.0f) && (ub <= 1.0f);
+}
+
+__global__ void k_line_segment_intersect(int T, const double* __restrict__ xy1,
+                                         int G, const double* __restrict__ xy2,
+                                         int* __restrict__ cross) {
+    extern __shared__ float sseg[];   // 4*G: x3, y3, x43, y43
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        sseg[g] = (float)xy2[g];
+        sseg[G + g] = (float)xy2[g + G];
+        sseg[2 * G + g] = (float)(xy2[g + 2 * G] - xy2[g]);
+        sseg[3 * G + g] = (float)(xy2[g + 3 * G] - xy2[g + G]);
+    }
+    __syncthreads();
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T;
+         t += gridDim.x * blockDim.x) {
+        float x1 = (float)xy1[t], y1 = (float)xy1[t + T];
+        float x21 = (float)(xy1[t + 2 * T] - xy1[t]);
+        float y21 = (float)(xy1[t + 3 * T] - xy1[t + T]);
+        int c = 0;
+        for (int g = 0; g < G; ++g)
+            c += seg_cross(x1, y1, x21, y21, sseg[g], sseg[G + g],
+                           sseg[2 * G + g], sseg[3 * G + g]);
+        cross[t] = c;
+    }
+}
+
+// One CTA per (road, species): the whole species-road model.
+__global__ void __launch_bounds__(1024)
+k_species_model(to_model_args a) {
+    extern __shared__ int smem[];
+    const int rs = blockIdx.x;                 // road*S + species
+    const int road = rs / a.S, sp = rs - road * a.S;
+    const int W = a.W, H = a.H, n = W * H;
+    int* par = smem;
+    int* s_tmp = smem + n;                     // 33 ints
+    int* s_misc = s_tmp + 40;                  // counters
+    const int* hab = a.hab_map;
+    const int c0 = a.cell_off ? a.cell_off[road] : 0;
+    const int c1 = a.cell_off ? a.cell_off[road + 1] : 0;
+    const to_model_species& S = a.species[sp];
+    const int NM = a.max_patches;
+    double* area = a.area + (size_t)rs * NM;
+    double* cap = a.cap + (size_t)rs * NM;
+    double* popd = a.pop + (size_t)rs * NM;
+    double* cx = a.cx + (size_t)rs * NM;
+    double* cy = a.cy + (size_t)rs * NM;
+    int* ptype = a.type + (size_t)rs * NM;
+    const float* popmap = a.pop_map + (size_t)sp * n;
+
+    if (threadIdx.x == 0) { s_misc[0] = 0; s_misc[1] = -1; }
+    __syncthreads();
+    bool ok = true;
+    for (int h = 0; h < S.n_hab; ++h) {
+        int typ = S.hab_type[h];
+        if (typ == 3 || typ == 4) continue;      // CLEAR, ROAD
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            par[i] = (hab[i] == typ) ? i : -1;
+        __syncthreads();
+        for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) par[a.cells[q]] = -1;
+        __syncthreads();
+        int nreg = cta_label(n, W, par, s_tmp, a.d_flags);
+        if (nreg == 0) continue;
+        float maxpop = (float)S.hab_max_pop[h];
+        int before = s_misc[0];
+        auto lab = [&](int c) { return par[c]; };
+        auto popf = [&](int c) { return popmap[c]; };
+        auto emit = [&](int o, const BlockPatches& bp, int q, int bx, int by) {
+            float v[5];
+            finish_patch(bp, q, bx, by, a.skpx, a.skpy, a.xs, a.ys, a.spa,
+                         maxpop, v);
+            area[o] = (double)v[0];
+            cap[o] = (double)v[1];
+            popd[o] = (double)v[2];
+            cx[o] = (double)v[3];
+            cy[o] = (double)v[4];
+            ptype[o] = h;
+        };
+        ok &= cta_block_patches(W, H, a.skpx, a.skpy, a.xres, a.yres, NM,
+                                &s_misc[0], s_tmp, lab, popf, emit);
+        (void)before;
+        __syncthreads();
+    }
+    if (!ok && a.d_flags) atomicExch(a.d_flags, TO_DEVERR_PATCHES);
+    __syncthreads();
+    const int N = min(s_misc[0], NM);
+    if (threadIdx.x == 0) a.n_patches[rs] = N;
+    __threadfence_block();
+    __syncthreads();
+
+    // Distances and the crossing pair filter (SpeciesRoadPatches.cpp:270-381)
+    const double lam = S.lambda_mean + S.lambda_sd * S.lambda_mult;
+    const double max_dist_x = log(0.05) / (-lam);
+    int* cross = a.crossings_scratch + (size_t)rs * NM * NM;
+    if (threadIdx.x == 0) s_misc[2] = 0;
+    __syncthreads();
+    {
+        // count the valid pairs; the reference never tests its last valid
+        // pair (its counter starts at -1), so find that pair too
+        int last = -1, cnt = 0;
+        for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+            int i = q / N, j = q - i * N;
+            if (j <= i) continue;
+            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+            if (sqrt(dx * dx + dy * dy) <= max_dist_x) { last = max(last, q); ++cnt; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if ((threadIdx.x & 31) == 0) { atomicMax(&s_misc[1], last); atomicAdd(&s_misc[2], cnt); }
+    }
+    __syncthreads();
+    const int last_pair = (a.sem == 0) ? s_misc[1] : -1;
+    if (threadIdx.x == 0) {
+        int cnt = s_misc[2];
+        a.n_transitions[rs] = (a.sem == 0 && cnt > 0) ? cnt - 1 : cnt;
+    }
+    const int G = a.seg_off[road + 1] - a.seg_off[road];
+    const double* rseg = a.segs + (size_t)a.seg_off[road] * 4;
+    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+        int i = q / N, j = q - i * N;
+        if (j < i) continue;
+        int c = 0;
+        if (i != j) {
+            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+            bool valid = sqrt(dx * dx + dy * dy) <= max_dist_x;
+            if (q == last_pair) valid = false;
+            if (valid) {
+                float x1 = (float)cx[i], y1 = (float)cy[i];
+                float x21 = (float)(cx[j] - cx[i]);
+                float y21 = (float)(cy[j] - cy[i]);
+                for (int g = 0; g < G; ++g) {
+                    const double* sg = rseg + 4 * g;
+                    float x3 = (float)sg[0], y3 = (float)sg[1];
+                    float x43 = (float)(sg[2] - sg[0]);
+                    float y43 = (float)(sg[3] - sg[1]);
+                    c += seg_cross(x1, y1, x21, y21, x3, y3, x43, y43);
+                }
+            }
+        }
+        cross[(size_t)i * N + j] = c;
+        cross[(size_t)j * N + i] = c;
+    }
+    // per-habitat attraction and per-crossing-count survival tables
+    double* s_attr = reinterpret_cast<double*>(par);          // [n_hab]
+    double* s_surv = s_attr + TO_MAX_HAB;                      // [C][G+1]
+    const double lda = S.lambda_mult * S.lambda_sd + S.lambda_mean;
+    for (int h = threadIdx.x; h < S.n_hab; h += blockDim.x)
+        s_attr[h] = exp(S.hab_pref_mean[h] + S.hab_pref_sd[h] * S.hab_pref_mult);
+    for (int q = threadIdx.x; q < a.C * (G + 1); q += blockDim.x) {
+        int c = q / (G + 1), cr = q - c * (G + 1);
+        s_surv[q] = exp(-(double)cr * S.hazard[c]);
+    }
+    __syncthreads();
+
+    // Transition probabilities (SpeciesRoadPatches.cpp:383-426) and the
+    // migration matrices.  One thread per origin row, j ascending.
+    const double max_dist_t = (a.sem == 0)
+        ? log(0.05) / (-(S.lambda_mean + S.lambda_sd * lda))
+        : log(0.05) / (-lda);
+    const int NP = a.npad;
+    float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
+    double* tv = a.trans_scratch + (size_t)rs * NM * NM;
+    double* trans = a.trans ? a.trans + (size_t)rs * NM * NM : nullptr;
+    double* surv = a.surv ? a.surv + (size_t)rs * a.C * NM * NM : nullptr;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        double summ = 0.0;
+        for (int j = 0; j < N; ++j) {
+            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+            double d = sqrt(dx * dx + dy * dy);
+            double v = 0.0;
+            if (d <= max_dist_t) {
+                double w = area[j] * lda * s_attr[ptype[j]];
+                v = (i == j) ? w
+                  : (a.sem == 0 ? w / exp(-lda * d) : w * exp(-lda * d));
+                summ += v;
+            }
+            tv[(size_t)i * NM + j] = v;
+        }
+        for (int j = 0; j < N; ++j) {
+            double tr = tv[(size_t)i * NM + j] / summ;
+            if (trans) trans[(size_t)i * NM + j] = tr;
+            int cr = cross[(size_t)i * N + j];
+            for (int c = 0; c < a.C; ++c) {
+                double s = s_surv[c * (G + 1) + cr];
+                if (surv) surv[((size_t)c * NM + i) * NM + j] = s;
+                float m = (float)(tr * s);
+                mmm[((size_t)c * NP + j) * NP + i] = ((double)m > 0.00001) ? m : 0.0f;
+            }
+        }
+    }
+    // zero padding of the migration matrices, initial pops and capacities
+    for (int q = threadIdx.x; q < a.C * NP * NP; q += blockDim.x) {
+        int c = q / (NP * NP), r = q - c * NP * NP;
+        int k = r / NP, l = r - k * NP;
+        if (k >= N || l >= N) mmm[((size_t)c * NP + k) * NP + l] = 0.0f;
+    }
+    float* ip = a.init_pops + (size_t)rs * NP;
+    float* cp = a.caps + (size_t)rs * NP;
+    for (int k = threadIdx.x; k < NP; k += blockDim.x) {
+        ip[k] = (k < N) ? (float)popd[k] : 0.0f;
+        cp[k] = (k < N) ? (float)cap[k] : 1.0f;
+    }
+    if (a.crossings_out) {
+        int* co = a.crossings_out + (size_t)rs * NM * NM;
+        for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+            int i = q / N, j = q - i * N;
+            co[(size_t)i * NM + j] = cross[q];
+        }
+    }
+}
+
+}  // namespace
+
+namespace to_k {
+
+to_status label_image(to_ctx ctx, int W, int H, const int* d_in, int* d_out,
+                      int* d_nreg) {
+    size_t smem = (size_t)W * H * sizeof(int) + 64 * sizeof(int);
+    if (smem > ctx->smem_optin)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "label image of %d x %d exceeds shared memory", W, H);
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_label_image,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_label_image<<<1, 1024, smem, ctx->stream>>>(W, H, d_in, d_out, d_nreg,
+                                                  ctx->d_flags);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+to_status build_patches(to_ctx ctx, int W, int H, int skpx, int skpy, int xres,
+                        int yres, int nreg, float xs, float ys, float spa,
+                        float maxpop, const int* d_labels, const float* d_pops,
+                        int max_patches, double* d_out5, int* d_count) {
+    (void)nreg;
+    k_build_patches<<<1, 256, 0, ctx->stream>>>(W, H, skpx, skpy, xres, yres,
+        xs, ys, spa, maxpop, d_labels, d_pops, max_patches, d_out5, d_count,
+        ctx->d_flags);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+to_status line_segment_intersect(to_ctx ctx, int T, const double* d_xy1, int G,
+                                 const double* d_xy2, int* d_cross) {
+    if (T <= 0) return TO_OK;
+    int threads = 256;
+    int blocks = (T + threads - 1) / threads;
+    if (blocks > 4 * ctx->sm_count) blocks = 4 * ctx->sm_count;
+    size_t smem = (size_t)4 * (G > 0 ? G : 1) * sizeof(float);
+    k_line_segment_intersect<<<blocks, threads, smem, ctx->stream>>>(
+        T, d_xy1, G, d_xy2, d_cross);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
+    size_t smem = (size_t)a.W * a.H * sizeof(int) + 64 * sizeof(int);
+    if (smem > ctx->smem_optin)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "grid of %d x %d exceeds shared memory", a.W, a.H);
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_species_model,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    to_prof_begin(ctx, "species_model");
+    k_species_model<<<n_rs, 1024, smem, ctx->stream>>>(a);
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+}  // namespace to_k

@@ -1,0 +1,175 @@
+"""Python mirror of TransportOptimiser's ``namespace SimulateGPU``
+(include/gpuCode/SimulateGPU.h:34-482) over the C ABI of libtransopt.so.
+
+The reference's entry points take Eigen matrices and shared_ptr object
+graphs; these take numpy arrays with the same layouts and return the same
+quantities.  Every call runs on the GPU through ``_capi``; there is no CPU
+fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import Context, ptr
+
+_default_ctx: Context | None = None
+
+
+def context(device: int = 0) -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(device)
+    return _default_ctx
+
+
+def deviceCount() -> int:
+    """SimulateGPU::deviceCount (SimulateGPU.h:44)."""
+    lib = _capi.load()
+    n = C.c_int(0)
+    lib.to_device_count(C.byref(n))
+    return n.value
+
+
+def labelImage(W: int, H: int, inp: np.ndarray, ctx: Context | None = None):
+    """LabelImage (include/utilities/labelmethod.cpp:34) on the GPU."""
+    ctx = ctx or context()
+    inp = np.ascontiguousarray(inp, dtype=np.int32).reshape(-1)
+    out = np.zeros(W * H, dtype=np.int32)
+    n = C.c_int(0)
+    ctx.check(ctx.lib.to_label_image(ctx.handle, W, H, ptr(inp, C.c_int), ptr(out, C.c_int),
+                                     C.byref(n)), "to_label_image")
+    return out, n.value
+
+
+def buildPatches(W, H, skpx, skpy, xres, yres, noRegions, xspacing, yspacing, subPatchArea,
+                 maxPop, labelledImage, populations, max_patches=None, start=0,
+                 ctx: Context | None = None):
+    """SimulateGPU::buildPatches (SimulateGPU.cu:3573) for one habitat type.
+
+    Returns (patches dict of area/cap/pop/cx/cy arrays, initPop increment)."""
+    ctx = ctx or context()
+    cap_n = max_patches or (start + xres * yres * max(noRegions, 1))
+    arrs = [np.zeros(cap_n) for _ in range(5)]
+    lab = np.ascontiguousarray(labelledImage, dtype=np.int32).reshape(-1)
+    pops = np.ascontiguousarray(populations, dtype=np.float64).reshape(-1)
+    n = C.c_int(start)
+    ip = C.c_double(0.0)
+    ctx.check(ctx.lib.to_build_patches(
+        ctx.handle, W, H, skpx, skpy, xres, yres, noRegions, xspacing, yspacing, subPatchArea,
+        maxPop, ptr(lab, C.c_int), ptr(pops, C.c_double), cap_n,
+        *[ptr(a, C.c_double) for a in arrs], C.byref(ip), C.byref(n)), "to_build_patches")
+    k = n.value
+    keys = ("area", "cap", "pop", "cx", "cy")
+    return {kk: a[start:k].copy() for kk, a in zip(keys, arrs)}, ip.value
+
+
+def lineSegmentIntersect(XY1: np.ndarray, XY2: np.ndarray, ctx: Context | None = None):
+    """SimulateGPU::lineSegmentIntersect (SimulateGPU.cu:3478).  XY1 is T x 4
+    and XY2 G x 4 (rows x1, y1, x2, y2); returns the crossings per row of XY1."""
+    ctx = ctx or context()
+    XY1 = np.asarray(XY1, dtype=np.float64)
+    XY2 = np.asarray(XY2, dtype=np.float64)
+    T, G = XY1.shape[0], XY2.shape[0]
+    a = np.ascontiguousarray(XY1.T.reshape(-1))
+    b = np.ascontiguousarray(XY2.T.reshape(-1))
+    out = np.zeros(T, dtype=np.int32)
+    ctx.check(ctx.lib.to_line_segment_intersect(ctx.handle, T, ptr(a, C.c_double), G,
+                                                ptr(b, C.c_double), ptr(out, C.c_int)),
+              "to_line_segment_intersect")
+    return out
+
+
+def createSpeciesModel(hab_map, pop_map, W, H, res, habitats, road_colmajor, G, hazard,
+                       lambda_mean, lambda_sd=0.0, lambda_mult=0.0, hab_pref_mult=0.0,
+                       sem=0, max_patches=1024, xspacing=1.0, yspacing=1.0,
+                       ctx: Context | None = None):
+    """SpeciesRoadPatches::createSpeciesModel (SpeciesRoadPatches.cpp:12) on
+    the GPU: patches, crossings, transition / survival probabilities and the
+    per-control migration matrices."""
+    ctx = ctx or context()
+    hab_map = np.ascontiguousarray(hab_map, dtype=np.int32).reshape(-1)
+    pop_map = np.ascontiguousarray(pop_map, dtype=np.float64).reshape(-1)
+    road = np.ascontiguousarray(road_colmajor, dtype=np.float64)
+    hz = np.ascontiguousarray(hazard, dtype=np.float64)
+    habs = (_capi.Habitat * len(habitats))(*[_capi.Habitat(h.type, h.max_pop, h.pref_mean,
+                                                           h.pref_sd) for h in habitats])
+    inp = _capi.SpeciesIn(W, H, res, xspacing, yspacing, len(habitats), habs,
+                          ptr(hab_map, C.c_int), ptr(pop_map, C.c_double), G,
+                          ptr(road, C.c_double) if G > 0 else None, lambda_mean, lambda_sd,
+                          lambda_mult, hab_pref_mult, len(hz), ptr(hz, C.c_double), sem)
+    NM = max_patches
+    Cn = len(hz)
+    b = dict(area=np.zeros(NM), cap=np.zeros(NM), pop=np.zeros(NM), cx=np.zeros(NM),
+             cy=np.zeros(NM), type=np.zeros(NM, np.int32))
+    big = dict(crossings=np.zeros(NM * NM, np.int32), trans=np.zeros(NM * NM),
+               surv=np.zeros(Cn * NM * NM), mmm=np.zeros(Cn * NM * NM, np.float32))
+    out = _capi.SpeciesOut()
+    out.max_patches = NM
+    for k in ("area", "cap", "pop", "cx", "cy"):
+        setattr(out, k, ptr(b[k], C.c_double))
+    out.type = ptr(b["type"], C.c_int)
+    out.crossings = ptr(big["crossings"], C.c_int)
+    out.trans = ptr(big["trans"], C.c_double)
+    out.surv = ptr(big["surv"], C.c_double)
+    out.mmm = ptr(big["mmm"], C.c_float)
+    ctx.check(ctx.lib.to_species_model(ctx.handle, C.byref(inp), C.byref(out)),
+              "to_species_model")
+    N = out.n_patches
+    res_ = {k: v[:N].copy() for k, v in b.items()}
+    res_["N"] = N
+    res_["n_transitions"] = out.n_transitions
+    res_["crossings"] = big["crossings"][:N * N].reshape(N, N).copy()
+    res_["trans"] = big["trans"][:N * N].reshape(N, N).copy()
+    res_["surv"] = big["surv"][:Cn * N * N].reshape(Cn, N, N).copy()
+    res_["mmm"] = big["mmm"][:Cn * N * N].reshape(Cn, N, N).copy()
+    res_["init_pops"] = res_["pop"].astype(np.float32)
+    res_["caps"] = res_["cap"].astype(np.float32)
+    return res_
+
+
+def simulateMTECUDA(species_models, params, n_paths, n_years, dt=1.0, seed=0, road=0, sem=0,
+                    migration=_capi.MIG_SIMT_FP32, control=-1, ctx: Context | None = None):
+    """SimulateGPU::simulateMTECUDA (SimulateGPU.cu:3650).
+
+    species_models: list of dicts with N, init_pops, caps, mmm (C x N x N,
+    destination-major); params: list of float32[8].  Uses the highest-flow
+    control's matrix as the reference does.  Returns (endPops P x S, stats)."""
+    ctx = ctx or context()
+    S = len(species_models)
+    keep = []
+    sps = (_capi.MteSpecies * S)()
+    for s, m in enumerate(species_models):
+        prm = np.ascontiguousarray(params[s], np.float32)
+        ip = np.ascontiguousarray(m["init_pops"], np.float32)
+        cp = np.ascontiguousarray(m["caps"], np.float32)
+        mm = np.ascontiguousarray(m["mmm"][control], np.float32)
+        keep += [prm, ip, cp, mm]
+        sps[s] = _capi.MteSpecies(int(m["N"]), ptr(prm, C.c_float), ptr(ip, C.c_float),
+                                  ptr(cp, C.c_float), ptr(mm, C.c_float))
+    prob = _capi.MteProblem(S, n_paths, n_years, dt, seed, road, sem, migration, sps)
+    end = np.zeros(S * n_paths, np.float64)
+    st = (_capi.MteStats * S)()
+    ctx.check(ctx.lib.to_simulate_mte(ctx.handle, C.byref(prob), ptr(end, C.c_double), st),
+              "to_simulate_mte")
+    stats = [dict(mean=x.mean, sd=x.sd, se=x.se, p_below=x.p_below, init_total=x.init_total)
+             for x in st]
+    return end.reshape(S, n_paths).T.copy(), stats
+
+
+def expPV(gr, mean, time_step, rrr, current, reversion, jump_prob, noise_sd, jump_sd,
+          n_paths, n_years, seed=0, road=0, sem=0, return_values=False,
+          ctx: Context | None = None):
+    """SimulateGPU::expPV (SimulateGPU.cu:3163): (expPV, expPVSD)."""
+    ctx = ctx or context()
+    prm = _capi.ExpPvParams(gr, mean, time_step, rrr, current, reversion, jump_prob,
+                            noise_sd, jump_sd)
+    vals = np.zeros(n_paths, np.float32)
+    m, s = C.c_double(), C.c_double()
+    ctx.check(ctx.lib.to_exp_pv(ctx.handle, C.byref(prm), n_paths, n_years, seed, road, sem,
+                                ptr(vals, C.c_float), C.byref(m), C.byref(s)), "to_exp_pv")
+    if return_values:
+        return m.value, s.value, vals
+    return m.value, s.value
