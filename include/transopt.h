@@ -196,6 +196,60 @@ to_status to_exp_pv(to_ctx ctx, const to_exp_pv_params* prm, int n_paths,
                      float* values, double* mean, double* sd);
 
 
+
+/* ---- ROV (controlled traffic) --------------------------------------------- */
+typedef struct {
+    int n_patches;           /* N                                              */
+    const float* params;     /* [8] (SimulateGPU.cu:3993-4015 layout)          */
+    const float* init_pops;  /* [N]                                           */
+    const float* caps;       /* [N]                                           */
+    const float* mmm;        /* [C][N][N] destination-major, one per control  */
+} to_rov_species;
+
+typedef struct {
+    int n_species, n_paths, n_years, n_controls, dim_res;
+    const to_rov_species* species;   /* host [n_species]                      */
+    const float* flows;      /* [C] traffic flow of each control (Q)           */
+    int n_uncertainties;
+    const float* uncert;     /* [U*6] current, mean, sd, reversion, jump size,
+                                jump prob; fuels first (SimulateGPU.cu:4020-4070) */
+    int n_fuels;
+    const float* fuel_costs; /* [n_fuels]                                     */
+    const int* fuel_idx;     /* [n_fuels] process index of each fuel term     */
+    int n_commodities;
+    const float* ore_content;/* [Cm]                                          */
+    const float* ore_sd;     /* [Cm] (x multiplier)                           */
+    float unit_cost, unit_revenue, dt, rrr;
+    int demand_idx;          /* process multiplying the unit profit, -1: none */
+    uint64_t seed;
+    int road, sem, migration;
+} to_rov_problem;
+
+typedef struct {
+    double* cond_exp;        /* [Y][P] optional (reference condExp, P x Y)    */
+    int* opt_cont;           /* [Y][P] optional                               */
+    double* unit_profits;    /* [Y][P] optional                               */
+    double* adj_pops;        /* [Y][S][P] optional                            */
+    double* regression;      /* [Y*C*(R*d + 2 R^d)] optional, d = S + 1       */
+    double value;            /* stats: road value (condExp(0))                */
+    double control;          /* optimal first-period control                  */
+    double sd;               /* the reference's SD statistic                  */
+    double se;               /* Monte Carlo standard error of the value       */
+    int n_best;              /* paths behind the value                        */
+} to_rov_result;
+
+/* SimulateGPU::simulateROVCUDA with ALGO4, SimulateGPU.h:187-191 /
+ * SimulateGPU.cu:3870-5003.  Reference semantics (sem 0) need one species
+ * (the reference indexes multi-species patch vectors as if shared). */
+to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* prob,
+                          to_rov_result* res);
+
+/* knn_cuda_with_indexes::knn, knn_cuda_with_indexes.h:4-47: ref (dim x n)
+ * and query (dim x Q) dim-major, host pointers; dist / ind are k x Q
+ * (dist[kk*Q + q], ind 1-based) in ascending (distance, index) order. */
+to_status to_knn(to_ctx ctx, const float* ref, int n, const float* query,
+                 int Q, int dim, int k, float* dist, int* ind);
+
 /* ---- batched GA generation ------------------------------------------------
  * A scene (habitat map, species, initial-population maps) is uploaded once
  * and stays resident in HBM; each GA generation then streams in only the

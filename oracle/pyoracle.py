@@ -83,6 +83,12 @@ def oracle() -> C.CDLL:
         _oracle.or_fill_pv_stream.argtypes = [C.c_uint64, C.c_int, C.c_int, C.c_int,
                                               C.c_long, c_float_p]
         _oracle.or_species_model.argtypes = [C.POINTER(OrSpeciesIn), C.POINTER(OrSpeciesOut)]
+        _oracle.or_knn.argtypes = [c_float_p, C.c_int, c_float_p, C.c_int, C.c_int, C.c_int,
+                                   c_float_p, c_int_p]
+        _oracle.or_build_surrogate_1d.argtypes = [C.c_int, c_float_p, c_float_p, C.c_int,
+                                                  c_float_p]
+        _oracle.or_build_surrogate_nd.argtypes = [C.c_int, C.c_int, c_float_p, c_float_p,
+                                                  C.c_int, C.c_int, C.c_int, c_float_p]
     return _oracle
 
 
@@ -107,6 +113,10 @@ def ref() -> C.CDLL:
             c_int_p, c_double_p] + [c_double_p] * 5 + [c_int_p]
         _ref.ref_line_segment_intersect.argtypes = [C.c_int, c_double_p, C.c_int, c_double_p, c_int_p]
         _ref.ref_label_image.argtypes = [C.c_int, C.c_int, c_int_p, c_int_p]
+        _ref.ref_knn.argtypes = [c_float_p, C.c_int, c_float_p, C.c_int, C.c_int, C.c_int,
+                                 c_float_p, c_int_p]
+        _ref.ref_build_surrogate_rov.argtypes = [C.c_int, C.c_int, c_float_p, c_float_p,
+                                                 C.c_int, C.c_int, c_float_p]
     return _ref
 
 
@@ -271,3 +281,171 @@ def ref_exp_pv(P, Y, prm9, seed, road):
     lib.ref_exp_pv(P, Y, _p(prm, C.c_float), _p(br, C.c_float), _p(js, C.c_float),
                    _p(uj, C.c_float), _p(vals, C.c_float), C.byref(m), C.byref(s))
     return vals, m.value, s.value
+
+
+# ---------------------------------------------------------------------------
+# ROV (oracle_rov.c) and the reference ALGO4 on the CPU
+# ---------------------------------------------------------------------------
+class OrRovProblem(C.Structure):
+    _fields_ = [("n_paths", C.c_int), ("n_years", C.c_int), ("n_species", C.c_int),
+                ("n_controls", C.c_int), ("n_uncertainties", C.c_int), ("dim_res", C.c_int),
+                ("n_patches", c_int_p), ("params", C.POINTER(c_float_p)),
+                ("params_flat", c_float_p), ("init_pops", C.POINTER(c_float_p)),
+                ("caps", C.POINTER(c_float_p)), ("mmm", C.POINTER(c_float_p)),
+                ("flows", c_float_p), ("uncert", c_float_p), ("n_fuels", C.c_int),
+                ("fuel_costs", c_float_p), ("fuel_idx", c_int_p), ("n_commodities", C.c_int),
+                ("ore_content", c_float_p), ("ore_sd", c_float_p), ("unit_cost", C.c_float),
+                ("unit_revenue", C.c_float), ("dt", C.c_float), ("rrr", C.c_float),
+                ("scaling", C.c_float), ("demand_idx", C.c_int), ("seed", C.c_uint64),
+                ("road", C.c_int), ("sem", C.c_int), ("n_threads", C.c_int)]
+
+
+class OrRovResult(C.Structure):
+    _fields_ = [("cond_exp", c_float_p), ("opt_cont", c_int_p), ("unit_profits", c_float_p),
+                ("adj_pops", c_float_p), ("regression", c_float_p), ("controls", c_int_p),
+                ("total_pops", c_float_p), ("aars", c_float_p), ("u_results", c_float_p),
+                ("stats", C.c_double * 3), ("value_se", C.c_double), ("n_best", C.c_int)]
+
+
+def rov_problem_arrays(rp):
+    """Normalise a ROV problem dict (see transportoptimiser_gb300.rov) into
+    contiguous arrays; returns (arrays dict)."""
+    S = len(rp["species"])
+    out = dict(S=S)
+    out["N"] = np.array([sp["N"] for sp in rp["species"]], np.int32)
+    out["params"] = [np.ascontiguousarray(sp["params"], np.float32) for sp in rp["species"]]
+    out["init"] = [np.ascontiguousarray(sp["init_pops"], np.float32) for sp in rp["species"]]
+    out["caps"] = [np.ascontiguousarray(sp["caps"], np.float32) for sp in rp["species"]]
+    out["mmm"] = [np.ascontiguousarray(sp["mmm"], np.float32) for sp in rp["species"]]
+    out["flat"] = np.ascontiguousarray(np.concatenate(out["params"]), np.float32)
+    for k in ("flows", "uncert", "fuel_costs", "ore_content", "ore_sd"):
+        out[k] = np.ascontiguousarray(rp[k], np.float32)
+    out["fuel_idx"] = np.ascontiguousarray(rp["fuel_idx"], np.int32)
+    return out
+
+
+def simulate_rov(rp, threads=1, want_paths=False):
+    lib = oracle()
+    lib.or_simulate_rov.argtypes = [C.POINTER(OrRovProblem), C.POINTER(OrRovResult)]
+    a = rov_problem_arrays(rp)
+    S, P, Y, C_, R = a["S"], rp["n_paths"], rp["n_years"], len(rp["flows"]), rp["dim_res"]
+    U = len(rp["uncert"]) // 6
+    fp = lambda arrs: (c_float_p * len(arrs))(*[_p(x, C.c_float) for x in arrs])
+    pr = OrRovProblem(P, Y, S, C_, U, R, _p(a["N"], C.c_int), fp(a["params"]),
+                      _p(a["flat"], C.c_float), fp(a["init"]), fp(a["caps"]), fp(a["mmm"]),
+                      _p(a["flows"], C.c_float), _p(a["uncert"], C.c_float),
+                      len(a["fuel_costs"]), _p(a["fuel_costs"], C.c_float),
+                      _p(a["fuel_idx"], C.c_int), len(a["ore_content"]),
+                      _p(a["ore_content"], C.c_float), _p(a["ore_sd"], C.c_float),
+                      rp["unit_cost"], rp["unit_revenue"], rp["dt"], rp["rrr"], 2.0,
+                      rp.get("demand_idx", -1), rp["seed"], rp["road"], rp["sem"], threads)
+    d = S + 1
+    blk = R * d + 2 * R ** d
+    res = dict(cond_exp=np.zeros(P * Y, np.float32), opt_cont=np.zeros(P * Y, np.int32),
+               unit_profits=np.zeros(P * Y, np.float32), adj_pops=np.zeros(Y * S * P, np.float32),
+               regression=np.zeros(Y * C_ * blk, np.float32))
+    extra = {}
+    if want_paths:
+        extra = dict(controls=np.zeros(P * Y, np.int32),
+                     total_pops=np.zeros(P * (Y + 1) * S, np.float32),
+                     aars=np.zeros(P * (Y + 1) * S * C_, np.float32),
+                     u_results=np.zeros(P * (Y + 1) * U, np.float32))
+    r = OrRovResult()
+    r.cond_exp = _p(res["cond_exp"], C.c_float)
+    r.opt_cont = _p(res["opt_cont"], C.c_int)
+    r.unit_profits = _p(res["unit_profits"], C.c_float)
+    r.adj_pops = _p(res["adj_pops"], C.c_float)
+    r.regression = _p(res["regression"], C.c_float)
+    for k, v in extra.items():
+        setattr(r, k, _p(v, C.c_int if v.dtype == np.int32 else C.c_float))
+    assert lib.or_simulate_rov(C.byref(pr), C.byref(r)) == 0
+    res.update(extra)
+    res["stats"] = np.array(list(r.stats))
+    res["value_se"] = r.value_se
+    res["n_best"] = r.n_best
+    return res
+
+
+def ref_simulate_rov(rp):
+    """The reference's ALGO4 (one species) on the CPU, fed the same streams."""
+    lib = ref()
+    assert len(rp["species"]) == 1
+    sp = rp["species"][0]
+    P, Y, R = rp["n_paths"], rp["n_years"], rp["dim_res"]
+    N = int(sp["N"])
+    C_ = len(rp["flows"])
+    U = len(rp["uncert"]) // 6
+    Cm = len(rp["ore_content"])
+    seed, road = rp["seed"], rp["road"]
+    N4 = (N + 3) & ~3
+    rand_cont = fill_stream(seed, STREAM["CONTROL"], road, 0, P, Y, 1, 0)
+    rgr = fill_stream(seed, STREAM["GROWTH"], road, 1, P, Y, N, 0)
+    sp_br = fill_stream(seed, STREAM["SP_BROWNIAN"], road, 1, P, Y, 1, 0)
+    sp_js = fill_stream(seed, STREAM["SP_JUMPSIZE"], road, 1, P, Y, 1, 0)
+    sp_jp = fill_stream(seed, STREAM["SP_JUMP"], road, 0, P, Y, 1, 0)
+    ex_br = fill_stream(seed, STREAM["EX_BROWNIAN"], road, 1, P, Y, U, 0)
+    ex_js = fill_stream(seed, STREAM["EX_JUMPSIZE"], road, 1, P, Y, U, 0)
+    ex_jp = fill_stream(seed, STREAM["EX_JUMP"], road, 0, P, Y, U, 0)
+    zore = fill_pv_stream(seed, STREAM["ORE"], road, 1, P * Y * max(Cm, 1))
+    ucomp = np.zeros(P * Y * max(Cm, 1), np.float32)
+    for c in range(Cm):
+        sl = slice(c * P * Y, (c + 1) * P * Y)
+        ucomp[sl] = np.float32(rp["ore_content"][c]) + np.float32(rp["ore_sd"][c]) * zore[sl]
+    d = 2
+    blk = R * d + 2 * R ** d
+    out = dict(cond_exp=np.zeros(P * Y, np.float32), opt_cont=np.zeros(P * Y, np.int32),
+               unit_profits=np.zeros(P * Y, np.float32), adj_pops=np.zeros(Y * P, np.float32),
+               regression=np.zeros(Y * C_ * blk, np.float32), stats=np.zeros(3, np.float32))
+    f32 = lambda x: np.ascontiguousarray(x, np.float32)
+    args = [P, Y, N, C_, U, R, C.c_float(rp["dt"]), f32(sp["params"]), f32(sp["init_pops"]),
+            f32(sp["caps"]), f32(sp["mmm"]), f32(rp["flows"]), f32(rp["uncert"]),
+            len(rp["fuel_costs"]), f32(rp["fuel_costs"]),
+            np.ascontiguousarray(rp["fuel_idx"], np.int32), Cm,
+            C.c_float(rp["unit_cost"]), C.c_float(rp["unit_revenue"]), C.c_float(rp["rrr"]),
+            rand_cont, rgr, sp_br, sp_js, sp_jp, ex_br, ex_js, ex_jp, ucomp,
+            out["cond_exp"], out["opt_cont"], out["unit_profits"], out["adj_pops"],
+            out["regression"], out["stats"]]
+    conv = []
+    for x in args:
+        if isinstance(x, np.ndarray):
+            conv.append(_p(x, C.c_int if x.dtype == np.int32 else C.c_float))
+        else:
+            conv.append(x)
+    lib.ref_simulate_rov(*conv)
+    return out
+
+
+def knn(ref_pts, n, query, Q, dim, k, use_ref=False):
+    dist = np.zeros(k * Q, np.float32)
+    ind = np.zeros(k * Q, np.int32)
+    rp_ = np.ascontiguousarray(ref_pts, np.float32)
+    q_ = np.ascontiguousarray(query, np.float32)
+    if use_ref:
+        ref().ref_knn(_p(rp_, C.c_float), n, _p(q_, C.c_float), Q, dim, k,
+                      _p(dist, C.c_float), _p(ind, C.c_int))
+    else:
+        oracle().or_knn(_p(rp_, C.c_float), n, _p(q_, C.c_float), Q, dim, k,
+                        _p(dist, C.c_float), _p(ind, C.c_int))
+    return dist, ind
+
+
+def build_surrogate_1d(x, y, R):
+    out = np.zeros(2 * R, np.float32)
+    x = np.ascontiguousarray(x, np.float32); y = np.ascontiguousarray(y, np.float32)
+    oracle().or_build_surrogate_1d(len(x), _p(x, C.c_float), _p(y, C.c_float), R,
+                                   _p(out, C.c_float))
+    return out
+
+
+def build_surrogate_nd(pred, y, R, sem=0, clip=1, use_ref=False):
+    pred = np.ascontiguousarray(pred, np.float32)
+    d, n = pred.shape
+    y = np.ascontiguousarray(y, np.float32)
+    out = np.zeros(R * d + R ** d, np.float32)
+    if use_ref:
+        ref().ref_build_surrogate_rov(n, d, _p(pred, C.c_float), _p(y, C.c_float), R, clip,
+                                      _p(out, C.c_float))
+    else:
+        oracle().or_build_surrogate_nd(n, d, _p(pred, C.c_float), _p(y, C.c_float), R, sem, clip,
+                                       _p(out, C.c_float))
+    return out

@@ -73,12 +73,52 @@ def exppv_case(seed: int):
     return dict(prm=prm, P=200, Y=40, seed=seed, values=vals, mean=mean, sd=sd)
 
 
+def rov_problem(seed: int, P=600, Y=12, R=8):
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    sc = synth.mte_road(seed)
+    m = po.species_model(sc, sc.species[0], sc.roads[0], sem=0)
+    return rov_problem_from_models([m], sc, n_paths=P, n_years=Y, dim_res=R, n_processes=2,
+                                   seed=seed)
+
+
+def rov_case(seed: int):
+    rp = rov_problem(seed)
+    out = po.ref_simulate_rov(rp)
+    sp = rp["species"][0]
+    flat = {k: v for k, v in rp.items() if k != "species"}
+    flat.update({"sp_" + k: np.asarray(v) for k, v in sp.items()})
+    flat.update({"out_" + k: v for k, v in out.items()})
+    return flat
+
+
+def knn_case(seed: int):
+    rng = np.random.default_rng(seed)
+    n, Q, dim, k = 500, 200, 3, 30
+    ref_pts = rng.random((dim, n)).astype(np.float32)
+    ref_pts[:, 10] = ref_pts[:, 3]          # an exact duplicate: tie on distance
+    q = rng.random((dim, Q)).astype(np.float32)
+    dist, ind = po.knn(ref_pts, n, q, Q, dim, k, use_ref=True)
+    return dict(ref=ref_pts, query=q, k=k, dist=dist, ind=ind)
+
+
+def surrogate_case(seed: int):
+    rng = np.random.default_rng(seed)
+    n, d, R = 300, 2, 8
+    pred = rng.random((d, n)).astype(np.float32) * np.array([[2.0], [50.0]], np.float32)
+    y = (-(pred[0] ** 2) * 10 - pred[1]).astype(np.float32)
+    mean = po.build_surrogate_nd(pred, y, R, clip=1, use_ref=True)
+    return dict(pred=pred, y=y, R=R, mean=mean)
+
+
 def main():
     if not po.ref_available():
         po.ref()
     np.savez_compressed(OUT / "patches_crossings.npz", **patches_case(0))
     np.savez_compressed(OUT / "mte.npz", **mte_case(0))
     np.savez_compressed(OUT / "exppv.npz", **exppv_case(0))
+    np.savez_compressed(OUT / "rov.npz", **rov_case(0))
+    np.savez_compressed(OUT / "knn.npz", **knn_case(0))
+    np.savez_compressed(OUT / "surrogate_rov.npz", **surrogate_case(0))
     print("golden fixtures written to", OUT)
 
 

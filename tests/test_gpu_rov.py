@@ -1,0 +1,86 @@
+"""GPU ROV valuation (ALGO4) and kNN against the oracle (SIMT path: bit for
+bit on identical inputs) and against the reference's golden outputs."""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from rov_util import problem_from_golden, ref_outputs
+from transportoptimiser_gb300 import simulate_gpu as sg
+from transportoptimiser_gb300 import synth
+from transportoptimiser_gb300.rov import rov_problem_from_models
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare_exact(gpu, orc, P, Y, S):
+    assert np.array_equal(gpu["opt_cont"], orc["opt_cont"])
+    assert np.array_equal(gpu["cond_exp"].astype(np.float32), orc["cond_exp"])
+    assert np.array_equal(gpu["unit_profits"].astype(np.float32)[P:], orc["unit_profits"][P:])
+    assert np.array_equal(gpu["adj_pops"].astype(np.float32).reshape(Y, S, P)[1:],
+                          orc["adj_pops"].reshape(Y, S, P)[1:])
+    assert np.array_equal(gpu["regression"].astype(np.float32), orc["regression"])
+    assert gpu["stats"][1] == orc["stats"][1]
+    assert math.isclose(gpu["stats"][0], orc["stats"][0], rel_tol=1e-7)
+    assert math.isclose(gpu["stats"][2], orc["stats"][2], rel_tol=1e-9)
+    assert math.isclose(gpu["value_se"], orc["value_se"], rel_tol=1e-9)
+
+
+def test_rov_reference_semantics_bit_exact(ctx, golden):
+    rp = problem_from_golden(golden["rov"])
+    gpu = sg.simulateROVCUDA(rp, ctx=ctx)
+    orc = po.simulate_rov(rp)
+    _compare_exact(gpu, orc, rp["n_paths"], rp["n_years"], 1)
+
+
+def test_rov_matches_reference_golden(ctx, golden):
+    g = golden["rov"]
+    rp = problem_from_golden(g)
+    ref = ref_outputs(g)
+    gpu = sg.simulateROVCUDA(rp, ctx=ctx)
+    assert np.array_equal(gpu["opt_cont"], ref["opt_cont"])
+    assert abs(gpu["stats"][0] - ref["stats"][0]) <= 1e-5 * abs(ref["stats"][0])
+    assert np.abs(gpu["regression"] - ref["regression"]).max() <= 1e-5 * np.abs(ref["regression"]).max()
+
+
+@pytest.mark.parametrize("S,R,P,Y", [(2, 8, 900, 10), (1, 16, 1500, 8)])
+def test_rov_corrected_semantics_bit_exact(ctx, S, R, P, Y):
+    sc = synth.rov_road(3, n_species=S)
+    models = [po.species_model(sc, sc.species[s], sc.roads[0], sem=1) for s in range(S)]
+    rp = rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                 n_processes=3, demand=True, seed=4, road=7)
+    gpu = sg.simulateROVCUDA(rp, ctx=ctx)
+    orc = po.simulate_rov(rp, threads=8)
+    _compare_exact(gpu, orc, P, Y, S)
+
+
+def test_rov_independent_seeds(ctx):
+    sc = synth.mte_road(1)
+    m = po.species_model(sc, sc.species[0], sc.roads[0], sem=0)
+    vals = []
+    for seed in (11, 12):
+        rp = rov_problem_from_models([m], sc, n_paths=3000, n_years=15, dim_res=8, seed=seed)
+        out = sg.simulateROVCUDA(rp, want=(), ctx=ctx)
+        vals.append((out["stats"][0], out["value_se"]))
+    (a, sa), (b, sb) = vals
+    assert sa > 0 and sb > 0
+    assert abs(a - b) < 3 * math.hypot(sa, sb)
+
+
+def test_knn_matches_oracle_and_reference(ctx, golden):
+    g = golden["knn"]
+    k = int(g["k"])
+    dist, ind = sg.knn(g["ref"], g["query"], k, ctx=ctx)
+    od, oi = po.knn(g["ref"], g["ref"].shape[1], g["query"], g["query"].shape[1], 3, k)
+    assert np.array_equal(ind.reshape(-1), oi)
+    assert np.array_equal(dist.reshape(-1), od)
+    assert np.array_equal(ind.reshape(-1), g["ind"])
+    rng = np.random.default_rng(5)
+    for n, Q, dim, k in [(5000, 300, 4, 100), (40, 17, 1, 40), (3000, 64, 2, 256)]:
+        ref_pts = rng.integers(0, 20, (dim, n)).astype(np.float32)   # many exact ties
+        q = rng.random((dim, Q)).astype(np.float32) * 20
+        dist, ind = sg.knn(ref_pts, q, k, ctx=ctx)
+        od, oi = po.knn(ref_pts, n, q, Q, dim, k)
+        assert np.array_equal(ind.reshape(-1), oi)
+        assert np.array_equal(dist.reshape(-1), od)

@@ -1,0 +1,47 @@
+"""The ROV / kNN / surrogate oracle against the reference's own kernels
+(golden fixtures from oracle/_ref, see tests/golden/make_golden.py).
+
+The reference solves the local linear systems in FP32 Gaussian elimination
+and compiles here without fused multiply-adds; the oracle solves in FP64
+Cholesky with FMAs.  Decisions (optimal controls) and kNN indices must
+match exactly; values within 1e-5 relative (regression grid: 1e-5 of its
+largest magnitude)."""
+import numpy as np
+
+from oracle import pyoracle as po
+from rov_util import problem_from_golden, ref_outputs
+
+RTOL = 1e-5
+
+
+def test_rov_matches_reference_golden(golden):
+    g = golden["rov"]
+    rp = problem_from_golden(g)
+    ref = ref_outputs(g)
+    out = po.simulate_rov(rp)
+    P, Y = rp["n_paths"], rp["n_years"]
+    assert np.array_equal(out["opt_cont"], ref["opt_cont"])
+    ce, rce = out["cond_exp"].reshape(Y, P), ref["cond_exp"].reshape(Y, P)
+    for t in range(Y):
+        np.testing.assert_allclose(ce[t], rce[t], rtol=RTOL, atol=RTOL * np.abs(rce[t]).max())
+    up, rup = out["unit_profits"].reshape(Y, P), ref["unit_profits"].reshape(Y, P)
+    np.testing.assert_array_equal(up[1:], rup[1:])
+    reg, rreg = out["regression"], ref["regression"]
+    assert np.abs(reg - rreg).max() <= RTOL * np.abs(rreg).max()
+    assert abs(out["stats"][0] - ref["stats"][0]) <= RTOL * abs(ref["stats"][0])
+    assert out["stats"][1] == ref["stats"][1]
+    assert abs(out["stats"][2] - ref["stats"][2]) <= RTOL * abs(ref["stats"][2])
+
+
+def test_knn_matches_reference_golden(golden):
+    g = golden["knn"]
+    dist, ind = po.knn(g["ref"], g["ref"].shape[1], g["query"], g["query"].shape[1],
+                       g["ref"].shape[0], int(g["k"]))
+    assert np.array_equal(ind, g["ind"])
+    np.testing.assert_allclose(dist, g["dist"], rtol=1e-6)
+
+
+def test_rov_surrogate_matches_reference_golden(golden):
+    g = golden["surrogate_rov"]
+    out = po.build_surrogate_nd(g["pred"], g["y"], int(g["R"]), sem=0, clip=1)
+    assert np.abs(out - g["mean"]).max() <= RTOL * np.abs(g["mean"]).max()

@@ -100,6 +100,30 @@ class EvalOpts(C.Structure):
 
 RESULT_STRIDE = 8
 
+
+class RovSpecies(C.Structure):
+    _fields_ = [("n_patches", C.c_int), ("params", c_float_p), ("init_pops", c_float_p),
+                ("caps", c_float_p), ("mmm", c_float_p)]
+
+
+class RovProblem(C.Structure):
+    _fields_ = [("n_species", C.c_int), ("n_paths", C.c_int), ("n_years", C.c_int),
+                ("n_controls", C.c_int), ("dim_res", C.c_int),
+                ("species", C.POINTER(RovSpecies)), ("flows", c_float_p),
+                ("n_uncertainties", C.c_int), ("uncert", c_float_p), ("n_fuels", C.c_int),
+                ("fuel_costs", c_float_p), ("fuel_idx", c_int_p), ("n_commodities", C.c_int),
+                ("ore_content", c_float_p), ("ore_sd", c_float_p), ("unit_cost", C.c_float),
+                ("unit_revenue", C.c_float), ("dt", C.c_float), ("rrr", C.c_float),
+                ("demand_idx", C.c_int), ("seed", C.c_uint64), ("road", C.c_int),
+                ("sem", C.c_int), ("migration", C.c_int)]
+
+
+class RovResult(C.Structure):
+    _fields_ = [("cond_exp", c_double_p), ("opt_cont", c_int_p), ("unit_profits", c_double_p),
+                ("adj_pops", c_double_p), ("regression", c_double_p), ("value", C.c_double),
+                ("control", C.c_double), ("sd", C.c_double), ("se", C.c_double),
+                ("n_best", C.c_int)]
+
 # name -> (restype, argtypes); every symbol declared in include/transopt.h
 SIGNATURES = {
     "to_device_count": (C.c_int, [c_int_p]),
@@ -127,6 +151,9 @@ SIGNATURES = {
     "to_exp_pv": (C.c_int, [C.c_void_p, C.POINTER(ExpPvParams), C.c_int, C.c_int,
                             C.c_uint64, C.c_int, C.c_int, c_float_p, c_double_p,
                             c_double_p]),
+    "to_simulate_rov": (C.c_int, [C.c_void_p, C.POINTER(RovProblem), C.POINTER(RovResult)]),
+    "to_knn": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, C.c_int, C.c_int, C.c_int,
+                         c_float_p, c_int_p]),
     "to_scene_create": (C.c_int, [C.c_void_p, C.POINTER(Scene), C.POINTER(C.c_void_p)]),
     "to_scene_destroy": (C.c_int, [C.c_void_p]),
     "to_evaluate_roads": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, c_int_p, c_int_p,

@@ -75,13 +75,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = ORACLE_DIR / "oracle.c"
-    deps = [src, ORACLE_DIR / "oracle.h", CSRC / "to_math.h"]
+    srcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "oracle_rov.c"]
+    deps = srcs + [ORACLE_DIR / "oracle.h", ORACLE_DIR / "oracle_rov.h",
+                   CSRC / "to_math.h", CSRC / "to_lsm_math.h"]
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     if force or _stale(ORACLE_LIB, deps):
         cc = shutil.which("gcc") or "cc"
         _run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
-              "-pthread", str(src), "-o", str(ORACLE_LIB), "-lm"])
+              "-pthread", *map(str, srcs), "-o", str(ORACLE_LIB), "-lm"])
     return ORACLE_LIB
 
 

@@ -1,0 +1,674 @@
+// rov.cu - controlled-traffic real-options valuation on the device
+// (ALGO4: forward paths under random controls, regression Monte Carlo
+// backward induction with multiple local linear regression on k nearest
+// neighbours).
+//
+// Reference (include/gpuCode/SimulateGPU.cu): simulateROVCUDA :3870-5003,
+// randControls :720, forwardPathKernel :789, computePathStates :959,
+// allocateXYRegressionData :1012, computeStateMinMax :1073,
+// createQueryPoints :1152, firstPeriodInduction :2210, backwardInduction
+// :2333, multiLocLinReg :2934, knn_cuda_with_indexes::knn (kNN).
+//
+// What changes on GB300:
+//  * the forward pass keeps every path tile's populations in shared memory
+//    for all years and evaluates all controls' migrations from one read of
+//    the populations; the random streams are regenerated from Philox where
+//    they are consumed (nothing of size P*Y*N is stored);
+//  * the reference's serial <<<1,1>>> compaction and min/max kernels become
+//    one CTA-wide stable scan per year;
+//  * kNN runs on the device with a warp per query: radix select of the k-th
+//    smallest (squared distance, index) key, then a bitonic sort of the k
+//    survivors - the same neighbour set and order as the reference's stable
+//    insertion sort, without its P x Q distance matrix or host round trips;
+//  * the local linear systems are accumulated in FP32 and solved in FP64
+//    (Cholesky); expectations are reduced in FP64.
+// Every per-query / per-path formula comes from to_lsm_math.h so the SIMT
+// path reproduces the oracle bit for bit.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "to_internal.cuh"
+#include "to_lsm_math.h"
+#include "to_rov.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// exogenous processes and random controls (forwardPathKernel :930-952,
+// randControls :720-730): uRes[u][t][p], controls[t][p]
+// ---------------------------------------------------------------------------
+__global__ void k_rov_exog(to_rov_args a) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const int Y = a.Y, U = a.U, P = a.P;
+    const uint32_t road = (uint32_t)a.road;
+    for (int u = 0; u < U; ++u) a.uRes[((size_t)u * (Y + 1)) * P + p] = a.uncert[6 * u];
+    for (int t = 0; t < Y; ++t) {
+        float uc = to_uniform1(a.seed, TO_STREAM_CONTROL, road, p, t, 0);
+        int control = (int)(uc * (float)a.C);
+        if (control == a.C) control--;
+        a.controls[(size_t)t * P + p] = control;
+        for (int u = 0; u < U; ++u) {
+            const float* up = a.uncert + 6 * u;
+            float uj = to_uniform1(a.seed, TO_STREAM_EX_JUMP, road, p, t, u);
+            float zb = to_normal1(a.seed, TO_STREAM_EX_BROWNIAN, road, p, t, u);
+            float zj = to_normal1(a.seed, TO_STREAM_EX_JUMPSIZE, road, p, t, u);
+            float jump = (uj < up[5]) ? 1.0f : 0.0f;
+            float curr = a.uRes[((size_t)u * (Y + 1) + t) * P + p];
+            float brown = zb * up[2];
+            float s4 = up[4] * up[4];
+            float jsz = (a.sem == 0) ? (zj * s4 - s4 / 2.0f) : (zj * up[4] - s4 / 2.0f);
+            a.uRes[((size_t)u * (Y + 1) + t + 1) * P + p] =
+                curr + up[3] * (up[1] - curr) * a.dt + curr * brown
+                + (to_expf(jsz) - 1.0f) * curr * jump;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// forward paths (forwardPathKernel :789-956).  One CTA = a tile of TP paths,
+// one species at a time, all years; thread (pg, kg) owns paths 4pg..4pg+3
+// and patches 4kg..4kg+3 for every control.
+// ---------------------------------------------------------------------------
+template <int CMAX>
+__global__ void __launch_bounds__(512)
+k_rov_forward(to_rov_args a) {
+    extern __shared__ float smem[];
+    const int NE = a.ne, KG = NE >> 2, TP = a.tile_paths, LC = a.l_chunk;
+    const int C = a.C, Y = a.Y, P = a.P;
+    const int tid = threadIdx.x, pg = tid / KG, kg = tid - pg * KG;
+    const bool active = pg < (TP >> 2);
+    const int path0 = blockIdx.x * TP;
+    float* Mt = smem;                               // [C][LC][NE]
+    float* pop = Mt + (size_t)C * LC * NE;          // [TP][NE]
+    float* mig = pop + (size_t)TP * NE;             // [TP][NE]
+    float* gm = mig + (size_t)TP * NE;              // [TP]
+    float* tot = gm + TP;                           // [TP]
+    int* ctl = reinterpret_cast<int*>(tot + TP);    // [TP]
+    const uint32_t road = (uint32_t)a.road;
+    const bool resident = (LC == NE);
+
+    for (int s = 0; s < a.S; ++s) {
+        const int N = a.n_patches[s];
+        const int N4 = (N + 3) & ~3;
+        const float* sp = a.params + 8 * s;
+        const float* M = a.mmm + (size_t)s * C * a.np * a.np;
+        const float* ip = a.init_pops + (size_t)s * a.np;
+        float cap4[4];
+        for (int j = 0; j < 4; ++j) cap4[j] = a.caps[(size_t)s * a.np + kg * 4 + j];
+        __syncthreads();
+        for (int q = tid; q < TP * NE; q += blockDim.x) {
+            int l = q % NE;
+            pop[q] = (l < N) ? ip[l] : 0.0f;
+        }
+        if (resident) {
+            for (int q = tid; q < C * NE * NE; q += blockDim.x) {
+                int c = q / (NE * NE), r = q - c * NE * NE;
+                int k = r / NE, l = r - k * NE;
+                Mt[((size_t)c * NE + l) * NE + k] = M[((size_t)c * a.np + k) * a.np + l];
+            }
+        }
+        __syncthreads();
+        for (int q = tid; q < TP; q += blockDim.x) {
+            gm[q] = sp[0];
+            float tt = 0.0f;
+            for (int k = 0; k < N; ++k) tt += pop[(size_t)q * NE + k];
+            tot[q] = tt;
+            int path = path0 + q;
+            if (path < P) a.totalPops[((size_t)s * (Y + 1) + 0) * P + path] = tt;
+        }
+        __syncthreads();
+        for (int t = 0; t < Y; ++t) {
+            for (int q = tid; q < TP; q += blockDim.x) {
+                uint32_t path = (uint32_t)(path0 + q);
+                float uj = to_uniform1(a.seed, TO_STREAM_SP_JUMP, road, path, t, s);
+                float zb = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road, path, t, s);
+                float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road, path, t, s);
+                float jp = (a.sem == 0) ? sp[5] : sp[6];
+                float jump = (uj < jp) ? 1.0f : 0.0f;
+                float brown = zb * sp[2];
+                float s5 = sp[5] * sp[5];
+                float jsz = (a.sem == 0) ? (zj * s5 - s5 / 2.0f) : (zj * sp[5] - s5 / 2.0f);
+                float g = gm[q];
+                gm[q] = g + sp[4] * (sp[1] - g) * a.dt + g * brown
+                        + (to_expf(jsz) - 1.0f) * g * jump;
+                ctl[q] = (path0 + q < P) ? a.controls[(size_t)t * P + path0 + q] : 0;
+            }
+            float acc[CMAX][4][4];
+#pragma unroll
+            for (int c = 0; c < CMAX; ++c)
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[c][i][j] = 0.0f;
+            for (int l0 = 0; l0 < NE; l0 += LC) {
+                if (!resident) {
+                    __syncthreads();
+                    for (int q = tid; q < C * LC * NE; q += blockDim.x) {
+                        int c = q / (LC * NE), r = q - c * LC * NE;
+                        int k = r / LC, l = r - k * LC;
+                        Mt[((size_t)c * LC + l) * NE + k] =
+                            M[((size_t)c * a.np + k) * a.np + l0 + l];
+                    }
+                    __syncthreads();
+                }
+                if (active) {
+                    const float* pr = pop + (size_t)(pg * 4) * NE + l0;
+                    for (int l = 0; l < LC; ++l) {
+                        float a0 = pr[l], a1 = pr[NE + l], a2 = pr[2 * NE + l],
+                              a3 = pr[3 * NE + l];
+#pragma unroll
+                        for (int c = 0; c < CMAX; ++c) {
+                            if (c >= C) break;
+                            float4 m = *reinterpret_cast<const float4*>(
+                                Mt + ((size_t)c * LC + l) * NE + kg * 4);
+                            acc[c][0][0] = fmaf(a0, m.x, acc[c][0][0]); acc[c][0][1] = fmaf(a0, m.y, acc[c][0][1]);
+                            acc[c][0][2] = fmaf(a0, m.z, acc[c][0][2]); acc[c][0][3] = fmaf(a0, m.w, acc[c][0][3]);
+                            acc[c][1][0] = fmaf(a1, m.x, acc[c][1][0]); acc[c][1][1] = fmaf(a1, m.y, acc[c][1][1]);
+                            acc[c][1][2] = fmaf(a1, m.z, acc[c][1][2]); acc[c][1][3] = fmaf(a1, m.w, acc[c][1][3]);
+                            acc[c][2][0] = fmaf(a2, m.x, acc[c][2][0]); acc[c][2][1] = fmaf(a2, m.y, acc[c][2][1]);
+                            acc[c][2][2] = fmaf(a2, m.z, acc[c][2][2]); acc[c][2][3] = fmaf(a2, m.w, acc[c][2][3]);
+                            acc[c][3][0] = fmaf(a3, m.x, acc[c][3][0]); acc[c][3][1] = fmaf(a3, m.y, acc[c][3][1]);
+                            acc[c][3][2] = fmaf(a3, m.z, acc[c][3][2]); acc[c][3][3] = fmaf(a3, m.w, acc[c][3][3]);
+                        }
+                    }
+                }
+            }
+            // per-control totals (AAR numerators) summed patch-ascending
+            for (int c = 0; c < C; ++c) {
+                __syncthreads();
+                if (active) {
+#pragma unroll
+                    for (int cc = 0; cc < CMAX; ++cc) {
+                        if (cc != c) continue;
+#pragma unroll
+                        for (int i = 0; i < 4; ++i)
+                            *reinterpret_cast<float4*>(mig + (size_t)(pg * 4 + i) * NE + kg * 4) =
+                                make_float4(acc[cc][i][0], acc[cc][i][1], acc[cc][i][2], acc[cc][i][3]);
+                    }
+                }
+                __syncthreads();
+                for (int q = tid; q < TP; q += blockDim.x) {
+                    float tc = 0.0f;
+                    for (int k = 0; k < N; ++k) tc += mig[(size_t)q * NE + k];
+                    int path = path0 + q;
+                    if (path < P)
+                        a.aars[(((size_t)s * C + c) * Y + t) * P + path] = tc / tot[q];
+                }
+            }
+            __syncthreads();
+            // growth under the path's random control
+            if (active) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    int pl = pg * 4 + i;
+                    uint32_t path = (uint32_t)(path0 + pl);
+                    float z[4];
+                    to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
+                               (uint32_t)((s * N4) >> 2) + kg, z);
+                    int c = ctl[pl];
+                    float mv[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+                    for (int cc = 0; cc < CMAX; ++cc)
+                        if (cc == c)
+#pragma unroll
+                            for (int j = 0; j < 4; ++j) mv[j] = acc[cc][i][j];
+                    float g = gm[pl];
+                    float4 np;
+                    float* npv = &np.x;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        float m = mv[j];
+                        float gr = g + z[j] * sp[7];
+                        float cp = cap4[j];
+                        npv[j] = (a.sem == 0) ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
+                                              : m * (1.0f + gr * (cp - m) / cp);
+                    }
+                    *reinterpret_cast<float4*>(pop + (size_t)pl * NE + kg * 4) = np;
+                }
+            }
+            __syncthreads();
+            for (int q = tid; q < TP; q += blockDim.x) {
+                float tt = 0.0f;
+                for (int k = 0; k < N; ++k) tt += pop[(size_t)q * NE + k];
+                tot[q] = tt;
+                int path = path0 + q;
+                if (path < P) a.totalPops[((size_t)s * (Y + 1) + t + 1) * P + path] = tt;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// shared pieces of the backward pass
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ure(const to_rov_args& a, int p, int t, int u, int stride_y) {
+    // value at the reference's flat index (p*stride_y + t)*U + u of its
+    // [P][Y+1][U] array, read from the [U][Y+1][P] layout
+    const int U = a.U, Y1 = a.Y + 1;
+    long F = ((long)p * stride_y + t) * U + u;
+    long per = (long)Y1 * U;
+    int pp = (int)(F / per);
+    long rem = F - (long)pp * per;
+    int tt = (int)(rem / U), uu = (int)(rem - (long)tt * U);
+    return a.uRes[((size_t)uu * Y1 + tt) * a.P + pp];
+}
+
+__device__ __forceinline__ float ore_at(const to_rov_args& a, int p, int t, int c) {
+    long f, gen;
+    if (a.sem == 0) {
+        f = ((long)p * a.Y + t) * a.Cm + c;
+        gen = f / ((long)a.Y * a.P);
+    } else {
+        gen = c;
+        f = (long)c * a.Y * a.P + (long)p * a.Y + t;
+    }
+    float z = to_normal1(a.seed, TO_STREAM_ORE, (uint32_t)a.road, (uint32_t)(f >> 2), 0,
+                         (uint32_t)(f & 3));
+    return a.ore_content[gen] + a.ore_sd[gen] * z;
+}
+
+__device__ __forceinline__ float unit_profit(const to_rov_args& a, int p, int t,
+                                             int fuel_stride_y, int ore_stride_y) {
+    float uf = 0.0f, ore = 0.0f;
+    for (int f = 0; f < a.nF; ++f)
+        uf = fmaf(a.fuel_costs[f], ure(a, p, t, a.fuel_idx[f], fuel_stride_y), uf);
+    for (int c = 0; c < a.Cm; ++c)
+        ore = fmaf(ore_at(a, p, t, c), ure(a, p, t, a.nF + c, ore_stride_y), ore);
+    float prof = (a.unit_cost + uf) - a.unit_revenue * ore;
+    if (a.demand_idx >= 0)
+        prof = prof * a.uRes[((size_t)a.demand_idx * (a.Y + 1) + t) * a.P + p];
+    return prof;
+}
+
+__device__ __forceinline__ float adj_pop(const to_rov_args& a, int p, int t, int s, int c) {
+    return a.totalPops[((size_t)s * (a.Y + 1) + t) * a.P + p] *
+           a.aars[(((size_t)s * a.C + c) * a.Y + t) * a.P + p];
+}
+
+__device__ __forceinline__ float threshold(const to_rov_args& a, int s) {
+    return (a.sem == 0) ? a.params[a.S * s + 3] : a.params[8 * s + 3];
+}
+
+// terminal year (backwardInduction :2375-2463)
+__global__ void k_rov_terminal(to_rov_args a) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const int t = a.Y - 1, C = a.C, S = a.S;
+    float prof = unit_profit(a, p, t, a.Y + 1, a.sem == 0 ? a.Y : a.Y + 1);
+    float best = 0.0f;
+    int bc = 0;
+    for (int c = 0; c < C; ++c) {
+        bool valid = true;
+        for (int s = 0; s < S; ++s)
+            if (adj_pop(a, p, t, s, c) < threshold(a, s) && c > 0) { valid = false; break; }
+        float pay = 0.0f;
+        if (valid) {
+            float v = a.flows[c] * prof;
+            pay = v > 0.0f ? 0.0f : v;
+        }
+        if (c == 0) best = pay;
+        else if (valid && pay < best) { best = pay; bc = c; }
+    }
+    a.condExp[(size_t)t * a.P + p] = best;
+    a.optCont[(size_t)t * a.P + p] = bc;
+    a.unitProfits[(size_t)t * a.P + p] = prof;
+    for (int s = 0; s < S; ++s)
+        a.adjPops[((size_t)t * S + s) * a.P + p] = adj_pop(a, p, t, s, C - 1);
+}
+
+// Per year: regression states, stable compaction by the year's random
+// control (allocateXYRegressionData :1012-1069), per-control and global
+// min/max (computeStateMinMax :1073-1148), k, normalised points and the
+// axis values of the regression grid.  One CTA.
+__global__ void __launch_bounds__(1024) k_lsm_prepare(to_rov_args a, int t) {
+    const int P = a.P, S = a.S, C = a.C, d = S + 1, R = a.R;
+    __shared__ int s_cnt[TO_ROV_MAXC];
+    __shared__ int s_scan[32 * TO_ROV_MAXC];
+    __shared__ float s_min[TO_ROV_MAXC + 1][TO_LSM_MAXD], s_max[TO_ROV_MAXC + 1][TO_LSM_MAXD];
+    __shared__ unsigned s_umin[TO_ROV_MAXC][TO_LSM_MAXD], s_umax[TO_ROV_MAXC][TO_LSM_MAXD];
+    __shared__ float s_first[TO_ROV_MAXC][TO_LSM_MAXD];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    if (tid < C) s_cnt[tid] = 0;
+    __syncthreads();
+    for (int base = 0; base < P; base += blockDim.x) {
+        int p = base + tid;
+        int grp = -1;
+        float xv[TO_LSM_MAXD];
+        if (p < P) {
+            for (int s = 0; s < S; ++s) xv[s] = adj_pop(a, p, t, s, C - 1);
+            xv[S] = unit_profit(a, p, t, a.Y + 1, a.Y + 1);
+            int ctl = a.controls[(size_t)t * P + p];
+            bool valid = true;
+            for (int s = 0; s < S; ++s)
+                if (xv[s] < a.params[8 * s + 3]) { valid = false; break; }
+            if (valid || ctl == 0) grp = ctl;
+        }
+        // one CTA scan per control, in path order
+        for (int c = 0; c < C; ++c) {
+            unsigned m = __ballot_sync(0xffffffffu, grp == c);
+            int before = __popc(m & ((1u << lane) - 1u));
+            if (lane == 0) s_scan[c * 32 + warp] = __popc(m);
+            __syncthreads();
+            int wbase = 0;
+            for (int w = 0; w < warp; ++w) wbase += s_scan[c * 32 + w];
+            int total = 0;
+            for (int w = 0; w < nw; ++w) total += s_scan[c * 32 + w];
+            if (grp == c) {
+                int pos = s_cnt[c] + wbase + before;
+                a.yv[(size_t)c * P + pos] = a.condExp[(size_t)(t + 1) * P + p];
+                for (int j = 0; j < d; ++j) a.xraw[((size_t)c * d + j) * P + pos] = xv[j];
+            }
+            __syncthreads();
+            if (tid == 0) s_cnt[c] += total;
+            __syncthreads();
+        }
+    }
+    // min / max per control: the reference scans from the first point with
+    // "if (xmin > x) ... else if (xmax < x)", i.e. plain min and max
+    for (int q = tid; q < C * d; q += blockDim.x) {
+        int c = q / d, j = q - c * d;
+        s_umin[c][j] = 0xFFFFFFFFu;
+        s_umax[c][j] = 0u;
+        s_first[c][j] = s_cnt[c] > 0 ? a.xraw[((size_t)c * d + j) * P] : 0.0f;
+    }
+    __syncthreads();
+    for (int c = 0; c < C; ++c) {
+        int n = s_cnt[c];
+        for (int j = 0; j < d; ++j) {
+            const float* xs = a.xraw + ((size_t)c * d + j) * P;
+            float lo = INFINITY, hi = -INFINITY;
+            for (int m = tid; m < n; m += blockDim.x) { lo = fminf(lo, xs[m]); hi = fmaxf(hi, xs[m]); }
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            // order-preserving integer keys for shared atomics
+            unsigned kl = __float_as_uint(lo), kh = __float_as_uint(hi);
+            kl = (kl & 0x80000000u) ? ~kl : (kl | 0x80000000u);
+            kh = (kh & 0x80000000u) ? ~kh : (kh | 0x80000000u);
+            if (lane == 0) { atomicMin(&s_umin[c][j], kl); atomicMax(&s_umax[c][j], kh); }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int c = 0; c < C; ++c) {
+            bool own = (c == 0) || (s_cnt[c] > d + 1);
+            for (int j = 0; j < d; ++j) {
+                if (own && s_cnt[c] > 0) {
+                    unsigned kl = s_umin[c][j], kh = s_umax[c][j];
+                    kl = (kl & 0x80000000u) ? (kl & 0x7FFFFFFFu) : ~kl;
+                    kh = (kh & 0x80000000u) ? (kh & 0x7FFFFFFFu) : ~kh;
+                    float lo = __uint_as_float(kl), hi = __uint_as_float(kh);
+                    // the scan starts from the first point, so a first value
+                    // of -0/+0 keeps its sign when it is the extreme
+                    if (lo == s_first[c][j]) lo = s_first[c][j];
+                    if (hi == s_first[c][j]) hi = s_first[c][j];
+                    s_min[c][j] = lo; s_max[c][j] = hi;
+                } else if (own) {
+                    s_min[c][j] = 0.0f; s_max[c][j] = 0.0f;
+                } else {
+                    s_min[c][j] = s_min[0][j]; s_max[c][j] = s_max[0][j];
+                }
+            }
+        }
+        for (int j = 0; j < d; ++j) {
+            float lo = s_min[0][j], hi = s_max[0][j];
+            for (int c = 1; c < C; ++c) {
+                if (lo > s_min[c][j]) lo = s_min[c][j];
+                if (hi < s_max[c][j]) hi = s_max[c][j];
+            }
+            s_min[C][j] = lo; s_max[C][j] = hi;
+            a.gmin[j] = lo; a.gmax[j] = hi;
+        }
+        for (int c = 0; c < C; ++c) {
+            int n = s_cnt[c];
+            int k = 0;
+            if (n > 3) {
+                k = (int)(10.0 * (log((double)n) + 1.0));
+                if (k > n) k = n;
+            }
+            a.npts[c] = n;
+            a.kc[c] = k;
+        }
+    }
+    __syncthreads();
+    // normalised points (host normalisation, SimulateGPU.cu:4591-4603)
+    for (int c = 0; c < C; ++c) {
+        int n = s_cnt[c];
+        for (int q = tid; q < n * d; q += blockDim.x) {
+            int j = q / n, m = q - j * n;
+            a.xn[((size_t)c * d + j) * P + m] = to_lsm_normalise(
+                a.xraw[((size_t)c * d + j) * P + m], s_min[C][j], s_max[C][j], j == S,
+                a.scaling);
+        }
+    }
+    // axis values of the regression grid (createQueryPoints :1187-1190)
+    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+    for (int q = tid; q < C * d * R; q += blockDim.x) {
+        int c = q / (d * R), r = q - c * d * R;
+        int j = r / R, di = r - j * R;
+        a.reg[(size_t)t * C * blk + (size_t)c * blk + (size_t)j * R + di] =
+            to_lsm_query_axis(di, s_min[C][j], s_max[C][j], R);
+    }
+}
+
+}  // namespace
+
+namespace {
+
+// backwardInduction for 0 < t < Y-1 (:2464-2776)
+__global__ void k_rov_backward(to_rov_args a, int t) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.P) return;
+    const int C = a.C, S = a.S, d = S + 1, R = a.R;
+    float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
+    for (int c = 0; c < C; ++c)
+        for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
+    for (int s = 0; s < S; ++s)
+        a.adjPops[((size_t)t * S + s) * a.P + p] = state[(C - 1) * S + s];
+    int sy = (a.sem == 0) ? a.Y : a.Y + 1;
+    float prof = unit_profit(a, p, t, sy, sy);
+    state[S * C] = prof;
+    a.unitProfits[(size_t)t * a.P + p] = prof;
+    const float disc = 1.0f + a.rrr * a.dt / 100.0f;
+    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+    float best = 0.0f;
+    int bc = 0;
+    for (int c = 0; c < C; ++c) {
+        bool valid = true;
+        for (int s = 0; s < S; ++s)
+            if (state[c * S + s] < threshold(a, s) && c > 0) { valid = false; break; }
+        float pay = 0.0f;
+        if (valid) {
+            float cur = a.flows[c] * state[S * C];
+            const float* rb = a.reg + (size_t)t * C * blk + (size_t)c * blk;
+            float v = (a.sem == 0) ? to_lsm_interp_ref(rb, R, S, C, state)
+                                   : to_lsm_interp(rb, R, S, state + c * S, state[S * C]);
+            double ce = (double)(v / disc);
+            if (ce > 0.0) ce = 0.0;
+            pay = (float)((double)cur + ce);
+        }
+        if (c == 0) { best = pay; continue; }
+        if (!valid) continue;
+        bool better = (a.sem == 0) ? ((double)pay < 0.975 * (double)best) : (pay < best);
+        if (better) { best = pay; bc = c; }
+    }
+    a.condExp[(size_t)t * a.P + p] = best;
+    a.optCont[(size_t)t * a.P + p] = bc;
+}
+
+// firstPeriodInduction (:2210-2330) with FP64 reductions; one CTA.
+__global__ void k_rov_first(to_rov_args a) {
+    const int P = a.P, C = a.C, S = a.S, Y = a.Y;
+    __shared__ double s_sum[TO_ROV_MAXC][32], s_cnt[TO_ROV_MAXC][32];
+    __shared__ double s_best;
+    __shared__ int s_bc;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double sum[TO_ROV_MAXC], cnt[TO_ROV_MAXC];
+    for (int c = 0; c < C; ++c) { sum[c] = 0.0; cnt[c] = 0.0; }
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        int c = a.controls[p];
+        sum[c] += (double)a.condExp[(size_t)P + p];
+        cnt[c] += 1.0;
+    }
+    for (int c = 0; c < C; ++c) {
+        for (int o = 16; o > 0; o >>= 1) {
+            sum[c] += __shfl_xor_sync(0xffffffffu, sum[c], o);
+            cnt[c] += __shfl_xor_sync(0xffffffffu, cnt[c], o);
+        }
+        if (lane == 0) { s_sum[c][warp] = sum[c]; s_cnt[c][warp] = cnt[c]; }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float uf = 0.0f, ore = 0.0f;
+        for (int f = 0; f < a.nF; ++f)
+            uf = fmaf(a.fuel_costs[f], a.uRes[((size_t)a.fuel_idx[f] * (Y + 1)) * P], uf);
+        for (int c = 0; c < a.Cm; ++c)
+            ore = fmaf(ore_at(a, 0, 0, c), a.uRes[((size_t)(a.nF + c) * (Y + 1)) * P], ore);
+        float prof0 = (a.unit_cost + uf) - a.unit_revenue * ore;
+        if (a.demand_idx >= 0) prof0 = prof0 * a.uRes[((size_t)a.demand_idx * (Y + 1)) * P];
+        const double discd = (double)(1.0f + a.rrr * a.dt / 100.0f);
+        double pay[TO_ROV_MAXC];
+        int stop = C;
+        for (int c = 0; c < C; ++c) {
+            double sm = 0.0, cn = 0.0;
+            for (int w = 0; w < nw; ++w) { sm += s_sum[c][w]; cn += s_cnt[c][w]; }
+            if (cn > 0.0) pay[c] = sm / (cn * discd);
+            else { stop = c; break; }
+            bool valid = true;
+            for (int s = 0; s < S; ++s) {
+                float adj = a.totalPops[((size_t)s * (Y + 1)) * P] *
+                            a.aars[(((size_t)s * C + c) * Y) * P];
+                if (adj < threshold(a, s) && c > 0) { valid = false; break; }
+            }
+            if (valid) {
+                pay[c] += (double)(a.flows[c] * prof0);
+                if (pay[c] > 0.0) pay[c] = 0.0;
+            } else pay[c] = NAN;
+        }
+        for (int c = stop; c < C; ++c) pay[c] = (c == 0) ? 0.0 : NAN;
+        double best = pay[0];
+        int bc = 0;
+        for (int c = 1; c < C; ++c)
+            if (isfinite(pay[c]) && pay[c] < best) { best = pay[c]; bc = c; }
+        s_best = best;
+        s_bc = bc;
+    }
+    __syncthreads();
+    const double best = s_best;
+    const int bc = s_bc;
+    double ss = 0.0, m1 = 0.0, n1 = 0.0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        if (a.controls[p] == bc) {
+            double v = (double)a.condExp[(size_t)P + p];
+            ss += (v - best) * (v - best);
+            m1 += v;
+            n1 += 1.0;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        m1 += __shfl_xor_sync(0xffffffffu, m1, o);
+        n1 += __shfl_xor_sync(0xffffffffu, n1, o);
+    }
+    __syncthreads();
+    if (lane == 0) { s_sum[0][warp] = ss; s_sum[1][warp] = m1; s_cnt[0][warp] = n1; }
+    __syncthreads();
+    double SS = 0.0, M1 = 0.0, N1 = 0.0;
+    for (int w = 0; w < nw; ++w) { SS += s_sum[0][w]; M1 += s_sum[1][w]; N1 += s_cnt[0][w]; }
+    const double discd = (double)(1.0f + a.rrr * a.dt / 100.0f);
+    // sample variance of the chosen control's year-1 values
+    double mean = N1 > 0.0 ? M1 / N1 : 0.0;
+    double vv = 0.0;
+    for (int p = threadIdx.x; p < P; p += blockDim.x)
+        if (a.controls[p] == bc) {
+            double v = (double)a.condExp[(size_t)P + p] - mean;
+            vv += v * v;
+        }
+    for (int o = 16; o > 0; o >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, o);
+    __syncthreads();
+    if (lane == 0) s_sum[2 % TO_ROV_MAXC][warp] = vv;
+    __syncthreads();
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        a.condExp[p] = (float)best;
+        a.optCont[p] = bc;
+    }
+    if (threadIdx.x == 0) {
+        double V = 0.0;
+        for (int w = 0; w < nw; ++w) V += s_sum[2 % TO_ROV_MAXC][w];
+        double sdfac = (a.sem == 0) ? (1.0 + (double)a.rrr / (100.0 * (double)a.dt)) : discd;
+        a.stats[0] = (double)(float)best;
+        a.stats[1] = (double)bc;
+        a.stats[2] = (N1 > 0.0) ? sqrt(SS / (N1 * sdfac)) : 0.0;
+        a.stats[3] = (N1 > 1.0) ? sqrt(V / (N1 - 1.0)) / sqrt(N1) / discd : 0.0;
+        a.stats[4] = N1;
+    }
+}
+
+}  // namespace
+
+namespace to_k {
+
+to_status rov_run(to_ctx ctx, to_rov_args a) {
+    const int P = a.P;
+    const int tpb = 128;
+    const int pblocks = (P + tpb - 1) / tpb;
+    to_prof_begin(ctx, "rov_exog");
+    k_rov_exog<<<pblocks, tpb, 0, ctx->stream>>>(a);
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
+    // forward tile shape
+    const int NE = a.ne, KG = NE / 4;
+    int pgroups = 256 / KG;
+    if (pgroups < 1) pgroups = 1;
+    if (pgroups > 16) pgroups = 16;
+    if (pgroups * KG > 1024) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NE);
+    a.tile_paths = 4 * pgroups;
+    size_t fixed = (size_t)(2 * a.tile_paths * NE + 3 * a.tile_paths) * sizeof(float);
+    size_t budget = 200 * 1024;
+    if (fixed + (size_t)a.C * NE * NE * 4 <= budget) a.l_chunk = NE;
+    else {
+        int lc = 64;
+        while (lc > 4 && (fixed + (size_t)a.C * lc * NE * 4 > budget || NE % lc)) lc >>= 1;
+        if (NE % lc) lc = 4;
+        a.l_chunk = lc;
+    }
+    size_t smem = fixed + (size_t)a.C * a.l_chunk * NE * sizeof(float);
+    dim3 grid((P + a.tile_paths - 1) / a.tile_paths);
+    int threads = ((pgroups * KG + 31) / 32) * 32;
+    if (a.C > TO_ROV_MAXC) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "controls %d", a.C);
+    to_prof_begin(ctx, "rov_forward");
+    if (a.C <= 3) {
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward<3>,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_rov_forward<3><<<grid, threads, smem, ctx->stream>>>(a);
+    } else {
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward<TO_ROV_MAXC>,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_rov_forward<TO_ROV_MAXC><<<grid, threads, smem, ctx->stream>>>(a);
+    }
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
+    k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
+    TO_LAUNCHED(ctx);
+    for (int t = a.Y - 2; t > 0; --t) {
+        to_prof_begin(ctx, "lsm_prepare");
+        k_lsm_prepare<<<1, 1024, 0, ctx->stream>>>(a, t);
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+        TO_TRY(knn_rov(ctx, a, t));
+        TO_TRY(regress_rov(ctx, a, t));
+        to_prof_begin(ctx, "rov_backward");
+        k_rov_backward<<<pblocks, tpb, 0, ctx->stream>>>(a, t);
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+    }
+    k_rov_first<<<1, 1024, 0, ctx->stream>>>(a);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+}  // namespace to_k

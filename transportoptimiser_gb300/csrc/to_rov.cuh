@@ -1,0 +1,80 @@
+// to_rov.cuh - argument block of the ROV kernels and the kNN / regression
+// launchers shared with the surrogate builders.
+#pragma once
+#include "to_internal.cuh"
+#include "to_lsm_math.h"
+
+#define TO_ROV_MAXC 8
+#define TO_KNN_KMAX 256
+
+struct to_rov_args {
+    int P, Y, S, C, U, R, Q;          // paths, years, species, controls, processes, dimRes, R^d
+    int nF, Cm, demand_idx, sem, road;
+    float dt, rrr, unit_cost, unit_revenue, scaling;
+    uint64_t seed;
+    int np, ne;                       // stride / effective width of patch arrays
+    int tile_paths, l_chunk;          // forward tile (launcher)
+    // inputs (device)
+    const int* n_patches;             // [S]
+    const float* params;              // [S*8]
+    const float* init_pops;           // [S][np]
+    const float* caps;                // [S][np] (padding 1)
+    const float* mmm;                 // [S][C][np][np] destination-major
+    const float* flows;               // [C]
+    const float* uncert;              // [U*6]
+    const float* fuel_costs;          // [nF]
+    const int* fuel_idx;              // [nF]
+    const float* ore_content;         // [Cm]
+    const float* ore_sd;              // [Cm]
+    // path state (device)
+    int* controls;                    // [Y][P]
+    float* uRes;                      // [U][Y+1][P]
+    float* totalPops;                 // [S][Y+1][P]
+    float* aars;                      // [S][C][Y][P]
+    // regression scratch (device)
+    float* xraw;                      // [C][d][P] compacted raw states
+    float* xn;                        // [C][d][P] normalised
+    float* yv;                        // [C][P]
+    int* npts;                        // [C]
+    int* kc;                          // [C]
+    float* gmin;                      // [d]
+    float* gmax;                      // [d]
+    float* dist;                      // [C][kmax][Q]
+    int* ind;                         // [C][kmax][Q]
+    int kmax;
+    // outputs (device)
+    float* reg;                       // [Y][C][R*d + 2Q]
+    float* condExp;                   // [Y][P]
+    int* optCont;                     // [Y][P]
+    float* unitProfits;               // [Y][P]
+    float* adjPops;                   // [Y][S][P]
+    double* stats;                    // [5]: value, control, SD, SE, n
+};
+
+// grid query q of the current year: normalised coordinates (for kNN) and
+// the coordinates the regression centres on (createQueryPoints + host
+// normalisation; sem 0 centres on the unit grid, SimulateGPU.cu:2964-2966)
+__device__ __forceinline__ void to_rov_query(const to_rov_args& a, int q, float* qn,
+                                             float* xq) {
+    const int d = a.S + 1, R = a.R;
+    int rem = q;
+    int div = a.Q / R;
+    for (int j = 0; j < d; ++j) {
+        int di = rem / div;
+        rem -= di * div;
+        div /= R;
+        float raw = to_lsm_query_axis(di, a.gmin[j], a.gmax[j], R);
+        float nv = to_lsm_normalise(raw, a.gmin[j], a.gmax[j], j == a.S, a.scaling);
+        qn[j] = nv;
+        xq[j] = (a.sem == 0) ? to_lsm_unit_axis(di, R) : nv;
+    }
+}
+
+namespace to_k {
+to_status rov_run(to_ctx ctx, to_rov_args a);
+to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t);
+to_status regress_rov(to_ctx ctx, const to_rov_args& a, int t);
+// generic kNN: ref dim-major [dim][n], query dim-major [dim][Q]
+to_status knn(to_ctx ctx, const float* ref, int n, const float* query, int Q,
+              int dim, int k, float* dist, int* ind);
+}

@@ -173,3 +173,67 @@ def expPV(gr, mean, time_step, rrr, current, reversion, jump_prob, noise_sd, jum
     if return_values:
         return m.value, s.value, vals
     return m.value, s.value
+
+
+def simulateROVCUDA(problem: dict, want=("cond_exp", "opt_cont", "unit_profits", "adj_pops",
+                                        "regression"), migration=_capi.MIG_SIMT_FP32,
+                    ctx: Context | None = None) -> dict:
+    """SimulateGPU::simulateROVCUDA, ALGO4 (SimulateGPU.cu:3870-5003).
+
+    ``problem`` follows transportoptimiser_gb300.rov.  Returns condExp,
+    optCont, unitProfits ([Y][P]), adjPops ([Y][S][P]), the regression
+    surfaces and the stats (value, control, sd) plus the Monte Carlo SE."""
+    ctx = ctx or context()
+    S = len(problem["species"])
+    P, Y, R = problem["n_paths"], problem["n_years"], problem["dim_res"]
+    Cn = len(problem["flows"])
+    keep = []
+    sps = (_capi.RovSpecies * S)()
+    for s, sp in enumerate(problem["species"]):
+        arrs = [np.ascontiguousarray(sp[k], np.float32) for k in ("params", "init_pops", "caps", "mmm")]
+        keep += arrs
+        sps[s] = _capi.RovSpecies(int(sp["N"]), *[ptr(a_, C.c_float) for a_ in arrs])
+    f32 = lambda k: np.ascontiguousarray(problem[k], np.float32)
+    flows, unc, fc, oc, osd = (f32(k) for k in ("flows", "uncert", "fuel_costs", "ore_content",
+                                                  "ore_sd"))
+    fi = np.ascontiguousarray(problem["fuel_idx"], np.int32)
+    keep += [flows, unc, fc, oc, osd, fi]
+    pr = _capi.RovProblem(S, P, Y, Cn, R, sps, ptr(flows, C.c_float), len(unc) // 6,
+                          ptr(unc, C.c_float), len(fc), ptr(fc, C.c_float), ptr(fi, C.c_int),
+                          len(oc), ptr(oc, C.c_float), ptr(osd, C.c_float),
+                          problem["unit_cost"], problem["unit_revenue"], problem["dt"],
+                          problem["rrr"], problem.get("demand_idx", -1), problem["seed"],
+                          problem["road"], problem["sem"], migration)
+    d = S + 1
+    out = {}
+    if "cond_exp" in want: out["cond_exp"] = np.zeros(Y * P)
+    if "opt_cont" in want: out["opt_cont"] = np.zeros(Y * P, np.int32)
+    if "unit_profits" in want: out["unit_profits"] = np.zeros(Y * P)
+    if "adj_pops" in want: out["adj_pops"] = np.zeros(Y * S * P)
+    if "regression" in want: out["regression"] = np.zeros(Y * Cn * (R * d + 2 * R ** d))
+    r = _capi.RovResult()
+    r.cond_exp = ptr(out.get("cond_exp"), C.c_double)
+    r.opt_cont = ptr(out.get("opt_cont"), C.c_int)
+    r.unit_profits = ptr(out.get("unit_profits"), C.c_double)
+    r.adj_pops = ptr(out.get("adj_pops"), C.c_double)
+    r.regression = ptr(out.get("regression"), C.c_double)
+    ctx.check(ctx.lib.to_simulate_rov(ctx.handle, C.byref(pr), C.byref(r)), "to_simulate_rov")
+    out["stats"] = np.array([r.value, r.control, r.sd])
+    out["value_se"] = r.se
+    out["n_best"] = r.n_best
+    return out
+
+
+def knn(ref_pts: np.ndarray, query: np.ndarray, k: int, ctx: Context | None = None):
+    """knn_cuda_with_indexes::knn: ref (dim x n), query (dim x Q), dim-major.
+    Returns dist, ind (k x Q, ind 1-based)."""
+    ctx = ctx or context()
+    ref_pts = np.ascontiguousarray(ref_pts, np.float32)
+    query = np.ascontiguousarray(query, np.float32)
+    dim, n = ref_pts.shape
+    Q = query.shape[1]
+    dist = np.zeros(k * Q, np.float32)
+    ind = np.zeros(k * Q, np.int32)
+    ctx.check(ctx.lib.to_knn(ctx.handle, ptr(ref_pts, C.c_float), n, ptr(query, C.c_float), Q,
+                             dim, k, ptr(dist, C.c_float), ptr(ind, C.c_int)), "to_knn")
+    return dist.reshape(k, Q), ind.reshape(k, Q)
