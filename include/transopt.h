@@ -175,6 +175,7 @@ typedef struct {
 to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
                           double* end_pops, to_mte_stats* stats);
 
+
 /* ---- expected present value of an uncertain price ---------------------- */
 typedef struct {
     float gr;                /* traffic growth x time step                     */
@@ -249,6 +250,26 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* prob,
  * (dist[kk*Q + q], ind 1-based) in ascending (distance, index) order. */
 to_status to_knn(to_ctx ctx, const float* ref, int n, const float* query,
                  int Q, int dim, int k, float* dist, int* ind);
+
+
+/* ---- surrogates ------------------------------------------------------------
+ * SimulateGPU::buildSurrogateMTECUDA, SimulateGPU.h:235 / SimulateGPU.cu:5533:
+ * 1-D local-linear surrogate of the end population (mean, then SD) against
+ * the initial animals-at-risk over dim_res grid points.  out_mean / out_sd
+ * (optional) hold [dim_res x values | dim_res y values]. */
+to_status to_build_surrogate_mte(to_ctx ctx, int samples, const double* iars,
+                                 const double* pops_mean, const double* pops_sd,
+                                 int dim_res, double* out_mean, double* out_sd);
+
+/* SimulateGPU::buildSurrogateROVCUDA, SimulateGPU.h:244 / SimulateGPU.cu:5694:
+ * predictors dim-major [n_dims][samples] (IAR per species, then unit use);
+ * outputs [dim_res*n_dims axis values | dim_res^n_dims values]; the mean
+ * surface is clipped at zero (rovCorrection).  sem 0 regresses on the raw
+ * predictors as the reference reads them (see TO_SEM_REFERENCE). */
+to_status to_build_surrogate_rov(to_ctx ctx, int samples, int n_dims,
+                                 const double* predictors, const double* values,
+                                 const double* values_sd, int dim_res, int sem,
+                                 double* out_mean, double* out_sd);
 
 /* ---- batched GA generation ------------------------------------------------
  * A scene (habitat map, species, initial-population maps) is uploaded once

@@ -154,6 +154,10 @@ SIGNATURES = {
     "to_simulate_rov": (C.c_int, [C.c_void_p, C.POINTER(RovProblem), C.POINTER(RovResult)]),
     "to_knn": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, C.c_int, C.c_int, C.c_int,
                          c_float_p, c_int_p]),
+    "to_build_surrogate_mte": (C.c_int, [C.c_void_p, C.c_int, c_double_p, c_double_p,
+                                         c_double_p, C.c_int, c_double_p, c_double_p]),
+    "to_build_surrogate_rov": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_double_p, c_double_p,
+                                         c_double_p, C.c_int, C.c_int, c_double_p, c_double_p]),
     "to_scene_create": (C.c_int, [C.c_void_p, C.POINTER(Scene), C.POINTER(C.c_void_p)]),
     "to_scene_destroy": (C.c_int, [C.c_void_p]),
     "to_evaluate_roads": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, c_int_p, c_int_p,

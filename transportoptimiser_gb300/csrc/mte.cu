@@ -241,3 +241,4 @@ to_status mte_stats(to_ctx ctx, const to_mte_args& a, int n_rs, double* d_stats)
 }
 
 }  // namespace to_k
+

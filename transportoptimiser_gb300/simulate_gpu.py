@@ -237,3 +237,36 @@ def knn(ref_pts: np.ndarray, query: np.ndarray, k: int, ctx: Context | None = No
     ctx.check(ctx.lib.to_knn(ctx.handle, ptr(ref_pts, C.c_float), n, ptr(query, C.c_float), Q,
                              dim, k, ptr(dist, C.c_float), ptr(ind, C.c_int)), "to_knn")
     return dist.reshape(k, Q), ind.reshape(k, Q)
+
+
+def buildSurrogateMTECUDA(iars, pops_mean, pops_sd, dim_res, ctx: Context | None = None):
+    """SimulateGPU::buildSurrogateMTECUDA (SimulateGPU.cu:5533) for one
+    species: returns the (mean, sd) surrogate vectors [R x | R y]."""
+    ctx = ctx or context()
+    x = np.ascontiguousarray(iars, np.float64)
+    m = np.ascontiguousarray(pops_mean, np.float64)
+    sd = np.ascontiguousarray(pops_sd, np.float64)
+    om, osd = np.zeros(2 * dim_res), np.zeros(2 * dim_res)
+    ctx.check(ctx.lib.to_build_surrogate_mte(ctx.handle, len(x), ptr(x, C.c_double),
+                                             ptr(m, C.c_double), ptr(sd, C.c_double), dim_res,
+                                             ptr(om, C.c_double), ptr(osd, C.c_double)),
+              "to_build_surrogate_mte")
+    return om, osd
+
+
+def buildSurrogateROVCUDA(predictors, values, values_sd, dim_res, sem=0,
+                          ctx: Context | None = None):
+    """SimulateGPU::buildSurrogateROVCUDA (SimulateGPU.cu:5694): predictors
+    d x n (IARs, unit use).  Returns the (mean, sd) surrogate vectors."""
+    ctx = ctx or context()
+    pr = np.ascontiguousarray(predictors, np.float64)
+    d, n = pr.shape
+    v = np.ascontiguousarray(values, np.float64)
+    vs = np.ascontiguousarray(values_sd, np.float64)
+    size = dim_res * d + dim_res ** d
+    om, osd = np.zeros(size), np.zeros(size)
+    ctx.check(ctx.lib.to_build_surrogate_rov(ctx.handle, n, d, ptr(pr, C.c_double),
+                                             ptr(v, C.c_double), ptr(vs, C.c_double), dim_res,
+                                             sem, ptr(om, C.c_double), ptr(osd, C.c_double)),
+              "to_build_surrogate_rov")
+    return om, osd
