@@ -176,6 +176,38 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
                           double* end_pops, to_mte_stats* stats);
 
 
+/* ---- MTE without device allocation ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory - a host program that has handed the whole device to its own pool
+ * allocator, or one that must not add allocations (and the synchronisation
+ * they imply) to a GA loop - this entry point takes every input and output
+ * as caller-owned device memory and allocates nothing: the per-path end
+ * populations it needs go to a fixed array compiled into the library
+ * (species x paths <= 2,097,152 floats, 8 MiB held by every GPU that loads
+ * the library until exit; larger problems return TO_ERR_UNSUPPORTED).
+ * The first call on a device looks up that array's device address, so make
+ * it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race on it.  Work is enqueued on `stream`
+ * (cudaStream_t, may be 0); d_stats receives [n_species][5] doubles: mean,
+ * SD, standard error, P(end < 0.2 x initial), initial population. */
+typedef struct {
+    int n_species, n_paths, n_years;
+    int npad;                /* row stride of the arrays below, multiple of 4 */
+    float dt;
+    uint64_t seed;
+    int road, sem;
+    const int* n_patches;    /* device [n_species]                            */
+    const float* params;     /* device [n_species][8]                         */
+    const float* init_pops;  /* device [n_species][npad], zero padded         */
+    const float* caps;       /* device [n_species][npad], padding 1.0         */
+    const float* mmm;        /* device [n_species][npad][npad] destination-major,
+                                zero padded                                   */
+} to_mte_device_problem;
+
+to_status to_simulate_mte_noalloc_d(void* stream,
+                                    const to_mte_device_problem* prob,
+                                    double* d_stats);
+
 /* ---- expected present value of an uncertain price ---------------------- */
 typedef struct {
     float gr;                /* traffic growth x time step                     */

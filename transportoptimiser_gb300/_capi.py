@@ -70,6 +70,13 @@ class MteStats(C.Structure):
                 ("p_below", C.c_double), ("init_total", C.c_double)]
 
 
+class MteDeviceProblem(C.Structure):
+    _fields_ = [("n_species", C.c_int), ("n_paths", C.c_int), ("n_years", C.c_int),
+                ("npad", C.c_int), ("dt", C.c_float), ("seed", C.c_uint64), ("road", C.c_int),
+                ("sem", C.c_int), ("n_patches", C.c_void_p), ("params", C.c_void_p),
+                ("init_pops", C.c_void_p), ("caps", C.c_void_p), ("mmm", C.c_void_p)]
+
+
 class ExpPvParams(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("gr", "mean", "time_step", "rrr",
                                          "current", "reversion", "jump_prob",
@@ -148,6 +155,8 @@ SIGNATURES = {
                                    C.POINTER(SpeciesOut)]),
     "to_simulate_mte": (C.c_int, [C.c_void_p, C.POINTER(MteProblem), c_double_p,
                                   C.POINTER(MteStats)]),
+    "to_simulate_mte_noalloc_d": (C.c_int, [C.c_void_p, C.POINTER(MteDeviceProblem),
+                                            C.c_void_p]),
     "to_exp_pv": (C.c_int, [C.c_void_p, C.POINTER(ExpPvParams), C.c_int, C.c_int,
                             C.c_uint64, C.c_int, C.c_int, c_float_p, c_double_p,
                             c_double_p]),

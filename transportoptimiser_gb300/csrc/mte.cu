@@ -242,3 +242,88 @@ to_status mte_stats(to_ctx ctx, const to_mte_args& a, int n_rs, double* d_stats)
 
 }  // namespace to_k
 
+// ---------------------------------------------------------------------------
+// to_simulate_mte_noalloc_d: the MTE statistics entry point for callers that
+// cannot allocate device memory.  The per-path end populations, the only
+// scratch this computation needs, live in a fixed file-scope device array
+// that every GPU loading the library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#define TO_NOALLOC_MTE_MAX_VALUES (1 << 21)   // species x paths; 8 MiB of floats
+
+static __device__ __align__(256) float g_mte_noalloc_end[TO_NOALLOC_MTE_MAX_VALUES];
+
+namespace {
+
+struct NoallocDevice {
+    std::once_flag once;
+    cudaError_t status = cudaSuccess;
+    float* end = nullptr;   // device address of g_mte_noalloc_end on this device
+};
+NoallocDevice g_noalloc_dev[64];
+
+}  // namespace
+
+extern "C" to_status to_simulate_mte_noalloc_d(void* stream,
+                                               const to_mte_device_problem* pr,
+                                               double* d_stats) {
+    if (!pr || !d_stats || pr->n_species <= 0 || pr->n_paths <= 0 || pr->n_years < 0 ||
+        pr->npad <= 0 || pr->npad % 4 != 0 || pr->npad > 1020 || !pr->n_patches ||
+        !pr->params || !pr->init_pops || !pr->caps || !pr->mmm)
+        return TO_ERR_INVALID;
+    if ((long long)pr->n_species * pr->n_paths > TO_NOALLOC_MTE_MAX_VALUES)
+        return TO_ERR_UNSUPPORTED;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return TO_ERR_NO_DEVICE;
+    }
+    // one-time set-up on this device (the device is current here): the
+    // host-side name of the array is not a device address, so fetch the
+    // device address once and keep it
+    NoallocDevice& nd = g_noalloc_dev[dev];
+    std::call_once(nd.once, [&nd]() {
+        void* p = nullptr;
+        nd.status = cudaGetSymbolAddress(&p, g_mte_noalloc_end);
+        nd.end = static_cast<float*>(p);
+    });
+    if (nd.status != cudaSuccess || !nd.end) return TO_ERR_CUDA;
+
+    to_mte_args a;
+    memset(&a, 0, sizeof(a));
+    a.n_paths = pr->n_paths; a.n_years = pr->n_years; a.S = pr->n_species;
+    a.C = 1; a.c_use = 0; a.dt = pr->dt; a.seed = pr->seed; a.sem = pr->sem;
+    a.road0 = pr->road; a.npad = pr->npad; a.npe = pr->npad;
+    a.n_patches = pr->n_patches; a.mmm = pr->mmm; a.init_pops = pr->init_pops;
+    a.caps = pr->caps; a.params = pr->params; a.end_pops = nd.end;
+    // tile shape as the allocating entry point chooses it
+    const int NP = a.npe, KG = NP / 4;
+    int pgroups = 256 / KG;
+    if (pgroups < 1) pgroups = 1;
+    if (pgroups > 16) pgroups = 16;
+    a.tile_paths = 4 * pgroups;
+    const size_t budget = 200 * 1024;
+    const size_t fixed = (size_t)(2 * a.tile_paths * NP + a.tile_paths) * sizeof(float);
+    if (fixed + (size_t)NP * NP * sizeof(float) <= budget) a.l_chunk = NP;
+    else {
+        int lc = 64;
+        while (lc > 4 && (fixed + (size_t)lc * NP * sizeof(float) > budget || NP % lc)) lc >>= 1;
+        if (NP % lc) lc = 4;
+        a.l_chunk = lc;
+    }
+    const size_t smem = fixed + (size_t)a.l_chunk * NP * sizeof(float);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (cudaFuncSetAttribute(k_mte_simt, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return TO_ERR_CUDA;
+    }
+    dim3 grid((a.n_paths + a.tile_paths - 1) / a.tile_paths, a.S);
+    int threads = ((pgroups * KG + 31) / 32) * 32;
+    k_mte_simt<<<grid, threads, smem, st>>>(a);
+    k_mte_stats<<<a.S, 256, 0, st>>>(a.n_paths, a.end_pops, a.init_pops, a.npad,
+                                     a.n_patches, d_stats);
+    if (cudaGetLastError() != cudaSuccess) return TO_ERR_CUDA;
+    return TO_OK;
+}
