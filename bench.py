@@ -196,7 +196,7 @@ def main():
     torch.cuda.set_device(local)
 
     from transportoptimiser_gb300 import synth
-    from transportoptimiser_gb300._capi import MIG_SIMT_FP32, Context
+    from transportoptimiser_gb300._capi import MIG_AUTO, Context
     from transportoptimiser_gb300.generation import Generation, pack_roads
     from transportoptimiser_gb300 import simulate_gpu as sg
 
@@ -210,10 +210,10 @@ def main():
 
     # pilot (untimed): N* per road
     pilot = gen.evaluate(packed, gen.opts(PILOT_PATHS, YEARS, seed=1, road0=road0,
-                                          migration=MIG_SIMT_FP32))
+                                          migration=MIG_AUTO))
     need = n_star(pilot)
     P = min(int(math.ceil(max(need) / 64.0) * 64), 16384)
-    opts = gen.opts(P, YEARS, seed=0, road0=road0, migration=MIG_SIMT_FP32)
+    opts = gen.opts(P, YEARS, seed=0, road0=road0, migration=MIG_AUTO)
     Ns = pilot[:, :, 0].astype(int)
 
     # device-resident inputs for `value`
@@ -255,7 +255,7 @@ def main():
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall0
         launches = (ctx.launches - l0) // args.steps
-        mte_ms, mte_n = ctx.kernel_time("mte_simt")
+        mte_ms, mte_n = ctx.kernel_time("mte_sparse")
         sm_ms, sm_n = ctx.kernel_time("species_model")
         ctx.profile(False)
         clocks = clocks_stop(clk, local)
@@ -298,7 +298,7 @@ def main():
                     rd.colmajor(), rd.G, sp.hazard, sp.lambda_mean, sp.lambda_sd,
                     sp.lambda_mult, sp.hab_pref_mult, sem=0, max_patches=512, ctx=ctx))
             sg.simulateMTECUDA(models, [sp.params for sp in scene.species], P, YEARS,
-                               seed=0, road=road0 + r, migration=MIG_SIMT_FP32, ctx=ctx)
+                               seed=0, road=road0 + r, migration=MIG_AUTO, ctx=ctx)
         plain_value = args.plain_roads / (time.perf_counter() - t0)
 
     # roofline of the dominant kernel (migration + growth, SIMT FP32)

@@ -46,10 +46,14 @@ typedef enum {
 typedef enum { TO_SEM_REFERENCE = 0, TO_SEM_CORRECTED = 1 } to_sem;
 
 typedef enum {
-    TO_MIG_AUTO = 0,         /* tensor cores where supported                 */
-    TO_MIG_SIMT_FP32 = 1,    /* CUDA-core FP32, bit-identical to the oracle  */
-    TO_MIG_TC_3XTF32 = 2     /* tcgen05 kind::tf32, 3 MMAs (hi/lo split)     */
+    TO_MIG_AUTO = 0,         /* sparse when the matrices fit, else dense     */
+    TO_MIG_SIMT_FP32 = 1,    /* dense CUDA-core FP32                         */
+    TO_MIG_TC_3XTF32 = 2,    /* dense tcgen05 kind::tf32, 3 MMAs (hi/lo)     */
+    TO_MIG_SPARSE_FP32 = 3   /* compressed columns in shared memory          */
 } to_migration;
+/* Every FP32 form sums each destination's terms in ascending origin order
+ * with fused multiply-adds, so the sparse and dense CUDA-core forms are
+ * bit-identical to each other and to the CPU oracle. */
 
 typedef struct to_ctx_s* to_ctx;
 

@@ -302,6 +302,19 @@ int or_species_model(const or_species_in* in, or_species_out* out) {
 /*   Q2: no /100 in the logistic step (the ROV kernel has it).                */
 /*   Q3 (sem 0): jump size = z*s^2 - s^2/2; sem 1: z*s - s^2/2.               */
 /* ------------------------------------------------------------------------ */
+/* Patch totals are summed in groups of four consecutive patches,
+ * ((v0 + v1) + v2) + v3, the groups then in ascending order - the order the
+ * CUDA kernels use (one warp lane owns a group of four patches). */
+float or_grouped_sum(const float* v, int N) {
+    float tot = 0.0f;
+    for (int g = 0; g < N; g += 4) {
+        float s = v[g];
+        for (int j = 1; j < 4; ++j) s = s + (g + j < N ? v[g + j] : 0.0f);
+        tot = tot + s;
+    }
+    return tot;
+}
+
 typedef struct {
     int p0, p1, n_years, N, species, road, sem;
     float dt;
@@ -345,10 +358,8 @@ static void mte_paths(const mte_job* j) {
                 pop[k] = m * (1.0f + gr * (c - m) / c);
             }
         }
-        float e = 0.0f;
-        if (j->sem == 0) { for (int k = 0; k < N; ++k) e += mig[k]; }
-        else             { for (int k = 0; k < N; ++k) e += pop[k]; }
-        if (j->n_years == 0) { e = 0.0f; for (int k = 0; k < N; ++k) e += j->init[k]; }
+        float e = (j->n_years == 0) ? or_grouped_sum(j->init, N)
+                : (j->sem == 0 ? or_grouped_sum(mig, N) : or_grouped_sum(pop, N));
         j->out[p] = e;
     }
     free(pop);

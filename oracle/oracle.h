@@ -98,6 +98,9 @@ void or_simulate_mte(int n_paths, int n_years, int N, float dt,
 void or_exp_pv(int n_paths, int n_years, const float* params, uint64_t seed,
                int road, int sem, float* values, double* mean, double* sd);
 
+/* patch totals: groups of four, ((v0 + v1) + v2) + v3, groups ascending */
+float or_grouped_sum(const float* v, int N);
+
 /* stream helpers for tests (materialise the fused streams) */
 void or_fill_stream(uint64_t seed, int stream, int road, int normal,
                     int n_paths, int n_years, int L, int lane_offset,

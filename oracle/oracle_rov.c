@@ -25,6 +25,7 @@
  * the reference's stable insertion sort returns.
  */
 #include "oracle_rov.h"
+#include "oracle.h"
 #include "../transportoptimiser_gb300/csrc/to_math.h"
 #include "../transportoptimiser_gb300/csrc/to_lsm_math.h"
 
@@ -132,12 +133,8 @@ static void rov_forward_paths(rov_fwd_job* j) {
     for (int p = j->p0; p < j->p1; ++p) {
         for (int s = 0; s < S; ++s) {
             int N = pr->n_patches[s];
-            float tot = 0.0f;
-            for (int k = 0; k < N; ++k) {
-                pop[(size_t)s * maxN + k] = pr->init_pops[s][k];
-                tot += pr->init_pops[s][k];
-            }
-            j->totalPops[((size_t)p * (Y + 1) + 0) * S + s] = tot;
+            for (int k = 0; k < N; ++k) pop[(size_t)s * maxN + k] = pr->init_pops[s][k];
+            j->totalPops[((size_t)p * (Y + 1) + 0) * S + s] = or_grouped_sum(pr->init_pops[s], N);
             gm[s] = pr->params[s][0];
         }
         for (int u = 0; u < U; ++u)
@@ -162,36 +159,36 @@ static void rov_forward_paths(rov_fwd_job* j) {
                 float jsz = (pr->sem == 0) ? (zj * s5 - s5 / 2.0f) : (zj * sp[5] - s5 / 2.0f);
                 gm[s] = gm[s] + sp[4] * (sp[1] - gm[s]) * pr->dt + gm[s] * brown
                         + (to_expf(jsz) - 1.0f) * gm[s] * jump;
-                float initial = 0.0f;
-                for (int k = 0; k < N; ++k) initial += ps[k];
-                float newtot = 0.0f;
+                float initial = or_grouped_sum(ps, N);
                 for (int c = 0; c < C; ++c) {
                     const float* M = pr->mmm[s] + (size_t)c * N * N;
-                    float totc = 0.0f;
                     for (int k = 0; k < N; ++k) {
                         float a = 0.0f;
                         const float* col = M + (size_t)k * N;
                         for (int l = 0; l < N; ++l) a = fmaf(ps[l], col[l], a);
                         mig[k] = a;
-                        totc += a;
                     }
+                    float totc = or_grouped_sum(mig, N);
                     if (c == control) {
                         for (int k = 0; k < N; ++k) {
                             float z = to_normal1(pr->seed, TO_STREAM_GROWTH, pr->road, p, t,
                                                  (uint32_t)(s * N4 + k));
-                            float gr = gm[s] + z * sp[7];
+                            /* Q25: the reference adds the local variability
+                             * (gr = gm + z p7); sem 1 scales it by the mean
+                             * as the MTE kernel does and keeps pops >= 0 */
+                            float gr = (pr->sem == 0) ? gm[s] + z * sp[7]
+                                                      : fmaf(sp[7] * z, gm[s], gm[s]);
                             float m = mig[k], cp = pr->caps[s][k];
                             float v = (pr->sem == 0)
                                 ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
-                                : m * (1.0f + gr * (cp - m) / cp);
+                                : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
                             npop[k] = v;
-                            newtot += v;
                         }
                     }
                     j->aars[(((size_t)p * (Y + 1) + t) * S + s) * C + c] = totc / initial;
                 }
                 memcpy(ps, npop, sizeof(float) * (size_t)N);
-                j->totalPops[((size_t)p * (Y + 1) + t + 1) * S + s] = newtot;
+                j->totalPops[((size_t)p * (Y + 1) + t + 1) * S + s] = or_grouped_sum(ps, N);
             }
             for (int u = 0; u < U; ++u) {
                 const float* up = pr->uncert + 6 * u;

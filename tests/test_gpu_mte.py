@@ -8,7 +8,9 @@ import pytest
 from oracle import pyoracle as po
 from transportoptimiser_gb300 import simulate_gpu as sg
 from transportoptimiser_gb300 import synth
-from transportoptimiser_gb300._capi import MIG_SIMT_FP32, TransOptError
+from transportoptimiser_gb300._capi import MIG_SIMT_FP32, MIG_SPARSE_FP32, TransOptError
+
+MIGS = [MIG_SIMT_FP32, MIG_SPARSE_FP32]
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-5
@@ -18,14 +20,15 @@ def _model(sc, s=0):
     return po.species_model(sc, sc.species[s], sc.roads[0], sem=0)
 
 
+@pytest.mark.parametrize("mig", MIGS)
 @pytest.mark.parametrize("sem", [0, 1])
-def test_mte_simt_bit_exact_vs_oracle(ctx, sem):
+def test_mte_simt_bit_exact_vs_oracle(ctx, sem, mig):
     sc = synth.mte_road(0)
     sp = sc.species[0]
     m = _model(sc)
     P, Y = 300, 50
     end, st = sg.simulateMTECUDA([m], [sp.params], P, Y, seed=11, road=2, sem=sem,
-                                 migration=MIG_SIMT_FP32, ctx=ctx)
+                                 migration=mig, ctx=ctx)
     ref = po.simulate_mte(P, Y, m["N"], 1.0, sp.params, m["init_pops"], m["caps"], m["mmm"][2],
                           11, 2, 0, sem)
     assert np.array_equal(end[:, 0].astype(np.float32), ref)
@@ -35,15 +38,17 @@ def test_mte_simt_bit_exact_vs_oracle(ctx, sem):
     assert math.isclose(st[0]["p_below"], float((e < 0.2 * m["init_pops"].astype(np.float64).sum()).mean()))
 
 
-def test_mte_matches_reference_golden(ctx, golden):
+@pytest.mark.parametrize("mig", MIGS)
+def test_mte_matches_reference_golden(ctx, golden, mig):
     g = golden["mte"]
     m = dict(N=int(g["N"]), init_pops=g["init"], caps=g["caps"], mmm=g["mmm"][None])
     end, _ = sg.simulateMTECUDA([m], [g["params"]], int(g["P"]), int(g["Y"]), seed=int(g["seed"]),
-                                road=0, sem=0, migration=MIG_SIMT_FP32, control=0, ctx=ctx)
+                                road=0, sem=0, migration=mig, control=0, ctx=ctx)
     np.testing.assert_allclose(end[:, 0], g["end"], rtol=RTOL)
 
 
-def test_mte_multi_species_and_padding(ctx):
+@pytest.mark.parametrize("mig", MIGS)
+def test_mte_multi_species_and_padding(ctx, mig):
     sc = synth.rov_road(2, n_species=2)
     ms = [po.species_model(sc, sc.species[s], sc.roads[0], sem=0) for s in range(2)]
     # give species 1 a different patch count by dropping patches
@@ -53,7 +58,7 @@ def test_mte_multi_species_and_padding(ctx):
               mmm=np.ascontiguousarray(m1["mmm"][:, :n, :n]))
     P, Y = 150, 20
     end, _ = sg.simulateMTECUDA([ms[0], m1], [sc.species[0].params, sc.species[1].params], P, Y,
-                                seed=3, road=1, ctx=ctx)
+                                seed=3, road=1, migration=mig, ctx=ctx)
     for s, m in enumerate([ms[0], m1]):
         ref = po.simulate_mte(P, Y, m["N"], 1.0, sc.species[s].params, m["init_pops"], m["caps"],
                               m["mmm"][2], 3, 1, s, 0)

@@ -9,7 +9,10 @@ from oracle import pyoracle as po
 from rov_util import problem_from_golden, ref_outputs
 from transportoptimiser_gb300 import simulate_gpu as sg
 from transportoptimiser_gb300 import synth
+from transportoptimiser_gb300._capi import MIG_SIMT_FP32, MIG_SPARSE_FP32
 from transportoptimiser_gb300.rov import rov_problem_from_models
+
+MIGS = [MIG_SIMT_FP32, MIG_SPARSE_FP32]
 
 pytestmark = pytest.mark.gpu
 
@@ -27,9 +30,10 @@ def _compare_exact(gpu, orc, P, Y, S):
     assert math.isclose(gpu["value_se"], orc["value_se"], rel_tol=1e-9)
 
 
-def test_rov_reference_semantics_bit_exact(ctx, golden):
+@pytest.mark.parametrize("mig", MIGS)
+def test_rov_reference_semantics_bit_exact(ctx, golden, mig):
     rp = problem_from_golden(golden["rov"])
-    gpu = sg.simulateROVCUDA(rp, ctx=ctx)
+    gpu = sg.simulateROVCUDA(rp, migration=mig, ctx=ctx)
     orc = po.simulate_rov(rp)
     _compare_exact(gpu, orc, rp["n_paths"], rp["n_years"], 1)
 
@@ -44,14 +48,16 @@ def test_rov_matches_reference_golden(ctx, golden):
     assert np.abs(gpu["regression"] - ref["regression"]).max() <= 1e-5 * np.abs(ref["regression"]).max()
 
 
-@pytest.mark.parametrize("S,R,P,Y", [(2, 8, 900, 10), (1, 16, 1500, 8)])
-def test_rov_corrected_semantics_bit_exact(ctx, S, R, P, Y):
+@pytest.mark.parametrize("mig", MIGS)
+@pytest.mark.parametrize("S,R,P,Y", [(2, 8, 900, 10), (1, 16, 1500, 8), (2, 8, 700, 50)])
+def test_rov_corrected_semantics_bit_exact(ctx, S, R, P, Y, mig):
     sc = synth.rov_road(3, n_species=S)
     models = [po.species_model(sc, sc.species[s], sc.roads[0], sem=1) for s in range(S)]
     rp = rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
                                  n_processes=3, demand=True, seed=4, road=7)
-    gpu = sg.simulateROVCUDA(rp, ctx=ctx)
+    gpu = sg.simulateROVCUDA(rp, migration=mig, ctx=ctx)
     orc = po.simulate_rov(rp, threads=8)
+    assert np.isfinite(orc["stats"][0])
     _compare_exact(gpu, orc, P, Y, S)
 
 

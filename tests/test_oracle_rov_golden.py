@@ -45,3 +45,14 @@ def test_rov_surrogate_matches_reference_golden(golden):
     g = golden["surrogate_rov"]
     out = po.build_surrogate_nd(g["pred"], g["y"], int(g["R"]), sem=0, clip=1)
     assert np.abs(out - g["mean"]).max() <= RTOL * np.abs(g["mean"]).max()
+
+
+def test_corrected_rov_stays_finite_over_fifty_years():
+    from transportoptimiser_gb300 import synth
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    sc = synth.rov_road(0, n_species=2)
+    ms = [po.species_model(sc, sc.species[s], sc.roads[0], sem=1) for s in range(2)]
+    rp = rov_problem_from_models(ms, sc, n_paths=300, n_years=50, dim_res=8, sem=1,
+                                 n_processes=3, demand=True)
+    out = po.simulate_rov(rp, threads=4)
+    assert np.isfinite(out["cond_exp"]).all() and np.isfinite(out["stats"]).all()

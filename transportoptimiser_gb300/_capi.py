@@ -19,7 +19,7 @@ STATUS_NAMES = {
     7: "TO_ERR_NO_DEVICE",
 }
 SEM_REFERENCE, SEM_CORRECTED = 0, 1
-MIG_AUTO, MIG_SIMT_FP32, MIG_TC_3XTF32 = 0, 1, 2
+MIG_AUTO, MIG_SIMT_FP32, MIG_TC_3XTF32, MIG_SPARSE_FP32 = 0, 1, 2, 3
 
 c_int_p = C.POINTER(C.c_int)
 c_double_p = C.POINTER(C.c_double)

@@ -17,6 +17,7 @@
 #include "to_internal.cuh"
 #include "to_model.cuh"
 #include "to_pop.cuh"
+#include "to_sparse.cuh"
 
 struct to_gen_s {
     to_ctx ctx = nullptr;
@@ -44,6 +45,7 @@ struct to_gen_s {
     size_t end_cap = 0;
     double* d_stats;                     // [RS][5]
     double* d_results;                   // [RS][8]
+    to_csc csc;                          // [RS*C] packed migration matrices
 };
 
 namespace {
@@ -72,6 +74,25 @@ __global__ void k_max_int(int n, const int* __restrict__ v, int* out) {
         int r = 0;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = max(r, s[i]);
         *out = r;
+    }
+}
+
+// out[0] = min, out[1] = max of v[0..n)
+__global__ void k_min_max_int(int n, const int* __restrict__ v, int* out) {
+    int lo = 0x7fffffff, hi = -0x7fffffff;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { lo = min(lo, v[i]); hi = max(hi, v[i]); }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    __shared__ int s_lo[32], s_hi[32];
+    if ((threadIdx.x & 31) == 0) { s_lo[threadIdx.x >> 5] = lo; s_hi[threadIdx.x >> 5] = hi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) { lo = min(lo, s_lo[i]); hi = max(hi, s_hi[i]); }
+        lo = min(lo, s_lo[0]); hi = max(hi, s_hi[0]);
+        out[0] = lo;
+        out[1] = hi;
     }
 }
 
@@ -107,12 +128,24 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
     k_max_int<<<1, 1024, 0, ctx->stream>>>(RS, g->d_np, d_max);
     TO_LAUNCHED(ctx);
-    int maxN = 0;
-    TO_CUDA(ctx, cudaMemcpyAsync(&maxN, d_max, sizeof(int), cudaMemcpyDeviceToHost,
+    const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32);
+    if (try_sparse) {
+        TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
+        k_min_max_int<<<1, 1024, 0, ctx->stream>>>(RS * g->C, g->csc.nnz, d_max + 1);
+        TO_LAUNCHED(ctx);
+    }
+    int mm[3] = {0, 0, 0};
+    TO_CUDA(ctx, cudaMemcpyAsync(mm, d_max, 3 * sizeof(int), cudaMemcpyDeviceToHost,
                                  ctx->stream));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int maxN = mm[0];
     if (maxN <= 0) maxN = 4;
     int NE = (maxN + 3) & ~3;
+    g->csc.cap_smem = (mm[2] + 7) & ~7;
+    bool sparse = try_sparse && mm[1] >= 0 &&
+                  to_k::mte_sparse_smem(NE, g->csc.cap_smem) <= ctx->smem_optin;
+    if (try_sparse && !sparse && o->migration == TO_MIG_SPARSE_FP32)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
 
     const int P = o->mte_paths;
     if ((size_t)RS * P > g->end_cap) {
@@ -128,7 +161,9 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     m.npad = NP; m.npe = NE; m.n_patches = g->d_np; m.mmm = g->d_mmm;
     m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
     m.end_pops = g->d_end;
-    if (o->migration == TO_MIG_TC_3XTF32) {
+    if (sparse) {
+        TO_TRY(to_k::mte_sparse(ctx, m, RS, g->csc));
+    } else if (o->migration == TO_MIG_TC_3XTF32) {
         TO_TRY(to_k::mte_tc(ctx, m, RS));
     } else {
         TO_TRY(to_k::mte_simt(ctx, m, RS));
@@ -216,6 +251,8 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     acc(RS * NP * 4); acc(RS * NP * 4);
     acc(RS * 5 * 8);
     acc((RS * TO_RESULT_STRIDE + 64) * 8);
+    const size_t cap = (size_t)NP * 32;
+    acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
     if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
     g->buf_bytes = bytes;
     char* p = g->buf;
@@ -238,6 +275,12 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->d_cp = carve<float>(p, RS * NP);
     g->d_stats = carve<double>(p, RS * 5);
     g->d_results = carve<double>(p, RS * TO_RESULT_STRIDE + 64);
+    g->csc.ptr = carve<int>(p, RS * C * (NP + 1));
+    g->csc.idx = carve<uint16_t>(p, RS * C * cap);
+    g->csc.val = carve<float>(p, RS * C * cap);
+    g->csc.nnz = carve<int>(p, RS * C);
+    g->csc.cap = (int)cap;
+    g->csc.cap_smem = 0;
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
     *out = g;
     return TO_OK;

@@ -11,6 +11,7 @@
 #include "to_internal.cuh"
 #include "to_model.cuh"
 #include "to_pop.cuh"
+#include "to_sparse.cuh"
 
 to_status to_set_error(to_ctx ctx, to_status s, const char* fmt, ...) {
     if (ctx) {
@@ -475,9 +476,12 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
         }
         for (int q = 0; q < 8; ++q) prm[(size_t)s * 8 + q] = sp.params[q];
     }
+    const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
     size_t bytes = to_align256(mmm.size() * 4) + 2 * to_align256(ip.size() * 4) +
                    to_align256(prm.size() * 4) + to_align256((size_t)S * 4) +
-                   to_align256((size_t)S * P * 4) + to_align256((size_t)S * 5 * 8);
+                   to_align256((size_t)S * P * 4) + to_align256((size_t)S * 5 * 8) +
+                   to_align256((size_t)S * (NP + 1) * 4) + to_align256((size_t)S * cap * 2) +
+                   to_align256((size_t)S * cap * 4) + to_align256((size_t)S * 4);
     TO_TRY(to_arena_reserve(ctx, bytes));
     to_mte_args a;
     memset(&a, 0, sizeof(a));
@@ -488,6 +492,13 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
     int* d_np = to_arena_take<int>(ctx, S);
     float* d_end = to_arena_take<float>(ctx, (size_t)S * P);
     double* d_stats = to_arena_take<double>(ctx, (size_t)S * 5);
+    to_csc csc;
+    csc.ptr = to_arena_take<int>(ctx, (size_t)S * (NP + 1));
+    csc.idx = to_arena_take<uint16_t>(ctx, (size_t)S * cap);
+    csc.val = to_arena_take<float>(ctx, (size_t)S * cap);
+    csc.nnz = to_arena_take<int>(ctx, S);
+    csc.cap = cap;
+    csc.cap_smem = 0;
     TO_TRY(h2d(ctx, d_mmm, mmm.data(), mmm.size()));
     TO_TRY(h2d(ctx, d_ip, ip.data(), ip.size()));
     TO_TRY(h2d(ctx, d_cp, cp.data(), cp.size()));
@@ -497,7 +508,24 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
     a.dt = prob->dt; a.seed = prob->seed; a.sem = prob->sem; a.road0 = prob->road;
     a.npad = NP; a.npe = NP; a.n_patches = d_np; a.mmm = d_mmm; a.init_pops = d_ip;
     a.caps = d_cp; a.params = d_prm; a.end_pops = d_end;
-    if (prob->migration == TO_MIG_TC_3XTF32) {
+    bool sparse = false;
+    if (prob->migration == TO_MIG_AUTO || prob->migration == TO_MIG_SPARSE_FP32) {
+        TO_TRY(to_k::pack_csc(ctx, d_mmm, NP, 1, d_np, S, csc));
+        std::vector<int> nz(S);
+        TO_CUDA(ctx, cudaMemcpyAsync(nz.data(), csc.nnz, S * sizeof(int), cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+        TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int mx = 0;
+        bool ok = true;
+        for (int v : nz) { if (v < 0) ok = false; mx = v > mx ? v : mx; }
+        csc.cap_smem = (mx + 7) & ~7;
+        sparse = ok && to_k::mte_sparse_smem(NP, csc.cap_smem) <= ctx->smem_optin;
+        if (!sparse && prob->migration == TO_MIG_SPARSE_FP32)
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
+    }
+    if (sparse) {
+        TO_TRY(to_k::mte_sparse(ctx, a, S, csc));
+    } else if (prob->migration == TO_MIG_TC_3XTF32) {
         TO_TRY(to_k::mte_tc(ctx, a, S));
     } else {
         TO_TRY(to_k::mte_simt(ctx, a, S));

@@ -137,8 +137,8 @@ k_mte_simt(to_mte_args a) {
         if (path >= a.n_paths) continue;
         const float* src = (a.n_years == 0) ? pop + (size_t)q * NE
                          : (a.sem == 0 ? mig : pop) + (size_t)q * NE;
-        float e = 0.0f;
-        for (int k = 0; k < N; ++k) e += src[k];
+        float e = 0.0f;     // groups of four, ((v0 + v1) + v2) + v3, ascending
+        for (int g = 0; g < NE; g += 4) e = e + (((src[g] + src[g + 1]) + src[g + 2]) + src[g + 3]);
         a.end_pops[(size_t)rs * a.n_paths + path] = e;
     }
 }

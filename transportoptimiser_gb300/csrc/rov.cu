@@ -31,6 +31,7 @@
 #include "to_internal.cuh"
 #include "to_lsm_math.h"
 #include "to_rov.cuh"
+#include "to_sparse.cuh"
 
 namespace {
 
@@ -112,8 +113,9 @@ k_rov_forward(to_rov_args a) {
         __syncthreads();
         for (int q = tid; q < TP; q += blockDim.x) {
             gm[q] = sp[0];
-            float tt = 0.0f;
-            for (int k = 0; k < N; ++k) tt += pop[(size_t)q * NE + k];
+            const float* v = pop + (size_t)q * NE;
+            float tt = 0.0f;    // groups of four, ((v0 + v1) + v2) + v3, ascending
+            for (int g4 = 0; g4 < NE; g4 += 4) tt = tt + (((v[g4] + v[g4 + 1]) + v[g4 + 2]) + v[g4 + 3]);
             tot[q] = tt;
             int path = path0 + q;
             if (path < P) a.totalPops[((size_t)s * (Y + 1) + 0) * P + path] = tt;
@@ -190,8 +192,10 @@ k_rov_forward(to_rov_args a) {
                 }
                 __syncthreads();
                 for (int q = tid; q < TP; q += blockDim.x) {
+                    const float* v = mig + (size_t)q * NE;
                     float tc = 0.0f;
-                    for (int k = 0; k < N; ++k) tc += mig[(size_t)q * NE + k];
+                    for (int g4 = 0; g4 < NE; g4 += 4)
+                        tc = tc + (((v[g4] + v[g4 + 1]) + v[g4 + 2]) + v[g4 + 3]);
                     int path = path0 + q;
                     if (path < P)
                         a.aars[(((size_t)s * C + c) * Y + t) * P + path] = tc / tot[q];
@@ -220,18 +224,20 @@ k_rov_forward(to_rov_args a) {
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         float m = mv[j];
-                        float gr = g + z[j] * sp[7];
+                        float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
                         float cp = cap4[j];
                         npv[j] = (a.sem == 0) ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
-                                              : m * (1.0f + gr * (cp - m) / cp);
+                                              : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
                     }
                     *reinterpret_cast<float4*>(pop + (size_t)pl * NE + kg * 4) = np;
                 }
             }
             __syncthreads();
             for (int q = tid; q < TP; q += blockDim.x) {
+                const float* v = pop + (size_t)q * NE;
                 float tt = 0.0f;
-                for (int k = 0; k < N; ++k) tt += pop[(size_t)q * NE + k];
+                for (int g4 = 0; g4 < NE; g4 += 4)
+                    tt = tt + (((v[g4] + v[g4 + 1]) + v[g4 + 2]) + v[g4 + 3]);
                 tot[q] = tt;
                 int path = path0 + q;
                 if (path < P) a.totalPops[((size_t)s * (Y + 1) + t + 1) * P + path] = tt;
@@ -612,7 +618,9 @@ __global__ void k_rov_first(to_rov_args a) {
 
 namespace to_k {
 
-to_status rov_run(to_ctx ctx, to_rov_args a) {
+to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb);
+
+to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
     const int P = a.P;
     const int tpb = 128;
     const int pblocks = (P + tpb - 1) / tpb;
@@ -620,6 +628,10 @@ to_status rov_run(to_ctx ctx, to_rov_args a) {
     k_rov_exog<<<pblocks, tpb, 0, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
+    if (csc) {
+        TO_TRY(rov_forward_sparse(ctx, a, *csc));
+        return rov_backward(ctx, a, pblocks, tpb);
+    }
     // forward tile shape
     const int NE = a.ne, KG = NE / 4;
     int pgroups = 256 / KG;
@@ -652,6 +664,10 @@ to_status rov_run(to_ctx ctx, to_rov_args a) {
     }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
+    return rov_backward(ctx, a, pblocks, tpb);
+}
+
+to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb) {
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
     for (int t = a.Y - 2; t > 0; --t) {

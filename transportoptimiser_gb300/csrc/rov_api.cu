@@ -6,6 +6,7 @@
 
 #include "to_internal.cuh"
 #include "to_rov.cuh"
+#include "to_sparse.cuh"
 
 namespace {
 template <class T>
@@ -93,6 +94,9 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     acc((size_t)C * kmax * Q * 4); acc((size_t)C * kmax * Q * 4);
     acc((size_t)Y * C * blk * 4); acc((size_t)Y * P * 4); acc((size_t)Y * P * 4);
     acc((size_t)Y * P * 4); acc((size_t)Y * S * P * 4); acc(5 * 8);
+    const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
+    acc((size_t)S * C * (NP + 1) * 4); acc((size_t)S * C * cap * 2); acc((size_t)S * C * cap * 4);
+    acc((size_t)S * C * 4);
     TO_TRY(to_arena_reserve(ctx, bytes + 4096));
     TO_CUDA(ctx, cudaMemsetAsync(ctx->arena, 0, bytes, ctx->stream));
     to_rov_args a;
@@ -133,6 +137,13 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.unitProfits = to_arena_take<float>(ctx, (size_t)Y * P);
     a.adjPops = to_arena_take<float>(ctx, (size_t)Y * S * P);
     a.stats = to_arena_take<double>(ctx, 5);
+    to_csc csc;
+    csc.ptr = to_arena_take<int>(ctx, (size_t)S * C * (NP + 1));
+    csc.idx = to_arena_take<uint16_t>(ctx, (size_t)S * C * cap);
+    csc.val = to_arena_take<float>(ctx, (size_t)S * C * cap);
+    csc.nnz = to_arena_take<int>(ctx, (size_t)S * C);
+    csc.cap = cap;
+    csc.cap_smem = 0;
     if (!a.stats) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
     TO_TRY(up(ctx, d_mmm, mmm.data(), mmm.size()));
     TO_TRY(up(ctx, d_ip, ip.data(), ip.size()));
@@ -148,7 +159,22 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.n_patches = d_np; a.params = d_prm; a.init_pops = d_ip; a.caps = d_cp;
     a.mmm = d_mmm; a.flows = d_flows; a.uncert = d_unc; a.fuel_costs = d_fc;
     a.fuel_idx = d_fi; a.ore_content = d_oc; a.ore_sd = d_os;
-    TO_TRY(to_k::rov_run(ctx, a));
+    bool sparse = false;
+    if (pr->migration == TO_MIG_AUTO || pr->migration == TO_MIG_SPARSE_FP32) {
+        TO_TRY(to_k::pack_csc(ctx, d_mmm, NP, C, d_np, S, csc));
+        std::vector<int> nz((size_t)S * C);
+        TO_CUDA(ctx, cudaMemcpyAsync(nz.data(), csc.nnz, nz.size() * sizeof(int),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        int mx = 0;
+        bool ok = true;
+        for (int v : nz) { if (v < 0) ok = false; mx = v > mx ? v : mx; }
+        csc.cap_smem = (mx + 7) & ~7;
+        sparse = ok && to_k::rov_sparse_smem(NP, C, csc.cap_smem) <= ctx->smem_optin;
+        if (!sparse && pr->migration == TO_MIG_SPARSE_FP32)
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
+    }
+    TO_TRY(to_k::rov_run(ctx, a, sparse ? &csc : nullptr));
     double st[5];
     TO_TRY(down(ctx, st, a.stats, 5));
     std::vector<float> f;

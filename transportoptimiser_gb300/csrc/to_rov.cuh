@@ -70,8 +70,10 @@ __device__ __forceinline__ void to_rov_query(const to_rov_args& a, int q, float*
     }
 }
 
+struct to_csc;
 namespace to_k {
-to_status rov_run(to_ctx ctx, to_rov_args a);
+// csc: the packed migration matrices for the sparse forward pass, or null
+to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc);
 to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t);
 to_status regress_rov(to_ctx ctx, const to_rov_args& a, int t);
 // generic kNN: ref dim-major [dim][n], query dim-major [dim][Q]

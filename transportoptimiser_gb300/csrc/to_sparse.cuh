@@ -1,0 +1,25 @@
+// to_sparse.cuh - compressed-column migration matrices and the sparse
+// population kernels (sparse_pop.cu).
+#pragma once
+#include "to_internal.cuh"
+
+struct to_csc {
+    int* ptr;          // [matrices][NP + 1] column starts
+    uint16_t* idx;     // [matrices][cap] origin patch of each non-zero
+    float* val;        // [matrices][cap]
+    int* nnz;          // [matrices] non-zeros, -1 when above cap
+    int cap;           // capacity per matrix in global memory
+    int cap_smem;      // largest nnz of the launch (shared-memory lists)
+};
+
+struct to_mte_args;
+struct to_rov_args;
+
+namespace to_k {
+to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_patches,
+                   int n_rs, to_csc& csc);
+size_t mte_sparse_smem(int NE, int cap_smem);
+size_t rov_sparse_smem(int NE, int C, int cap_smem);
+to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc);
+to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc);
+}

@@ -63,7 +63,7 @@ class Generation:
         self.max_roads = max_roads
 
     def opts(self, mte_paths, n_years=50, dt=1.0, seed=0, road0=0, sem=0,
-             migration=_capi.MIG_SIMT_FP32):
+             migration=_capi.MIG_AUTO):
         return _capi.EvalOpts(mte_paths, n_years, dt, seed, road0, sem, migration)
 
     def evaluate(self, packed: dict, opts) -> np.ndarray:

@@ -131,7 +131,7 @@ def createSpeciesModel(hab_map, pop_map, W, H, res, habitats, road_colmajor, G, 
 
 
 def simulateMTECUDA(species_models, params, n_paths, n_years, dt=1.0, seed=0, road=0, sem=0,
-                    migration=_capi.MIG_SIMT_FP32, control=-1, ctx: Context | None = None):
+                    migration=_capi.MIG_AUTO, control=-1, ctx: Context | None = None):
     """SimulateGPU::simulateMTECUDA (SimulateGPU.cu:3650).
 
     species_models: list of dicts with N, init_pops, caps, mmm (C x N x N,
@@ -176,7 +176,7 @@ def expPV(gr, mean, time_step, rrr, current, reversion, jump_prob, noise_sd, jum
 
 
 def simulateROVCUDA(problem: dict, want=("cond_exp", "opt_cont", "unit_profits", "adj_pops",
-                                        "regression"), migration=_capi.MIG_SIMT_FP32,
+                                        "regression"), migration=_capi.MIG_AUTO,
                     ctx: Context | None = None) -> dict:
     """SimulateGPU::simulateROVCUDA, ALGO4 (SimulateGPU.cu:3870-5003).
 
