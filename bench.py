@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
                     help="one pilot + one step, for profiler launch lists")
+    ap.add_argument("--profile-rov", action="store_true",
+                    help="one ROV valuation of a configuration-1 road (2 species, ~115 "
+                         "patches, 3 controls, 16 bins per dimension), for profilers")
+    ap.add_argument("--rov-paths", type=int, default=10000)
     return ap.parse_args()
 
 
@@ -179,10 +183,32 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------
+def profile_rov(args):
+    """One ROV valuation (ALGO4) of a configuration-1 road on the GPU."""
+    from transportoptimiser_gb300 import synth
+    from transportoptimiser_gb300 import simulate_gpu as sg
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    sc = synth.rov_road(0, n_species=2)
+    models = []
+    for s in range(2):
+        sp = sc.species[s]
+        hab = sc.hab_map(sc.roads[0])
+        models.append(sg.createSpeciesModel(hab, sc.pop_map(sp, hab), sc.W, sc.H, sc.res,
+                                            sp.habitats, sc.roads[0].colmajor(), sc.roads[0].G,
+                                            sp.hazard, sp.lambda_mean, sem=1, max_patches=512))
+    rp = rov_problem_from_models(models, sc, n_paths=args.rov_paths, n_years=YEARS, dim_res=16,
+                                 sem=1, n_processes=3, demand=True)
+    out = sg.simulateROVCUDA(rp, want=())
+    print(json.dumps({"rov_value": out["stats"][0], "se": out["value_se"]}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_rov:
+        return profile_rov(args)
 
     import numpy as np
     import torch
@@ -301,9 +327,13 @@ def main():
                                seed=0, road=road0 + r, migration=MIG_AUTO, ctx=ctx)
         plain_value = args.plain_roads / (time.perf_counter() - t0)
 
-    # roofline of the dominant kernel (migration + growth, SIMT FP32)
+    # roofline of the migration kernel: useful FLOPs are 2 per stored
+    # non-zero per path-year (the dense-equivalent count is reported too)
     Nsum2 = float((Ns.astype(np.float64) ** 2).sum())
-    flops_per_launch = 2.0 * P * Nsum2 * YEARS
+    nnz = res[:, :, 7].astype(np.float64)
+    flops_per_launch = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() \
+        else 2.0 * P * Nsum2 * YEARS
+    dense_equiv_flops = 2.0 * P * Nsum2 * YEARS
     mte_avg_s = (mte_ms / max(mte_n, 1)) / 1000.0
     achieved_tf = flops_per_launch / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
@@ -325,16 +355,18 @@ def main():
             "config": {"workload": WORKLOAD, "roads": args.roads, "species": len(scene.species),
                        "paths_per_road": P, "pilot_paths": PILOT_PATHS, "years": YEARS,
                        "patches_min_max": [int(Ns.min()), int(Ns.max())],
-                       "migration": "simt_fp32", "l2": "flushed (256 MB write) between steps",
+                       "migration": "sparse_fp32 (CSC in shared memory)",
+                       "l2": "flushed (256 MB write) between steps",
                        "wall_s_timed": t_wall},
             "e2e": {"value": e2e_value, "unit": "designs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "plain": {"value": plain_value, "unit": "designs/s",
                       "roads": args.plain_roads, "note": "one road per call, host entry points"},
-            "roofline": {"kernel": "k_mte_simt", "bound": "tensor", "achieved": achieved_tf,
+            "roofline": {"kernel": "k_mte_sparse", "bound": "tensor", "achieved": achieved_tf,
                          "peak": bf16_peak, "unit": "TFLOP/s",
                          "frac": achieved_tf / bf16_peak, "peak_kind": peak_kind + " bf16 dense",
                          "traffic": None, "flops_per_launch": flops_per_launch,
+                         "dense_equivalent_flops": dense_equiv_flops,
                          "kernel_ms": mte_ms / max(mte_n, 1),
                          "species_model_ms": sm_ms / max(sm_n, 1)},
             "cpu_baseline": cpu,

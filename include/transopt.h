@@ -352,7 +352,8 @@ typedef struct {
 
 /* result block per (road, species), TO_RESULT_STRIDE doubles:
  *   0 n_patches, 1 n_transitions, 2 mte mean, 3 mte sd, 4 mte se,
- *   5 P(end < 0.2 init), 6 initial population, 7 reserved */
+ *   5 P(end < 0.2 init), 6 initial population, 7 non-zeros of the
+ *   highest-flow migration matrix (-1 when the dense form ran) */
 #define TO_RESULT_STRIDE 8
 
 to_status to_scene_create(to_ctx ctx, const to_scene* scene, to_gen* gen);

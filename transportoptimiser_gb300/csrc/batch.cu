@@ -53,6 +53,7 @@ namespace {
 __global__ void k_pack_results(int n_rs, const int* __restrict__ np,
                                const int* __restrict__ nt,
                                const double* __restrict__ stats,
+                               const int* __restrict__ nnz, int C,
                                double* __restrict__ out) {
     int rs = blockIdx.x * blockDim.x + threadIdx.x;
     if (rs >= n_rs) return;
@@ -60,7 +61,8 @@ __global__ void k_pack_results(int n_rs, const int* __restrict__ np,
     o[0] = np[rs];
     o[1] = nt[rs];
     for (int q = 0; q < 5; ++q) o[2 + q] = stats[5 * (size_t)rs + q];
-    o[7] = 0.0;
+    // non-zeros of the highest-flow migration matrix (-1: dense path used)
+    o[7] = nnz ? (double)nnz[(size_t)rs * C + C - 1] : -1.0;
 }
 
 __global__ void k_max_int(int n, const int* __restrict__ v, int* out) {
@@ -169,8 +171,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
         TO_TRY(to_k::mte_simt(ctx, m, RS));
     }
     TO_TRY(to_k::mte_stats(ctx, m, RS, g->d_stats));
-    k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(RS, g->d_np, g->d_nt,
-                                                             g->d_stats, d_results_out);
+    k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(
+        RS, g->d_np, g->d_nt, g->d_stats, sparse ? g->csc.nnz : nullptr, g->C, d_results_out);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }

@@ -5,14 +5,16 @@
 // insertion sort over it, a sqrt pass, with host copies around each call)
 // and multiLocLinReg (SimulateGPU.cu:2934-3053).
 //
-// Here a warp owns one query.  The reference points of the problem sit in
-// shared memory; the k-th smallest key (squared distance as float bits,
-// which order like the floats for non-negative values; ties broken by
-// point index) is found by a 4 x 8-bit radix select with warp-aggregated
-// shared-memory histograms, the k survivors are gathered in index order
-// and bitonic-sorted by (key, index).  That is exactly the set and order the
-// reference's stable insertion sort returns, and nothing of size P x Q is
-// written.  The regression kernel then runs one thread per query.
+// Here a warp owns a run of neighbouring grid queries.  The reference points
+// of the problem sit in shared memory.  For each query the warp gathers
+// every point within a squared-distance threshold in one ballot-compaction
+// pass (the threshold adapts until between k and 256 points qualify and is
+// carried to the next, neighbouring, query), then bitonic-sorts the
+// survivors by (squared distance, index): exactly the set and order the
+// reference's stable insertion sort returns.  When exact ties prevent the
+// window, a 4 x 8-bit radix select on the same keys takes over.  Nothing of
+// size P x Q is written; for the ROV the local linear regression runs in the
+// same warp right after the selection.
 #include "to_internal.cuh"
 #include "to_lsm_math.h"
 #include "to_rov.cuh"
@@ -24,6 +26,8 @@ constexpr int kWarps = 8;
 struct WarpScratch {
     unsigned hist[256];
     unsigned long long sel[TO_KNN_KMAX];
+    float gy[TO_KNN_KMAX];                    // neighbour responses
+    float gx[TO_KNN_KMAX * TO_LSM_MAXD];      // neighbour predictors
 };
 
 __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int dim,
@@ -132,16 +136,90 @@ __device__ void warp_select(const float* ref, int stride, int n, int dim,
     }
 }
 
-// ROV: grid (ceil(Q / kWarps), C).  Points of control c are xn[c][j][P].
+// Threshold form of the same selection.  All points with squared distance
+// <= T are gathered (ballot compaction, one pass); T is adapted until at
+// least k and at most TO_KNN_KMAX points qualify, then the survivors are
+// bitonic-sorted by (key, index).  Every point closer than the k-th is kept,
+// so the result equals warp_select's.  T is carried over from the previous
+// (neighbouring) query, so one pass usually suffices.  Returns false when
+// exact ties keep the count from entering the window (caller falls back to
+// warp_select).
+__device__ bool warp_select_threshold(const float* ref, int stride, int n, int dim,
+                                      const float* q, int k, float& T, WarpScratch& ws) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > cap
+    int cnt = 0;
+    for (int iter = 0; iter < 64; ++iter) {
+        cnt = 0;
+        for (int base = 0; base < n; base += 32) {
+            int i = base + lane;
+            float key = (i < n) ? sqdist(ref, stride, i, dim, q) : INFINITY;
+            bool le = (i < n) && key <= T;
+            unsigned m = __ballot_sync(0xffffffffu, le);
+            int pos = cnt + __popc(m & lt_mask);
+            if (le && pos < TO_KNN_KMAX)
+                ws.sel[pos] = ((unsigned long long)__float_as_uint(key) << 32) | (unsigned)i;
+            cnt += __popc(m);
+        }
+        if (cnt >= k && cnt <= TO_KNN_KMAX) break;
+        if (cnt < k) lo = T; else hi = T;
+        float nt;
+        if (lo < 0.0f) nt = T * 0.25f;
+        else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
+        else nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
+        if (!(nt > lo) || (hi >= 0.0f && !(nt < hi))) { cnt = -1; break; }
+        T = nt;
+    }
+    __syncwarp();
+    if (cnt < k || cnt > TO_KNN_KMAX) return false;
+    int kp = 1;
+    while (kp < cnt) kp <<= 1;
+    for (int i = cnt + lane; i < kp; i += 32) ws.sel[i] = ~0ull;
+    __syncwarp();
+    for (int size = 2; size <= kp; size <<= 1) {
+        for (int stride2 = size >> 1; stride2 > 0; stride2 >>= 1) {
+            for (int i = lane; i < kp; i += 32) {
+                int j = i ^ stride2;
+                if (j > i) {
+                    unsigned long long a = ws.sel[i], b = ws.sel[j];
+                    bool up = ((i & size) == 0);
+                    if ((a > b) == up) { ws.sel[i] = b; ws.sel[j] = a; }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    // next query starts from a threshold a little above this k-th distance
+    float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+    T = (kth > 0.0f) ? kth * 1.5f : 1e-30f;
+    return true;
+}
+
+// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / (kWarps*kRun)), C); a
+// warp handles kRun consecutive grid queries of control c, whose points
+// (xn[c][j][P]) sit in shared memory.  After the selection the warp gathers
+// the neighbours' responses and predictors, and lane 0 accumulates the
+// normal equations in neighbour order and solves them (to_lsm_math.h).
+constexpr int kRun = 4;
+
 __global__ void __launch_bounds__(kWarps * 32)
-k_knn_rov(to_rov_args a, int smem_points) {
+k_knn_rov(to_rov_args a, int t, int smem_points) {
     extern __shared__ unsigned char sm_raw[];
     WarpScratch* wsa = reinterpret_cast<WarpScratch*>(sm_raw);
     float* sref = reinterpret_cast<float*>(sm_raw + sizeof(WarpScratch) * kWarps);
     const int c = blockIdx.y;
-    const int d = a.S + 1;
+    const int d = a.S + 1, R = a.R;
     const int n = a.npts[c], k = a.kc[c];
-    if (n < 3 || k <= 0) return;
+    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * d;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q0 = (blockIdx.x * kWarps + warp) * kRun;
+    if (n < 3 || k <= 0) {
+        for (int r = lane; r < kRun; r += 32)
+            if (q0 + r < a.Q) yout[q0 + r] = 0.0f;
+        return;
+    }
     const float* src = a.xn + (size_t)c * d * a.P;
     const float* ref = src;
     int stride = a.P;
@@ -154,19 +232,50 @@ k_knn_rov(to_rov_args a, int smem_points) {
         ref = sref;
         stride = n;
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int qi = blockIdx.x * kWarps + warp;
-    if (qi >= a.Q) return;
-    float qn[TO_LSM_MAXD], xq[TO_LSM_MAXD];
-    to_rov_query(a, qi, qn, xq);
     WarpScratch& ws = wsa[warp];
-    warp_select(ref, stride, n, d, qn, k, ws);
-    float* dist = a.dist + (size_t)c * a.kmax * a.Q;
-    int* ind = a.ind + (size_t)c * a.kmax * a.Q;
-    for (int kk = lane; kk < k; kk += 32) {
-        unsigned long long v = ws.sel[kk];
-        dist[(size_t)kk * a.Q + qi] = sqrtf(__uint_as_float((unsigned)(v >> 32)));
-        ind[(size_t)kk * a.Q + qi] = (int)(v & 0xFFFFFFFFu) + 1;
+    const float* y = a.yv + (size_t)c * a.P;
+    const float* xr = a.xraw + (size_t)c * d * a.P;
+    float T = powf((float)k / (float)n, 2.0f / (float)d);
+    for (int r = 0; r < kRun; ++r) {
+        const int qi = q0 + r;
+        if (qi >= a.Q) break;
+        float qn[TO_LSM_MAXD], xq[TO_LSM_MAXD];
+        to_rov_query(a, qi, qn, xq);
+        if (!warp_select_threshold(ref, stride, n, d, qn, k, T, ws)) {
+            warp_select(ref, stride, n, d, qn, k, ws);
+            T = powf((float)k / (float)n, 2.0f / (float)d);
+        }
+        // gather the neighbours' responses and predictors
+        for (int kk = lane; kk < k; kk += 32) {
+            int i = (int)(ws.sel[kk] & 0xFFFFFFFFu);
+            ws.gy[kk] = y[i];
+            for (int j = 0; j < d; ++j) {
+                float xv;
+                if (a.sem == 0) {
+                    // the reference reads its dim-major buffer (stride n)
+                    // point-major (multiLocLinReg, SimulateGPU.cu:3002)
+                    int f = i * d + j;
+                    int jj = f / n, m = f - jj * n;
+                    xv = xr[(size_t)jj * a.P + m];
+                } else {
+                    xv = ref[(size_t)j * stride + i];
+                }
+                ws.gx[kk * TO_LSM_MAXD + j] = xv;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) {
+            float acc[TO_LSM_ACC];
+            to_lsm_acc_init(d, acc);
+            const float h = sqrtf(__uint_as_float((unsigned)(ws.sel[k - 1] >> 32)));
+            for (int kk = 0; kk < k; ++kk) {
+                float dd = sqrtf(__uint_as_float((unsigned)(ws.sel[kk] >> 32)));
+                to_lsm_acc_add(d, acc, to_lsm_weight(dd, h), ws.gy[kk],
+                               &ws.gx[kk * TO_LSM_MAXD], xq);
+            }
+            yout[qi] = to_lsm_solve_intercept(d, acc);
+        }
+        __syncwarp();
     }
 }
 
@@ -189,51 +298,13 @@ k_knn_generic(const float* ref_g, int n, const float* query, int Q, int dim, int
     float q[TO_LSM_MAXD + 3];
     for (int j = 0; j < dim; ++j) q[j] = query[(size_t)j * Q + qi];
     WarpScratch& ws = wsa[warp];
-    warp_select(ref, n, n, dim, q, k, ws);
+    float T = powf((float)k / (float)n, 2.0f / (float)dim);
+    if (!warp_select_threshold(ref, n, n, dim, q, k, T, ws)) warp_select(ref, n, n, dim, q, k, ws);
     for (int kk = lane; kk < k; kk += 32) {
         unsigned long long v = ws.sel[kk];
         dist[(size_t)kk * Q + qi] = sqrtf(__uint_as_float((unsigned)(v >> 32)));
         ind[(size_t)kk * Q + qi] = (int)(v & 0xFFFFFFFFu) + 1;
     }
-}
-
-// multiLocLinReg for the ROV grid: thread per (query, control)
-__global__ void k_regress_rov(to_rov_args a, int t) {
-    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
-    const int c = blockIdx.y;
-    if (qi >= a.Q) return;
-    const int d = a.S + 1, R = a.R;
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
-    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * d;
-    const int n = a.npts[c], k = a.kc[c];
-    if (n < 3 || k <= 0) { yout[qi] = 0.0f; return; }
-    float qn[TO_LSM_MAXD], xq[TO_LSM_MAXD];
-    to_rov_query(a, qi, qn, xq);
-    const float* dist = a.dist + (size_t)c * a.kmax * a.Q;
-    const int* ind = a.ind + (size_t)c * a.kmax * a.Q;
-    const float* y = a.yv + (size_t)c * a.P;
-    const float* xr = a.xraw + (size_t)c * d * a.P;
-    const float* xnn = a.xn + (size_t)c * d * a.P;
-    float acc[TO_LSM_ACC];
-    to_lsm_acc_init(d, acc);
-    const float h = dist[(size_t)(k - 1) * a.Q + qi];
-    for (int kk = 0; kk < k; ++kk) {
-        float dd = dist[(size_t)kk * a.Q + qi];
-        int i = ind[(size_t)kk * a.Q + qi] - 1;
-        float xv[TO_LSM_MAXD];
-        if (a.sem == 0) {
-            // the reference reads its dim-major buffer (stride n) point-major
-            for (int j = 0; j < d; ++j) {
-                int f = i * d + j;
-                int jj = f / n, m = f - jj * n;
-                xv[j] = xr[(size_t)jj * a.P + m];
-            }
-        } else {
-            for (int j = 0; j < d; ++j) xv[j] = xnn[(size_t)j * a.P + i];
-        }
-        to_lsm_acc_add(d, acc, to_lsm_weight(dd, h), y[i], xv, xq);
-    }
-    yout[qi] = to_lsm_solve_intercept(d, acc);
 }
 
 size_t knn_smem(int dim, int points) {
@@ -245,7 +316,6 @@ size_t knn_smem(int dim, int points) {
 namespace to_k {
 
 to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
-    (void)t;
     const int d = a.S + 1;
     if (a.kmax > TO_KNN_KMAX)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d exceeds %d", a.kmax, TO_KNN_KMAX);
@@ -255,18 +325,9 @@ to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     size_t smem = knn_smem(d, pts);
     TO_CUDA(ctx, cudaFuncSetAttribute(k_knn_rov, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-    dim3 grid((a.Q + kWarps - 1) / kWarps, a.C);
+    dim3 grid((a.Q + kWarps * kRun - 1) / (kWarps * kRun), a.C);
     to_prof_begin(ctx, "knn");
-    k_knn_rov<<<grid, kWarps * 32, smem, ctx->stream>>>(a, pts);
-    to_prof_end(ctx);
-    TO_LAUNCHED(ctx);
-    return TO_OK;
-}
-
-to_status regress_rov(to_ctx ctx, const to_rov_args& a, int t) {
-    dim3 grid((a.Q + 127) / 128, a.C);
-    to_prof_begin(ctx, "regress");
-    k_regress_rov<<<grid, 128, 0, ctx->stream>>>(a, t);
+    k_knn_rov<<<grid, kWarps * 32, smem, ctx->stream>>>(a, t, pts);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;

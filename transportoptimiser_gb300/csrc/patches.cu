@@ -306,6 +306,14 @@ __global__ void k_line_segment_intersect(int T, const double* __restrict__ xy1,
     }
 }
 
+// sqrt(d2) <= md, decided on d2 with an exact sqrt only within 1e-9 of the
+// cut-off (identical to the reference's test on the distance itself)
+__device__ __forceinline__ bool within(double d2, double md, double md2lo, double md2hi) {
+    if (d2 < md2lo) return true;
+    if (d2 > md2hi) return false;
+    return sqrt(d2) <= md;
+}
+
 // One CTA per (road, species): the whole species-road model.
 __global__ void __launch_bounds__(1024)
 k_species_model(to_model_args a) {
@@ -372,6 +380,8 @@ k_species_model(to_model_args a) {
     // Distances and the crossing pair filter (SpeciesRoadPatches.cpp:270-381)
     const double lam = S.lambda_mean + S.lambda_sd * S.lambda_mult;
     const double max_dist_x = log(0.05) / (-lam);
+    const double mx2lo = max_dist_x * max_dist_x * (1.0 - 1e-9);
+    const double mx2hi = max_dist_x * max_dist_x * (1.0 + 1e-9);
     int* cross = a.crossings_scratch + (size_t)rs * NM * NM;
     if (threadIdx.x == 0) s_misc[2] = 0;
     __syncthreads();
@@ -383,7 +393,7 @@ k_species_model(to_model_args a) {
             int i = q / N, j = q - i * N;
             if (j <= i) continue;
             double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            if (sqrt(dx * dx + dy * dy) <= max_dist_x) { last = max(last, q); ++cnt; }
+            if (within(dx * dx + dy * dy, max_dist_x, mx2lo, mx2hi)) { last = max(last, q); ++cnt; }
         }
         for (int o = 16; o > 0; o >>= 1) {
             last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
@@ -405,7 +415,7 @@ k_species_model(to_model_args a) {
         int c = 0;
         if (i != j) {
             double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            bool valid = sqrt(dx * dx + dy * dy) <= max_dist_x;
+            bool valid = within(dx * dx + dy * dy, max_dist_x, mx2lo, mx2hi);
             if (q == last_pair) valid = false;
             if (valid) {
                 float x1 = (float)cx[i], y1 = (float)cy[i];
@@ -440,6 +450,8 @@ k_species_model(to_model_args a) {
     const double max_dist_t = (a.sem == 0)
         ? log(0.05) / (-(S.lambda_mean + S.lambda_sd * lda))
         : log(0.05) / (-lda);
+    const double mt2lo = max_dist_t * max_dist_t * (1.0 - 1e-9);
+    const double mt2hi = max_dist_t * max_dist_t * (1.0 + 1e-9);
     const int NP = a.npad;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
     double* tv = a.trans_scratch + (size_t)rs * NM * NM;
@@ -449,12 +461,15 @@ k_species_model(to_model_args a) {
         double summ = 0.0;
         for (int j = 0; j < N; ++j) {
             double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            double d = sqrt(dx * dx + dy * dy);
+            double d2 = dx * dx + dy * dy;
             double v = 0.0;
-            if (d <= max_dist_t) {
+            if (within(d2, max_dist_t, mt2lo, mt2hi)) {
                 double w = area[j] * lda * s_attr[ptype[j]];
-                v = (i == j) ? w
-                  : (a.sem == 0 ? w / exp(-lda * d) : w * exp(-lda * d));
+                if (i == j) v = w;
+                else {
+                    double d = sqrt(d2);
+                    v = (a.sem == 0) ? w / exp(-lda * d) : w * exp(-lda * d);
+                }
                 summ += v;
             }
             tv[(size_t)i * NM + j] = v;

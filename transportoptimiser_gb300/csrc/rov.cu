@@ -675,8 +675,7 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb) {
         k_lsm_prepare<<<1, 1024, 0, ctx->stream>>>(a, t);
         to_prof_end(ctx);
         TO_LAUNCHED(ctx);
-        TO_TRY(knn_rov(ctx, a, t));
-        TO_TRY(regress_rov(ctx, a, t));
+        TO_TRY(knn_rov(ctx, a, t));      // kNN and the local linear regressions
         to_prof_begin(ctx, "rov_backward");
         k_rov_backward<<<pblocks, tpb, 0, ctx->stream>>>(a, t);
         to_prof_end(ctx);

@@ -74,9 +74,14 @@ __device__ __forceinline__ float grouped4(float a, float b, float c, float d) {
 }
 
 // ---------------------------------------------------------------------------
-// MTE (mteKernel :595-717) - grid (ceil(P/32), RS)
+// MTE (mteKernel :595-717) - grid (ceil(P/32), RS).  Warp w owns groups
+// w, w+W, ... (at most MAXG); the next year's populations wait in registers
+// until every warp has read this year's, so one shared buffer suffices.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
+constexpr int kMaxG = 4;
+
+template <int MAXG>
+__global__ void __launch_bounds__(1024, 1)
 k_mte_sparse(to_mte_args a, to_csc csc) {
     extern __shared__ unsigned char sm_raw[];
     const int NE = a.npe, NG = NE >> 2, NP = a.npad;
@@ -86,13 +91,12 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     const int mtx = rs * a.C + a.c_use;
     const int nnz = csc.nnz[mtx];
     float* cur = reinterpret_cast<float*>(sm_raw);             // [NE][32]
-    float* nxt = cur + (size_t)NE * kLanes;                    // [NE][32]
-    float* part = nxt + (size_t)NE * kLanes;                   // [NG][32]
+    float* part = cur + (size_t)NE * kLanes;                   // [NG][32]
     float* capv = part + (size_t)NG * kLanes;                  // [NE]
     float* gm = capv + NE;                                     // [32]
     int* cptr = reinterpret_cast<int*>(gm + kLanes);           // [NE+1]
-    float* cval = reinterpret_cast<float*>(cptr + NE + 1);     // [nnz]
-    uint16_t* cidx = reinterpret_cast<uint16_t*>(cval + csc.cap_smem);   // [nnz]
+    float* cval = reinterpret_cast<float*>(cptr + NE + 1);     // [cap_smem]
+    uint16_t* cidx = reinterpret_cast<uint16_t*>(cval + csc.cap_smem);   // [cap_smem]
 
     const int N = a.n_patches[rs];
     const int N4 = (N + 3) & ~3;
@@ -133,7 +137,11 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
         __syncthreads();
         const float g = gm[lane];
         const bool last = (t == a.n_years - 1);
-        for (int grp = warp; grp < NG; grp += W) {
+        float nv[MAXG][4];
+#pragma unroll
+        for (int gi = 0; gi < MAXG; ++gi) {
+            const int grp = warp + gi * W;
+            if (grp < NG) {
             float z[4];
             to_normal4(a.seed, TO_STREAM_GROWTH, road_id, path, t,
                        (uint32_t)((sp * N4) >> 2) + grp, z);
@@ -147,13 +155,22 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
                 m4[j] = acc;
                 float gr = fmaf(p7 * z[j], g, g);
                 float c = capv[k];
-                nxt[k * kLanes + lane] = acc * (1.0f + gr * (c - acc) / c);
+                nv[gi][j] = acc * (1.0f + gr * (c - acc) / c);
             }
             if (last) part[grp * kLanes + lane] = grouped4(m4[0], m4[1], m4[2], m4[3]);
+            }
         }
         __syncthreads();
-        float* tmp = cur; cur = nxt; nxt = tmp;
+#pragma unroll
+        for (int gi = 0; gi < MAXG; ++gi) {
+            const int grp = warp + gi * W;
+            if (grp < NG) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
+            }
+        }
     }
+    __syncthreads();
     if (warp == 0 && path < a.n_paths) {
         float e = 0.0f;
         if (a.n_years > 0 && a.sem == 0) {
@@ -171,16 +188,15 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 // ---------------------------------------------------------------------------
 // ROV forward paths (forwardPathKernel :789-956) - grid ceil(P/32)
 // ---------------------------------------------------------------------------
-template <int CMAX>
-__global__ void __launch_bounds__(256)
+template <int CMAX, int MAXG>
+__global__ void __launch_bounds__(1024, 1)
 k_rov_forward_sparse(to_rov_args a, to_csc csc) {
     extern __shared__ unsigned char sm_raw[];
     const int NE = a.ne, NG = NE >> 2, NP = a.np, C = a.C, Y = a.Y, P = a.P;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int path = blockIdx.x * kLanes + lane;
     float* cur = reinterpret_cast<float*>(sm_raw);                 // [NE][32]
-    float* nxt = cur + (size_t)NE * kLanes;                        // [NE][32]
-    float* part = nxt + (size_t)NE * kLanes;                       // [C+1][NG][32]
+    float* part = cur + (size_t)NE * kLanes;                       // [C+1][NG][32]
     float* capv = part + (size_t)(C + 1) * NG * kLanes;            // [NE]
     float* gm = capv + NE;                                         // [32]
     float* tot = gm + kLanes;                                      // [32]
@@ -242,7 +258,11 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
             __syncthreads();
             const float g = gm[lane];
             const int my_c = ctl[lane];
-            for (int grp = warp; grp < NG; grp += W) {
+            float nv[MAXG][4];
+#pragma unroll
+            for (int gi = 0; gi < MAXG; ++gi) {
+                const int grp = warp + gi * W;
+                if (grp < NG) {
                 float z[4];
                 to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
                            (uint32_t)((s * N4) >> 2) + grp, z);
@@ -268,7 +288,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                     float cpk = capv[k];
                     float v = (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
                                            : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
-                    nxt[k * kLanes + lane] = v;
+                    nv[gi][j] = v;
                     np4[j] = v;
                 }
 #pragma unroll
@@ -279,6 +299,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 }
                 part[((size_t)C * NG + grp) * kLanes + lane] =
                     grouped4(np4[0], np4[1], np4[2], np4[3]);
+                }
             }
             __syncthreads();
             // totals: warp c sums control c's AAR numerator, warp C the new
@@ -293,9 +314,17 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 }
                 if (c == C) ntot[lane] = tt;
             }
+            if (warp == 0) tot[lane] = 0.0f;   // replaced below, after the barrier
             __syncthreads();
             if (warp == 0) tot[lane] = ntot[lane];
-            float* tmp = cur; cur = nxt; nxt = tmp;
+#pragma unroll
+            for (int gi = 0; gi < MAXG; ++gi) {
+                const int grp = warp + gi * W;
+                if (grp < NG) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
+                }
+            }
             __syncthreads();
         }
     }
@@ -315,9 +344,20 @@ to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_pat
 }
 
 size_t mte_sparse_smem(int NE, int cap_smem) {
+    if (NE > 32 * kMaxG * 4) return ~size_t(0);
     int NG = NE / 4;
-    return (size_t)(2 * NE * kLanes + NG * kLanes + NE + kLanes) * 4 + (size_t)(NE + 1) * 4 +
+    return (size_t)(NE * kLanes + NG * kLanes + NE + kLanes) * 4 + (size_t)(NE + 1) * 4 +
            (size_t)cap_smem * 4 + (size_t)cap_smem * 2 + 16;
+}
+
+// warps per CTA: enough that no warp owns more than kMaxG groups of four
+// (32 warps at most, so NE <= 512 for the sparse kernels)
+static int warps_for(int NE, int min_warps) {
+    int NG = NE / 4;
+    int w = (NG + kMaxG - 1) / kMaxG;
+    if (w < min_warps) w = min_warps;
+    if (w > 32) w = 32;
+    return w;
 }
 
 to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
@@ -326,21 +366,23 @@ to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
     size_t smem = mte_sparse_smem(NE, csc.cap_smem);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "sparse MTE needs %zu B", smem);
-    TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-    int groups = NE / 4;
-    int warps = groups < 8 ? (groups > 0 ? groups : 1) : 8;
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int warps = warps_for(NE, 4);
+    if ((NE / 4 + warps - 1) / warps > kMaxG)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NE);
     dim3 grid((a.n_paths + kLanes - 1) / kLanes, n_rs);
     to_prof_begin(ctx, "mte_sparse");
-    k_mte_sparse<<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
+    k_mte_sparse<kMaxG><<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }
 
 size_t rov_sparse_smem(int NE, int C, int cap_smem) {
+    if (NE > 32 * kMaxG * 4 || C + 1 > 32) return ~size_t(0);
     int NG = NE / 4;
-    return (size_t)(2 * NE * kLanes + (C + 1) * NG * kLanes + NE + 4 * kLanes) * 4 +
+    return (size_t)(NE * kLanes + (C + 1) * NG * kLanes + NE + 4 * kLanes) * 4 +
            (size_t)C * (NE + 1) * 4 + (size_t)C * cap_smem * 6 + 16;
 }
 
@@ -348,19 +390,19 @@ to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc) {
     size_t smem = rov_sparse_smem(a.ne, a.C, csc.cap_smem);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "sparse ROV needs %zu B", smem);
-    int groups = a.ne / 4;
-    int warps = groups < 8 ? (groups > a.C + 1 ? groups : a.C + 1) : 8;
-    if (warps > 8) warps = 8;
+    int warps = warps_for(a.ne, a.C + 1 > 4 ? a.C + 1 : 4);
+    if ((a.ne / 4 + warps - 1) / warps > kMaxG)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", a.ne);
     const int blocks = (a.P + kLanes - 1) / kLanes;
     to_prof_begin(ctx, "rov_forward_sparse");
     if (a.C <= 3) {
-        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_sparse<3>,
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_sparse<3, kMaxG>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_rov_forward_sparse<3><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
+        k_rov_forward_sparse<3, kMaxG><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
     } else {
-        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_sparse<TO_ROV_MAXC>,
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_sparse<TO_ROV_MAXC, kMaxG>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_rov_forward_sparse<TO_ROV_MAXC><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
+        k_rov_forward_sparse<TO_ROV_MAXC, kMaxG><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
     }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);

@@ -75,7 +75,6 @@ namespace to_k {
 // csc: the packed migration matrices for the sparse forward pass, or null
 to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc);
 to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t);
-to_status regress_rov(to_ctx ctx, const to_rov_args& a, int t);
 // generic kNN: ref dim-major [dim][n], query dim-major [dim][Q]
 to_status knn(to_ctx ctx, const float* ref, int n, const float* query, int Q,
               int dim, int k, float* dist, int* ind);
