@@ -81,12 +81,18 @@ void or_knn(const float* ref, int n, const float* query, int Q, int dim, int k,
 /* ------------------------------------------------------------------------ */
 /* multiLocLinReg at one query (SimulateGPU.cu:2942-3052).                   */
 /* xraw(i, j): x of neighbour i in dimension j as the kernel reads it.       */
+/* lanes = 1: neighbours summed in order (surrogate builders).  lanes = 32:  */
+/* neighbour kk goes to partial sum kk % 32, and the 32 partial sums are     */
+/* combined by the butterfly s[l] = s[l] + s[l ^ o], o = 16, 8, 4, 2, 1,     */
+/* which is the order the device's warp shuffle reduction adds them in.     */
 /* ------------------------------------------------------------------------ */
 static float local_linear(int dim, int k, int Q, int qi, const float* dist,
                           const int* ind, const float* y, const float* xbuf,
-                          int n, int pointmajor, const float* xq) {
-    float acc[TO_LSM_MAXD + 1 + (TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
-    to_lsm_acc_init(dim, acc);
+                          int n, int pointmajor, const float* xq, int lanes) {
+    enum { ACC = TO_LSM_MAXD + 1 + (TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1) };
+    float acc[32][ACC], tmp[32][ACC];
+    const int na = (dim + 1) + (dim + 1) * (dim + 1);
+    for (int l = 0; l < lanes; ++l) to_lsm_acc_init(dim, acc[l]);
     float h = dist[(size_t)(k - 1) * Q + qi];
     for (int kk = 0; kk < k; ++kk) {
         float d = dist[(size_t)kk * Q + qi];
@@ -94,9 +100,14 @@ static float local_linear(int dim, int k, int Q, int qi, const float* dist,
         float xv[TO_LSM_MAXD];
         for (int j = 0; j < dim; ++j)
             xv[j] = pointmajor ? xbuf[(size_t)i * dim + j] : xbuf[(size_t)j * n + i];
-        to_lsm_acc_add(dim, acc, to_lsm_weight(d, h), y[i], xv, xq);
+        to_lsm_acc_add(dim, acc[kk % lanes], to_lsm_weight(d, h), y[i], xv, xq);
     }
-    return to_lsm_solve_intercept(dim, acc);
+    for (int o = lanes / 2; o > 0; o >>= 1) {
+        for (int l = 0; l < lanes; ++l)
+            for (int e = 0; e < na; ++e) tmp[l][e] = acc[l][e] + acc[l ^ o][e];
+        memcpy(acc, tmp, sizeof(float) * ACC * (size_t)lanes);
+    }
+    return to_lsm_solve_intercept(dim, acc[0]);
 }
 
 /* k rule of the ALGO4 loop (SimulateGPU.cu:4542-4545); 0 when n <= 3, and
@@ -406,8 +417,8 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
             for (int q = 0; q < Q; ++q) {
                 for (int j = 0; j < d; ++j) xq[j] = xqg[(size_t)j * Q + q];
                 yout[q] = (pr->sem == 0)
-                    ? local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xr, n, 1, xq)
-                    : local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xn, n, 0, xq);
+                    ? local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xr, n, 1, xq, 32)
+                    : local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xn, n, 0, xq, 32);
             }
             free(xr);
         }
@@ -574,7 +585,7 @@ void or_build_surrogate_1d(int n, const float* x, const float* y, int R, float* 
         or_knn(x, n, q, R, 1, k, dist, ind);
         for (int i = 0; i < R; ++i) {
             float xq[1] = {q[i]};
-            out[R + i] = local_linear(1, k, R, i, dist, ind, y, x, n, 1, xq);
+            out[R + i] = local_linear(1, k, R, i, dist, ind, y, x, n, 1, xq, 1);
         }
     }
     free(q); free(dist); free(ind);
@@ -626,8 +637,8 @@ void or_build_surrogate_nd(int n, int d, const float* pred, const float* y, int 
         float xq[TO_LSM_MAXD];
         for (int q = 0; q < Q; ++q) {
             for (int j = 0; j < d; ++j) xq[j] = xq_all[(size_t)j * Q + q];
-            float v = (sem == 0) ? local_linear(d, k, Q, q, dist, ind, y, pred, n, 1, xq)
-                                 : local_linear(d, k, Q, q, dist, ind, y, pn, n, 0, xq);
+            float v = (sem == 0) ? local_linear(d, k, Q, q, dist, ind, y, pred, n, 1, xq, 1)
+                                 : local_linear(d, k, Q, q, dist, ind, y, pn, n, 0, xq, 1);
             if (clip && v > 0.0f) v = 0.0f;
             yout[q] = v;
         }

@@ -5,16 +5,23 @@
 // insertion sort over it, a sqrt pass, with host copies around each call)
 // and multiLocLinReg (SimulateGPU.cu:2934-3053).
 //
-// Here a warp owns a run of neighbouring grid queries.  The reference points
-// of the problem sit in shared memory.  For each query the warp gathers
-// every point within a squared-distance threshold in one ballot-compaction
-// pass (the threshold adapts until between k and 256 points qualify and is
-// carried to the next, neighbouring, query), then bitonic-sorts the
-// survivors by (squared distance, index): exactly the set and order the
-// reference's stable insertion sort returns.  When exact ties prevent the
-// window, a 4 x 8-bit radix select on the same keys takes over.  Nothing of
-// size P x Q is written; for the ROV the local linear regression runs in the
-// same warp right after the selection.
+// A warp owns a run of neighbouring grid queries.  For each query it
+// gathers every point within a squared-distance threshold T by ballot
+// compaction; T adapts until between k and 256 points qualify (and is
+// carried to the next, neighbouring, query).  The survivors are
+// bitonic-sorted by (squared distance, index): exactly the set and order the
+// reference's stable insertion sort returns.  When exact ties keep the count
+// out of that window, a 4 x 8-bit radix select on the same keys takes over.
+//
+// For the ROV the points of each control are first binned into a uniform
+// cell grid (k_knn_grid, a counting sort), so a threshold pass visits only
+// the cells a ball of radius sqrt(T) can touch - cell rows of dimension 0
+// are contiguous in the sorted order - instead of all n points.  The ranges
+// are widened by a small tolerance, so no point with key <= T is missed.
+// The local linear regression runs in the same warp right after the
+// selection: lane l accumulates neighbours l, l+32, ... and the partial
+// normal equations are summed by an xor butterfly (the oracle does the same).
+// Nothing of size P x Q is written.
 #include "to_internal.cuh"
 #include "to_lsm_math.h"
 #include "to_rov.cuh"
@@ -22,12 +29,11 @@
 namespace {
 
 constexpr int kWarps = 8;
+constexpr unsigned kFull = 0xffffffffu;
 
 struct WarpScratch {
     unsigned hist[256];
     unsigned long long sel[TO_KNN_KMAX];
-    float gy[TO_KNN_KMAX];                    // neighbour responses
-    float gx[TO_KNN_KMAX * TO_LSM_MAXD];      // neighbour predictors
 };
 
 __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int dim,
@@ -136,43 +142,9 @@ __device__ void warp_select(const float* ref, int stride, int n, int dim,
     }
 }
 
-// Threshold form of the same selection.  All points with squared distance
-// <= T are gathered (ballot compaction, one pass); T is adapted until at
-// least k and at most TO_KNN_KMAX points qualify, then the survivors are
-// bitonic-sorted by (key, index).  Every point closer than the k-th is kept,
-// so the result equals warp_select's.  T is carried over from the previous
-// (neighbouring) query, so one pass usually suffices.  Returns false when
-// exact ties keep the count from entering the window (caller falls back to
-// warp_select).
-__device__ bool warp_select_threshold(const float* ref, int stride, int n, int dim,
-                                      const float* q, int k, float& T, WarpScratch& ws) {
+// bitonic sort of ws.sel[0..cnt), padded to a power of two
+__device__ void warp_sort_sel(WarpScratch& ws, int cnt) {
     const int lane = threadIdx.x & 31;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > cap
-    int cnt = 0;
-    for (int iter = 0; iter < 64; ++iter) {
-        cnt = 0;
-        for (int base = 0; base < n; base += 32) {
-            int i = base + lane;
-            float key = (i < n) ? sqdist(ref, stride, i, dim, q) : INFINITY;
-            bool le = (i < n) && key <= T;
-            unsigned m = __ballot_sync(0xffffffffu, le);
-            int pos = cnt + __popc(m & lt_mask);
-            if (le && pos < TO_KNN_KMAX)
-                ws.sel[pos] = ((unsigned long long)__float_as_uint(key) << 32) | (unsigned)i;
-            cnt += __popc(m);
-        }
-        if (cnt >= k && cnt <= TO_KNN_KMAX) break;
-        if (cnt < k) lo = T; else hi = T;
-        float nt;
-        if (lo < 0.0f) nt = T * 0.25f;
-        else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
-        else nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
-        if (!(nt > lo) || (hi >= 0.0f && !(nt < hi))) { cnt = -1; break; }
-        T = nt;
-    }
-    __syncwarp();
-    if (cnt < k || cnt > TO_KNN_KMAX) return false;
     int kp = 1;
     while (kp < cnt) kp <<= 1;
     for (int i = cnt + lane; i < kp; i += 32) ws.sel[i] = ~0ull;
@@ -190,29 +162,275 @@ __device__ bool warp_select_threshold(const float* ref, int stride, int n, int d
             __syncwarp();
         }
     }
+}
+
+__device__ __forceinline__ unsigned long long pack_sel(float key, int i) {
+    return ((unsigned long long)__float_as_uint(key) << 32) | (unsigned)i;
+}
+
+// Threshold form of the selection.  pass(T) gathers into ws.sel every point
+// whose key is <= T (entries past TO_KNN_KMAX dropped) and returns how many
+// qualified.  T is adapted until at least k and at most TO_KNN_KMAX points
+// qualify; then the survivors are sorted by (key, index).  Every point
+// closer than the k-th is kept, so the result equals warp_select's.
+// Returns false when exact ties keep the count out of the window.
+template <class Pass>
+__device__ bool threshold_select(int k, float& T, WarpScratch& ws, Pass pass) {
+    float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > cap
+    int cnt = -1;
+    for (int iter = 0; iter < 64; ++iter) {
+        if (!(T < INFINITY) || !(T >= 0.0f)) { cnt = -1; break; }
+        cnt = pass(T);
+        if (cnt >= k && cnt <= TO_KNN_KMAX) break;
+        if (cnt < k) lo = T; else hi = T;
+        float nt;
+        if (lo < 0.0f) nt = T * 0.25f;
+        else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
+        else nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
+        if (!(nt > lo) || (hi >= 0.0f && !(nt < hi))) { cnt = -1; break; }
+        T = nt;
+    }
+    __syncwarp();
+    if (cnt < k || cnt > TO_KNN_KMAX) return false;
+    warp_sort_sel(ws, cnt);
     // next query starts from a threshold a little above this k-th distance
     float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
     T = (kth > 0.0f) ? kth * 1.5f : 1e-30f;
     return true;
 }
 
-// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / (kWarps*kRun)), C); a
-// warp handles kRun consecutive grid queries of control c, whose points
-// (xn[c][j][P]) sit in shared memory.  After the selection the warp gathers
-// the neighbours' responses and predictors, and lane 0 accumulates the
-// normal equations in neighbour order and solves them (to_lsm_math.h).
-constexpr int kRun = 4;
+// full scan over n points in index order (dim-major, given stride)
+struct ScanPass {
+    const float* ref;
+    int stride, n, dim;
+    const float* q;
+    WarpScratch* ws;
+    __device__ int operator()(float T) const {
+        const int lane = threadIdx.x & 31;
+        const unsigned lt_mask = (1u << lane) - 1u;
+        int cnt = 0;
+        for (int base = 0; base < n; base += 32) {
+            int i = base + lane;
+            float key = (i < n) ? sqdist(ref, stride, i, dim, q) : INFINITY;
+            bool le = (i < n) && key <= T;
+            unsigned m = __ballot_sync(kFull, le);
+            int pos = cnt + __popc(m & lt_mask);
+            if (le && pos < TO_KNN_KMAX) ws->sel[pos] = pack_sel(key, i);
+            cnt += __popc(m);
+        }
+        return cnt;
+    }
+};
 
-__global__ void __launch_bounds__(kWarps * 32)
-k_knn_rov(to_rov_args a, int t, int smem_points) {
-    extern __shared__ unsigned char sm_raw[];
-    WarpScratch* wsa = reinterpret_cast<WarpScratch*>(sm_raw);
-    float* sref = reinterpret_cast<float*>(sm_raw + sizeof(WarpScratch) * kWarps);
-    const int c = blockIdx.y;
-    const int d = a.S + 1, R = a.R;
+__device__ __forceinline__ int cell_of(float x, float lo, float inv, int G) {
+    float f = (x - lo) * inv;
+    if (!(f > 0.0f)) return 0;
+    if (f >= (float)G) return G - 1;
+    int c = (int)f;
+    return c < G - 1 ? c : G - 1;
+}
+
+// pass over the cells a ball of radius sqrt(T) around q can touch
+template <int D>
+struct GridPass {
+    const to_knn_grid* g;
+    const float* gs;      // [D][stride] points in cell order
+    const int* gi;        // original indices
+    const int* gc;        // cell starts
+    int stride;
+    const float* q;
+    WarpScratch* ws;
+    __device__ int operator()(float T) const {
+        const int lane = threadIdx.x & 31;
+        const unsigned lt_mask = (1u << lane) - 1u;
+        const float r = sqrtf(T);
+        const float Tp = T * 1.0002f + 1e-30f;
+        int cl[D], span[D];
+        float tol[D];
+#pragma unroll
+        for (int j = 0; j < D; ++j) {
+            tol[j] = r * 1e-4f + 1e-6f * (1.0f + fabsf(q[j]) + fabsf(g->lo[j]) + fabsf(g->hi[j]));
+            cl[j] = cell_of(q[j] - (r + tol[j]), g->lo[j], g->inv[j], g->G[j]);
+            span[j] = cell_of(q[j] + (r + tol[j]), g->lo[j], g->inv[j], g->G[j]) - cl[j] + 1;
+        }
+        int nrows = 1;
+#pragma unroll
+        for (int j = 1; j < D; ++j) nrows *= span[j];
+        int cnt = 0;
+        for (int row = 0; row < nrows; ++row) {
+            int rem = row, cell = 0, mul = g->G[0];
+            float lb2 = 0.0f;
+#pragma unroll
+            for (int j = 1; j < D; ++j) {
+                int cj = cl[j] + rem % span[j];
+                rem /= span[j];
+                cell += cj * mul;
+                mul *= g->G[j];
+                if (g->inv[j] > 0.0f) {
+                    float slo = g->lo[j] + (float)cj / g->inv[j];
+                    float shi = g->lo[j] + (float)(cj + 1) / g->inv[j];
+                    float e = fmaxf(slo - q[j], q[j] - shi) - tol[j];
+                    if (e > 0.0f) lb2 = lb2 + e * e;
+                }
+            }
+            if (lb2 > Tp) continue;
+            float r0 = sqrtf(Tp - lb2) + tol[0];
+            int a0 = cell_of(q[0] - r0, g->lo[0], g->inv[0], g->G[0]);
+            int b0 = cell_of(q[0] + r0, g->lo[0], g->inv[0], g->G[0]);
+            const int s = gc[cell + a0], e = gc[cell + b0 + 1];
+            for (int base = s; base < e; base += 32) {
+                int i = base + lane;
+                bool in = i < e;
+                float key = in ? sqdist(gs, stride, i, D, q) : INFINITY;
+                bool le = in && key <= T;
+                unsigned m = __ballot_sync(kFull, le);
+                int pos = cnt + __popc(m & lt_mask);
+                if (le && pos < TO_KNN_KMAX) ws->sel[pos] = pack_sel(key, gi[i]);
+                cnt += __popc(m);
+            }
+        }
+        return cnt;
+    }
+};
+
+// Per control: bounding box of the normalised points, a cell grid of about
+// 8n/k cells (at most TO_KNN_GCELLS), and a counting sort of the points into
+// it.  One CTA per control.
+__global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
+    const int c = blockIdx.x, d = a.S + 1, P = a.P;
     const int n = a.npts[c], k = a.kc[c];
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
-    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * d;
+    __shared__ int s_cnt[TO_KNN_GCELLS];
+    __shared__ unsigned s_umin[TO_LSM_MAXD], s_umax[TO_LSM_MAXD];
+    __shared__ int s_bad;
+    __shared__ int s_wsum[32];
+    __shared__ to_knn_grid s_g;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float* xs = a.xn + (size_t)c * d * P;
+    if (tid < d) { s_umin[tid] = 0xFFFFFFFFu; s_umax[tid] = 0u; }
+    if (tid == 0) s_bad = 0;
+    __syncthreads();
+    for (int j = 0; j < d; ++j) {
+        float lo = INFINITY, hi = -INFINITY;
+        bool bad = false;
+        for (int m = tid; m < n; m += blockDim.x) {
+            float x = xs[(size_t)j * P + m];
+            bad = bad || !isfinite(x);
+            lo = fminf(lo, x);
+            hi = fmaxf(hi, x);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(kFull, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(kFull, hi, o));
+        }
+        unsigned kl = __float_as_uint(lo), kh = __float_as_uint(hi);
+        kl = (kl & 0x80000000u) ? ~kl : (kl | 0x80000000u);
+        kh = (kh & 0x80000000u) ? ~kh : (kh | 0x80000000u);
+        if (__any_sync(kFull, bad) && lane == 0) s_bad = 1;
+        if (lane == 0) { atomicMin(&s_umin[j], kl); atomicMax(&s_umax[j], kh); }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        to_knn_grid g;
+        g.ok = (!s_bad && n >= 3 && k > 0) ? 1 : 0;
+        int target = (k > 0) ? (int)(8LL * n / k) : 1;
+        if (target < 1) target = 1;
+        int gd = (int)floorf(powf((float)target, 1.0f / (float)d));
+        if (gd < 1) gd = 1;
+        if (gd > 64) gd = 64;
+        for (;;) {
+            long long cells = 1;
+            for (int j = 0; j < d; ++j) cells *= gd;
+            if (cells <= TO_KNN_GCELLS || gd == 1) break;
+            --gd;
+        }
+        for (int j = 0; j < TO_LSM_MAXD; ++j) {
+            g.lo[j] = 0.0f; g.hi[j] = 0.0f; g.inv[j] = 0.0f; g.G[j] = 1;
+        }
+        for (int j = 0; j < d; ++j) {
+            unsigned kl = s_umin[j], kh = s_umax[j];
+            kl = (kl & 0x80000000u) ? (kl & 0x7FFFFFFFu) : ~kl;
+            kh = (kh & 0x80000000u) ? (kh & 0x7FFFFFFFu) : ~kh;
+            float lo = __uint_as_float(kl), hi = __uint_as_float(kh);
+            float ext = hi - lo;
+            g.lo[j] = lo;
+            g.hi[j] = hi;
+            if (ext > 0.0f && isfinite(ext) && (float)gd / ext < INFINITY) {
+                g.G[j] = gd;
+                g.inv[j] = (float)gd / ext;
+            }
+        }
+        if (!g.ok) for (int j = 0; j < TO_LSM_MAXD; ++j) { g.lo[j] = g.hi[j] = 0.0f; }
+        s_g = g;
+        a.ggrid[c] = g;
+    }
+    __syncthreads();
+    if (!s_g.ok) return;
+    int ncell = 1;
+    for (int j = 0; j < d; ++j) ncell *= s_g.G[j];
+    for (int i = tid; i < ncell; i += blockDim.x) s_cnt[i] = 0;
+    __syncthreads();
+    auto cell_idx = [&](int m) {
+        int cell = 0, mul = 1;
+        for (int j = 0; j < d; ++j) {
+            cell += cell_of(xs[(size_t)j * P + m], s_g.lo[j], s_g.inv[j], s_g.G[j]) * mul;
+            mul *= s_g.G[j];
+        }
+        return cell;
+    };
+    for (int m = tid; m < n; m += blockDim.x) atomicAdd(&s_cnt[cell_idx(m)], 1);
+    __syncthreads();
+    // exclusive scan of the counts: 4 consecutive cells per thread
+    int* gc = a.gcell + (size_t)c * (TO_KNN_GCELLS + 1);
+    int v[4], loc = 0;
+    for (int u = 0; u < 4; ++u) {
+        int i = tid * 4 + u;
+        v[u] = (i < ncell) ? s_cnt[i] : 0;
+        loc += v[u];
+    }
+    int incl = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t2 = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += t2;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    int wbase = 0;
+    for (int w = 0; w < warp; ++w) wbase += s_wsum[w];
+    int run = wbase + incl - loc;
+    __syncthreads();
+    for (int u = 0; u < 4; ++u) {
+        int i = tid * 4 + u;
+        if (i < ncell) { s_cnt[i] = run; gc[i] = run; }
+        run += v[u];
+    }
+    if (tid == 0) gc[ncell] = n;
+    __syncthreads();
+    float* gs = a.gsx + (size_t)c * d * P;
+    int* gi = a.gsi + (size_t)c * P;
+    for (int m = tid; m < n; m += blockDim.x) {
+        int pos = atomicAdd(&s_cnt[cell_idx(m)], 1);
+        for (int j = 0; j < d; ++j) gs[(size_t)j * P + pos] = xs[(size_t)j * P + m];
+        gi[pos] = m;
+    }
+}
+
+// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / (kWarps*kRun)), C); a
+// warp handles kRun consecutive grid queries of control c.  After the
+// selection every lane accumulates the normal equations of neighbours
+// lane, lane+32, ...; the butterfly sum leaves the same totals in every
+// lane and lane 0 solves them (to_lsm_math.h).
+constexpr int kRun = 2;
+
+template <int D>
+__global__ void __launch_bounds__(kWarps * 32)
+k_knn_rov(to_rov_args a, int t) {
+    __shared__ WarpScratch wsa[kWarps];
+    constexpr int M = D + 1;
+    const int c = blockIdx.y;
+    const int P = a.P, R = a.R;
+    const int n = a.npts[c], k = a.kc[c];
+    const size_t blk = (size_t)R * D + 2 * (size_t)a.Q;
+    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * D;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q0 = (blockIdx.x * kWarps + warp) * kRun;
     if (n < 3 || k <= 0) {
@@ -220,61 +438,68 @@ k_knn_rov(to_rov_args a, int t, int smem_points) {
             if (q0 + r < a.Q) yout[q0 + r] = 0.0f;
         return;
     }
-    const float* src = a.xn + (size_t)c * d * a.P;
-    const float* ref = src;
-    int stride = a.P;
-    if (n <= smem_points) {
-        for (int q = threadIdx.x; q < n * d; q += blockDim.x) {
-            int j = q / n, m = q - j * n;
-            sref[(size_t)j * n + m] = src[(size_t)j * a.P + m];
-        }
-        __syncthreads();
-        ref = sref;
-        stride = n;
-    }
+    const to_knn_grid g = a.ggrid[c];
+    const float* xs = a.xn + (size_t)c * D * P;
+    const float* y = a.yv + (size_t)c * P;
+    const float* xr = a.xraw + (size_t)c * D * P;
     WarpScratch& ws = wsa[warp];
-    const float* y = a.yv + (size_t)c * a.P;
-    const float* xr = a.xraw + (size_t)c * d * a.P;
-    float T = powf((float)k / (float)n, 2.0f / (float)d);
+    float T0 = 0.0f;
+    for (int j = 0; j < D; ++j)
+        if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
+    if (!(T0 > 0.0f)) T0 = powf((float)k / (float)n, 2.0f / (float)D);
+    float T = T0;
     for (int r = 0; r < kRun; ++r) {
         const int qi = q0 + r;
         if (qi >= a.Q) break;
-        float qn[TO_LSM_MAXD], xq[TO_LSM_MAXD];
-        to_rov_query(a, qi, qn, xq);
-        if (!warp_select_threshold(ref, stride, n, d, qn, k, T, ws)) {
-            warp_select(ref, stride, n, d, qn, k, ws);
-            T = powf((float)k / (float)n, 2.0f / (float)d);
+        float qn[D], xq[D];
+        to_rov_query<D>(a, qi, qn, xq);
+        bool ok = false;
+        if (g.ok) {
+            GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
+                           a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws};
+            ok = threshold_select(k, T, ws, gp);
+        } else {
+            ScanPass sp{xs, P, n, D, qn, &ws};
+            ok = threshold_select(k, T, ws, sp);
         }
-        // gather the neighbours' responses and predictors
+        if (!ok) {
+            warp_select(xs, P, n, D, qn, k, ws);
+            T = T0;
+        }
+        // lane-strided local linear regression
+        float acc[M + M * M];
+        to_lsm_acc_init(D, acc);
+        const float h = sqrtf(__uint_as_float((unsigned)(ws.sel[k - 1] >> 32)));
         for (int kk = lane; kk < k; kk += 32) {
-            int i = (int)(ws.sel[kk] & 0xFFFFFFFFu);
-            ws.gy[kk] = y[i];
-            for (int j = 0; j < d; ++j) {
-                float xv;
+            const unsigned long long v = ws.sel[kk];
+            const int i = (int)(v & 0xFFFFFFFFu);
+            const float dd = sqrtf(__uint_as_float((unsigned)(v >> 32)));
+            float xv[D];
+#pragma unroll
+            for (int j = 0; j < D; ++j) {
                 if (a.sem == 0) {
                     // the reference reads its dim-major buffer (stride n)
                     // point-major (multiLocLinReg, SimulateGPU.cu:3002)
-                    int f = i * d + j;
+                    int f = i * D + j;
                     int jj = f / n, m = f - jj * n;
-                    xv = xr[(size_t)jj * a.P + m];
+                    xv[j] = xr[(size_t)jj * P + m];
                 } else {
-                    xv = ref[(size_t)j * stride + i];
+                    xv[j] = xs[(size_t)j * P + i];
                 }
-                ws.gx[kk * TO_LSM_MAXD + j] = xv;
             }
+            to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
         }
-        __syncwarp();
-        if (lane == 0) {
-            float acc[TO_LSM_ACC];
-            to_lsm_acc_init(d, acc);
-            const float h = sqrtf(__uint_as_float((unsigned)(ws.sel[k - 1] >> 32)));
-            for (int kk = 0; kk < k; ++kk) {
-                float dd = sqrtf(__uint_as_float((unsigned)(ws.sel[kk] >> 32)));
-                to_lsm_acc_add(d, acc, to_lsm_weight(dd, h), ws.gy[kk],
-                               &ws.gx[kk * TO_LSM_MAXD], xq);
+#pragma unroll
+        for (int e = 0; e < M; ++e)
+            for (int o = 16; o > 0; o >>= 1) acc[e] = acc[e] + __shfl_xor_sync(kFull, acc[e], o);
+#pragma unroll
+        for (int i = 0; i < M; ++i)
+#pragma unroll
+            for (int j = i; j < M; ++j) {
+                float& x = acc[M + i * M + j];
+                for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
             }
-            yout[qi] = to_lsm_solve_intercept(d, acc);
-        }
+        if (lane == 0) yout[qi] = to_lsm_solve_intercept(D, acc);
         __syncwarp();
     }
 }
@@ -299,7 +524,8 @@ k_knn_generic(const float* ref_g, int n, const float* query, int Q, int dim, int
     for (int j = 0; j < dim; ++j) q[j] = query[(size_t)j * Q + qi];
     WarpScratch& ws = wsa[warp];
     float T = powf((float)k / (float)n, 2.0f / (float)dim);
-    if (!warp_select_threshold(ref, n, n, dim, q, k, T, ws)) warp_select(ref, n, n, dim, q, k, ws);
+    ScanPass sp{ref, n, n, dim, q, &ws};
+    if (!threshold_select(k, T, ws, sp)) warp_select(ref, n, n, dim, q, k, ws);
     for (int kk = lane; kk < k; kk += 32) {
         unsigned long long v = ws.sel[kk];
         dist[(size_t)kk * Q + qi] = sqrtf(__uint_as_float((unsigned)(v >> 32)));
@@ -319,15 +545,20 @@ to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     const int d = a.S + 1;
     if (a.kmax > TO_KNN_KMAX)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d exceeds %d", a.kmax, TO_KNN_KMAX);
-    size_t cap = ctx->smem_optin > 8192 ? ctx->smem_optin - 8192 : 48 * 1024;
-    int pts = a.P;
-    while (pts > 0 && knn_smem(d, pts) > cap) pts = pts * 3 / 4;
-    size_t smem = knn_smem(d, pts);
-    TO_CUDA(ctx, cudaFuncSetAttribute(k_knn_rov, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
+    if (d < 2 || d > TO_LSM_MAXD)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "regression dimension %d", d);
+    to_prof_begin(ctx, "knn_grid");
+    k_knn_grid<<<a.C, 1024, 0, ctx->stream>>>(a);
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
     dim3 grid((a.Q + kWarps * kRun - 1) / (kWarps * kRun), a.C);
     to_prof_begin(ctx, "knn");
-    k_knn_rov<<<grid, kWarps * 32, smem, ctx->stream>>>(a, t, pts);
+    switch (d) {
+        case 2: k_knn_rov<2><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
+        case 3: k_knn_rov<3><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
+        case 4: k_knn_rov<4><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
+        default: k_knn_rov<5><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
+    }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;

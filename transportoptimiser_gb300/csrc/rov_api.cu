@@ -91,7 +91,8 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     acc((size_t)S * (Y + 1) * P * 4); acc((size_t)S * C * Y * P * 4);
     acc((size_t)C * d * P * 4); acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
     acc(C * 4); acc(C * 4); acc(d * 4); acc(d * 4);
-    acc((size_t)C * kmax * Q * 4); acc((size_t)C * kmax * Q * 4);
+    acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
+    acc((size_t)C * (TO_KNN_GCELLS + 1) * 4); acc((size_t)C * sizeof(to_knn_grid));
     acc((size_t)Y * C * blk * 4); acc((size_t)Y * P * 4); acc((size_t)Y * P * 4);
     acc((size_t)Y * P * 4); acc((size_t)Y * S * P * 4); acc(5 * 8);
     const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
@@ -129,8 +130,10 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.kc = to_arena_take<int>(ctx, C);
     a.gmin = to_arena_take<float>(ctx, d);
     a.gmax = to_arena_take<float>(ctx, d);
-    a.dist = to_arena_take<float>(ctx, (size_t)C * kmax * Q);
-    a.ind = to_arena_take<int>(ctx, (size_t)C * kmax * Q);
+    a.gsx = to_arena_take<float>(ctx, (size_t)C * d * P);
+    a.gsi = to_arena_take<int>(ctx, (size_t)C * P);
+    a.gcell = to_arena_take<int>(ctx, (size_t)C * (TO_KNN_GCELLS + 1));
+    a.ggrid = to_arena_take<to_knn_grid>(ctx, C);
     a.reg = to_arena_take<float>(ctx, (size_t)Y * C * blk);
     a.condExp = to_arena_take<float>(ctx, (size_t)Y * P);
     a.optCont = to_arena_take<int>(ctx, (size_t)Y * P);

@@ -6,6 +6,16 @@
 
 #define TO_ROV_MAXC 8
 #define TO_KNN_KMAX 256
+#define TO_KNN_GCELLS 4096
+
+// uniform cell grid over one control's normalised regression points:
+// cell_j(x) = clamp(floor((x - lo_j) * inv_j), 0, G_j - 1), dimension 0
+// fastest; ok = 0 when a coordinate is not finite (full scan instead)
+struct to_knn_grid {
+    float lo[TO_LSM_MAXD], hi[TO_LSM_MAXD], inv[TO_LSM_MAXD];
+    int G[TO_LSM_MAXD];
+    int ok;
+};
 
 struct to_rov_args {
     int P, Y, S, C, U, R, Q;          // paths, years, species, controls, processes, dimRes, R^d
@@ -39,8 +49,10 @@ struct to_rov_args {
     int* kc;                          // [C]
     float* gmin;                      // [d]
     float* gmax;                      // [d]
-    float* dist;                      // [C][kmax][Q]
-    int* ind;                         // [C][kmax][Q]
+    float* gsx;                       // [C][d][P] points in cell order
+    int* gsi;                         // [C][P] their original indices
+    int* gcell;                       // [C][TO_KNN_GCELLS + 1] cell starts
+    to_knn_grid* ggrid;               // [C]
     int kmax;
     // outputs (device)
     float* reg;                       // [Y][C][R*d + 2Q]
@@ -54,12 +66,14 @@ struct to_rov_args {
 // grid query q of the current year: normalised coordinates (for kNN) and
 // the coordinates the regression centres on (createQueryPoints + host
 // normalisation; sem 0 centres on the unit grid, SimulateGPU.cu:2964-2966)
+template <int D>
 __device__ __forceinline__ void to_rov_query(const to_rov_args& a, int q, float* qn,
                                              float* xq) {
-    const int d = a.S + 1, R = a.R;
+    const int R = a.R;
     int rem = q;
     int div = a.Q / R;
-    for (int j = 0; j < d; ++j) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
         int di = rem / div;
         rem -= di * div;
         div /= R;
@@ -74,6 +88,7 @@ struct to_csc;
 namespace to_k {
 // csc: the packed migration matrices for the sparse forward pass, or null
 to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc);
+// kNN + local linear regressions of year t (cell grid, then fused kernel)
 to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t);
 // generic kNN: ref dim-major [dim][n], query dim-major [dim][Q]
 to_status knn(to_ctx ctx, const float* ref, int n, const float* query, int Q,
