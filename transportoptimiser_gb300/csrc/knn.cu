@@ -31,9 +31,16 @@ namespace {
 constexpr int kWarps = 8;
 constexpr unsigned kFull = 0xffffffffu;
 
+// a threshold pass keeps up to kStore candidates; the k nearest are then
+// refined out of them without another pass over the points
+constexpr int kStore = 2 * TO_KNN_KMAX;
+
 struct WarpScratch {
-    unsigned hist[256];
-    unsigned long long sel[TO_KNN_KMAX];
+    unsigned long long sel[kStore];
+    union {
+        unsigned hist[256];                   // radix select
+        unsigned long long out[TO_KNN_KMAX];  // refinement compaction
+    };
 };
 
 __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int dim,
@@ -169,33 +176,80 @@ __device__ __forceinline__ unsigned long long pack_sel(float key, int i) {
 }
 
 // Threshold form of the selection.  pass(T) gathers into ws.sel every point
-// whose key is <= T (entries past TO_KNN_KMAX dropped) and returns how many
-// qualified.  T is adapted until at least k and at most TO_KNN_KMAX points
-// qualify; then the survivors are sorted by (key, index).  Every point
-// closer than the k-th is kept, so the result equals warp_select's.
-// Returns false when exact ties keep the count out of the window.
+// whose key is <= T (entries past kStore dropped) and returns how many
+// qualified (a pass may stop counting early once far above the window).
+// T is adapted until at least k and at most kStore points qualify.  When
+// more than TO_KNN_KMAX qualified, the threshold is narrowed among the
+// stored keys alone.  The survivors are sorted by (key, index).  Every point
+// closer than the k-th is kept, so the result equals warp_select's.  The
+// update assumes a locally uniform density, count ~ T^(dim/2), kept inside
+// the bracket of thresholds already seen.  Returns false when exact ties
+// keep the count out of the window.
+__device__ __forceinline__ bool next_threshold(int cnt, int k, float target, float expo,
+                                               float& T, float& lo, float& hi) {
+    if (cnt < k) lo = T; else hi = T;
+    float nt;
+    if (cnt == 0) nt = (T > 0.0f) ? T * 16.0f : 1e-30f;
+    else nt = T * powf(target / (float)cnt, expo);
+    if ((lo >= 0.0f && !(nt > lo)) || (hi >= 0.0f && !(nt < hi))) {
+        if (lo >= 0.0f && hi >= 0.0f) nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
+        else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
+        else nt = T * 0.25f;
+    }
+    if (!(nt > lo) || (hi >= 0.0f && !(nt < hi))) return false;
+    T = nt;
+    return true;
+}
+
 template <class Pass>
-__device__ bool threshold_select(int k, float& T, WarpScratch& ws, Pass pass) {
-    float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > cap
+__device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass pass) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > window
+    const float expo = 2.0f / (float)dim;
+    const float target = sqrtf((float)k * (float)kStore);
     int cnt = -1;
     for (int iter = 0; iter < 64; ++iter) {
         if (!(T < INFINITY) || !(T >= 0.0f)) { cnt = -1; break; }
         cnt = pass(T);
-        if (cnt >= k && cnt <= TO_KNN_KMAX) break;
-        if (cnt < k) lo = T; else hi = T;
-        float nt;
-        if (lo < 0.0f) nt = T * 0.25f;
-        else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
-        else nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
-        if (!(nt > lo) || (hi >= 0.0f && !(nt < hi))) { cnt = -1; break; }
-        T = nt;
+        if (cnt >= k && cnt <= kStore) break;
+        if (!next_threshold(cnt, k, target, expo, T, lo, hi)) { cnt = -1; break; }
     }
     __syncwarp();
-    if (cnt < k || cnt > TO_KNN_KMAX) return false;
+    if (cnt < k || cnt > kStore) return false;
+    if (cnt > TO_KNN_KMAX) {
+        // narrow among the stored candidates
+        const float target2 = 0.5f * (float)(k + TO_KNN_KMAX);
+        float lo2 = -1.0f, hi2 = T, T2 = T;
+        int c2 = cnt;
+        bool ok = false;
+        for (int iter = 0; iter < 64; ++iter) {
+            if (!next_threshold(c2, k, target2, expo, T2, lo2, hi2)) break;
+            unsigned cl = 0;
+            for (int i = lane; i < cnt; i += 32)
+                cl += (__uint_as_float((unsigned)(ws.sel[i] >> 32)) <= T2) ? 1u : 0u;
+            c2 = (int)__reduce_add_sync(kFull, cl);
+            if (c2 >= k && c2 <= TO_KNN_KMAX) { ok = true; break; }
+        }
+        if (!ok) return false;
+        int pos0 = 0;
+        for (int base = 0; base < cnt; base += 32) {
+            int i = base + lane;
+            unsigned long long v = (i < cnt) ? ws.sel[i] : ~0ull;
+            bool le = (i < cnt) && __uint_as_float((unsigned)(v >> 32)) <= T2;
+            unsigned m = __ballot_sync(kFull, le);
+            if (le) ws.out[pos0 + __popc(m & lt_mask)] = v;
+            pos0 += __popc(m);
+        }
+        __syncwarp();
+        for (int i = lane; i < c2; i += 32) ws.sel[i] = ws.out[i];
+        __syncwarp();
+        cnt = c2;
+    }
     warp_sort_sel(ws, cnt);
     // next query starts from a threshold a little above this k-th distance
     float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
-    T = (kth > 0.0f) ? kth * 1.5f : 1e-30f;
+    T = (kth > 0.0f) ? kth * 1.3f : 1e-30f;
     return true;
 }
 
@@ -215,8 +269,13 @@ struct ScanPass {
             bool le = (i < n) && key <= T;
             unsigned m = __ballot_sync(kFull, le);
             int pos = cnt + __popc(m & lt_mask);
-            if (le && pos < TO_KNN_KMAX) ws->sel[pos] = pack_sel(key, i);
+            if (le && pos < kStore) ws->sel[pos] = pack_sel(key, i);
             cnt += __popc(m);
+            if (cnt > 4 * kStore) {
+                // far above the window: extrapolate over the unscanned part
+                float f = (float)(base + 32) / (float)n;
+                return (int)fminf((float)cnt / f, 1e9f);
+            }
         }
         return cnt;
     }
@@ -267,8 +326,8 @@ struct GridPass {
                 cell += cj * mul;
                 mul *= g->G[j];
                 if (g->inv[j] > 0.0f) {
-                    float slo = g->lo[j] + (float)cj / g->inv[j];
-                    float shi = g->lo[j] + (float)(cj + 1) / g->inv[j];
+                    float slo = g->lo[j] + (float)cj * g->w[j];
+                    float shi = slo + g->w[j];
                     float e = fmaxf(slo - q[j], q[j] - shi) - tol[j];
                     if (e > 0.0f) lb2 = lb2 + e * e;
                 }
@@ -285,9 +344,10 @@ struct GridPass {
                 bool le = in && key <= T;
                 unsigned m = __ballot_sync(kFull, le);
                 int pos = cnt + __popc(m & lt_mask);
-                if (le && pos < TO_KNN_KMAX) ws->sel[pos] = pack_sel(key, gi[i]);
+                if (le && pos < kStore) ws->sel[pos] = pack_sel(key, gi[i]);
                 cnt += __popc(m);
             }
+            if (cnt > 4 * kStore) return cnt;   // far above the window
         }
         return cnt;
     }
@@ -344,7 +404,7 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
             --gd;
         }
         for (int j = 0; j < TO_LSM_MAXD; ++j) {
-            g.lo[j] = 0.0f; g.hi[j] = 0.0f; g.inv[j] = 0.0f; g.G[j] = 1;
+            g.lo[j] = 0.0f; g.hi[j] = 0.0f; g.inv[j] = 0.0f; g.w[j] = 0.0f; g.G[j] = 1;
         }
         for (int j = 0; j < d; ++j) {
             unsigned kl = s_umin[j], kh = s_umax[j];
@@ -357,6 +417,7 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
             if (ext > 0.0f && isfinite(ext) && (float)gd / ext < INFINITY) {
                 g.G[j] = gd;
                 g.inv[j] = (float)gd / ext;
+                g.w[j] = ext / (float)gd;
             }
         }
         if (!g.ok) for (int j = 0; j < TO_LSM_MAXD; ++j) { g.lo[j] = g.hi[j] = 0.0f; }
@@ -414,28 +475,37 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     }
 }
 
-// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / (kWarps*kRun)), C); a
-// warp handles kRun consecutive grid queries of control c.  After the
-// selection every lane accumulates the normal equations of neighbours
-// lane, lane+32, ...; the butterfly sum leaves the same totals in every
-// lane and lane 0 solves them (to_lsm_math.h).
-constexpr int kRun = 2;
+// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / kQ), C); a warp
+// handles kRun consecutive grid queries of control c, starting its
+// threshold from the k-th distance the same query had in the year before.  After the selection
+// every lane accumulates the normal equations of neighbours lane, lane+32,
+// ...; the butterfly sum leaves the same totals in every lane.  The CTA's
+// kQ systems are then solved one per thread of warp 0, so each FP64
+// instruction of the Cholesky solve serves kQ queries (to_lsm_math.h).
+constexpr int kRun = 1;
+constexpr int kQ = kWarps * kRun;       // queries per CTA, <= 32
+
+template <int D>
+size_t knn_rov_smem() {
+    return sizeof(WarpScratch) * kWarps + sizeof(float) * kQ * ((D + 1) + (D + 1) * (D + 1));
+}
 
 template <int D>
 __global__ void __launch_bounds__(kWarps * 32)
 k_knn_rov(to_rov_args a, int t) {
-    __shared__ WarpScratch wsa[kWarps];
-    constexpr int M = D + 1;
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    WarpScratch* wsa = reinterpret_cast<WarpScratch*>(sm_raw);
+    constexpr int M = D + 1, NA = M + M * M;
+    float* s_acc = reinterpret_cast<float*>(sm_raw + sizeof(WarpScratch) * kWarps);
     const int c = blockIdx.y;
     const int P = a.P, R = a.R;
     const int n = a.npts[c], k = a.kc[c];
     const size_t blk = (size_t)R * D + 2 * (size_t)a.Q;
     float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * D;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int q0 = (blockIdx.x * kWarps + warp) * kRun;
+    const int qc = blockIdx.x * kQ;
     if (n < 3 || k <= 0) {
-        for (int r = lane; r < kRun; r += 32)
-            if (q0 + r < a.Q) yout[q0 + r] = 0.0f;
+        if (threadIdx.x < kQ && qc + threadIdx.x < a.Q) yout[qc + threadIdx.x] = 0.0f;
         return;
     }
     const to_knn_grid g = a.ggrid[c];
@@ -448,26 +518,30 @@ k_knn_rov(to_rov_args a, int t) {
         if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
     if (!(T0 > 0.0f)) T0 = powf((float)k / (float)n, 2.0f / (float)D);
     float T = T0;
+    float* kth_prev = a.kth + (size_t)c * a.Q;
     for (int r = 0; r < kRun; ++r) {
-        const int qi = q0 + r;
+        const int ql = warp * kRun + r;
+        const int qi = qc + ql;
         if (qi >= a.Q) break;
+        if (r == 0 && kth_prev[qi] > 0.0f) T = kth_prev[qi] * 1.3f;
         float qn[D], xq[D];
         to_rov_query<D>(a, qi, qn, xq);
         bool ok = false;
         if (g.ok) {
             GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
                            a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws};
-            ok = threshold_select(k, T, ws, gp);
+            ok = threshold_select(k, D, T, ws, gp);
         } else {
             ScanPass sp{xs, P, n, D, qn, &ws};
-            ok = threshold_select(k, T, ws, sp);
+            ok = threshold_select(k, D, T, ws, sp);
         }
         if (!ok) {
             warp_select(xs, P, n, D, qn, k, ws);
             T = T0;
         }
+        if (lane == 0) kth_prev[qi] = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
         // lane-strided local linear regression
-        float acc[M + M * M];
+        float acc[NA];
         to_lsm_acc_init(D, acc);
         const float h = sqrtf(__uint_as_float((unsigned)(ws.sel[k - 1] >> 32)));
         for (int kk = lane; kk < k; kk += 32) {
@@ -489,19 +563,26 @@ k_knn_rov(to_rov_args a, int t) {
             }
             to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
         }
+        float* sa = s_acc + (size_t)ql * NA;
 #pragma unroll
-        for (int e = 0; e < M; ++e)
-            for (int o = 16; o > 0; o >>= 1) acc[e] = acc[e] + __shfl_xor_sync(kFull, acc[e], o);
+        for (int e = 0; e < M; ++e) {
+            float x = acc[e];
+            for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
+            if (lane == 0) sa[e] = x;
+        }
 #pragma unroll
         for (int i = 0; i < M; ++i)
 #pragma unroll
             for (int j = i; j < M; ++j) {
-                float& x = acc[M + i * M + j];
+                float x = acc[M + i * M + j];
                 for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
+                if (lane == 0) sa[M + i * M + j] = x;
             }
-        if (lane == 0) yout[qi] = to_lsm_solve_intercept(D, acc);
         __syncwarp();
     }
+    __syncthreads();
+    if (threadIdx.x < kQ && qc + threadIdx.x < a.Q)
+        yout[qc + threadIdx.x] = to_lsm_solve_intercept(D, s_acc + (size_t)threadIdx.x * NA);
 }
 
 // generic: explicit dim-major queries
@@ -525,12 +606,21 @@ k_knn_generic(const float* ref_g, int n, const float* query, int Q, int dim, int
     WarpScratch& ws = wsa[warp];
     float T = powf((float)k / (float)n, 2.0f / (float)dim);
     ScanPass sp{ref, n, n, dim, q, &ws};
-    if (!threshold_select(k, T, ws, sp)) warp_select(ref, n, n, dim, q, k, ws);
+    if (!threshold_select(k, dim, T, ws, sp)) warp_select(ref, n, n, dim, q, k, ws);
     for (int kk = lane; kk < k; kk += 32) {
         unsigned long long v = ws.sel[kk];
         dist[(size_t)kk * Q + qi] = sqrtf(__uint_as_float((unsigned)(v >> 32)));
         ind[(size_t)kk * Q + qi] = (int)(v & 0xFFFFFFFFu) + 1;
     }
+}
+
+template <int D>
+to_status launch_knn_rov(to_ctx ctx, dim3 grid, const to_rov_args& a, int t) {
+    const size_t smem = knn_rov_smem<D>();
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_knn_rov<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    k_knn_rov<D><<<grid, kWarps * 32, smem, ctx->stream>>>(a, t);
+    return TO_OK;
 }
 
 size_t knn_smem(int dim, int points) {
@@ -551,13 +641,13 @@ to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     k_knn_grid<<<a.C, 1024, 0, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
-    dim3 grid((a.Q + kWarps * kRun - 1) / (kWarps * kRun), a.C);
+    dim3 grid((a.Q + kQ - 1) / kQ, a.C);
     to_prof_begin(ctx, "knn");
     switch (d) {
-        case 2: k_knn_rov<2><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
-        case 3: k_knn_rov<3><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
-        case 4: k_knn_rov<4><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
-        default: k_knn_rov<5><<<grid, kWarps * 32, 0, ctx->stream>>>(a, t); break;
+        case 2: TO_TRY(launch_knn_rov<2>(ctx, grid, a, t)); break;
+        case 3: TO_TRY(launch_knn_rov<3>(ctx, grid, a, t)); break;
+        case 4: TO_TRY(launch_knn_rov<4>(ctx, grid, a, t)); break;
+        default: TO_TRY(launch_knn_rov<5>(ctx, grid, a, t)); break;
     }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);

@@ -93,6 +93,7 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     acc(C * 4); acc(C * 4); acc(d * 4); acc(d * 4);
     acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
     acc((size_t)C * (TO_KNN_GCELLS + 1) * 4); acc((size_t)C * sizeof(to_knn_grid));
+    acc((size_t)C * Q * 4);
     acc((size_t)Y * C * blk * 4); acc((size_t)Y * P * 4); acc((size_t)Y * P * 4);
     acc((size_t)Y * P * 4); acc((size_t)Y * S * P * 4); acc(5 * 8);
     const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
@@ -134,6 +135,7 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.gsi = to_arena_take<int>(ctx, (size_t)C * P);
     a.gcell = to_arena_take<int>(ctx, (size_t)C * (TO_KNN_GCELLS + 1));
     a.ggrid = to_arena_take<to_knn_grid>(ctx, C);
+    a.kth = to_arena_take<float>(ctx, (size_t)C * Q);
     a.reg = to_arena_take<float>(ctx, (size_t)Y * C * blk);
     a.condExp = to_arena_take<float>(ctx, (size_t)Y * P);
     a.optCont = to_arena_take<int>(ctx, (size_t)Y * P);

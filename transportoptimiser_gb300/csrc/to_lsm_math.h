@@ -38,11 +38,14 @@ TO_HD float to_lsm_normalise(float x, float lo, float hi, int is_profit, float s
     return is_profit ? (x - lo) / (scaling * (hi - lo)) : (x - lo) / (hi - lo);
 }
 
-/* Gaussian kernel weight exp(-(d/h)^2/2)/sqrt(2 pi) */
+/* Gaussian kernel weight exp(-(d/h)^2/2)/sqrt(2 pi).  The reference
+ * divides by sqrt(2 pi) in double (SimulateGPU.cu:2995); the constant
+ * cancels in the normal equations, so it is applied here as one float
+ * multiply (results differ from the double form by at most one rounding). */
 TO_HD float to_lsm_weight(float d, float h) {
     float t = d / h;
     float w = ((-t) * t) / 2.0f;
-    return (float)((double)to_expf(w) / 2.5066282746310002);
+    return to_expf(w) * 0.3989422804f;
 }
 
 /* acc = [B (m) | A (m x m row-major)], m = dim + 1; only i <= j of A */

@@ -12,7 +12,7 @@
 // cell_j(x) = clamp(floor((x - lo_j) * inv_j), 0, G_j - 1), dimension 0
 // fastest; ok = 0 when a coordinate is not finite (full scan instead)
 struct to_knn_grid {
-    float lo[TO_LSM_MAXD], hi[TO_LSM_MAXD], inv[TO_LSM_MAXD];
+    float lo[TO_LSM_MAXD], hi[TO_LSM_MAXD], inv[TO_LSM_MAXD], w[TO_LSM_MAXD];
     int G[TO_LSM_MAXD];
     int ok;
 };
@@ -53,6 +53,7 @@ struct to_rov_args {
     int* gsi;                         // [C][P] their original indices
     int* gcell;                       // [C][TO_KNN_GCELLS + 1] cell starts
     to_knn_grid* ggrid;               // [C]
+    float* kth;                       // [C][Q] k-th squared distance, year before
     int kmax;
     // outputs (device)
     float* reg;                       // [Y][C][R*d + 2Q]
