@@ -374,6 +374,32 @@ to_status to_evaluate_roads_d(to_ctx ctx, to_gen gen, int n_roads,
                               const int* seg_off, const double* segs,
                               const to_eval_opts* opts, double* results);
 
+/* ------------------------------------------------------------------------
+ * Learned surrogate (no counterpart in the reference, whose GA fitness uses
+ * the local-linear grid surrogates): an MLP 16 -> 128 -> 128 -> 3 with ReLU,
+ * BF16 tensor-core GEMMs with FP32 accumulation, trained by Adam on FP32
+ * master parameters.  Parameter vector (FP32, TO_MLP_NPARAM):
+ *   W1[128][16], b1[128], W2[128][128], b2[128], W3[3][128], b3[3].
+ * Rows of x are TO_MLP_IN floats, rows of y / t are TO_MLP_OUT floats.
+ * ---------------------------------------------------------------------- */
+#define TO_MLP_IN 16
+#define TO_MLP_HID 128
+#define TO_MLP_OUT 3
+#define TO_MLP_NPARAM (16 * 128 + 128 + 128 * 128 + 128 + 3 * 128 + 3)
+
+/* y = f(x) for n rows (host buffers) */
+to_status to_mlp_predict(to_ctx ctx, const float* params, int n, const float* x, float* y);
+/* the same on device buffers, on the context's stream */
+to_status to_mlp_predict_d(to_ctx ctx, const float* d_params, int n, const float* d_x, float* d_y);
+/* gradient of mean((y - t)^2) over all n rows and outputs; *loss = that mean */
+to_status to_mlp_grad(to_ctx ctx, const float* params, int n, const float* x, const float* t,
+                      float* grad, double* loss);
+/* Adam (lr, 0.9, 0.999, 1e-8) over `epochs` seeded shuffles in mini-batches;
+ * params updated in place; loss_curve[epochs] = mean squared error seen in
+ * each epoch (may be NULL) */
+to_status to_mlp_train(to_ctx ctx, float* params, int n, const float* x, const float* t,
+                       int epochs, int batch, float lr, uint64_t seed, double* loss_curve);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,12 @@ def oracle() -> C.CDLL:
                                                   c_float_p]
         _oracle.or_build_surrogate_nd.argtypes = [C.c_int, C.c_int, c_float_p, c_float_p,
                                                   C.c_int, C.c_int, C.c_int, c_float_p]
+        _oracle.or_bf16.restype = C.c_float
+        _oracle.or_bf16.argtypes = [C.c_float]
+        _oracle.or_mlp_set_rounding.argtypes = [C.c_int]
+        _oracle.or_mlp_forward.argtypes = [c_float_p, C.c_int, c_float_p, c_float_p]
+        _oracle.or_mlp_grad.argtypes = [c_float_p, C.c_int, c_float_p, c_float_p, c_double_p,
+                                        c_double_p]
     return _oracle
 
 
@@ -449,3 +455,25 @@ def build_surrogate_nd(pred, y, R, sem=0, clip=1, use_ref=False):
         oracle().or_build_surrogate_nd(n, d, _p(pred, C.c_float), _p(y, C.c_float), R, sem, clip,
                                        _p(out, C.c_float))
     return out
+
+
+# ---- learned surrogate (oracle_mlp.c) ----------------------------------------
+def mlp_forward(params, x):
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.zeros((x.shape[0], 3), np.float32)
+    oracle().or_mlp_forward(_p(p, C.c_float), x.shape[0], _p(x, C.c_float), _p(y, C.c_float))
+    return y
+
+
+def mlp_grad(params, x, t, rounding=True):
+    oracle().or_mlp_set_rounding(1 if rounding else 0)
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(x, np.float32)
+    t = np.ascontiguousarray(t, np.float32)
+    g = np.zeros(p.size, np.float64)
+    loss = C.c_double(0.0)
+    oracle().or_mlp_grad(_p(p, C.c_float), x.shape[0], _p(x, C.c_float), _p(t, C.c_float),
+                         _p(g, C.c_double), C.byref(loss))
+    oracle().or_mlp_set_rounding(1)
+    return g, loss.value

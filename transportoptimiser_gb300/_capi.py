@@ -174,6 +174,12 @@ SIGNATURES = {
     "to_evaluate_roads_d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
+    "to_mlp_predict": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p]),
+    "to_mlp_predict_d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "to_mlp_grad": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p,
+                              c_double_p]),
+    "to_mlp_train": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p, C.c_int,
+                               C.c_int, C.c_float, C.c_uint64, c_double_p]),
 }
 
 _lib = None
