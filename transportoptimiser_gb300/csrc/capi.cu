@@ -194,6 +194,7 @@ to_status to_ctx_destroy(to_ctx ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->arena) cudaFree(ctx->arena);
+    if (ctx->tc_buf) cudaFree(ctx->tc_buf);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->d_flags) cudaFree(ctx->d_flags);
     for (int i = 0; i < ctx->prof_ev_alloc; ++i) {

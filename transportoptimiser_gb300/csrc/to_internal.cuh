@@ -23,6 +23,10 @@ struct to_ctx_s {
     // pinned host staging
     char* pinned = nullptr;
     size_t pinned_cap = 0;
+    // persistent device scratch of the tensor-core migration (packed
+    // hi/lo matrix blocks), grown on demand
+    char* tc_buf = nullptr;
+    size_t tc_cap = 0;
     // device error word for bounded waits / in-kernel checks
     int* d_flags = nullptr;
     uint64_t launches = 0;
