@@ -21,6 +21,7 @@
 namespace {
 
 constexpr int kMaxBlockRegions = 48;   // distinct regions per coarse block
+#define TO_SURV_TABLE_SEGS 255         // survival table by crossing count up to this
 
 __device__ __forceinline__ int uf_find(volatile int* par, int x) {
     int p = par[x];
@@ -321,9 +322,9 @@ k_species_model(to_model_args a) {
     const int rs = blockIdx.x;                 // road*S + species
     const int road = rs / a.S, sp = rs - road * a.S;
     const int W = a.W, H = a.H, n = W * H;
-    int* par = smem;
-    int* s_tmp = smem + n;                     // 33 ints
+    int* s_tmp = smem;                         // 33 ints
     int* s_misc = s_tmp + 40;                  // counters
+    int* par = smem + 64;                      // labels, later tables (8-byte aligned)
     const int* hab = a.hab_map;
     const int c0 = a.cell_off ? a.cell_off[road] : 0;
     const int c1 = a.cell_off ? a.cell_off[road + 1] : 0;
@@ -377,48 +378,57 @@ k_species_model(to_model_args a) {
     __threadfence_block();
     __syncthreads();
 
-    // Distances and the crossing pair filter (SpeciesRoadPatches.cpp:270-381)
+    // Distances and the crossing pair filter (SpeciesRoadPatches.cpp:270-381).
+    // FP64 is scarce on this part, so every distance test is first decided
+    // on a float d^2 (centroids are floats, so its relative error is below
+    // 4e-7); only pairs within 1e-6 of a cut-off take the exact FP64 test.
     const double lam = S.lambda_mean + S.lambda_sd * S.lambda_mult;
     const double max_dist_x = log(0.05) / (-lam);
-    const double mx2lo = max_dist_x * max_dist_x * (1.0 - 1e-9);
-    const double mx2hi = max_dist_x * max_dist_x * (1.0 + 1e-9);
+    const double mx2 = max_dist_x * max_dist_x;
+    const double mx2lo = mx2 * (1.0 - 1e-9), mx2hi = mx2 * (1.0 + 1e-9);
+    const float fx_lo = (float)(mx2 * (1.0 - 1e-6)), fx_hi = (float)(mx2 * (1.0 + 1e-6));
     int* cross = a.crossings_scratch + (size_t)rs * NM * NM;
+    float* cxf = reinterpret_cast<float*>(par);                // [N]
+    float* cyf = cxf + NM;                                      // [N]
+    double* s_attr = reinterpret_cast<double*>(cyf + NM + 2);   // [n_hab] (8-byte aligned)
+    double* s_surv = s_attr + TO_MAX_HAB;                       // [C][G+1]
+    const int G = a.seg_off[road + 1] - a.seg_off[road];
+    const double* rseg = a.segs + (size_t)a.seg_off[road] * 4;
+    const double lda = S.lambda_mult * S.lambda_sd + S.lambda_mean;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) { cxf[k] = (float)cx[k]; cyf[k] = (float)cy[k]; }
+    for (int h = threadIdx.x; h < S.n_hab; h += blockDim.x)
+        s_attr[h] = exp(S.hab_pref_mean[h] + S.hab_pref_sd[h] * S.hab_pref_mult);
+    const bool surv_tab = G <= TO_SURV_TABLE_SEGS;
+    if (surv_tab)
+        for (int q = threadIdx.x; q < a.C * (G + 1); q += blockDim.x) {
+            int c = q / (G + 1), cr = q - c * (G + 1);
+            s_surv[q] = exp(-(double)cr * S.hazard[c]);
+        }
+    auto surv_of = [&](int c, int cr) {
+        return surv_tab ? s_surv[c * (G + 1) + cr] : exp(-(double)cr * S.hazard[c]);
+    };
     if (threadIdx.x == 0) s_misc[2] = 0;
     __syncthreads();
+    auto in_range = [&](int i, int j, float flo, float fhi, double md, double lo2, double hi2) {
+        float dxf = cxf[i] - cxf[j], dyf = cyf[i] - cyf[j];
+        float d2f = dxf * dxf + dyf * dyf;
+        if (d2f < flo) return true;
+        if (d2f > fhi) return false;
+        double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+        return within(dx * dx + dy * dy, md, lo2, hi2);
+    };
     {
-        // count the valid pairs; the reference never tests its last valid
-        // pair (its counter starts at -1), so find that pair too
+        // one pass over i < j: count valid pairs, note the last one (the
+        // reference never tests its last valid pair: its counter starts at
+        // -1) and count road crossings of every valid pair in float
         int last = -1, cnt = 0;
         for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
             int i = q / N, j = q - i * N;
-            if (j <= i) continue;
-            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            if (within(dx * dx + dy * dy, max_dist_x, mx2lo, mx2hi)) { last = max(last, q); ++cnt; }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        }
-        if ((threadIdx.x & 31) == 0) { atomicMax(&s_misc[1], last); atomicAdd(&s_misc[2], cnt); }
-    }
-    __syncthreads();
-    const int last_pair = (a.sem == 0) ? s_misc[1] : -1;
-    if (threadIdx.x == 0) {
-        int cnt = s_misc[2];
-        a.n_transitions[rs] = (a.sem == 0 && cnt > 0) ? cnt - 1 : cnt;
-    }
-    const int G = a.seg_off[road + 1] - a.seg_off[road];
-    const double* rseg = a.segs + (size_t)a.seg_off[road] * 4;
-    for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-        int i = q / N, j = q - i * N;
-        if (j < i) continue;
-        int c = 0;
-        if (i != j) {
-            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            bool valid = within(dx * dx + dy * dy, max_dist_x, mx2lo, mx2hi);
-            if (q == last_pair) valid = false;
-            if (valid) {
-                float x1 = (float)cx[i], y1 = (float)cy[i];
+            int c = 0;
+            if (j > i && in_range(i, j, fx_lo, fx_hi, max_dist_x, mx2lo, mx2hi)) {
+                last = max(last, q);
+                ++cnt;
+                float x1 = cxf[i], y1 = cyf[i];
                 float x21 = (float)(cx[j] - cx[i]);
                 float y21 = (float)(cy[j] - cy[i]);
                 for (int g = 0; g < G; ++g) {
@@ -429,74 +439,115 @@ k_species_model(to_model_args a) {
                     c += seg_cross(x1, y1, x21, y21, x3, y3, x43, y43);
                 }
             }
+            if (j >= i) {
+                cross[(size_t)i * N + j] = c;
+                cross[(size_t)j * N + i] = c;
+            }
         }
-        cross[(size_t)i * N + j] = c;
-        cross[(size_t)j * N + i] = c;
-    }
-    // per-habitat attraction and per-crossing-count survival tables
-    double* s_attr = reinterpret_cast<double*>(par);          // [n_hab]
-    double* s_surv = s_attr + TO_MAX_HAB;                      // [C][G+1]
-    const double lda = S.lambda_mult * S.lambda_sd + S.lambda_mean;
-    for (int h = threadIdx.x; h < S.n_hab; h += blockDim.x)
-        s_attr[h] = exp(S.hab_pref_mean[h] + S.hab_pref_sd[h] * S.hab_pref_mult);
-    for (int q = threadIdx.x; q < a.C * (G + 1); q += blockDim.x) {
-        int c = q / (G + 1), cr = q - c * (G + 1);
-        s_surv[q] = exp(-(double)cr * S.hazard[c]);
+        for (int o = 16; o > 0; o >>= 1) {
+            last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if ((threadIdx.x & 31) == 0) { atomicMax(&s_misc[1], last); atomicAdd(&s_misc[2], cnt); }
     }
     __syncthreads();
-
-    // Transition probabilities (SpeciesRoadPatches.cpp:383-426) and the
-    // migration matrices.  One thread per origin row, j ascending.
-    const double max_dist_t = (a.sem == 0)
-        ? log(0.05) / (-(S.lambda_mean + S.lambda_sd * lda))
-        : log(0.05) / (-lda);
-    const double mt2lo = max_dist_t * max_dist_t * (1.0 - 1e-9);
-    const double mt2hi = max_dist_t * max_dist_t * (1.0 + 1e-9);
+    if (a.sem == 0 && s_misc[1] >= 0 && threadIdx.x == 0) {
+        const int q = s_misc[1], i = q / N, j = q - i * N;
+        cross[(size_t)i * N + j] = 0;
+        cross[(size_t)j * N + i] = 0;
+    }
+    if (threadIdx.x == 0) {
+        int cnt = s_misc[2];
+        a.n_transitions[rs] = (a.sem == 0 && cnt > 0) ? cnt - 1 : cnt;
+    }
+    // zero the migration matrices (destination-major, padded to NP), then
+    // scatter the non-zero entries below
     const int NP = a.npad;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
-    double* tv = a.trans_scratch + (size_t)rs * NM * NM;
-    double* trans = a.trans ? a.trans + (size_t)rs * NM * NM : nullptr;
-    double* surv = a.surv ? a.surv + (size_t)rs * a.C * NM * NM : nullptr;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        double summ = 0.0;
-        for (int j = 0; j < N; ++j) {
-            double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-            double d2 = dx * dx + dy * dy;
-            double v = 0.0;
-            if (within(d2, max_dist_t, mt2lo, mt2hi)) {
-                double w = area[j] * lda * s_attr[ptype[j]];
-                if (i == j) v = w;
-                else {
-                    double d = sqrt(d2);
-                    v = (a.sem == 0) ? w / exp(-lda * d) : w * exp(-lda * d);
-                }
-                summ += v;
-            }
-            tv[(size_t)i * NM + j] = v;
-        }
-        for (int j = 0; j < N; ++j) {
-            double tr = tv[(size_t)i * NM + j] / summ;
-            if (trans) trans[(size_t)i * NM + j] = tr;
-            int cr = cross[(size_t)i * N + j];
-            for (int c = 0; c < a.C; ++c) {
-                double s = s_surv[c * (G + 1) + cr];
-                if (surv) surv[((size_t)c * NM + i) * NM + j] = s;
-                float m = (float)(tr * s);
-                mmm[((size_t)c * NP + j) * NP + i] = ((double)m > 0.00001) ? m : 0.0f;
-            }
-        }
-    }
-    // zero padding of the migration matrices, initial pops and capacities
-    for (int q = threadIdx.x; q < a.C * NP * NP; q += blockDim.x) {
-        int c = q / (NP * NP), r = q - c * NP * NP;
-        int k = r / NP, l = r - k * NP;
-        if (k >= N || l >= N) mmm[((size_t)c * NP + k) * NP + l] = 0.0f;
+    {
+        float4* m4 = reinterpret_cast<float4*>(mmm);
+        const size_t n4 = (size_t)a.C * NP * NP / 4;
+        for (size_t q = threadIdx.x; q < n4; q += blockDim.x) m4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     float* ip = a.init_pops + (size_t)rs * NP;
     float* cp = a.caps + (size_t)rs * NP;
     for (int k = threadIdx.x; k < NP; k += blockDim.x) {
         ip[k] = (k < N) ? (float)popd[k] : 0.0f;
         cp[k] = (k < N) ? (float)cap[k] : 1.0f;
+    }
+    __syncthreads();
+
+    // Transition probabilities (SpeciesRoadPatches.cpp:383-426) and the
+    // migration matrices.  A warp per origin row i: lanes test the
+    // destinations j in parallel, the in-range terms are summed in j order
+    // by one lane (the reference's order), and only non-zero entries are
+    // divided, multiplied by survival and written.
+    const double max_dist_t = (a.sem == 0)
+        ? log(0.05) / (-(S.lambda_mean + S.lambda_sd * lda))
+        : log(0.05) / (-lda);
+    const double mt2 = max_dist_t * max_dist_t;
+    const double mt2lo = mt2 * (1.0 - 1e-9), mt2hi = mt2 * (1.0 + 1e-9);
+    const float ft_lo = (float)(mt2 * (1.0 - 1e-6)), ft_hi = (float)(mt2 * (1.0 + 1e-6));
+    double* trans = a.trans ? a.trans + (size_t)rs * NM * NM : nullptr;
+    double* surv = a.surv ? a.surv + (size_t)rs * a.C * NM * NM : nullptr;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    double* wv = a.trans_scratch + (size_t)rs * NM * NM;        // per-row values, [i][slot]
+    for (int i = warp; i < N; i += nwarp) {
+        double* rowv = wv + (size_t)i * NM;
+        int cnt = 0;
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
+            unsigned m = __ballot_sync(0xffffffffu, inr);
+            if (inr) {
+                double w = area[j] * lda * s_attr[ptype[j]];
+                double v = w;
+                if (i != j) {
+                    double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+                    double d = sqrt(dx * dx + dy * dy);
+                    v = (a.sem == 0) ? w / exp(-lda * d) : w * exp(-lda * d);
+                }
+                rowv[cnt + __popc(m & ((1u << lane) - 1u))] = v;
+            }
+            cnt += __popc(m);
+        }
+        __syncwarp();
+        double summ = 0.0;
+        if (lane == 0)
+            for (int q = 0; q < cnt; ++q) summ += rowv[q];
+        summ = __shfl_sync(0xffffffffu, summ, 0);
+        // second pass: the same in-range set, slot by slot
+        int base = 0;
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
+            unsigned m = __ballot_sync(0xffffffffu, inr);
+            if (inr) {
+                const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))] / summ;
+                const int cr = cross[(size_t)i * N + j];
+                for (int c = 0; c < a.C; ++c) {
+                    float mv = (float)(tr * surv_of(c, cr));
+                    if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
+                }
+                if (trans) trans[(size_t)i * NM + j] = tr;
+            }
+            base += __popc(m);
+        }
+        __syncwarp();
+    }
+    // dense FP64 transition / survival outputs (single-road API only)
+    if (trans || surv) {
+        __syncthreads();
+        for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
+            const int i = q / N, j = q - i * N;
+            if (trans && !in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi))
+                trans[(size_t)i * NM + j] = 0.0;
+            if (surv) {
+                const int cr = cross[(size_t)i * N + j];
+                for (int c = 0; c < a.C; ++c)
+                    surv[((size_t)c * NM + i) * NM + j] = surv_of(c, cr);
+            }
+        }
     }
     if (a.crossings_out) {
         int* co = a.crossings_out + (size_t)rs * NM * NM;
@@ -551,7 +602,13 @@ to_status line_segment_intersect(to_ctx ctx, int T, const double* d_xy1, int G,
 }
 
 to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
-    size_t smem = (size_t)a.W * a.H * sizeof(int) + 64 * sizeof(int);
+    // labels (W*H ints) first; later the same space holds float centroids
+    // and the attraction / survival tables
+    size_t smem = (size_t)a.W * a.H * sizeof(int);
+    const size_t tail = (size_t)2 * a.max_patches * sizeof(float) + 2 * sizeof(float) +
+                        (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
+    if (tail > smem) smem = tail;
+    smem += 64 * sizeof(int);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED,
                             "grid of %d x %d exceeds shared memory", a.W, a.H);
