@@ -20,7 +20,6 @@
 
 namespace {
 
-constexpr int kMaxBlockRegions = 48;   // distinct regions per coarse block
 #define TO_SURV_TABLE_SEGS 255         // survival table by crossing count up to this
 
 __device__ __forceinline__ int uf_find(volatile int* par, int x) {
@@ -82,19 +81,35 @@ __device__ int cta_exclusive_scan(int v, int* s_tmp, int* total) {
 // (par[i] = i for foreground, -1 for background on entry).  On exit par[i]
 // holds the LabelImage number (1.. in raster order of first pixel) or 0.
 // Returns the number of regions.
+//
+// Run-based: a thread per image row points every foreground pixel at the
+// start of its horizontal run; vertical unions are made only where a run
+// pair first touches (the pixel's left neighbour does not already link the
+// same two runs), so the lock-free unions touch run starts only.
 __device__ int cta_label(int n, int W, int* par, int* s_tmp, int* d_flags) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    const int H = n / W;
+    for (int y = tid; y < H; y += nt) {
+        int start = -1;
+        for (int x = 0; x < W; ++x) {
+            const int i = x + y * W;
+            if (par[i] < 0) { start = -1; continue; }
+            if (start < 0) start = i;
+            par[i] = start;
+        }
+    }
+    __syncthreads();
     bool ok = true;
-    for (int i = tid; i < n; i += nt) {
-        if (par[i] < 0) continue;
-        int x = i % W;
-        if (x > 0 && par[i - 1] >= 0) ok &= uf_union(par, i, i - 1);
-        if (i >= W && par[i - W] >= 0) ok &= uf_union(par, i, i - W);
+    for (int i = W + tid; i < n; i += nt) {
+        if (par[i] < 0 || par[i - W] < 0) continue;
+        const int x = i % W;
+        if (x > 0 && par[i - 1] >= 0 && par[i - 1 - W] >= 0) continue;   // same run pair
+        ok &= uf_union(par, par[i], par[i - W]);
     }
     if (!ok && d_flags) atomicExch(d_flags, TO_DEVERR_UNION);
     __syncthreads();
     for (int i = tid; i < n; i += nt)
-        if (par[i] >= 0) par[i] = uf_find(par, i);
+        if (par[i] >= 0) par[i] = uf_find(par, par[i]);
     __syncthreads();
     // rank the roots (root = smallest raster index of its component)
     int chunk = (n + nt - 1) / nt;
@@ -120,110 +135,120 @@ __device__ int cta_label(int n, int W, int* par, int* s_tmp, int* d_flags) {
     return total;
 }
 
-// Patch statistics of one coarse block, scanned in the reference's order
-// (x offset outer, y offset inner), one region list per block.  Writes up
-// to kMaxBlockRegions entries sorted by region number.
-struct BlockPatches {
-    int n;
-    int reg[kMaxBlockRegions];
-    int cnt[kMaxBlockRegions];
-    float pop[kMaxBlockRegions];
-    float sx[kMaxBlockRegions];
-    float sy[kMaxBlockRegions];
-};
-
-template <class LabelFn, class PopFn>
-__device__ bool scan_block(int bx, int by, int W, int H, int skpx, int skpy,
-                           LabelFn lab, PopFn popf, BlockPatches& bp) {
-    int bsx = ((bx + 1) * skpx <= H) ? skpx : H - bx * skpx;
-    int bsy = ((by + 1) * skpy <= W) ? skpy : W - by * skpy;
-    bp.n = 0;
-    bool ok = true;
-    for (int ii = 0; ii < bsx; ++ii)
-        for (int jj = 0; jj < bsy; ++jj) {
-            int xc = bx * skpx + ii, yc = by * skpy + jj;
-            int c = xc + yc * W;
-            int r = lab(c);
-            if (r <= 0) continue;
-            int q = 0;
-            while (q < bp.n && bp.reg[q] != r) ++q;
-            if (q == bp.n) {
-                if (bp.n == kMaxBlockRegions) { ok = false; continue; }
-                bp.reg[q] = r; bp.cnt[q] = 0; bp.pop[q] = 0.0f;
-                bp.sx[q] = 0.0f; bp.sy[q] = 0.0f;
-                bp.n++;
-            }
-            bp.cnt[q] += 1;
-            bp.pop[q] = bp.pop[q] + popf(c);
-            bp.sx[q] = bp.sx[q] + (float)ii;
-            bp.sy[q] = bp.sy[q] + (float)jj;
-        }
-    // insertion sort by region number
-    for (int a = 1; a < bp.n; ++a) {
-        int r = bp.reg[a], c = bp.cnt[a];
-        float p = bp.pop[a], x = bp.sx[a], y = bp.sy[a];
-        int b = a - 1;
-        while (b >= 0 && bp.reg[b] > r) {
-            bp.reg[b + 1] = bp.reg[b]; bp.cnt[b + 1] = bp.cnt[b];
-            bp.pop[b + 1] = bp.pop[b]; bp.sx[b + 1] = bp.sx[b];
-            bp.sy[b + 1] = bp.sy[b];
-            --b;
-        }
-        bp.reg[b + 1] = r; bp.cnt[b + 1] = c; bp.pop[b + 1] = p;
-        bp.sx[b + 1] = x; bp.sy[b + 1] = y;
-    }
-    return ok;
+// Extent of coarse block (bx, by) as patchComputation has it
+// (SimulateGPU.cu:510-520: the x extent is bounded by H and the y extent by W).
+__device__ __forceinline__ void block_extent(int bx, int by, int W, int H, int skpx, int skpy,
+                                             int& bsx, int& bsy) {
+    bsx = ((bx + 1) * skpx <= H) ? skpx : H - bx * skpx;
+    bsy = ((by + 1) * skpy <= W) ? skpy : W - by * skpy;
 }
 
 // Finishes one patch exactly as patchComputation (SimulateGPU.cu:560-563).
-__device__ __forceinline__ void finish_patch(const BlockPatches& bp, int q,
-        int bx, int by, int skpx, int skpy, float xs, float ys, float spa,
-        float maxpop, float out[5]) {
-    float area = (float)bp.cnt[q];
-    float cx = xs * (bp.sx[q] / area + (float)(bx * skpx));
-    float cy = ys * (bp.sy[q] / area + (float)(by * skpy));
+__device__ __forceinline__ void finish_patch(int cnt, float pop, float sx, float sy, int bx,
+        int by, int skpx, int skpy, float xs, float ys, float spa, float maxpop, float out[5]) {
+    float area = (float)cnt;
+    float cx = xs * (sx / area + (float)(bx * skpx));
+    float cy = ys * (sy / area + (float)(by * skpy));
     area = area * spa;
     out[0] = area;
     out[1] = area * maxpop;
-    out[2] = bp.pop[q];
+    out[2] = pop;
     out[3] = cx;
     out[4] = cy;
 }
 
-// All coarse blocks of one labelled image: block b is handled by thread b
-// (serial scan of its cells); a CTA scan orders the output.  Appends to
-// the patch list at *s_count (shared).  Returns false on overflow.
+// In-place exclusive scan of v[0..n) by the whole CTA; returns the total.
+__device__ int cta_scan_array(int* v, int n, int* s_tmp) {
+    const int nt = blockDim.x;
+    const int chunk = (n + nt - 1) / nt;
+    const int lo = threadIdx.x * chunk, hi = min(n, lo + chunk);
+    int sum = 0;
+    for (int i = lo; i < hi; ++i) sum += v[i];
+    int total = 0;
+    int run = cta_exclusive_scan(sum, s_tmp, &total);
+    for (int i = lo; i < hi; ++i) { int c = v[i]; v[i] = run; run += c; }
+    __syncthreads();
+    return total;
+}
+
+// Patches of one labelled image: every (coarse block, region) pair in block
+// order (b = by * xres + bx), regions ascending within a block - the order
+// the reference compacts them in.  A warp per block lists its distinct
+// regions (counted first, then written at scanned offsets); then a thread
+// per (block, region) accumulates count, population and centroid sums over
+// the block's cells in the reference's order (x offset outer, y offset
+// inner), so the float sums match it bit for bit.  Appends to the patch
+// list at *s_count (shared).  s_list: nblocks + 1 + max_out ints of shared
+// memory.  Returns false on overflow.
 template <class LabelFn, class PopFn, class Emit>
-__device__ bool cta_block_patches(int W, int H, int skpx, int skpy, int xres,
-                                  int yres, int max_out, int* s_count,
-                                  int* s_tmp, LabelFn lab, PopFn popf,
-                                  Emit emit) {
-    int nblocks = xres * yres;
-    bool ok = true;
-    for (int b0 = 0; b0 < nblocks; b0 += blockDim.x) {
-        int b = b0 + threadIdx.x;
-        BlockPatches bp;
-        bp.n = 0;
-        if (b < nblocks) {
-            int by = b / xres, bx = b - by * xres;
-            ok &= scan_block(bx, by, W, H, skpx, skpy, lab, popf, bp);
-        }
-        int total = 0;
-        int off = cta_exclusive_scan(bp.n, s_tmp, &total);
-        int base = *s_count;
-        if (b < nblocks) {
-            int by = b / xres, bx = b - by * xres;
-            for (int q = 0; q < bp.n; ++q) {
-                int o = base + off + q;
-                if (o < max_out) emit(o, bp, q, bx, by);
+__device__ bool cta_block_patches(int W, int H, int skpx, int skpy, int xres, int yres,
+                                  int max_out, int* s_count, int* s_tmp, int* s_list,
+                                  LabelFn lab, PopFn popf, Emit emit) {
+    const int nblocks = xres * yres;
+    int* s_off = s_list;                  // [nblocks + 1]
+    int* s_lab = s_list + nblocks + 1;    // [max_out]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int base = *s_count;
+    const int room = max_out - base;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int b = warp; b < nblocks; b += nw) {
+            const int by = b / xres, bx = b - by * xres;
+            int bsx, bsy;
+            block_extent(bx, by, W, H, skpx, skpy, bsx, bsy);
+            const int ncell = (bsx > 0 && bsy > 0) ? bsx * bsy : 0;
+            const int out = pass ? s_off[b] : 0;
+            int lastr = 0, cnt = 0;
+            for (;;) {
+                int mn = 0x7fffffff;
+                for (int e = lane; e < ncell; e += 32) {
+                    const int ii = e / bsy, jj = e - ii * bsy;
+                    const int r = lab((bx * skpx + ii) + (by * skpy + jj) * W);
+                    if (r > lastr && r < mn) mn = r;
+                }
+                mn = __reduce_min_sync(0xffffffffu, mn);
+                if (mn == 0x7fffffff) break;
+                if (pass && lane == 0 && out + cnt < room) s_lab[out + cnt] = mn;
+                ++cnt;
+                lastr = mn;
             }
+            if (!pass && lane == 0) s_off[b] = cnt;
         }
         __syncthreads();
-        if (threadIdx.x == 0) *s_count = base + total;
-        __syncthreads();
+        if (!pass) {
+            const int total = cta_scan_array(s_off, nblocks, s_tmp);
+            if (threadIdx.x == 0) s_off[nblocks] = total;
+            __syncthreads();
+        }
     }
-    if (*s_count > max_out) ok = false;
-    return ok;
+    const int total = s_off[nblocks];
+    const int nemit = min(total, room > 0 ? room : 0);
+    for (int t = threadIdx.x; t < nemit; t += blockDim.x) {
+        int lo = 0, hi = nblocks;                 // block: last b with s_off[b] <= t
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_off[mid] <= t) lo = mid; else hi = mid;
+        }
+        const int b = lo, by = b / xres, bx = b - by * xres;
+        int bsx, bsy;
+        block_extent(bx, by, W, H, skpx, skpy, bsx, bsy);
+        const int r = s_lab[t];
+        int cnt = 0;
+        float pop = 0.0f, sx = 0.0f, sy = 0.0f;
+        for (int ii = 0; ii < bsx; ++ii)
+            for (int jj = 0; jj < bsy; ++jj) {
+                const int c = (bx * skpx + ii) + (by * skpy + jj) * W;
+                if (lab(c) != r) continue;
+                cnt += 1;
+                pop = pop + popf(c);
+                sx = sx + (float)ii;
+                sy = sy + (float)jj;
+            }
+        emit(base + t, cnt, pop, sx, sy, bx, by);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *s_count = base + total;
+    __syncthreads();
+    return base + total <= max_out;
 }
 
 // ---- kernels ---------------------------------------------------------------
@@ -249,22 +274,21 @@ __global__ void k_build_patches(int W, int H, int skpx, int skpy, int xres,
                                 const float* __restrict__ pops, int max_out,
                                 double* __restrict__ out5, int* count,
                                 int* d_flags) {
+    extern __shared__ int s_list[];
     __shared__ int s_tmp[33];
     __shared__ int s_count;
     if (threadIdx.x == 0) s_count = *count;
     __syncthreads();
-    int start = s_count;
     auto lab = [&](int c) { return labels[c]; };
     auto popf = [&](int c) { return pops[c]; };
-    auto emit = [&](int o, const BlockPatches& bp, int q, int bx, int by) {
+    auto emit = [&](int o, int cnt, float pop, float sx, float sy, int bx, int by) {
         float v[5];
-        finish_patch(bp, q, bx, by, skpx, skpy, xs, ys, spa, maxpop, v);
+        finish_patch(cnt, pop, sx, sy, bx, by, skpx, skpy, xs, ys, spa, maxpop, v);
         for (int f = 0; f < 5; ++f) out5[5 * (size_t)o + f] = (double)v[f];
     };
-    bool ok = cta_block_patches(W, H, skpx, skpy, xres, yres, max_out,
-                                &s_count, s_tmp, lab, popf, emit);
+    bool ok = cta_block_patches(W, H, skpx, skpy, xres, yres, max_out, &s_count, s_tmp,
+                                s_list, lab, popf, emit);
     if (!ok && d_flags) atomicExch(d_flags, TO_DEVERR_PATCHES);
-    (void)start;
     if (threadIdx.x == 0) *count = min(s_count, max_out);
 }
 
@@ -325,6 +349,7 @@ k_species_model(to_model_args a) {
     int* s_tmp = smem;                         // 33 ints
     int* s_misc = s_tmp + 40;                  // counters
     int* par = smem + 64;                      // labels, later tables (8-byte aligned)
+    int* s_list = par + (size_t)((a.W * a.H + 1) & ~1);   // block region lists
     const int* hab = a.hab_map;
     const int c0 = a.cell_off ? a.cell_off[road] : 0;
     const int c1 = a.cell_off ? a.cell_off[road + 1] : 0;
@@ -352,13 +377,11 @@ k_species_model(to_model_args a) {
         int nreg = cta_label(n, W, par, s_tmp, a.d_flags);
         if (nreg == 0) continue;
         float maxpop = (float)S.hab_max_pop[h];
-        int before = s_misc[0];
         auto lab = [&](int c) { return par[c]; };
         auto popf = [&](int c) { return popmap[c]; };
-        auto emit = [&](int o, const BlockPatches& bp, int q, int bx, int by) {
+        auto emit = [&](int o, int cnt, float pop, float sx, float sy, int bx, int by) {
             float v[5];
-            finish_patch(bp, q, bx, by, a.skpx, a.skpy, a.xs, a.ys, a.spa,
-                         maxpop, v);
+            finish_patch(cnt, pop, sx, sy, bx, by, a.skpx, a.skpy, a.xs, a.ys, a.spa, maxpop, v);
             area[o] = (double)v[0];
             cap[o] = (double)v[1];
             popd[o] = (double)v[2];
@@ -366,9 +389,8 @@ k_species_model(to_model_args a) {
             cy[o] = (double)v[4];
             ptype[o] = h;
         };
-        ok &= cta_block_patches(W, H, a.skpx, a.skpy, a.xres, a.yres, NM,
-                                &s_misc[0], s_tmp, lab, popf, emit);
-        (void)before;
+        ok &= cta_block_patches(W, H, a.skpx, a.skpy, a.xres, a.yres, NM, &s_misc[0], s_tmp,
+                                s_list, lab, popf, emit);
         __syncthreads();
     }
     if (!ok && a.d_flags) atomicExch(a.d_flags, TO_DEVERR_PATCHES);
@@ -581,7 +603,13 @@ to_status build_patches(to_ctx ctx, int W, int H, int skpx, int skpy, int xres,
                         float maxpop, const int* d_labels, const float* d_pops,
                         int max_patches, double* d_out5, int* d_count) {
     (void)nreg;
-    k_build_patches<<<1, 256, 0, ctx->stream>>>(W, H, skpx, skpy, xres, yres,
+    const size_t smem = (size_t)(xres * yres + 1 + max_patches) * sizeof(int);
+    if (smem > ctx->smem_optin)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d blocks, %d patches exceed shared memory",
+                            xres * yres, max_patches);
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_build_patches,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_build_patches<<<1, 256, smem, ctx->stream>>>(W, H, skpx, skpy, xres, yres,
         xs, ys, spa, maxpop, d_labels, d_pops, max_patches, d_out5, d_count,
         ctx->d_flags);
     TO_LAUNCHED(ctx);
@@ -608,6 +636,7 @@ to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
     const size_t tail = (size_t)2 * a.max_patches * sizeof(float) + 2 * sizeof(float) +
                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
     if (tail > smem) smem = tail;
+    smem = ((smem + 7) & ~(size_t)7) + (size_t)(a.xres * a.yres + 1 + a.max_patches) * sizeof(int);
     smem += 64 * sizeof(int);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED,
