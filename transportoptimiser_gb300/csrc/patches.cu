@@ -341,7 +341,7 @@ __device__ __forceinline__ bool within(double d2, double md, double md2lo, doubl
 
 // One CTA per (road, species): the whole species-road model.
 __global__ void __launch_bounds__(1024)
-k_species_model(to_model_args a) {
+k_species_patches(to_model_args a) {
     extern __shared__ int smem[];
     const int rs = blockIdx.x;                 // road*S + species
     const int road = rs / a.S, sp = rs - road * a.S;
@@ -397,10 +397,29 @@ k_species_model(to_model_args a) {
     __syncthreads();
     const int N = min(s_misc[0], NM);
     if (threadIdx.x == 0) a.n_patches[rs] = N;
-    __threadfence_block();
-    __syncthreads();
+}
 
-    // Distances and the crossing pair filter (SpeciesRoadPatches.cpp:270-381).
+// Second half of the species-road model, one CTA per (road, species):
+// patch-pair distances, road crossings, transition and survival
+// probabilities and the migration matrices.  Small shared memory, so two
+// CTAs share an SM and the FP64-bound transition rows of one overlap the
+// integer work of the other.
+__global__ void __launch_bounds__(512, 2)
+k_species_links(to_model_args a) {
+    extern __shared__ __align__(16) unsigned char sml[];
+    __shared__ int s_last, s_cnt, s_npair;
+    const int rs = blockIdx.x;
+    const int road = rs / a.S, sp = rs - road * a.S;
+    const to_model_species& S = a.species[sp];
+    const int NM = a.max_patches;
+    const int N = a.n_patches[rs];
+    const double* area = a.area + (size_t)rs * NM;
+    const double* cap = a.cap + (size_t)rs * NM;
+    const double* popd = a.pop + (size_t)rs * NM;
+    const double* cx = a.cx + (size_t)rs * NM;
+    const double* cy = a.cy + (size_t)rs * NM;
+    const int* ptype = a.type + (size_t)rs * NM;
+
     // FP64 is scarce on this part, so every distance test is first decided
     // on a float d^2 (centroids are floats, so its relative error is below
     // 4e-7); only pairs within 1e-6 of a cut-off take the exact FP64 test.
@@ -410,80 +429,44 @@ k_species_model(to_model_args a) {
     const double mx2lo = mx2 * (1.0 - 1e-9), mx2hi = mx2 * (1.0 + 1e-9);
     const float fx_lo = (float)(mx2 * (1.0 - 1e-6)), fx_hi = (float)(mx2 * (1.0 + 1e-6));
     int* cross = a.crossings_scratch + (size_t)rs * NM * NM;
-    float* cxf = reinterpret_cast<float*>(par);                // [N]
-    float* cyf = cxf + NM;                                      // [N]
-    double* s_attr = reinterpret_cast<double*>(cyf + NM + 2);   // [n_hab] (8-byte aligned)
-    double* s_surv = s_attr + TO_MAX_HAB;                       // [C][G+1]
     const int G = a.seg_off[road + 1] - a.seg_off[road];
     const double* rseg = a.segs + (size_t)a.seg_off[road] * 4;
+    const bool seg_tab = G <= TO_SURV_TABLE_SEGS;
+    constexpr int SC = TO_SURV_TABLE_SEGS;
+    float* cxf = reinterpret_cast<float*>(sml);                 // [NM]
+    float* cyf = cxf + NM;                                      // [NM]
+    float* sgf = cyf + NM;                                      // [4][SC]
+    double* s_attr = reinterpret_cast<double*>(sgf + 4 * SC);   // [TO_MAX_HAB]
+    double* s_surv = s_attr + TO_MAX_HAB;                       // [C][G+1]
     const double lda = S.lambda_mult * S.lambda_sd + S.lambda_mean;
     for (int k = threadIdx.x; k < N; k += blockDim.x) { cxf[k] = (float)cx[k]; cyf[k] = (float)cy[k]; }
+    if (seg_tab)
+        for (int g = threadIdx.x; g < G; g += blockDim.x) {
+            const double* sg = rseg + 4 * g;
+            sgf[g] = (float)sg[0];
+            sgf[SC + g] = (float)sg[1];
+            sgf[2 * SC + g] = (float)(sg[2] - sg[0]);
+            sgf[3 * SC + g] = (float)(sg[3] - sg[1]);
+        }
     for (int h = threadIdx.x; h < S.n_hab; h += blockDim.x)
         s_attr[h] = exp(S.hab_pref_mean[h] + S.hab_pref_sd[h] * S.hab_pref_mult);
-    const bool surv_tab = G <= TO_SURV_TABLE_SEGS;
-    if (surv_tab)
+    if (seg_tab)
         for (int q = threadIdx.x; q < a.C * (G + 1); q += blockDim.x) {
             int c = q / (G + 1), cr = q - c * (G + 1);
             s_surv[q] = exp(-(double)cr * S.hazard[c]);
         }
     auto surv_of = [&](int c, int cr) {
-        return surv_tab ? s_surv[c * (G + 1) + cr] : exp(-(double)cr * S.hazard[c]);
+        return seg_tab ? s_surv[c * (G + 1) + cr] : exp(-(double)cr * S.hazard[c]);
     };
-    if (threadIdx.x == 0) s_misc[2] = 0;
-    __syncthreads();
-    auto in_range = [&](int i, int j, float flo, float fhi, double md, double lo2, double hi2) {
-        float dxf = cxf[i] - cxf[j], dyf = cyf[i] - cyf[j];
-        float d2f = dxf * dxf + dyf * dyf;
-        if (d2f < flo) return true;
-        if (d2f > fhi) return false;
-        double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-        return within(dx * dx + dy * dy, md, lo2, hi2);
-    };
+    if (threadIdx.x == 0) { s_last = -1; s_cnt = 0; s_npair = 0; }
+    // zero the crossing counts and the migration matrices (destination-major,
+    // padded to NP); initial populations and capacities
     {
-        // one pass over i < j: count valid pairs, note the last one (the
-        // reference never tests its last valid pair: its counter starts at
-        // -1) and count road crossings of every valid pair in float
-        int last = -1, cnt = 0;
-        for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
-            int i = q / N, j = q - i * N;
-            int c = 0;
-            if (j > i && in_range(i, j, fx_lo, fx_hi, max_dist_x, mx2lo, mx2hi)) {
-                last = max(last, q);
-                ++cnt;
-                float x1 = cxf[i], y1 = cyf[i];
-                float x21 = (float)(cx[j] - cx[i]);
-                float y21 = (float)(cy[j] - cy[i]);
-                for (int g = 0; g < G; ++g) {
-                    const double* sg = rseg + 4 * g;
-                    float x3 = (float)sg[0], y3 = (float)sg[1];
-                    float x43 = (float)(sg[2] - sg[0]);
-                    float y43 = (float)(sg[3] - sg[1]);
-                    c += seg_cross(x1, y1, x21, y21, x3, y3, x43, y43);
-                }
-            }
-            if (j >= i) {
-                cross[(size_t)i * N + j] = c;
-                cross[(size_t)j * N + i] = c;
-            }
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
-            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        }
-        if ((threadIdx.x & 31) == 0) { atomicMax(&s_misc[1], last); atomicAdd(&s_misc[2], cnt); }
+        int4* c4 = reinterpret_cast<int4*>(cross);
+        const int n4 = (N * N) / 4;
+        for (int q = threadIdx.x; q < n4; q += blockDim.x) c4[q] = make_int4(0, 0, 0, 0);
+        for (int q = n4 * 4 + threadIdx.x; q < N * N; q += blockDim.x) cross[q] = 0;
     }
-    __syncthreads();
-    if (a.sem == 0 && s_misc[1] >= 0 && threadIdx.x == 0) {
-        const int q = s_misc[1], i = q / N, j = q - i * N;
-        cross[(size_t)i * N + j] = 0;
-        cross[(size_t)j * N + i] = 0;
-    }
-    if (threadIdx.x == 0) {
-        int cnt = s_misc[2];
-        a.n_transitions[rs] = (a.sem == 0 && cnt > 0) ? cnt - 1 : cnt;
-    }
-    // zero the migration matrices (destination-major, padded to NP), then
-    // scatter the non-zero entries below
     const int NP = a.npad;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
     {
@@ -496,6 +479,72 @@ k_species_model(to_model_args a) {
     for (int k = threadIdx.x; k < NP; k += blockDim.x) {
         ip[k] = (k < N) ? (float)popd[k] : 0.0f;
         cp[k] = (k < N) ? (float)cap[k] : 1.0f;
+    }
+    __syncthreads();
+    auto in_range = [&](int i, int j, float flo, float fhi, double md, double lo2, double hi2) {
+        float dxf = cxf[i] - cxf[j], dyf = cyf[i] - cyf[j];
+        float d2f = dxf * dxf + dyf * dyf;
+        if (d2f < flo) return true;
+        if (d2f > fhi) return false;
+        double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+        return within(dx * dx + dy * dy, md, lo2, hi2);
+    };
+    // pass 1: valid pairs i < j (within the crossing distance) into a list;
+    // the reference never tests its last valid pair (its counter starts at
+    // -1), so the largest valid pair index is noted too
+    int* plist = reinterpret_cast<int*>(a.trans_scratch + (size_t)rs * NM * NM);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    {
+        int last = -1, cnt = 0;
+        const int npair = N * N;
+        for (int q0 = warp * 32; q0 < npair; q0 += blockDim.x) {
+            const int q = q0 + lane;
+            const int i = q / N, j = q - i * N;
+            const bool v = q < npair && j > i && in_range(i, j, fx_lo, fx_hi, max_dist_x, mx2lo, mx2hi);
+            const unsigned m = __ballot_sync(0xffffffffu, v);
+            int pos = 0;
+            if (lane == 0 && m) pos = atomicAdd(&s_npair, __popc(m));
+            pos = __shfl_sync(0xffffffffu, pos, 0);
+            if (v) {
+                plist[pos + __popc(m & ((1u << lane) - 1u))] = q;
+                last = max(last, q);
+                ++cnt;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) { atomicMax(&s_last, last); atomicAdd(&s_cnt, cnt); }
+    }
+    __syncthreads();
+    // pass 2: road crossings of the listed pairs in float without
+    // contraction (pathAdjacencyKernel, SimulateGPU.cu:454-493)
+    const int last_pair = (a.sem == 0) ? s_last : -1;
+    for (int t = threadIdx.x; t < s_npair; t += blockDim.x) {
+        const int q = plist[t];
+        if (q == last_pair) continue;
+        const int i = q / N, j = q - i * N;
+        const float x1 = cxf[i], y1 = cyf[i];
+        const float x21 = cxf[j] - cxf[i];       // = (float)(cx[j] - cx[i]): one rounding
+        const float y21 = cyf[j] - cyf[i];
+        int c = 0;
+        if (seg_tab) {
+            for (int g = 0; g < G; ++g)
+                c += seg_cross(x1, y1, x21, y21, sgf[g], sgf[SC + g], sgf[2 * SC + g], sgf[3 * SC + g]);
+        } else {
+            for (int g = 0; g < G; ++g) {
+                const double* sg = rseg + 4 * g;
+                c += seg_cross(x1, y1, x21, y21, (float)sg[0], (float)sg[1],
+                               (float)(sg[2] - sg[0]), (float)(sg[3] - sg[1]));
+            }
+        }
+        cross[(size_t)i * N + j] = c;
+        cross[(size_t)j * N + i] = c;
+    }
+    if (threadIdx.x == 0) {
+        const int cnt = s_cnt;
+        a.n_transitions[rs] = (a.sem == 0 && cnt > 0) ? cnt - 1 : cnt;
     }
     __syncthreads();
 
@@ -512,7 +561,6 @@ k_species_model(to_model_args a) {
     const float ft_lo = (float)(mt2 * (1.0 - 1e-6)), ft_hi = (float)(mt2 * (1.0 + 1e-6));
     double* trans = a.trans ? a.trans + (size_t)rs * NM * NM : nullptr;
     double* surv = a.surv ? a.surv + (size_t)rs * a.C * NM * NM : nullptr;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     double* wv = a.trans_scratch + (size_t)rs * NM * NM;        // per-row values, [i][slot]
     for (int i = warp; i < N; i += nwarp) {
         double* rowv = wv + (size_t)i * NM;
@@ -572,6 +620,7 @@ k_species_model(to_model_args a) {
         }
     }
     if (a.crossings_out) {
+        __syncthreads();
         int* co = a.crossings_out + (size_t)rs * NM * NM;
         for (int q = threadIdx.x; q < N * N; q += blockDim.x) {
             int i = q / N, j = q - i * N;
@@ -630,21 +679,28 @@ to_status line_segment_intersect(to_ctx ctx, int T, const double* d_xy1, int G,
 }
 
 to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
-    // labels (W*H ints) first; later the same space holds float centroids
-    // and the attraction / survival tables
+    // patches: labels (W*H ints) and the block region lists in shared memory
     size_t smem = (size_t)a.W * a.H * sizeof(int);
-    const size_t tail = (size_t)2 * a.max_patches * sizeof(float) + 2 * sizeof(float) +
-                        (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
-    if (tail > smem) smem = tail;
     smem = ((smem + 7) & ~(size_t)7) + (size_t)(a.xres * a.yres + 1 + a.max_patches) * sizeof(int);
     smem += 64 * sizeof(int);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED,
                             "grid of %d x %d exceeds shared memory", a.W, a.H);
-    TO_CUDA(ctx, cudaFuncSetAttribute(k_species_model,
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_species_patches,
                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // links: float centroids, segment and survival tables
+    const size_t smem2 = (size_t)2 * a.max_patches * sizeof(float) +
+                         (size_t)4 * TO_SURV_TABLE_SEGS * sizeof(float) +
+                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
+    if (smem2 > ctx->smem_optin)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d patches exceed shared memory",
+                            a.max_patches);
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_species_links,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
     to_prof_begin(ctx, "species_model");
-    k_species_model<<<n_rs, 1024, smem, ctx->stream>>>(a);
+    k_species_patches<<<n_rs, 1024, smem, ctx->stream>>>(a);
+    TO_LAUNCHED(ctx);
+    k_species_links<<<n_rs, 512, smem2, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;
