@@ -347,8 +347,16 @@ typedef struct {
     uint64_t seed;
     int road0;               /* stream id of the first road                    */
     int sem;
-    int migration;           /* to_migration                                   */
+    int migration;           /* to_migration; TO_MIG_AUTO = autotuned          */
+    int graph;               /* 1: capture the generation as a CUDA graph and
+                                replay it while the calls match (same roads
+                                pointers and options, shapes within the plan) */
 } to_eval_opts;
+
+/* The autotuner's record: one line per tuned shape, "kind ne paths rs ->
+ * choice (sparse ms, simt ms, tc ms)", -1 where a kernel was not feasible.
+ * Writes at most len bytes (NUL-terminated); returns the number of lines. */
+int to_ctx_tuning(to_ctx ctx, char* buf, int len);
 
 /* result block per (road, species), TO_RESULT_STRIDE doubles:
  *   0 n_patches, 1 n_transitions, 2 mte mean, 3 mte sd, 4 mte se,

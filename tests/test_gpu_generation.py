@@ -46,3 +46,46 @@ def test_generation_three_species_grid(ctx):
             assert int(res[r, s, 0]) == m["N"]
             assert int(res[r, s, 1]) == m["n_transitions"]
     gen.close()
+
+
+def test_autotuner_records_choice_and_matches_that_kernel(ctx):
+    from transportoptimiser_gb300._capi import MIG_TC_3XTF32
+    sc = synth.generation(2, n_roads=8)
+    gen = Generation(sc, max_roads=8, max_patches=512, ctx=ctx)
+    packed = pack_roads(sc, sc.roads)
+    auto = gen.evaluate(packed, gen.opts(64, 20, seed=4, migration=MIG_AUTO))
+    lines = [l for l in ctx.tuning().splitlines() if l.startswith("generation") and "paths=64" in l]
+    assert lines, ctx.tuning()
+    chosen = lines[-1].split("-> ")[1].split()[0]
+    mig = {"sparse": MIG_SPARSE_FP32, "simt": MIG_SIMT_FP32, "tc": MIG_TC_3XTF32}[chosen]
+    ref = gen.evaluate(packed, gen.opts(64, 20, seed=4, migration=mig))
+    np.testing.assert_array_equal(auto[:, :, :7], ref[:, :, :7])
+    gen.close()
+
+
+def test_graph_replay_matches_direct_and_replans(ctx):
+    sc = synth.generation(3, n_roads=48)
+    gen = Generation(sc, max_roads=16, max_patches=512, ctx=ctx)
+    # patch counts of every road (direct path), to build two generations
+    # whose second one exceeds the plan captured on the first
+    nmax = []
+    for r0 in range(0, 48, 16):
+        res = gen.evaluate(pack_roads(sc, sc.roads[r0:r0 + 16]), gen.opts(32, 5, seed=1))
+        nmax += list(res[:, :, 0].max(axis=1))
+    order = np.argsort(nmax)
+    small = [sc.roads[i] for i in order[:16]]
+    big = [sc.roads[i] for i in order[-16:]]
+    assert max(nmax) > sorted(nmax)[15] + 16, "need a generation beyond the plan margin"
+    for roads in (small, big):
+        packed = pack_roads(sc, roads)
+        direct = gen.evaluate(packed, gen.opts(64, 30, seed=7))
+        g1 = gen.evaluate(packed, gen.opts(64, 30, seed=7, graph=True))
+        g2 = gen.evaluate(packed, gen.opts(64, 30, seed=7, graph=True))
+        np.testing.assert_array_equal(g1, direct)
+        np.testing.assert_array_equal(g2, direct)
+    # replay of the first generation's graph on the second generation's roads
+    packed_s, packed_b = pack_roads(sc, small), pack_roads(sc, big)
+    gen.evaluate(packed_s, gen.opts(64, 30, seed=7, graph=True))      # capture on small
+    out = gen.evaluate(packed_b, gen.opts(64, 30, seed=7, graph=True))  # violates, re-plans
+    np.testing.assert_array_equal(out, gen.evaluate(packed_b, gen.opts(64, 30, seed=7)))
+    gen.close()

@@ -102,7 +102,7 @@ class Scene(C.Structure):
 class EvalOpts(C.Structure):
     _fields_ = [("mte_paths", C.c_int), ("n_years", C.c_int), ("dt", C.c_float),
                 ("seed", C.c_uint64), ("road0", C.c_int), ("sem", C.c_int),
-                ("migration", C.c_int)]
+                ("migration", C.c_int), ("graph", C.c_int)]
 
 
 RESULT_STRIDE = 8
@@ -174,6 +174,7 @@ SIGNATURES = {
     "to_evaluate_roads_d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
+    "to_ctx_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
     "to_mlp_predict": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p]),
     "to_mlp_predict_d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "to_mlp_grad": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p,
@@ -252,6 +253,12 @@ class Context:
         self.check(self.lib.to_ctx_kernel_time(self.handle, name.encode(), C.byref(ms),
                                                C.byref(n)), "to_ctx_kernel_time")
         return ms.value, n.value
+
+    def tuning(self) -> str:
+        """The autotuner's record of measured migration-kernel choices."""
+        buf = C.create_string_buffer(8192)
+        self.lib.to_ctx_tuning(self.handle, buf, len(buf))
+        return buf.value.decode()
 
     def close(self) -> None:
         if getattr(self, "handle", None):

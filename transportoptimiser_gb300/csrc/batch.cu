@@ -10,6 +10,14 @@
 //   2. one read of the largest patch count (the only host round trip);
 //   3. one launch over (path tile, road*species): every road's Monte Carlo;
 //   4. one launch: FP64 statistics per (road, species).
+// The migration kernel (sparse, dense SIMT or tensor-core 3xTF32) is chosen
+// by an autotuner that times the feasible ones on the first generation of
+// a shape and keeps the fastest (to_ctx_tuning reports the choices).  With
+// opts.graph the whole generation is captured once as a CUDA graph, with
+// the shapes planned from the previous generation plus a margin, and
+// replayed without any host round trip; kernels that meet a road outside
+// the plan write NaN and raise a flag, and the host entry point then
+// re-plans and re-runs.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -46,9 +54,19 @@ struct to_gen_s {
     double* d_stats;                     // [RS][5]
     double* d_results;                   // [RS][8]
     to_csc csc;                          // [RS*C] packed migration matrices
+    // captured generation (opts.graph)
+    cudaGraphExec_t exec = nullptr;
+    uint64_t graph_key = 0;
+    int plan_ne = 0, plan_cap = 0, plan_choice = -1;
 };
 
 namespace {
+
+inline uint32_t __float_as_uint_host(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    return u;
+}
 
 __global__ void k_pack_results(int n_rs, const int* __restrict__ np,
                                const int* __restrict__ nt,
@@ -105,27 +123,119 @@ T* carve(char*& p, size_t n) {
     return r;
 }
 
-to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
-                   const int* cells, const int* seg_off, const double* segs,
-                   const to_eval_opts* o, double* d_results_out) {
-    const int S = g->S, RS = R * S, NM = g->NM, NP = g->NP;
-    to_model_args a;
+enum { CH_SPARSE = 0, CH_SIMT = 1, CH_TC = 2 };
+
+uint64_t mix(uint64_t h, uint64_t v) {
+    h ^= v + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    return h;
+}
+
+void model_args(to_gen g, int R, const int* cell_off, const int* cells, const int* seg_off,
+                const double* segs, const to_eval_opts* o, to_ctx ctx, to_model_args& a) {
     memset(&a, 0, sizeof(a));
-    a.W = g->W; a.H = g->H; a.S = S; a.C = g->C;
+    a.W = g->W; a.H = g->H; a.S = g->S; a.C = g->C;
     a.skpx = g->skpx; a.skpy = g->skpy; a.xres = g->xres; a.yres = g->yres;
     a.xs = g->xs; a.ys = g->ys; a.spa = g->spa;
     a.hab_map = g->d_base; a.cell_off = cell_off; a.cells = cells;
     a.pop_map = g->d_popmap; a.species = g->d_species;
     a.seg_off = seg_off; a.segs = segs;
-    a.sem = o->sem; a.max_patches = NM; a.npad = NP;
+    a.sem = o->sem; a.max_patches = g->NM; a.npad = g->NP;
     a.n_patches = g->d_np; a.n_transitions = g->d_nt;
     a.area = g->d_area; a.cap = g->d_cap; a.pop = g->d_pop;
     a.cx = g->d_cx; a.cy = g->d_cy; a.type = g->d_type;
     a.crossings_scratch = g->d_cross; a.trans_scratch = g->d_tv;
     a.mmm = g->d_mmm; a.init_pops = g->d_ip; a.caps = g->d_cp;
     a.d_flags = ctx->d_flags;
-    TO_TRY(to_k::species_model(ctx, a, RS));
+}
 
+to_status grow_end(to_ctx ctx, to_gen g, size_t n) {
+    if (n > g->end_cap) {
+        if (g->d_end) TO_CUDA(ctx, cudaFree(g->d_end));
+        g->d_end = nullptr;
+        TO_CUDA(ctx, cudaMalloc(&g->d_end, n * sizeof(float)));
+        g->end_cap = n;
+    }
+    return TO_OK;
+}
+
+to_mte_args mte_args(to_ctx ctx, to_gen g, const to_eval_opts* o, int NE) {
+    to_mte_args m;
+    memset(&m, 0, sizeof(m));
+    m.n_paths = o->mte_paths; m.n_years = o->n_years; m.S = g->S; m.C = g->C;
+    m.c_use = g->C - 1;
+    m.dt = o->dt; m.seed = o->seed; m.sem = o->sem; m.road0 = o->road0;
+    m.npad = g->NP; m.npe = NE; m.n_patches = g->d_np; m.mmm = g->d_mmm;
+    m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
+    m.end_pops = g->d_end; m.flags = ctx->d_flags;
+    return m;
+}
+
+to_status run_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice) {
+    if (choice == CH_SPARSE) return to_k::mte_sparse(ctx, m, RS, g->csc);
+    if (choice == CH_TC) return to_k::mte_tc(ctx, m, RS);
+    return to_k::mte_simt(ctx, m, RS);
+}
+
+// The launches after the model: migration Monte Carlo, statistics, results.
+to_status tail(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice,
+               double* d_results_out) {
+    TO_TRY(run_choice(ctx, g, m, RS, choice));
+    TO_TRY(to_k::mte_stats(ctx, m, RS, g->d_stats));
+    k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(
+        RS, g->d_np, g->d_nt, g->d_stats, choice == CH_SPARSE ? g->csc.nnz : nullptr, g->C,
+        d_results_out);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+// Autotuner: time each feasible migration kernel once on this generation
+// (CUDA events on the context stream) and keep the fastest for the shape.
+to_status tuned_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int NE,
+                       bool sparse_ok, bool tc_ok, int* choice) {
+    const uint64_t key = mix(mix(mix(mix(0, 0), (uint64_t)NE), (uint64_t)m.n_paths),
+                             mix((uint64_t)RS, (uint64_t)m.n_years * 2 + (sparse_ok ? 1 : 0)));
+    for (const auto& e : ctx->tune)
+        if (e.key == key && e.kind == 0) { *choice = e.choice; return TO_OK; }
+    to_ctx_s::tune_entry te;
+    te.key = key; te.kind = 0; te.ne = NE; te.paths = m.n_paths; te.n_rs = RS;
+    te.ms[0] = te.ms[1] = te.ms[2] = -1.0f;
+    cudaEvent_t e0, e1;
+    TO_CUDA(ctx, cudaEventCreate(&e0));
+    TO_CUDA(ctx, cudaEventCreate(&e1));
+    int best = -1, last = -1;
+    const bool feas[3] = {sparse_ok, true, tc_ok};
+    for (int c = 0; c < 3; ++c) {
+        if (!feas[c]) continue;
+        TO_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        to_status st = run_choice(ctx, g, m, RS, c);
+        TO_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        TO_CUDA(ctx, cudaEventSynchronize(e1));
+        if (st != TO_OK) continue;
+        float ms = 0.0f;
+        TO_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        te.ms[c] = ms;
+        last = c;
+        if (best < 0 || ms < te.ms[best]) best = c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best < 0) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "no feasible migration kernel");
+    te.choice = best;
+    ctx->tune.push_back(te);
+    (void)last;
+    *choice = best;
+    return TO_OK;
+}
+
+// Direct (planning) evaluation: model, one read of the shapes, chosen
+// migration kernel.  Fills the plan when asked.
+to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
+                          const int* cells, const int* seg_off, const double* segs,
+                          const to_eval_opts* o, double* d_results_out, int* plan) {
+    const int S = g->S, RS = R * S, NP = g->NP;
+    to_model_args a;
+    model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
+    TO_TRY(to_k::species_model(ctx, a, RS));
     // the widest species model decides the tile shape of the path kernel
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
     k_max_int<<<1, 1024, 0, ctx->stream>>>(RS, g->d_np, d_max);
@@ -142,38 +252,84 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     int maxN = mm[0];
     if (maxN <= 0) maxN = 4;
-    int NE = (maxN + 3) & ~3;
+    const int NE = (maxN + 3) & ~3;
     g->csc.cap_smem = (mm[2] + 7) & ~7;
-    bool sparse = try_sparse && mm[1] >= 0 &&
-                  to_k::mte_sparse_smem(NE, g->csc.cap_smem) <= ctx->smem_optin;
-    if (try_sparse && !sparse && o->migration == TO_MIG_SPARSE_FP32)
+    const bool sparse_ok = try_sparse && mm[1] >= 0 &&
+                           to_k::mte_sparse_smem(NE, g->csc.cap_smem) <= ctx->smem_optin;
+    if (try_sparse && !sparse_ok && o->migration == TO_MIG_SPARSE_FP32)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
+    TO_TRY(grow_end(ctx, g, (size_t)RS * o->mte_paths));
+    to_mte_args m = mte_args(ctx, g, o, NE);
+    int choice;
+    if (o->migration == TO_MIG_SPARSE_FP32) choice = CH_SPARSE;
+    else if (o->migration == TO_MIG_TC_3XTF32) choice = CH_TC;
+    else if (o->migration == TO_MIG_SIMT_FP32) choice = CH_SIMT;
+    else TO_TRY(tuned_choice(ctx, g, m, RS, NE, sparse_ok, NE <= 512, &choice));
+    TO_TRY(tail(ctx, g, m, RS, choice, d_results_out));
+    if (plan) { plan[0] = NE; plan[1] = g->csc.cap_smem; plan[2] = choice; }
+    return TO_OK;
+}
 
-    const int P = o->mte_paths;
-    if ((size_t)RS * P > g->end_cap) {
-        if (g->d_end) TO_CUDA(ctx, cudaFree(g->d_end));
-        g->d_end = nullptr;
-        TO_CUDA(ctx, cudaMalloc(&g->d_end, (size_t)RS * P * sizeof(float)));
-        g->end_cap = (size_t)RS * P;
+// opts.graph: replay the captured generation when the call matches it,
+// else plan directly and capture.
+to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
+                   const int* cells, const int* seg_off, const double* segs,
+                   const to_eval_opts* o, double* d_results_out) {
+    if (!o->graph) return evaluate_direct(ctx, g, R, cell_off, cells, seg_off, segs, o,
+                                          d_results_out, nullptr);
+    uint64_t key = 0;
+    const uint64_t fields[] = {(uint64_t)R, (uint64_t)(uintptr_t)cell_off,
+                               (uint64_t)(uintptr_t)cells, (uint64_t)(uintptr_t)seg_off,
+                               (uint64_t)(uintptr_t)segs, (uint64_t)(uintptr_t)d_results_out,
+                               (uint64_t)o->mte_paths, (uint64_t)o->n_years,
+                               (uint64_t)__float_as_uint_host(o->dt), o->seed,
+                               (uint64_t)o->road0, (uint64_t)o->sem, (uint64_t)o->migration,
+                               (uint64_t)(uintptr_t)ctx->stream};
+    for (uint64_t f : fields) key = mix(key, f);
+    if (g->exec && g->graph_key == key) {
+        TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+        ctx->launches += 2 + (g->plan_choice == CH_SPARSE ? 1 : 0) +
+                         (g->plan_choice == CH_TC ? 2 : 1) + 2;
+        return TO_OK;
     }
-    to_mte_args m;
-    memset(&m, 0, sizeof(m));
-    m.n_paths = P; m.n_years = o->n_years; m.S = S; m.C = g->C; m.c_use = g->C - 1;
-    m.dt = o->dt; m.seed = o->seed; m.sem = o->sem; m.road0 = o->road0;
-    m.npad = NP; m.npe = NE; m.n_patches = g->d_np; m.mmm = g->d_mmm;
-    m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
-    m.end_pops = g->d_end;
-    if (sparse) {
-        TO_TRY(to_k::mte_sparse(ctx, m, RS, g->csc));
-    } else if (o->migration == TO_MIG_TC_3XTF32) {
-        TO_TRY(to_k::mte_tc(ctx, m, RS));
-    } else {
-        TO_TRY(to_k::mte_simt(ctx, m, RS));
+    if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
+    int plan[3];
+    TO_TRY(evaluate_direct(ctx, g, R, cell_off, cells, seg_off, segs, o, d_results_out, plan));
+    // plan with a margin so that the next generations of a GA still fit
+    const int S = g->S, RS = R * S;
+    int ne = (plan[0] + 16 + 3) & ~3;
+    if (ne > g->NP) ne = g->NP;
+    int cap = ((plan[1] + plan[1] / 4 + 64) + 7) & ~7;
+    if (cap > g->csc.cap) cap = g->csc.cap;
+    if ((plan[2] == CH_SPARSE && to_k::mte_sparse_smem(ne, cap) > ctx->smem_optin) ||
+        plan[2] == CH_TC) {
+        // no margin where it does not fit (or would resize the tensor-core
+        // scratch, which cannot be allocated inside a capture)
+        ne = plan[0];
+        cap = plan[1];
     }
-    TO_TRY(to_k::mte_stats(ctx, m, RS, g->d_stats));
-    k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(
-        RS, g->d_np, g->d_nt, g->d_stats, sparse ? g->csc.nnz : nullptr, g->C, d_results_out);
-    TO_LAUNCHED(ctx);
+    const int choice = plan[2];
+    g->csc.cap_smem = cap;
+    to_model_args a;
+    model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
+    to_mte_args m = mte_args(ctx, g, o, ne);
+    const bool prof = ctx->profile;
+    ctx->profile = false;                      // no event records inside the capture
+    TO_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    to_status st = to_k::species_model(ctx, a, RS);
+    if (st == TO_OK && choice == CH_SPARSE)
+        st = to_k::pack_csc(ctx, g->d_mmm, g->NP, g->C, g->d_np, RS, g->csc);
+    if (st == TO_OK) st = tail(ctx, g, m, RS, choice, d_results_out);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->profile = prof;
+    if (st != TO_OK) { if (graph) cudaGraphDestroy(graph); return st; }
+    TO_CUDA(ctx, ce);
+    ce = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TO_CUDA(ctx, ce);
+    g->graph_key = key;
+    g->plan_ne = ne; g->plan_cap = cap; g->plan_choice = choice;
     return TO_OK;
 }
 
@@ -292,6 +448,7 @@ to_status to_scene_destroy(to_gen g) {
     if (!g) return TO_OK;
     if (g->ctx) cudaSetDevice(g->ctx->device);
     cudaDeviceSynchronize();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
     cudaFree(g->d_base);
     cudaFree(g->d_popmap);
     cudaFree(g->d_species);
@@ -344,6 +501,19 @@ to_status to_evaluate_roads(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     int f = 0;
     TO_TRY(to_read_device_flags(ctx, &f));
+    if (f == TO_DEVERR_PLAN && o->graph) {
+        // a road outside the captured plan: drop the graph, plan and run again
+        int z = 0;
+        TO_CUDA(ctx, cudaMemcpy(ctx->d_flags, &z, sizeof(int), cudaMemcpyHostToDevice));
+        if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
+        TO_TRY(evaluate(ctx, g, R, g->d_cell_off, g->d_cells, g->d_seg_off, g->d_segs, o,
+                        g->d_results));
+        TO_CUDA(ctx, cudaMemcpyAsync(results, g->d_results,
+                                     (size_t)R * g->S * TO_RESULT_STRIDE * sizeof(double),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
+        TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        TO_TRY(to_read_device_flags(ctx, &f));
+    }
     if (f != 0) {
         cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream);
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "device check %d failed", f);

@@ -6,6 +6,7 @@
 // cudaDeviceSynchronize / D2H / cudaFree inside every call).
 #include <cmath>
 #include <cstdarg>
+#include <string>
 #include <vector>
 
 #include "to_internal.cuh"
@@ -215,6 +216,25 @@ to_status to_ctx_set_stream(to_ctx ctx, void* stream) {
     ctx->stream = (cudaStream_t)stream;
     ctx->own_stream = false;
     return TO_OK;
+}
+
+int to_ctx_tuning(to_ctx ctx, char* buf, int len) {
+    if (!ctx) return 0;
+    static const char* names[3] = {"sparse", "simt", "tc"};
+    std::string out;
+    for (const auto& e : ctx->tune) {
+        char line[256];
+        snprintf(line, sizeof(line), "%s ne=%d paths=%d rs=%d -> %s (sparse %.3f ms, simt %.3f ms, tc %.3f ms)\n",
+                 e.kind == 0 ? "generation" : "mte", e.ne, e.paths, e.n_rs,
+                 names[e.choice < 0 || e.choice > 2 ? 1 : e.choice], e.ms[0], e.ms[1], e.ms[2]);
+        out += line;
+    }
+    if (buf && len > 0) {
+        size_t n = out.size() < (size_t)(len - 1) ? out.size() : (size_t)(len - 1);
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    }
+    return (int)ctx->tune.size();
 }
 
 to_status to_ctx_synchronize(to_ctx ctx) {

@@ -34,6 +34,12 @@ k_mte_simt(to_mte_args a) {
     float* gm = mig + (size_t)TP * NE;      // [TP]
 
     const int N = a.n_patches[rs];
+    if (N > NE) {
+        if (tid == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_PLAN);
+        for (int q = tid; q < TP; q += blockDim.x)
+            if (blockIdx.x * TP + q < a.n_paths) a.end_pops[(size_t)rs * a.n_paths + blockIdx.x * TP + q] = NAN;
+        return;
+    }
     const float* M = a.mmm + ((size_t)rs * a.C + a.c_use) * NP * NP;
     const float* ip = a.init_pops + (size_t)rs * NP;
     const float* cp = a.caps + (size_t)rs * NP;
@@ -202,6 +208,7 @@ namespace to_k {
 
 to_status mte_simt(to_ctx ctx, to_mte_args a, int n_rs) {
     if (a.npe <= 0) a.npe = a.npad;
+    if (!a.flags) a.flags = ctx->d_flags;
     const int NP = a.npe;
     if (NP % 4 != 0 || NP <= 0 || a.npe > a.npad)
         return to_set_error(ctx, TO_ERR_INVALID, "npad %d npe %d", a.npad, a.npe);

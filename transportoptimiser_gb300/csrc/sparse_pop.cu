@@ -90,6 +90,13 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int mtx = rs * a.C + a.c_use;
     const int nnz = csc.nnz[mtx];
+    if (nnz < 0 || nnz > csc.cap_smem || a.n_patches[rs] > NE) {
+        // outside the shape this launch was planned for: flag, no result
+        if (threadIdx.x == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_PLAN);
+        const int p = blockIdx.x * kLanes + (int)threadIdx.x;
+        if (threadIdx.x < kLanes && p < a.n_paths) a.end_pops[(size_t)rs * a.n_paths + p] = NAN;
+        return;
+    }
     float* cur = reinterpret_cast<float*>(sm_raw);             // [NE][32]
     float* part = cur + (size_t)NE * kLanes;                   // [NG][32]
     float* capv = part + (size_t)NG * kLanes;                  // [NE]
@@ -362,6 +369,7 @@ static int warps_for(int NE, int min_warps) {
 
 to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
     if (a.npe <= 0) a.npe = a.npad;
+    if (!a.flags) a.flags = ctx->d_flags;
     const int NE = a.npe;
     size_t smem = mte_sparse_smem(NE, csc.cap_smem);
     if (smem > ctx->smem_optin)

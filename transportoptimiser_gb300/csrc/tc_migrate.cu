@@ -102,6 +102,12 @@ k_mte_tc(to_mte_args a, TcShape sh, const float* __restrict__ packed, int* __res
     const int rs = blockIdx.y;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int N = a.n_patches[rs], NP = a.npad;
+    if (N > KGN * KGRP || N > MT * 128) {
+        if (threadIdx.x == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_PLAN);
+        for (int q = threadIdx.x; q < TP; q += 128)
+            if (blockIdx.x * TP + q < a.n_paths) a.end_pops[(size_t)rs * a.n_paths + blockIdx.x * TP + q] = NAN;
+        return;
+    }
     const float* ip = a.init_pops + (size_t)rs * NP;
     const float* cp = a.caps + (size_t)rs * NP;
     const float* sp8 = a.params + 8 * sp;
@@ -316,6 +322,7 @@ namespace to_k {
 
 to_status mte_tc(to_ctx ctx, to_mte_args a, int n_rs) {
     int maxN = a.npe > 0 ? a.npe : a.npad;
+    if (!a.flags) a.flags = ctx->d_flags;
     TcShape sh;
     if (!pick_shape(maxN, ctx->smem_optin, sh))
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "tensor-core migration: %d patches", maxN);

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "../../include/transopt.h"
 #include "to_math.h"
@@ -39,12 +40,20 @@ struct to_ctx_s {
     int prof_ev_alloc = 0;
     int sm_count = 0;
     size_t smem_optin = 0;
+    // autotuner: measured migration-kernel choice per problem shape
+    struct tune_entry {
+        uint64_t key;
+        int kind;               // 0 batched generation, 1 single-road MTE
+        int ne, paths, n_rs, choice;
+        float ms[3];            // sparse, dense SIMT, tensor core (-1: not feasible)
+    };
+    std::vector<tune_entry> tune;
     char err[512] = {0};
 };
 
 // device-side error codes written to ctx->d_flags[0]
 enum { TO_DEVERR_NONE = 0, TO_DEVERR_REGIONS = 1, TO_DEVERR_UNION = 2,
-       TO_DEVERR_PATCHES = 3, TO_DEVERR_SPIN = 4 };
+       TO_DEVERR_PATCHES = 3, TO_DEVERR_SPIN = 4, TO_DEVERR_PLAN = 5 };
 
 to_status to_set_error(to_ctx ctx, to_status s, const char* fmt, ...);
 to_status to_check_cuda(to_ctx ctx, cudaError_t e, const char* what);

@@ -17,6 +17,7 @@ struct to_mte_args {
     const float* caps;           // [RS][NP]
     const float* params;         // [S][8]
     float* end_pops;             // [RS][P]
+    int* flags;                  // device error word (plan checks), may be null
 };
 
 namespace to_k {

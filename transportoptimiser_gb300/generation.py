@@ -63,8 +63,8 @@ class Generation:
         self.max_roads = max_roads
 
     def opts(self, mte_paths, n_years=50, dt=1.0, seed=0, road0=0, sem=0,
-             migration=_capi.MIG_AUTO):
-        return _capi.EvalOpts(mte_paths, n_years, dt, seed, road0, sem, migration)
+             migration=_capi.MIG_AUTO, graph=False):
+        return _capi.EvalOpts(mte_paths, n_years, dt, seed, road0, sem, migration, int(graph))
 
     def evaluate(self, packed: dict, opts) -> np.ndarray:
         """Host-pointer entry point; returns [R][S][RESULT_STRIDE]."""
