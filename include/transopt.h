@@ -353,6 +353,34 @@ typedef struct {
                                 pointers and options, shapes within the plan) */
 } to_eval_opts;
 
+/* ---- pathwise sensitivities (adjoint) ------------------------------------
+ * The controlled road valuation with the exercise policy frozen: per path
+ * the controls c[t][p] are given (e.g. to_rov_result.opt_cont).  Outputs
+ * (1 + S): E[PV] with PV = sum_t (1 + rrr dt/100)^-t flows[c_t] unit_profit_t, and
+ * E[end population] per species (corrected growth, sem 1).  Parameters
+ * theta (2U + 2S + C): OU reversion theta_u, OU volatility sigma_u, growth-
+ * rate mean mu_s (species params[1]), growth variability v_s (params[7]),
+ * crossing hazard h_c (the matrices of rov->species are taken as built
+ * with `hazard`; h_c rescales entry (k, l) of control c by
+ * exp(-crossings[s][l][k] (h_c - hazard[c]))).  No reference counterpart. */
+typedef struct {
+    const to_rov_problem* rov;
+    const int* controls;          /* [n_years][n_paths] frozen policy            */
+    const int* const* crossings;  /* per species [N][N] road crossings (i -> j)  */
+    const double* hazard;         /* [C] hazards the matrices were built with     */
+} to_adjoint_problem;
+
+typedef struct to_tape_s* to_tape;
+
+/* forward: outputs[1 + S]; keeps the population checkpoints (every 10
+ * years) in a tape for the backward call (tape may be NULL) */
+to_status to_adjoint_forward(to_ctx ctx, const to_adjoint_problem* prob,
+                             const double* theta, double* outputs, to_tape* tape);
+/* backward: grad_theta = sum_i grad_outputs[i] d outputs[i] / d theta */
+to_status to_adjoint_backward(to_ctx ctx, to_tape tape, const double* grad_outputs,
+                              double* grad_theta);
+to_status to_tape_destroy(to_tape tape);
+
 /* The autotuner's record: one line per tuned shape, "kind ne paths rs ->
  * choice (sparse ms, simt ms, tc ms)", -1 where a kernel was not feasible.
  * Writes at most len bytes (NUL-terminated); returns the number of lines. */

@@ -477,3 +477,65 @@ def mlp_grad(params, x, t, rounding=True):
                          _p(g, C.c_double), C.byref(loss))
     oracle().or_mlp_set_rounding(1)
     return g, loss.value
+
+
+# ---- frozen-policy valuation in FP64 (oracle_adjoint.c) ----------------------
+class OrAdjProblem(C.Structure):
+    _fields_ = [("P", C.c_int), ("Y", C.c_int), ("S", C.c_int), ("C", C.c_int), ("U", C.c_int),
+                ("NP", C.c_int), ("dt", C.c_float), ("rrr", C.c_float), ("seed", C.c_uint64),
+                ("road", C.c_int), ("uncert", c_float_p), ("flows", c_float_p), ("nF", C.c_int),
+                ("fuel_costs", c_float_p), ("fuel_idx", c_int_p), ("Cm", C.c_int),
+                ("ore_content", c_float_p), ("ore_sd", c_float_p), ("unit_cost", C.c_float),
+                ("unit_revenue", C.c_float), ("demand_idx", C.c_int), ("controls", c_int_p),
+                ("n_patches", c_int_p), ("params", c_float_p), ("init_pops", c_float_p),
+                ("caps", c_float_p), ("mmm", c_float_p), ("cross", c_int_p),
+                ("base_h", c_double_p)]
+
+
+def adjoint_forward(problem, controls, crossings, hazard, theta, threads=None):
+    """E[PV], E[end population_s] of the frozen-policy model in FP64."""
+    lib = oracle()
+    lib.or_adjoint_forward.argtypes = [C.POINTER(OrAdjProblem), c_double_p, c_double_p, C.c_int]
+    sps = problem["species"]
+    S, Cn = len(sps), len(problem["flows"])
+    NP = max(int(s["N"]) for s in sps)
+    NP = (NP + 3) & ~3
+    keep = []
+
+    def f32(a):
+        a = np.ascontiguousarray(a, np.float32)
+        keep.append(a)
+        return _p(a, C.c_float)
+
+    def i32(a):
+        a = np.ascontiguousarray(a, np.int32)
+        keep.append(a)
+        return _p(a, C.c_int)
+
+    ip = np.zeros((S, NP), np.float32)
+    cp = np.ones((S, NP), np.float32)
+    mm = np.zeros((S, Cn, NP, NP), np.float32)
+    cr = np.zeros((S, NP, NP), np.int32)
+    for s, sp in enumerate(sps):
+        N = int(sp["N"])
+        ip[s, :N] = sp["init_pops"]
+        cp[s, :N] = sp["caps"]
+        mm[s, :, :N, :N] = np.asarray(sp["mmm"], np.float32).reshape(Cn, N, N)
+        cr[s, :N, :N] = crossings[s]
+    hz = np.ascontiguousarray(hazard, np.float64)
+    keep.append(hz)
+    pr = OrAdjProblem(problem["n_paths"], problem["n_years"], S, Cn, len(problem["uncert"]) // 6,
+                      NP, problem["dt"], problem["rrr"], problem["seed"], problem["road"],
+                      f32(problem["uncert"]), f32(problem["flows"]), len(problem["fuel_costs"]),
+                      f32(problem["fuel_costs"]), i32(problem["fuel_idx"]),
+                      len(problem["ore_content"]), f32(problem["ore_content"]),
+                      f32(problem["ore_sd"]), problem["unit_cost"], problem["unit_revenue"],
+                      problem.get("demand_idx", -1), i32(controls),
+                      i32([int(s["N"]) for s in sps]),
+                      f32(np.concatenate([np.asarray(s["params"], np.float32) for s in sps])),
+                      f32(ip), f32(cp), f32(mm), i32(cr), _p(hz, C.c_double))
+    th = np.ascontiguousarray(theta, np.float64)
+    out = np.zeros(1 + S)
+    lib.or_adjoint_forward(C.byref(pr), _p(th, C.c_double), _p(out, C.c_double),
+                           threads or os.cpu_count() or 1)
+    return out

@@ -175,6 +175,10 @@ SIGNATURES = {
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
     "to_ctx_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "to_adjoint_forward": (C.c_int, [C.c_void_p, C.c_void_p, c_double_p, c_double_p,
+                                     C.POINTER(C.c_void_p)]),
+    "to_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, c_double_p, c_double_p]),
+    "to_tape_destroy": (C.c_int, [C.c_void_p]),
     "to_mlp_predict": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p]),
     "to_mlp_predict_d": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "to_mlp_grad": (C.c_int, [C.c_void_p, c_float_p, C.c_int, c_float_p, c_float_p, c_float_p,

@@ -175,6 +175,33 @@ def expPV(gr, mean, time_step, rrr, current, reversion, jump_prob, noise_sd, jum
     return m.value, s.value
 
 
+def rov_ctypes(problem: dict, migration=_capi.MIG_AUTO):
+    """to_rov_problem for a problem dict (transportoptimiser_gb300.rov);
+    returns (struct, arrays that must stay alive while it is used)."""
+    S = len(problem["species"])
+    P, Y, R = problem["n_paths"], problem["n_years"], problem["dim_res"]
+    Cn = len(problem["flows"])
+    keep = []
+    sps = (_capi.RovSpecies * S)()
+    for s, sp in enumerate(problem["species"]):
+        arrs = [np.ascontiguousarray(sp[k], np.float32) for k in ("params", "init_pops", "caps", "mmm")]
+        keep += arrs
+        sps[s] = _capi.RovSpecies(int(sp["N"]), *[ptr(a_, C.c_float) for a_ in arrs])
+    keep.append(sps)
+    f32 = lambda k: np.ascontiguousarray(problem[k], np.float32)
+    flows, unc, fc, oc, osd = (f32(k) for k in ("flows", "uncert", "fuel_costs", "ore_content",
+                                                  "ore_sd"))
+    fi = np.ascontiguousarray(problem["fuel_idx"], np.int32)
+    keep += [flows, unc, fc, oc, osd, fi]
+    pr = _capi.RovProblem(S, P, Y, Cn, R, sps, ptr(flows, C.c_float), len(unc) // 6,
+                          ptr(unc, C.c_float), len(fc), ptr(fc, C.c_float), ptr(fi, C.c_int),
+                          len(oc), ptr(oc, C.c_float), ptr(osd, C.c_float),
+                          problem["unit_cost"], problem["unit_revenue"], problem["dt"],
+                          problem["rrr"], problem.get("demand_idx", -1), problem["seed"],
+                          problem["road"], problem["sem"], migration)
+    return pr, keep
+
+
 def simulateROVCUDA(problem: dict, want=("cond_exp", "opt_cont", "unit_profits", "adj_pops",
                                         "regression"), migration=_capi.MIG_AUTO,
                     ctx: Context | None = None) -> dict:
@@ -187,23 +214,7 @@ def simulateROVCUDA(problem: dict, want=("cond_exp", "opt_cont", "unit_profits",
     S = len(problem["species"])
     P, Y, R = problem["n_paths"], problem["n_years"], problem["dim_res"]
     Cn = len(problem["flows"])
-    keep = []
-    sps = (_capi.RovSpecies * S)()
-    for s, sp in enumerate(problem["species"]):
-        arrs = [np.ascontiguousarray(sp[k], np.float32) for k in ("params", "init_pops", "caps", "mmm")]
-        keep += arrs
-        sps[s] = _capi.RovSpecies(int(sp["N"]), *[ptr(a_, C.c_float) for a_ in arrs])
-    f32 = lambda k: np.ascontiguousarray(problem[k], np.float32)
-    flows, unc, fc, oc, osd = (f32(k) for k in ("flows", "uncert", "fuel_costs", "ore_content",
-                                                  "ore_sd"))
-    fi = np.ascontiguousarray(problem["fuel_idx"], np.int32)
-    keep += [flows, unc, fc, oc, osd, fi]
-    pr = _capi.RovProblem(S, P, Y, Cn, R, sps, ptr(flows, C.c_float), len(unc) // 6,
-                          ptr(unc, C.c_float), len(fc), ptr(fc, C.c_float), ptr(fi, C.c_int),
-                          len(oc), ptr(oc, C.c_float), ptr(osd, C.c_float),
-                          problem["unit_cost"], problem["unit_revenue"], problem["dt"],
-                          problem["rrr"], problem.get("demand_idx", -1), problem["seed"],
-                          problem["road"], problem["sem"], migration)
+    pr, keep = rov_ctypes(problem, migration)
     d = S + 1
     out = {}
     if "cond_exp" in want: out["cond_exp"] = np.zeros(Y * P)
