@@ -381,6 +381,21 @@ to_status to_adjoint_backward(to_ctx ctx, to_tape tape, const double* grad_outpu
                               double* grad_theta);
 to_status to_tape_destroy(to_tape tape);
 
+/* 16 features per road for the learned surrogate (road cells rasterised on
+ * the device): 0 length / W, 1 segments / 64, 2 road cells / W, 3 / 4
+ * road crossings per animal of species 0 moving 5 / 12 cells, 5..7 share
+ * of the road's cells on habitat codes 2, 3, 5, 8 share of species 0's
+ * initial animals on road cells, 9 / 10 / 11 / 14 share of them within
+ * 3 / 6 / 12 / 24 cells (Chebyshev) of the road, 12 / 13 bounding-box
+ * width and height / W, 15 sinuosity / 10.  No reference counterpart.
+ * Host arrays; features [n_roads][16]. */
+to_status to_road_features(to_ctx ctx, to_gen gen, int n_roads, const int* seg_off,
+                           const double* segs, float* features);
+/* device arrays (cell_off / cells may be NULL: rasterised here) */
+to_status to_road_features_d(to_ctx ctx, to_gen gen, int n_roads, const int* seg_off,
+                             const double* segs, const int* cell_off, const int* cells,
+                             float* features);
+
 /* The autotuner's record: one line per tuned shape, "kind ne paths rs ->
  * choice (sparse ms, simt ms, tc ms)", -1 where a kernel was not feasible.
  * Writes at most len bytes (NUL-terminated); returns the number of lines. */
@@ -403,7 +418,11 @@ to_status to_evaluate_roads(to_ctx ctx, to_gen gen, int n_roads,
                             const int* cell_off, const int* cells,
                             const int* seg_off, const double* segs,
                             const to_eval_opts* opts, double* results);
-/* Same with every array (inputs and results) in device memory; enqueued on
+/* cell_off and cells may both be NULL: the road cells are then computed
+ * from the segments on the device (a segment of length L sampled at
+ * max(2, ceil(4L)) + 1 evenly spaced points, each in the cell of its
+ * coordinates rounded half to even, inside the grid).
+ * Same with every array (inputs and results) in device memory; enqueued on
  * the context stream without synchronising. */
 to_status to_evaluate_roads_d(to_ctx ctx, to_gen gen, int n_roads,
                               const int* cell_off, const int* cells,

@@ -54,6 +54,8 @@ struct to_gen_s {
     double* d_stats;                     // [RS][5]
     double* d_results;                   // [RS][8]
     to_csc csc;                          // [RS*C] packed migration matrices
+    int* d_counts = nullptr;             // [max_roads] road cell counts (device rasterisation)
+    float* d_feat = nullptr;             // [max_roads][16] surrogate features
     // captured generation (opts.graph)
     cudaGraphExec_t exec = nullptr;
     uint64_t graph_key = 0;
@@ -233,6 +235,13 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
                           const int* cells, const int* seg_off, const double* segs,
                           const to_eval_opts* o, double* d_results_out, int* plan) {
     const int S = g->S, RS = R * S, NP = g->NP;
+    if (!cell_off) {
+        // road cells from the segments, on the device
+        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off,
+                                     g->d_cells, g->max_cells, g->d_counts));
+        cell_off = g->d_cell_off;
+        cells = g->d_cells;
+    }
     to_model_args a;
     model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
     TO_TRY(to_k::species_model(ctx, a, RS));
@@ -316,7 +325,14 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     const bool prof = ctx->profile;
     ctx->profile = false;                      // no event records inside the capture
     TO_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    to_status st = to_k::species_model(ctx, a, RS);
+    to_status st = TO_OK;
+    if (!cell_off) {
+        st = to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off, g->d_cells,
+                                   g->max_cells, g->d_counts);
+        a.cell_off = g->d_cell_off;
+        a.cells = g->d_cells;
+    }
+    if (st == TO_OK) st = to_k::species_model(ctx, a, RS);
     if (st == TO_OK && choice == CH_SPARSE)
         st = to_k::pack_csc(ctx, g->d_mmm, g->NP, g->C, g->d_np, RS, g->csc);
     if (st == TO_OK) st = tail(ctx, g, m, RS, choice, d_results_out);
@@ -409,6 +425,8 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     acc(RS * NP * 4); acc(RS * NP * 4);
     acc(RS * 5 * 8);
     acc((RS * TO_RESULT_STRIDE + 64) * 8);
+    acc((R + 1) * 4);
+    acc(R * 16 * 4);
     const size_t cap = (size_t)NP * 32;
     acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
     if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
@@ -433,6 +451,8 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->d_cp = carve<float>(p, RS * NP);
     g->d_stats = carve<double>(p, RS * 5);
     g->d_results = carve<double>(p, RS * TO_RESULT_STRIDE + 64);
+    g->d_counts = carve<int>(p, R + 1);
+    g->d_feat = carve<float>(p, R * 16);
     g->csc.ptr = carve<int>(p, RS * C * (NP + 1));
     g->csc.idx = carve<uint16_t>(p, RS * C * cap);
     g->csc.val = carve<float>(p, RS * C * cap);
@@ -471,30 +491,35 @@ to_status to_evaluate_roads(to_ctx ctx, to_gen g, int R, const int* cell_off,
                             const double* segs, const to_eval_opts* o,
                             double* results) {
     TO_TRY(check_eval(ctx, g, R, o));
-    if (!cell_off || !seg_off || !segs || !results) return TO_ERR_INVALID;
+    if (!seg_off || !segs || !results || (!cell_off != !cells && cell_off && cell_off[R] > 0))
+        return TO_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    int ncell = cell_off[R] - cell_off[0], nseg = seg_off[R] - seg_off[0];
-    if (cell_off[0] != 0 || seg_off[0] != 0 || ncell > g->max_cells ||
+    const bool raster = (cell_off == nullptr);
+    const int ncell = raster ? 0 : cell_off[R] - cell_off[0];
+    const int nseg = seg_off[R] - seg_off[0];
+    if ((!raster && cell_off[0] != 0) || seg_off[0] != 0 || ncell > g->max_cells ||
         nseg > g->max_segs || (ncell > 0 && !cells))
         return TO_ERR_INVALID;
     for (int r = 0; r < R; ++r)
-        if (cell_off[r + 1] < cell_off[r] || seg_off[r + 1] < seg_off[r])
+        if ((!raster && cell_off[r + 1] < cell_off[r]) || seg_off[r + 1] < seg_off[r])
             return TO_ERR_INVALID;
     for (int q = 0; q < ncell; ++q)
         if (cells[q] < 0 || cells[q] >= g->W * g->H) return TO_ERR_INVALID;
     for (int q = 0; q < 4 * nseg; ++q)
         if (!std::isfinite(segs[q])) return to_set_error(ctx, TO_ERR_NONFINITE, "segment %d", q / 4);
-    TO_CUDA(ctx, cudaMemcpyAsync(g->d_cell_off, cell_off, (R + 1) * sizeof(int),
-                                 cudaMemcpyHostToDevice, ctx->stream));
-    if (ncell > 0)
-        TO_CUDA(ctx, cudaMemcpyAsync(g->d_cells, cells, ncell * sizeof(int),
+    if (!raster) {
+        TO_CUDA(ctx, cudaMemcpyAsync(g->d_cell_off, cell_off, (R + 1) * sizeof(int),
                                      cudaMemcpyHostToDevice, ctx->stream));
+        if (ncell > 0)
+            TO_CUDA(ctx, cudaMemcpyAsync(g->d_cells, cells, ncell * sizeof(int),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+    }
     TO_CUDA(ctx, cudaMemcpyAsync(g->d_seg_off, seg_off, (R + 1) * sizeof(int),
                                  cudaMemcpyHostToDevice, ctx->stream));
     TO_CUDA(ctx, cudaMemcpyAsync(g->d_segs, segs, (size_t)nseg * 4 * sizeof(double),
                                  cudaMemcpyHostToDevice, ctx->stream));
-    TO_TRY(evaluate(ctx, g, R, g->d_cell_off, g->d_cells, g->d_seg_off, g->d_segs, o,
-                    g->d_results));
+    TO_TRY(evaluate(ctx, g, R, raster ? nullptr : g->d_cell_off, raster ? nullptr : g->d_cells,
+                    g->d_seg_off, g->d_segs, o, g->d_results));
     TO_CUDA(ctx, cudaMemcpyAsync(results, g->d_results,
                                  (size_t)R * g->S * TO_RESULT_STRIDE * sizeof(double),
                                  cudaMemcpyDeviceToHost, ctx->stream));
@@ -506,8 +531,8 @@ to_status to_evaluate_roads(to_ctx ctx, to_gen g, int R, const int* cell_off,
         int z = 0;
         TO_CUDA(ctx, cudaMemcpy(ctx->d_flags, &z, sizeof(int), cudaMemcpyHostToDevice));
         if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
-        TO_TRY(evaluate(ctx, g, R, g->d_cell_off, g->d_cells, g->d_seg_off, g->d_segs, o,
-                        g->d_results));
+        TO_TRY(evaluate(ctx, g, R, raster ? nullptr : g->d_cell_off,
+                        raster ? nullptr : g->d_cells, g->d_seg_off, g->d_segs, o, g->d_results));
         TO_CUDA(ctx, cudaMemcpyAsync(results, g->d_results,
                                      (size_t)R * g->S * TO_RESULT_STRIDE * sizeof(double),
                                      cudaMemcpyDeviceToHost, ctx->stream));
@@ -526,9 +551,52 @@ to_status to_evaluate_roads_d(to_ctx ctx, to_gen g, int R, const int* cell_off,
                               const double* segs, const to_eval_opts* o,
                               double* results) {
     TO_TRY(check_eval(ctx, g, R, o));
-    if (!cell_off || !seg_off || !segs || !results) return TO_ERR_INVALID;
+    if (!seg_off || !segs || !results || (!cell_off != !cells)) return TO_ERR_INVALID;
     cudaSetDevice(ctx->device);
     return evaluate(ctx, g, R, cell_off, cells, seg_off, segs, o, results);
+}
+
+to_status to_road_features_d(to_ctx ctx, to_gen g, int R, const int* seg_off,
+                             const double* segs, const int* cell_off, const int* cells,
+                             float* features) {
+    if (!ctx || !g || R <= 0 || R > g->max_roads || !seg_off || !segs || !features ||
+        (!cell_off != !cells))
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    if (!cell_off) {
+        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off,
+                                     g->d_cells, g->max_cells, g->d_counts));
+        cell_off = g->d_cell_off;
+        cells = g->d_cells;
+    }
+    return to_k::road_features(ctx, R, g->W, g->H, g->d_base, g->d_popmap, seg_off, segs,
+                               cell_off, cells, features);
+}
+
+to_status to_road_features(to_ctx ctx, to_gen g, int R, const int* seg_off, const double* segs,
+                           float* features) {
+    if (!ctx || !g || R <= 0 || R > g->max_roads || !seg_off || !segs || !features)
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    const int nseg = seg_off[R] - seg_off[0];
+    if (seg_off[0] != 0 || nseg > g->max_segs) return TO_ERR_INVALID;
+    for (int q = 0; q < 4 * nseg; ++q)
+        if (!std::isfinite(segs[q])) return to_set_error(ctx, TO_ERR_NONFINITE, "segment %d", q / 4);
+    TO_CUDA(ctx, cudaMemcpyAsync(g->d_seg_off, seg_off, (R + 1) * sizeof(int),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    TO_CUDA(ctx, cudaMemcpyAsync(g->d_segs, segs, (size_t)nseg * 4 * sizeof(double),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    TO_TRY(to_road_features_d(ctx, g, R, g->d_seg_off, g->d_segs, nullptr, nullptr, g->d_feat));
+    TO_CUDA(ctx, cudaMemcpyAsync(features, g->d_feat, (size_t)R * 16 * sizeof(float),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int f = 0;
+    TO_TRY(to_read_device_flags(ctx, &f));
+    if (f != 0) {
+        cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream);
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "road cells exceed the scene capacity");
+    }
+    return TO_OK;
 }
 
 }  // extern "C"

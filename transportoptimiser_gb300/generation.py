@@ -27,6 +27,17 @@ def pack_roads(scene: SynthScene, roads) -> dict:
                 segs=np.ascontiguousarray(np.concatenate(segs) if segs else np.zeros(4)))
 
 
+def pack_segments(roads) -> dict:
+    """Segment CSR only (the device computes the road cells)."""
+    seg_off = np.zeros(len(roads) + 1, np.int32)
+    segs = []
+    for r, rd in enumerate(roads):
+        segs.append(np.asarray(rd.segments, np.float64).reshape(-1))
+        seg_off[r + 1] = seg_off[r] + rd.G
+    return dict(seg_off=seg_off,
+                segs=np.ascontiguousarray(np.concatenate(segs) if segs else np.zeros(4)))
+
+
 class Generation:
     """Resident scene + per-generation evaluation."""
 
@@ -76,6 +87,25 @@ class Generation:
             ptr(packed["seg_off"], C.c_int), ptr(packed["segs"], C.c_double),
             C.byref(opts), ptr(out, C.c_double)), "to_evaluate_roads")
         return out.reshape(R, self.S, _capi.RESULT_STRIDE)
+
+    def evaluate_segments(self, packed: dict, opts) -> np.ndarray:
+        """Host entry point with the road cells rasterised on the device."""
+        R = len(packed["seg_off"]) - 1
+        out = np.zeros(R * self.S * _capi.RESULT_STRIDE, np.float64)
+        self.ctx.check(self.ctx.lib.to_evaluate_roads(
+            self.ctx.handle, self.handle, R, None, None, ptr(packed["seg_off"], C.c_int),
+            ptr(packed["segs"], C.c_double), C.byref(opts), ptr(out, C.c_double)),
+            "to_evaluate_roads")
+        return out.reshape(R, self.S, _capi.RESULT_STRIDE)
+
+    def features(self, packed: dict) -> np.ndarray:
+        """[R][16] surrogate features (to_road_features)."""
+        R = len(packed["seg_off"]) - 1
+        out = np.zeros((R, 16), np.float32)
+        self.ctx.check(self.ctx.lib.to_road_features(
+            self.ctx.handle, self.handle, R, ptr(packed["seg_off"], C.c_int),
+            ptr(packed["segs"], C.c_double), ptr(out, C.c_float)), "to_road_features")
+        return out
 
     def evaluate_device(self, R, d_cell_off, d_cells, d_seg_off, d_segs, opts, d_results):
         """Device-pointer entry point (ints are raw device addresses)."""

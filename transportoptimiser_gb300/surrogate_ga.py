@@ -1,0 +1,161 @@
+"""Surrogate-assisted valuation of GA generations with the learned MLP.
+
+The reference's GA (RoadGA::evaluateGeneration / computeSurrogate,
+include/main/RoadGA.cpp:2040, 1553) values every design by Monte Carlo, or
+by local-linear grid surrogates of one or two aggregate predictors
+(buildSurrogateMTECUDA / buildSurrogateROVCUDA).  Here an ensemble of two
+MLPs (transportoptimiser_gb300.mlp, own tensor-core kernels) trained on
+pairs the batched simulator generates screens each generation: the plain
+Monte Carlo re-values every design whose ensemble members disagree by more
+than the tolerance (1%) and the top 10% by predicted fitness, and stays the
+judge of the surrogate's error.
+
+Per road the surrogate predicts:
+    0 mean over species of E[end population] / initial population
+    1 mean over species of P(end < 0.2 initial)
+    2 min over species of E[end population] / initial population
+from the 16 device-computed features of to_road_features.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import synth
+from .generation import Generation, pack_segments
+from .mlp import MLPSurrogate
+
+OUTPUTS = ("mean_end_ratio", "p_below", "min_end_ratio")
+
+
+def targets(results: np.ndarray) -> np.ndarray:
+    """[R][3] surrogate targets from to_evaluate_roads result blocks."""
+    init = results[:, :, 6]
+    ratio = results[:, :, 2] / np.where(init > 0, init, 1.0)
+    return np.stack([ratio.mean(1), results[:, :, 5].mean(1), ratio.min(1)], 1)
+
+
+def fitness(y: np.ndarray, feats: np.ndarray) -> np.ndarray:
+    """GA objective (higher is better): the weakest species' expected end
+    population ratio, less a road-length cost."""
+    return y[:, 2] - 0.05 * feats[:, 0]
+
+
+def _road(pts):
+    pts = pts[np.argsort(pts[:, 0])]
+    segs = np.column_stack([pts[:-1], pts[1:]])
+    keep = np.hypot(segs[:, 2] - segs[:, 0], segs[:, 3] - segs[:, 1]) > 1e-9
+    return synth.Road(points=pts, segments=segs[keep])
+
+
+def random_roads(scene, n, rng, lo=8, hi=64):
+    return [synth.random_road(scene.W, scene.H, int(rng.integers(lo, hi + 1)), rng)
+            for _ in range(n)]
+
+
+def mutate(road, scene, rng, scale=6.0):
+    """Jitter the control points; sometimes add or drop one (8..64 points)."""
+    pts = road.points + rng.normal(0.0, scale, road.points.shape)
+    if rng.random() < 0.2 and len(pts) < 64:
+        pts = np.vstack([pts, rng.uniform(0, scene.W - 1, (1, 2))])
+    elif rng.random() < 0.2 and len(pts) > 8:
+        pts = np.delete(pts, int(rng.integers(len(pts))), axis=0)
+    return _road(np.clip(pts, 0.0, scene.W - 1.0))
+
+
+def crossover(a, b, rng):
+    """Control points of a left of a random x, of b right of it."""
+    x = rng.uniform(0.0, max(a.points[:, 0].max(), 1.0))
+    pts = np.vstack([a.points[a.points[:, 0] <= x], b.points[b.points[:, 0] > x]])
+    if len(pts) < 8:
+        pts = np.vstack([pts, b.points[: 8 - len(pts)]])
+    return _road(pts[:64])
+
+
+def generate_dataset(gen: Generation, scene, n_samples: int, paths: int, rng,
+                     batch: int | None = None, years: int = 50, seed: int = 0):
+    """(features [n][16], targets [n][3]) of random roads valued by Monte Carlo."""
+    batch = batch or gen.max_roads
+    X, Y = [], []
+    done = 0
+    while done < n_samples:
+        m = min(batch, n_samples - done)
+        packed = pack_segments(random_roads(scene, m, rng))
+        X.append(gen.features(packed))
+        Y.append(targets(gen.evaluate_segments(packed, gen.opts(paths, years, seed=seed,
+                                                                road0=done))))
+        done += m
+    return np.concatenate(X), np.concatenate(Y).astype(np.float32)
+
+
+class Ensemble:
+    """Members with different initialisations; their spread is the surrogate's
+    error estimate."""
+
+    def __init__(self, n: int = 2, seed: int = 0):
+        self.members = [MLPSurrogate(seed + 17 * i) for i in range(n)]
+
+    def fit(self, X, Y, epochs=150, batch=512, lr=2e-3, ctx=None):
+        for m in self.members:
+            m.fit(X, Y, epochs=epochs, batch=batch, lr=lr, ctx=ctx)
+        return self
+
+    def predict(self, X, ctx=None):
+        P = np.stack([m.predict(X, ctx) for m in self.members])
+        mean = P.mean(0)
+        spread = np.abs(P - mean).max(0) / np.maximum(np.abs(mean), 1e-6)
+        return mean, spread
+
+
+def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.01, top=0.1):
+    """Values of a generation with surrogate screening.  Returns (y [R][3],
+    fitness [R], mask of the designs re-valued by Monte Carlo, features)."""
+    packed = pack_segments(roads)
+    feats = gen.features(packed)
+    y, spread = ens.predict(feats, gen.ctx)
+    score = fitness(y, feats)
+    sel = (spread[:, 0] > tol) | (spread[:, 2] > tol)
+    k = max(1, int(round(top * len(roads))))
+    sel[np.argsort(-score)[:k]] = True
+    idx = np.flatnonzero(sel)
+    if idx.size:
+        res = gen.evaluate_segments(pack_segments([roads[i] for i in idx]), opts)
+        y[idx] = targets(res)
+    return y, fitness(y, feats), sel, feats
+
+
+def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: Ensemble | None,
+           tol=0.01, top=0.1):
+    """A small GA (tournament selection, crossover, mutation, elitism).  With
+    an ensemble the generation is screened; without, every design is valued
+    by Monte Carlo.  Returns (best road, its fitness by Monte Carlo, number of
+    Monte Carlo valuations, seconds)."""
+    roads = random_roads(scene, pop, rng)
+    n_mc = 0
+    t0 = time.perf_counter()
+    best, best_fit = None, -np.inf
+    for _ in range(generations):
+        if ens is None:
+            packed = pack_segments(roads)
+            feats = gen.features(packed)
+            y = targets(gen.evaluate_segments(packed, opts))
+            fit = fitness(y, feats)
+            mc = np.ones(len(roads), bool)
+        else:
+            y, fit, mc, feats = screened_values(gen, ens, roads, opts, tol, top)
+        n_mc += int(mc.sum())
+        # only Monte Carlo values may become the incumbent
+        cand = np.flatnonzero(mc)
+        i = cand[np.argmax(fit[cand])]
+        if fit[i] > best_fit:
+            best, best_fit = roads[i], float(fit[i])
+        order = np.argsort(-fit)
+        children = [roads[j] for j in order[: max(1, pop // 10)]]
+        while len(children) < pop:
+            a = roads[max(rng.integers(pop, size=2), key=lambda j: fit[j])]
+            b = roads[max(rng.integers(pop, size=2), key=lambda j: fit[j])]
+            child = crossover(a, b, rng) if rng.random() < 0.5 else a
+            children.append(mutate(child, scene, rng))
+        roads = children
+    return best, best_fit, n_mc, time.perf_counter() - t0
