@@ -57,6 +57,9 @@ def parse():
                     help="one ROV valuation of a configuration-1 road (2 species, ~115 "
                          "patches, 3 controls, 16 bins per dimension), for profilers")
     ap.add_argument("--rov-paths", type=int, default=10000)
+    ap.add_argument("--surrogate-samples", type=int, default=50000,
+                    help="training pairs for the learned surrogate (0: skip that leg)")
+    ap.add_argument("--ga-generations", type=int, default=64)
     return ap.parse_args()
 
 
@@ -183,6 +186,47 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------
+def surrogate_leg(args, gen, scene, P, ctx):
+    """Learned surrogate: an ensemble of two MLPs (own BF16 tensor-core
+    kernels) trained on pairs the batched simulator generates, then a GA of
+    args.ga_generations x 256 roads valued with screening (Monte Carlo on
+    designs whose members disagree by > 1% and on the top 10%) against the
+    same GA valued by Monte Carlo throughout."""
+    import numpy as np
+    from transportoptimiser_gb300 import surrogate_ga as sga
+    t0 = time.perf_counter()
+    X, Y = sga.generate_dataset(gen, scene, args.surrogate_samples, paths=128,
+                                rng=np.random.default_rng(101), seed=77)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ens = sga.Ensemble(2).fit(X, Y, epochs=60, batch=512, lr=2e-3, ctx=ctx)
+    t_fit = time.perf_counter() - t0
+    Xt, Yt = sga.generate_dataset(gen, scene, 1024, paths=1024, rng=np.random.default_rng(202),
+                                  seed=88)
+    pred, _ = ens.predict(Xt, ctx)
+    err = np.abs(pred[:, 0] - Yt[:, 0]) / Yt[:, 0]
+    opts = gen.opts(P, YEARS, seed=5)
+    pop = args.roads
+    out = {}
+    for name, e, tol in (("screened_1pct", ens, 0.01), ("screened_3pct", ens, 0.03),
+                         ("plain_mc", None, 0.0)):
+        _, best, n_mc, secs = sga.run_ga(gen, scene, args.ga_generations, pop, opts,
+                                         np.random.default_rng(7), e, tol)
+        designs = args.ga_generations * pop
+        out[name] = {"designs_per_s": designs / secs, "mc_valuations": n_mc,
+                     "designs": designs, "best_fitness_mc": best, "seconds": secs}
+    return {"model": "MLP 16-128-128-3, ensemble of 2, BF16 tcgen05 GEMMs",
+            "train_pairs": int(len(X)), "train_paths": 128, "data_s": t_data, "fit_s": t_fit,
+            "final_loss": float(ens.members[0].loss_curve[-1]),
+            "heldout_median_rel_err_mean_end_ratio": float(np.median(err)),
+            "ga": out, "ga_generations": args.ga_generations, "ga_population": pop,
+            "screen_rule": "MC where the members disagree by > tol and on the top 10%",
+            "designs_per_s_ratio_screened_1pct_vs_mc":
+                out["screened_1pct"]["designs_per_s"] / out["plain_mc"]["designs_per_s"],
+            "designs_per_s_ratio_screened_3pct_vs_mc":
+                out["screened_3pct"]["designs_per_s"] / out["plain_mc"]["designs_per_s"]}
+
+
 def profile_rov(args):
     """One ROV valuation (ALGO4) of a configuration-1 road on the GPU."""
     from transportoptimiser_gb300 import synth
@@ -354,6 +398,10 @@ def main():
     achieved_tf = flops_per_launch / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
 
+    surrogate = None
+    if rank == 0 and args.surrogate_samples > 0:
+        surrogate = surrogate_leg(args, gen, scene, P, ctx)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         from transportoptimiser_gb300 import build as b
@@ -386,6 +434,7 @@ def main():
                          "dense_equivalent_flops": dense_equiv_flops,
                          "kernel_ms": mte_ms / max(mte_n, 1),
                          "species_model_ms": sm_ms / max(sm_n, 1)},
+            "surrogate": surrogate,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,

@@ -66,11 +66,28 @@ def test_surrogate_gain_over_local_linear_and_plain_ga(ctx):
     ll = np.interp(Xt[:, 9], om[:32], om[32:])
     err_ll = np.median(np.abs(ll - Yt[:, 0]) / Yt[:, 0])
     assert err_mlp < err_ll, (err_mlp, err_ll)
-    # a GA at equal settings: screened (Monte Carlo on designs whose members
-    # disagree by more than 1% and on the top 10%) against Monte Carlo on all
+    # ranking, which the screening relies on: recall of the true top 10% of
+    # held-out designs within each method's predicted top 25%
+    fit_true = sga.fitness(Yt, Xt)
+    true_top = set(np.argsort(-fit_true)[:51])
+
+    def recall(pred_y0):
+        yy = Yt.copy()
+        yy[:, 2] = pred_y0
+        return len(true_top & set(np.argsort(-sga.fitness(yy, Xt))[:128])) / 51
+
+    assert recall(pred[:, 2]) >= recall(ll), (recall(pred[:, 2]), recall(ll))
+    # GAs at equal settings (three seeds): screened (Monte Carlo on designs
+    # whose members disagree by more than the tolerance, 1% or 3%, and on the
+    # top 10%) against Monte Carlo on every design: fewer Monte Carlo
+    # valuations for the same outcome
     opts = gen.opts(128, 50, seed=9)
-    _, fit_s, n_s, _ = sga.run_ga(gen, sc, 6, 128, opts, np.random.default_rng(3), ens)
-    _, fit_p, n_p, _ = sga.run_ga(gen, sc, 6, 128, opts, np.random.default_rng(3), None)
-    assert n_s < 0.8 * n_p, (n_s, n_p)
-    assert fit_s >= fit_p - 0.01 * abs(fit_p), (fit_s, fit_p)
+    for tol, max_frac in ((0.01, 1.0), (0.03, 0.5)):
+        fs, fp, ns, npl = [], [], 0, 0
+        for seed in (3, 4, 5):
+            _, f1, n1, _ = sga.run_ga(gen, sc, 6, 128, opts, np.random.default_rng(seed), ens, tol)
+            _, f2, n2, _ = sga.run_ga(gen, sc, 6, 128, opts, np.random.default_rng(seed), None)
+            fs.append(f1); fp.append(f2); ns += n1; npl += n2
+        assert ns < max_frac * npl, (tol, ns, npl)
+        assert np.mean(fs) >= np.mean(fp) - 0.03 * abs(np.mean(fp)), (tol, fs, fp)
     gen.close()
