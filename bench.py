@@ -387,15 +387,21 @@ def main():
                                seed=0, road=road0 + r, migration=MIG_AUTO, ctx=ctx)
         plain_value = args.plain_roads / (time.perf_counter() - t0)
 
-    # roofline of the migration kernel: useful FLOPs are 2 per stored
-    # non-zero per path-year (the dense-equivalent count is reported too)
+    # roofline of the migration kernel.  The algorithmic count is the dense
+    # contraction's, 2 * P * N^2 * Y per (road, species); the sparse kernel
+    # skips the zeros, so its useful (non-zero) FLOPs are reported beside it.
+    # DRAM traffic per launch: an ncu capture (dram__bytes_read/write.sum) of
+    # the same kernel on 32 roads read 1.59 MB (the CSC matrices, initial
+    # populations and capacities, proportional to road-species count, not to
+    # paths); scaled to this launch's road-species count.
     Nsum2 = float((Ns.astype(np.float64) ** 2).sum())
     nnz = res[:, :, 7].astype(np.float64)
-    flops_per_launch = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() \
-        else 2.0 * P * Nsum2 * YEARS
+    useful_flops = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() else None
     dense_equiv_flops = 2.0 * P * Nsum2 * YEARS
     mte_avg_s = (mte_ms / max(mte_n, 1)) / 1000.0
-    achieved_tf = flops_per_launch / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
+    achieved_tf = dense_equiv_flops / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
+    useful_tf = (useful_flops / mte_avg_s / 1e12) if (useful_flops and mte_avg_s > 0) else None
+    traffic = 1.594368e6 * (args.roads * len(scene.species)) / 96.0
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
 
     surrogate = None
@@ -429,9 +435,13 @@ def main():
                       "roads": args.plain_roads, "note": "one road per call, host entry points"},
             "roofline": {"kernel": "k_" + mte_name, "bound": "tensor", "achieved": achieved_tf,
                          "peak": bf16_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tf / bf16_peak, "peak_kind": peak_kind + " bf16 dense",
-                         "traffic": None, "flops_per_launch": flops_per_launch,
-                         "dense_equivalent_flops": dense_equiv_flops,
+                         "frac": achieved_tf / bf16_peak,
+                         "peak_kind": peak_kind + " bf16 dense (TF32 is half, 3xTF32 a sixth)",
+                         "traffic": traffic, "traffic_note": "bytes per launch, ncu on "
+                         "32 roads scaled by road-species count",
+                         "flops_per_launch": dense_equiv_flops,
+                         "useful_flops_per_launch": useful_flops,
+                         "useful_achieved": useful_tf,
                          "kernel_ms": mte_ms / max(mte_n, 1),
                          "species_model_ms": sm_ms / max(sm_n, 1)},
             "surrogate": surrogate,
