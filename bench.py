@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--profile-only", action="store_true",
                     help="one pilot + one step, for profiler launch lists")
     ap.add_argument("--profile-rov", action="store_true",
-                    help="one ROV valuation of a configuration-1 road (2 species, ~115 "
+                    help="one ROV valuation of a one-road scene (2 species, ~115 "
                          "patches, 3 controls, 16 bins per dimension), for profilers")
     ap.add_argument("--rov-paths", type=int, default=10000)
     ap.add_argument("--surrogate-samples", type=int, default=50000,
@@ -228,7 +228,7 @@ def surrogate_leg(args, gen, scene, P, ctx):
 
 
 def profile_rov(args):
-    """One ROV valuation (ALGO4) of a configuration-1 road on the GPU."""
+    """One ROV valuation (ALGO4) of a 128 x 128 one-road scene with 2 species on the GPU."""
     from transportoptimiser_gb300 import synth
     from transportoptimiser_gb300 import simulate_gpu as sg
     from transportoptimiser_gb300.rov import rov_problem_from_models

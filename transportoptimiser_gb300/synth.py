@@ -129,7 +129,7 @@ def default_species(n_controls: int, flows, habitat_types, threshold: float,
 
 
 def mte_road(seed: int = 0, W: int = 64, tile: int = 12, res: int = 4) -> Scene:
-    """Configuration 0: one road, one species, fixed full traffic."""
+    """64 x 64 grid, one road, one species (the plain MTE workload)."""
     rng = _rng(seed)
     base = habitat_map(W, W, tile, [0.4, 0.3, 0.2, 0.1], [PRIMARY, MARGINAL, OTHER, CLEAR], rng)
     flows = np.array([0.0, 0.5, 1.0])
@@ -142,7 +142,7 @@ def mte_road(seed: int = 0, W: int = 64, tile: int = 12, res: int = 4) -> Scene:
 
 def rov_road(seed: int = 0, W: int = 128, tile: int = 24, res: int = 7,
              n_species: int = 2) -> Scene:
-    """Configuration 1: one road, two species, three flow controls."""
+    """128 x 128 grid, one road, two species, three flow controls (the ROV workload)."""
     rng = _rng(seed)
     base = habitat_map(W, W, tile, [0.4, 0.3, 0.2, 0.1], [PRIMARY, MARGINAL, OTHER, CLEAR], rng)
     flows = np.array([0.0, 0.5, 1.0])
@@ -158,7 +158,7 @@ def rov_road(seed: int = 0, W: int = 128, tile: int = 24, res: int = 7,
 
 def generation(seed: int = 0, n_roads: int = 256, W: int = 200, tile: int = 30,
                res: int = 10, n_species: int = 3) -> Scene:
-    """Configuration 2: a GA generation of roads of 8-64 control points."""
+    """200 x 200 grid, 5 habitat types, a GA generation of roads of 8-64 control points."""
     rng = _rng(seed)
     base = habitat_map(W, W, tile, [0.35, 0.25, 0.15, 0.15, 0.1],
                        [PRIMARY, MARGINAL, OTHER, 5, CLEAR], rng)
