@@ -29,11 +29,13 @@ namespace {
 constexpr int kLanes = 32;
 
 // One CTA per matrix (rs*C + c): row k of the destination-major matrix is
-// destination k's column.  Entries > 0 in ascending origin order.
-__global__ void k_pack_csc(const float* __restrict__ mmm, int NP, int C,
-                           const int* __restrict__ n_patches, int cap,
-                           int* __restrict__ ptr, uint16_t* __restrict__ idx,
-                           float* __restrict__ val, int* __restrict__ nnz) {
+// destination k's column.  Entries > 0 in ascending origin order.  A warp
+// per row reads it coalesced: a count pass, a CTA scan of the row counts,
+// then a ballot-compaction pass.
+__global__ void __launch_bounds__(1024)
+k_pack_csc(const float* __restrict__ mmm, int NP, int C, const int* __restrict__ n_patches,
+           int cap, int* __restrict__ ptr, uint16_t* __restrict__ idx, float* __restrict__ val,
+           int* __restrict__ nnz) {
     const int mtx = blockIdx.x;
     const int rs = mtx / C;
     const int N = n_patches[rs];
@@ -42,29 +44,48 @@ __global__ void k_pack_csc(const float* __restrict__ mmm, int NP, int C,
     uint16_t* ix = idx + (size_t)mtx * cap;
     float* vv = val + (size_t)mtx * cap;
     __shared__ int s_cnt[1024 + 1];
-    __shared__ int s_tot;
-    for (int k = threadIdx.x; k <= NP; k += blockDim.x) s_cnt[k] = 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < NP; k += blockDim.x) {
+    __shared__ int s_w[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int k = warp; k < NP; k += nw) {
         int c = 0;
         if (k < N)
-            for (int l = 0; l < N; ++l) c += M[(size_t)k * NP + l] > 0.0f;
-        s_cnt[k + 1] = c;
+            for (int l0 = 0; l0 < N; l0 += 32) {
+                const int l = l0 + lane;
+                c += __popc(__ballot_sync(0xffffffffu, l < N && M[(size_t)k * NP + l] > 0.0f));
+            }
+        if (lane == 0) s_cnt[k] = c;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < NP; ++k) s_cnt[k + 1] += s_cnt[k];
-        s_tot = s_cnt[NP];
-        nnz[mtx] = (s_tot <= cap) ? s_tot : -1;
+    // exclusive scan of s_cnt[0..NP) (NP <= 1024: one value per thread)
+    const int v = threadIdx.x < NP ? s_cnt[threadIdx.x] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
+    if (lane == 31) s_w[warp] = x;
+    __syncthreads();
+    int wb = 0, tot = 0;
+    for (int w = 0; w < nw; ++w) { if (w < warp) wb += s_w[w]; tot += s_w[w]; }
+    __syncthreads();
+    if (threadIdx.x < NP) s_cnt[threadIdx.x] = wb + x - v;
+    if (threadIdx.x == 0) { s_cnt[NP] = tot; nnz[mtx] = (tot <= cap) ? tot : -1; }
     __syncthreads();
     for (int k = threadIdx.x; k <= NP; k += blockDim.x) p[k] = s_cnt[k];
-    if (s_tot > cap) return;
-    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+    if (tot > cap) return;
+    for (int k = warp; k < N; k += nw) {
         int o = s_cnt[k];
-        for (int l = 0; l < N; ++l) {
-            float m = M[(size_t)k * NP + l];
-            if (m > 0.0f) { ix[o] = (uint16_t)l; vv[o] = m; ++o; }
+        for (int l0 = 0; l0 < N; l0 += 32) {
+            const int l = l0 + lane;
+            const float m = (l < N) ? M[(size_t)k * NP + l] : 0.0f;
+            const unsigned b = __ballot_sync(0xffffffffu, m > 0.0f);
+            if (m > 0.0f) {
+                const int q = o + __popc(b & lt);
+                ix[q] = (uint16_t)l;
+                vv[q] = m;
+            }
+            o += __popc(b);
         }
     }
 }
@@ -80,10 +101,13 @@ __device__ __forceinline__ float grouped4(float a, float b, float c, float d) {
 // ---------------------------------------------------------------------------
 constexpr int kMaxG = 4;
 
-template <int MAXG>
-__global__ void __launch_bounds__(1024, 1)
+template <int MAXG, int PPL>
+__global__ void __launch_bounds__(PPL == 1 ? 1024 : 768, 1)
 k_mte_sparse(to_mte_args a, to_csc csc) {
-    extern __shared__ unsigned char sm_raw[];
+    // PPL paths per lane: lane owns paths lane + 32 i; every non-zero read
+    // from shared memory serves all of them
+    constexpr int PW = kLanes * PPL;                           // paths per CTA
+    extern __shared__ __align__(16) unsigned char sm_raw[];
     const int NE = a.npe, NG = NE >> 2, NP = a.npad;
     const int rs = blockIdx.y;
     const int road = rs / a.S, sp = rs - road * a.S;
@@ -93,17 +117,16 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     if (nnz < 0 || nnz > csc.cap_smem || a.n_patches[rs] > NE) {
         // outside the shape this launch was planned for: flag, no result
         if (threadIdx.x == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_PLAN);
-        const int p = blockIdx.x * kLanes + (int)threadIdx.x;
-        if (threadIdx.x < kLanes && p < a.n_paths) a.end_pops[(size_t)rs * a.n_paths + p] = NAN;
+        const int p = blockIdx.x * PW + (int)threadIdx.x;
+        if (threadIdx.x < PW && p < a.n_paths) a.end_pops[(size_t)rs * a.n_paths + p] = NAN;
         return;
     }
-    float* cur = reinterpret_cast<float*>(sm_raw);             // [NE][32]
-    float* part = cur + (size_t)NE * kLanes;                   // [NG][32]
-    float* capv = part + (size_t)NG * kLanes;                  // [NE]
-    float* gm = capv + NE;                                     // [32]
-    int* cptr = reinterpret_cast<int*>(gm + kLanes);           // [NE+1]
-    float* cval = reinterpret_cast<float*>(cptr + NE + 1);     // [cap_smem]
-    uint16_t* cidx = reinterpret_cast<uint16_t*>(cval + csc.cap_smem);   // [cap_smem]
+    int2* cent = reinterpret_cast<int2*>(sm_raw);              // [cap_smem] (row byte offset, value)
+    float* cur = reinterpret_cast<float*>(cent + csc.cap_smem);// [NE][PW]
+    float* part = cur + (size_t)NE * PW;                       // [NG][PW]
+    float* capv = part + (size_t)NG * PW;                      // [NE]
+    float* gm = capv + NE;                                     // [PW]
+    int* cptr = reinterpret_cast<int*>(gm + PW);               // [NE+1]
 
     const int N = a.n_patches[rs];
     const int N4 = (N + 3) & ~3;
@@ -113,10 +136,10 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
                 p6 = sp8[6], p7 = sp8[7];
     const float sj2 = p5 * p5;
     const uint32_t road_id = (uint32_t)(a.road0 + road);
-    const int path = blockIdx.x * kLanes + lane;
+    const int path0 = blockIdx.x * PW + lane;
 
-    for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
-        int k = q / kLanes;
+    for (int q = threadIdx.x; q < NE * PW; q += blockDim.x) {
+        int k = q / PW;
         cur[q] = (k < N) ? ip[k] : 0.0f;
     }
     for (int k = threadIdx.x; k < NE; k += blockDim.x)
@@ -124,47 +147,69 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     for (int k = threadIdx.x; k <= NE; k += blockDim.x)
         cptr[k] = csc.ptr[(size_t)mtx * (NP + 1) + (k <= NP ? k : NP)];
     for (int e = threadIdx.x; e < nnz; e += blockDim.x) {
-        cval[e] = csc.val[(size_t)mtx * csc.cap + e];
-        cidx[e] = csc.idx[(size_t)mtx * csc.cap + e];
+        const int l = csc.idx[(size_t)mtx * csc.cap + e];
+        cent[e] = make_int2(l * PW * (int)sizeof(float),
+                            __float_as_int(csc.val[(size_t)mtx * csc.cap + e]));
     }
-    if (warp == 0) gm[lane] = p0;
+    for (int i = threadIdx.x; i < PW; i += blockDim.x) gm[i] = p0;
     __syncthreads();
 
     for (int t = 0; t < a.n_years; ++t) {
-        if (warp == 0) {
+        for (int i = threadIdx.x; i < PW; i += blockDim.x) {
+            const uint32_t path = (uint32_t)(blockIdx.x * PW + i);
             float uj = to_uniform1(a.seed, TO_STREAM_SP_JUMP, road_id, path, t, sp);
             float zb = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road_id, path, t, sp);
             float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road_id, path, t, sp);
             float jump = (uj < p6) ? 1.0f : 0.0f;
             float brown = zb * p2;
             float jsz = (a.sem == 0) ? (zj * sj2 - sj2 / 2.0f) : (zj * p5 - sj2 / 2.0f);
-            float g = gm[lane];
-            gm[lane] = g + p4 * (p1 - g) * a.dt + g * brown + (to_expf(jsz) - 1.0f) * g * jump;
+            float g = gm[i];
+            gm[i] = g + p4 * (p1 - g) * a.dt + g * brown + (to_expf(jsz) - 1.0f) * g * jump;
         }
         __syncthreads();
-        const float g = gm[lane];
+        float g[PPL];
+#pragma unroll
+        for (int i = 0; i < PPL; ++i) g[i] = gm[lane + kLanes * i];
         const bool last = (t == a.n_years - 1);
-        float nv[MAXG][4];
+        float nv[MAXG][4][PPL];
 #pragma unroll
         for (int gi = 0; gi < MAXG; ++gi) {
             const int grp = warp + gi * W;
             if (grp < NG) {
-            float z[4];
-            to_normal4(a.seed, TO_STREAM_GROWTH, road_id, path, t,
-                       (uint32_t)((sp * N4) >> 2) + grp, z);
-            float m4[4];
+                float z[PPL][4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                int k = grp * 4 + j;
-                float acc = 0.0f;
-                for (int e = cptr[k]; e < cptr[k + 1]; ++e)
-                    acc = fmaf(cur[(int)cidx[e] * kLanes + lane], cval[e], acc);
-                m4[j] = acc;
-                float gr = fmaf(p7 * z[j], g, g);
-                float c = capv[k];
-                nv[gi][j] = acc * (1.0f + gr * (c - acc) / c);
-            }
-            if (last) part[grp * kLanes + lane] = grouped4(m4[0], m4[1], m4[2], m4[3]);
+                for (int i = 0; i < PPL; ++i)
+                    to_normal4(a.seed, TO_STREAM_GROWTH, road_id, (uint32_t)(path0 + kLanes * i), t,
+                               (uint32_t)((sp * N4) >> 2) + grp, z[i]);
+                float m4[4][PPL];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = grp * 4 + j;
+                    float acc[PPL];
+#pragma unroll
+                    for (int i = 0; i < PPL; ++i) acc[i] = 0.0f;
+                    const int e1 = cptr[k + 1];
+                    for (int e = cptr[k]; e < e1; ++e) {
+                        const int2 ce = cent[e];
+                        const float* row = reinterpret_cast<const float*>(
+                            reinterpret_cast<const unsigned char*>(cur) + ce.x) + lane;
+                        const float v = __int_as_float(ce.y);
+#pragma unroll
+                        for (int i = 0; i < PPL; ++i) acc[i] = fmaf(row[kLanes * i], v, acc[i]);
+                    }
+                    const float c = capv[k];
+#pragma unroll
+                    for (int i = 0; i < PPL; ++i) {
+                        m4[j][i] = acc[i];
+                        float gr = fmaf(p7 * z[i][j], g[i], g[i]);
+                        nv[gi][j][i] = acc[i] * (1.0f + gr * (c - acc[i]) / c);
+                    }
+                }
+                if (last)
+#pragma unroll
+                    for (int i = 0; i < PPL; ++i)
+                        part[grp * PW + lane + kLanes * i] =
+                            grouped4(m4[0][i], m4[1][i], m4[2][i], m4[3][i]);
             }
         }
         __syncthreads();
@@ -173,19 +218,24 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
             const int grp = warp + gi * W;
             if (grp < NG) {
 #pragma unroll
-                for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
+                for (int j = 0; j < 4; ++j)
+#pragma unroll
+                    for (int i = 0; i < PPL; ++i)
+                        cur[(grp * 4 + j) * PW + lane + kLanes * i] = nv[gi][j][i];
             }
         }
     }
     __syncthreads();
-    if (warp == 0 && path < a.n_paths) {
+    for (int i = threadIdx.x; i < PW; i += blockDim.x) {
+        const int path = blockIdx.x * PW + i;
+        if (path >= a.n_paths) continue;
         float e = 0.0f;
         if (a.n_years > 0 && a.sem == 0) {
-            for (int grp = 0; grp < NG; ++grp) e = e + part[grp * kLanes + lane];
+            for (int grp = 0; grp < NG; ++grp) e = e + part[grp * PW + i];
         } else {
             for (int grp = 0; grp < NG; ++grp) {
-                const float* v = cur + (size_t)grp * 4 * kLanes + lane;
-                e = e + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
+                const float* v = cur + (size_t)grp * 4 * PW + i;
+                e = e + grouped4(v[0], v[PW], v[2 * PW], v[3 * PW]);
             }
         }
         a.end_pops[(size_t)rs * a.n_paths + path] = e;
@@ -344,17 +394,28 @@ namespace to_k {
 to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_patches,
                    int n_rs, to_csc& csc) {
     if (NP > 1024) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NP);
-    k_pack_csc<<<n_rs * C, 256, 0, ctx->stream>>>(mmm, NP, C, n_patches, csc.cap,
+    k_pack_csc<<<n_rs * C, 1024, 0, ctx->stream>>>(mmm, NP, C, n_patches, csc.cap,
                                                  csc.ptr, csc.idx, csc.val, csc.nnz);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }
 
-size_t mte_sparse_smem(int NE, int cap_smem) {
-    if (NE > 32 * kMaxG * 4) return ~size_t(0);
-    int NG = NE / 4;
-    return (size_t)(NE * kLanes + NG * kLanes + NE + kLanes) * 4 + (size_t)(NE + 1) * 4 +
-           (size_t)cap_smem * 4 + (size_t)cap_smem * 2 + 16;
+// paths per lane of the MTE kernel: two when the tile fits (every non-zero
+// read then serves two paths), else one
+static int mte_ppl(int NE, int cap_smem, size_t smem_cap);
+
+size_t mte_sparse_smem_ppl(int NE, int cap_smem, int ppl) {
+    const int maxg = kMaxG, maxw = ppl == 1 ? 32 : 24;
+    if (NE > maxw * maxg * 4) return ~size_t(0);
+    const int NG = NE / 4, PW = kLanes * ppl;
+    return (size_t)cap_smem * 8 + (size_t)(NE * PW + NG * PW + NE + PW) * 4 +
+           (size_t)(NE + 1) * 4 + 16;
+}
+
+size_t mte_sparse_smem(int NE, int cap_smem) { return mte_sparse_smem_ppl(NE, cap_smem, 1); }
+
+static int mte_ppl(int NE, int cap_smem, size_t smem_cap) {
+    return mte_sparse_smem_ppl(NE, cap_smem, 2) <= smem_cap ? 2 : 1;
 }
 
 // warps per CTA: enough that no warp owns more than kMaxG groups of four
@@ -371,17 +432,25 @@ to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
     if (a.npe <= 0) a.npe = a.npad;
     if (!a.flags) a.flags = ctx->d_flags;
     const int NE = a.npe;
-    size_t smem = mte_sparse_smem(NE, csc.cap_smem);
+    const int ppl = (a.n_paths > kLanes) ? mte_ppl(NE, csc.cap_smem, ctx->smem_optin) : 1;
+    size_t smem = mte_sparse_smem_ppl(NE, csc.cap_smem, ppl);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "sparse MTE needs %zu B", smem);
-    TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int warps = warps_for(NE, 4);
     if ((NE / 4 + warps - 1) / warps > kMaxG)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NE);
-    dim3 grid((a.n_paths + kLanes - 1) / kLanes, n_rs);
+    const int PW = kLanes * ppl;
+    dim3 grid((a.n_paths + PW - 1) / PW, n_rs);
     to_prof_begin(ctx, "mte_sparse");
-    k_mte_sparse<kMaxG><<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
+    if (ppl == 2) {
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG, 2>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_mte_sparse<kMaxG, 2><<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
+    } else {
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG, 1>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_mte_sparse<kMaxG, 1><<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
+    }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;
