@@ -270,13 +270,17 @@ def main():
     from transportoptimiser_gb300.generation import Generation, pack_roads
     from transportoptimiser_gb300 import simulate_gpu as sg
 
+    from transportoptimiser_gb300 import shard
     scene = synth.generation(0, n_roads=args.roads)
+    if rank > 0:
+        # each rank values its own generation of roads (weak scaling)
+        scene.roads = shard.rank_roads(scene, args.roads, rank)
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     gen = Generation(scene, max_roads=args.roads, max_patches=512, ctx=ctx)
     packed = pack_roads(scene, scene.roads)
-    road0 = rank * 1_000_000
+    road0 = shard.road0(rank)
 
     # pilot (untimed): N* per road
     pilot = gen.evaluate(packed, gen.opts(PILOT_PATHS, YEARS, seed=1, road0=road0,
@@ -347,10 +351,7 @@ def main():
         ctx.profile(False)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = sum(step_ms) / len(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = shard.max_over_ranks(ms)
     value = args.roads * world / (ms / 1000.0)
     res = d_res.cpu().numpy().reshape(args.roads, len(scene.species), 8)
 
