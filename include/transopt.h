@@ -396,6 +396,17 @@ to_status to_road_features_d(to_ctx ctx, to_gen gen, int n_roads, const int* seg
                              const double* segs, const int* cell_off, const int* cells,
                              float* features);
 
+/* Local-linear grid surrogate at n_points points (predictors [n][n_dims]),
+ * surrogate [R*d axis values | R^d values] as the builders return it.
+ * mode 0: SimulateGPU::interpolateSurrogateMulti (SimulateGPU.h:257 /
+ * SimulateGPU.cu:5919-5968 and its kernel :3077-3155) as it computes, in
+ * float; mode 1: multilinear interpolation in double; mode 2:
+ * Utility::interpolateSurrogate (Utility.cpp:253-363), the per-road host
+ * evaluation, in double, batched.  Host arrays. */
+to_status to_interpolate_surrogate(to_ctx ctx, int n_points, int n_dims, int dim_res,
+                                   const double* surrogate, const double* predictors,
+                                   double* results, int mode);
+
 /* The autotuner's record: one line per tuned shape, "kind ne paths rs ->
  * choice (sparse ms, simt ms, tc ms)", -1 where a kernel was not feasible.
  * Writes at most len bytes (NUL-terminated); returns the number of lines. */

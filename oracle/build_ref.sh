@@ -26,7 +26,14 @@ mkdir -p "$OUT"
 # dense2Sparse; kNN distance (texture form), insertion sort, sqrt.
 {
     cat "$HERE/ref_shim.h"
-    sed -n '129,190p;256,279p;454,493p;498,573p;595,717p;720,730p;789,1195p;2210,2784p;2934,3073p;3077,3155p;5973,5996p' "$SG"
+    sed -n '129,190p;256,279p;454,493p;498,573p;595,717p;720,730p;789,1195p;2210,2784p;2934,3073p' "$SG"
+    # interpolateMulti reads its coefficient buffer after freeing it (device
+    # heap memory keeps the value; the host allocator reuses it), so free is
+    # a no-op inside it here
+    echo '#define free(p) ((void)(p))'
+    sed -n '3077,3155p' "$SG"
+    echo '#undef free'
+    sed -n '5973,5996p' "$SG"
     sed -n '77,90p;340,411p;424,429p' "$KNN"
 } | g++ -x c++ -std=c++14 -O2 -fPIC -w -c - -o "$OUT/ref_kernels.o"
 g++ -std=c++14 -O2 -fPIC -w -I "$REF/include/utilities" -c "$LAB" -o "$OUT/labelmethod.o"

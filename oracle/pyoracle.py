@@ -539,3 +539,30 @@ def adjoint_forward(problem, controls, crossings, hazard, theta, threads=None):
     lib.or_adjoint_forward(C.byref(pr), _p(th, C.c_double), _p(out, C.c_double),
                            threads or os.cpu_count() or 1)
     return out
+
+
+# ---- surrogate evaluation (oracle_interp.c, reference kernel) -----------------
+def interpolate_surrogate(surrogate, predictors, R, d, mode):
+    lib = oracle()
+    lib.or_interpolate_surrogate.argtypes = [C.c_int, C.c_int, C.c_int, c_double_p, c_double_p,
+                                             c_double_p, C.c_int, c_float_p, c_float_p]
+    s = np.ascontiguousarray(surrogate, np.float64)
+    p = np.ascontiguousarray(predictors, np.float64).reshape(-1, d)
+    out = np.zeros(p.shape[0])
+    fs = np.zeros(s.size, np.float32)
+    fp = np.zeros(p.size, np.float32)
+    lib.or_interpolate_surrogate(p.shape[0], d, R, _p(s, C.c_double), _p(p, C.c_double),
+                                 _p(out, C.c_double), mode, _p(fs, C.c_float), _p(fp, C.c_float))
+    return out
+
+
+def ref_interpolate_multi(surrogate, predictors, R, d):
+    lib = ref()
+    lib.ref_interpolate_multi.argtypes = [C.c_int, C.c_int, C.c_int, c_float_p, c_float_p,
+                                          c_float_p]
+    s = np.ascontiguousarray(surrogate, np.float32)
+    p = np.ascontiguousarray(predictors, np.float32).reshape(-1, d)
+    out = np.zeros(p.shape[0], np.float32)
+    lib.ref_interpolate_multi(p.shape[0], d, R, _p(s, C.c_float), _p(p, C.c_float),
+                              _p(out, C.c_float))
+    return out

@@ -53,6 +53,8 @@ void allocateXYRegressionData(int noPaths, int noControls, int noDims,
         float* condExp, int* dataPoints, float* xvals, float* yvals);
 void computeStateMinMax(int noControls, int noDims, int noPaths,
         int* dataPoints, float* xvals, float* xmins, float* xmaxes);
+void interpolateMulti(int points, int noDims, int dimRes, float* surrogate,
+        float* predictors, float* results);
 void createQueryPoints(int noPoints, int noDims, int dimRes, int control,
         int noControls, int year, float* xmins, float* xmaxes,
         float* regression, float* queryPts);
@@ -450,6 +452,18 @@ void ref_build_surrogate_rov(int n, int d, const float* pred, const float* y, in
             rovCorrection(Qn, d, R, 1, 1, 0, 0, sur.data());
         }
     for (size_t i = 0; i < sur.size(); ++i) out[i] = sur[i];
+}
+
+/* SimulateGPU::interpolateSurrogateMulti's kernel (SimulateGPU.cu:3077-3155)
+ * over n points (float, as the wrapper casts its inputs) */
+void ref_interpolate_multi(int n, int d, int R, const float* sur, const float* pred,
+                           float* out) {
+    std::vector<float> s(sur, sur + (size_t)R * d + (size_t)std::pow((double)R, d));
+    std::vector<float> p(pred, pred + (size_t)n * d);
+    for (int i = 0; i < n; ++i) {
+        set_thread((unsigned)i, 0);
+        interpolateMulti(n, d, R, s.data(), p.data(), out);
+    }
 }
 
 }  /* extern "C" */

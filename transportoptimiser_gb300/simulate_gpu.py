@@ -265,6 +265,22 @@ def buildSurrogateMTECUDA(iars, pops_mean, pops_sd, dim_res, ctx: Context | None
     return om, osd
 
 
+def interpolateSurrogateMulti(surrogate, predictors, dim_res, n_dims, mode=0,
+                              ctx: Context | None = None):
+    """SimulateGPU::interpolateSurrogateMulti (SimulateGPU.cu:5919) batched:
+    predictors [n][n_dims].  mode 0 the reference kernel's float arithmetic,
+    1 multilinear in double, 2 Utility::interpolateSurrogate (Utility.cpp:253)."""
+    ctx = ctx or context()
+    s = np.ascontiguousarray(surrogate, np.float64)
+    p = np.ascontiguousarray(predictors, np.float64).reshape(-1, n_dims)
+    out = np.zeros(p.shape[0])
+    ctx.check(ctx.lib.to_interpolate_surrogate(ctx.handle, p.shape[0], n_dims, dim_res,
+                                               ptr(s, C.c_double), ptr(p, C.c_double),
+                                               ptr(out, C.c_double), mode),
+              "to_interpolate_surrogate")
+    return out
+
+
 def buildSurrogateROVCUDA(predictors, values, values_sd, dim_res, sem=0,
                           ctx: Context | None = None):
     """SimulateGPU::buildSurrogateROVCUDA (SimulateGPU.cu:5694): predictors
