@@ -407,6 +407,15 @@ to_status to_interpolate_surrogate(to_ctx ctx, int n_points, int n_dims, int dim
                                    const double* surrogate, const double* predictors,
                                    double* results, int mode);
 
+/* RoadGA::generateSample (RoadGA.cpp:3288-3462): choose n designs to
+ * simulate from candidates [n_candidates][n_dims] (host, row-major) given
+ * the current samples [n_current][n_dims] (may be 0: then the first two are
+ * the most distant pair), by the reference's max-min rule on its projected
+ * and Euclidean distances after joint normalisation.  sample[n] receives
+ * candidate indices. */
+to_status to_select_samples(to_ctx ctx, int n_current, const double* current, int n_candidates,
+                            const double* candidates, int n_dims, int n, int* sample);
+
 /* The autotuner's record: one line per tuned shape, "kind ne paths rs ->
  * choice (sparse ms, simt ms, tc ms)", -1 where a kernel was not feasible.
  * Writes at most len bytes (NUL-terminated); returns the number of lines. */

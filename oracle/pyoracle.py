@@ -566,3 +566,17 @@ def ref_interpolate_multi(surrogate, predictors, R, d):
     lib.ref_interpolate_multi(p.shape[0], d, R, _p(s, C.c_float), _p(p, C.c_float),
                               _p(out, C.c_float))
     return out
+
+
+# ---- GA sample selection (oracle_sample.c) ------------------------------------
+def select_samples(current, candidates, n):
+    lib = oracle()
+    lib.or_select_samples.argtypes = [C.c_int, c_double_p, C.c_int, c_double_p, C.c_int, C.c_int,
+                                      c_int_p]
+    cand = np.ascontiguousarray(candidates, np.float64)
+    d = cand.shape[1]
+    cur = np.ascontiguousarray(current if current is not None else np.zeros((0, d)), np.float64)
+    out = np.zeros(n, np.int32)
+    lib.or_select_samples(cur.shape[0], _p(cur, C.c_double) if cur.size else None, cand.shape[0],
+                          _p(cand, C.c_double), d, n, _p(out, C.c_int))
+    return out

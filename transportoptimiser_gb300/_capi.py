@@ -175,6 +175,8 @@ SIGNATURES = {
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
     "to_ctx_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "to_select_samples": (C.c_int, [C.c_void_p, C.c_int, c_double_p, C.c_int, c_double_p,
+                                    C.c_int, C.c_int, c_int_p]),
     "to_interpolate_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, c_double_p,
                                            c_double_p, c_double_p, C.c_int]),
     "to_road_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, c_int_p, c_double_p,

@@ -76,9 +76,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
 def build_oracle(force: bool = False) -> Path:
     srcs = [ORACLE_DIR / "oracle.c", ORACLE_DIR / "oracle_rov.c", ORACLE_DIR / "oracle_mlp.c",
-            ORACLE_DIR / "oracle_adjoint.c", ORACLE_DIR / "oracle_interp.c"]
+            ORACLE_DIR / "oracle_adjoint.c", ORACLE_DIR / "oracle_interp.c",
+            ORACLE_DIR / "oracle_sample.c"]
     deps = srcs + [ORACLE_DIR / "oracle.h", ORACLE_DIR / "oracle_rov.h", ORACLE_DIR / "oracle_mlp.h",
                    ORACLE_DIR / "oracle_adjoint.h", ORACLE_DIR / "oracle_interp.h",
+                   ORACLE_DIR / "oracle_sample.h",
                    CSRC / "to_math.h", CSRC / "to_lsm_math.h"]
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     if force or _stale(ORACLE_LIB, deps):

@@ -281,6 +281,20 @@ def interpolateSurrogateMulti(surrogate, predictors, dim_res, n_dims, mode=0,
     return out
 
 
+def generateSample(current, candidates, n, ctx: Context | None = None) -> np.ndarray:
+    """RoadGA::generateSample (RoadGA.cpp:3288) on the device: indices of n
+    candidates chosen by the reference's max-min rule."""
+    ctx = ctx or context()
+    cand = np.ascontiguousarray(candidates, np.float64)
+    d = cand.shape[1]
+    cur = np.ascontiguousarray(current if current is not None else np.zeros((0, d)), np.float64)
+    out = np.zeros(n, np.int32)
+    ctx.check(ctx.lib.to_select_samples(ctx.handle, cur.shape[0], ptr(cur, C.c_double) if cur.size else None,
+                                        cand.shape[0], ptr(cand, C.c_double), d, n,
+                                        ptr(out, C.c_int)), "to_select_samples")
+    return out
+
+
 def buildSurrogateROVCUDA(predictors, values, values_sd, dim_res, sem=0,
                           ctx: Context | None = None):
     """SimulateGPU::buildSurrogateROVCUDA (SimulateGPU.cu:5694): predictors
