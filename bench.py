@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--surrogate-samples", type=int, default=50000,
                     help="training pairs for the learned surrogate (0: skip that leg)")
     ap.add_argument("--ga-generations", type=int, default=64)
+    ap.add_argument("--no-rov-leg", dest="rov_leg", action="store_false",
+                    help="skip the one-road ROV and adjoint timings")
     return ap.parse_args()
 
 
@@ -225,6 +227,58 @@ def surrogate_leg(args, gen, scene, P, ctx):
                 out["screened_1pct"]["designs_per_s"] / out["plain_mc"]["designs_per_s"],
             "designs_per_s_ratio_screened_3pct_vs_mc":
                 out["screened_3pct"]["designs_per_s"] / out["plain_mc"]["designs_per_s"]}
+
+
+def rov_adjoint_leg(ctx, rov_paths=10000, adj_paths=20000, reps=3):
+    """One-road ROV (2 species, ~115 patches, 3 controls, 3 exogenous
+    processes, 16 bins per dimension, 50 years) timed through the public
+    entry point, then the adjoint of its frozen optimal policy (13
+    parameters) at adj_paths paths: forward and one backward per output."""
+    import numpy as np
+    from transportoptimiser_gb300 import synth
+    from transportoptimiser_gb300 import simulate_gpu as sg
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    from transportoptimiser_gb300.adjoint import FrozenPolicy, theta_from_problem
+    sc = synth.rov_road(0, n_species=2)
+    models = []
+    for s in range(2):
+        sp = sc.species[s]
+        hab = sc.hab_map(sc.roads[0])
+        models.append(sg.createSpeciesModel(hab, sc.pop_map(sp, hab), sc.W, sc.H, sc.res,
+                                            sp.habitats, sc.roads[0].colmajor(), sc.roads[0].G,
+                                            sp.hazard, sp.lambda_mean, sem=1, max_patches=512,
+                                            ctx=ctx))
+    rp = rov_problem_from_models(models, sc, n_paths=rov_paths, n_years=YEARS, dim_res=16,
+                                 sem=1, n_processes=3, demand=True)
+    out = sg.simulateROVCUDA(rp, want=(), ctx=ctx)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = sg.simulateROVCUDA(rp, want=(), ctx=ctx)
+        ts.append(time.perf_counter() - t0)
+    rov = {"paths": rov_paths, "ms_per_valuation": 1000.0 * statistics.median(ts),
+           "value": float(out["stats"][0]), "se": float(out["value_se"]),
+           "patches": [int(m["N"]) for m in models]}
+    ra = rov_problem_from_models(models, sc, n_paths=adj_paths, n_years=YEARS, dim_res=16,
+                                 sem=1, n_processes=3, demand=True)
+    pol = sg.simulateROVCUDA(ra, want=("opt_cont",), ctx=ctx)
+    ctl = pol["opt_cont"].reshape(YEARS, adj_paths).astype(np.int32)
+    hz = np.asarray(sc.species[0].hazard, np.float64)
+    fp = FrozenPolicy(ra, ctl, [m["crossings"] for m in models], hz, ctx)
+    th = theta_from_problem(ra, hz)
+    o, tape = fp.forward(th)
+    fp.free(tape)
+    t0 = time.perf_counter()
+    o, tape = fp.forward(th)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    J = [fp.backward(tape, np.eye(3)[i]) for i in range(3)]
+    t_bwd = (time.perf_counter() - t0) / 3
+    fp.free(tape)
+    adj = {"paths": adj_paths, "parameters": int(th.size), "forward_ms": 1000.0 * t_fwd,
+           "backward_ms_per_output": 1000.0 * t_bwd, "outputs": [float(x) for x in o],
+           "dPV_dtheta_fuel": float(J[0][0]), "checkpoint_years": 10}
+    return {"rov": rov, "adjoint": adj}
 
 
 def profile_rov(args):
@@ -405,6 +459,8 @@ def main():
     traffic = 1.594368e6 * (args.roads * len(scene.species)) / 96.0
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
 
+    rov_adj = rov_adjoint_leg(ctx) if rank == 0 and args.rov_leg else None
+
     surrogate = None
     if rank == 0 and args.surrogate_samples > 0:
         surrogate = surrogate_leg(args, gen, scene, P, ctx)
@@ -446,6 +502,8 @@ def main():
                          "kernel_ms": mte_ms / max(mte_n, 1),
                          "species_model_ms": sm_ms / max(sm_n, 1)},
             "surrogate": surrogate,
+            "rov_one_road": rov_adj["rov"] if rov_adj else None,
+            "adjoint": rov_adj["adjoint"] if rov_adj else None,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
             "clocks": clocks,
