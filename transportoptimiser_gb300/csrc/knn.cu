@@ -37,10 +37,7 @@ constexpr int kStore = 2 * TO_KNN_KMAX;
 
 struct WarpScratch {
     unsigned long long sel[kStore];
-    union {
-        unsigned hist[256];                   // radix select
-        unsigned long long out[TO_KNN_KMAX];  // refinement compaction
-    };
+    unsigned hist[256];                       // radix select
 };
 
 __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int dim,
@@ -51,6 +48,29 @@ __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int
         s = fmaf(t, t, s);
     }
     return s;
+}
+
+// bitonic sort of ws.sel[0..cnt), padded to a power of two; every lane
+// owns compare-exchange pairs, so no lane idles
+__device__ void warp_sort_sel(WarpScratch& ws, int cnt) {
+    const int lane = threadIdx.x & 31;
+    int kp = 1;
+    while (kp < cnt) kp <<= 1;
+    for (int i = cnt + lane; i < kp; i += 32) ws.sel[i] = ~0ull;
+    __syncwarp();
+    const int half = kp >> 1;
+    for (int size = 2; size <= kp; size <<= 1) {
+        for (int s2 = size >> 1; s2 > 0; s2 >>= 1) {
+            for (int pi = lane; pi < half; pi += 32) {
+                const int i = ((pi & ~(s2 - 1)) << 1) | (pi & (s2 - 1));
+                const int j = i + s2;
+                const unsigned long long a = ws.sel[i], b = ws.sel[j];
+                const bool up = ((i & size) == 0);
+                if ((a > b) == up) { ws.sel[i] = b; ws.sel[j] = a; }
+            }
+            __syncwarp();
+        }
+    }
 }
 
 // k smallest (key, index) of n points for one query; results in ws.sel[0..k)
@@ -129,46 +149,7 @@ __device__ void warp_select(const float* ref, int stride, int n, int dim,
         c_eq += __popc(me);
     }
     __syncwarp();
-    // bitonic sort of the k survivors (padded to a power of two)
-    int kp = 1;
-    while (kp < k) kp <<= 1;
-    for (int i = k + lane; i < kp; i += 32) ws.sel[i] = ~0ull;
-    __syncwarp();
-    for (int size = 2; size <= kp; size <<= 1) {
-        for (int stride2 = size >> 1; stride2 > 0; stride2 >>= 1) {
-            for (int i = lane; i < kp; i += 32) {
-                int j = i ^ stride2;
-                if (j > i) {
-                    unsigned long long a = ws.sel[i], b = ws.sel[j];
-                    bool up = ((i & size) == 0);
-                    if ((a > b) == up) { ws.sel[i] = b; ws.sel[j] = a; }
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// bitonic sort of ws.sel[0..cnt), padded to a power of two
-__device__ void warp_sort_sel(WarpScratch& ws, int cnt) {
-    const int lane = threadIdx.x & 31;
-    int kp = 1;
-    while (kp < cnt) kp <<= 1;
-    for (int i = cnt + lane; i < kp; i += 32) ws.sel[i] = ~0ull;
-    __syncwarp();
-    for (int size = 2; size <= kp; size <<= 1) {
-        for (int stride2 = size >> 1; stride2 > 0; stride2 >>= 1) {
-            for (int i = lane; i < kp; i += 32) {
-                int j = i ^ stride2;
-                if (j > i) {
-                    unsigned long long a = ws.sel[i], b = ws.sel[j];
-                    bool up = ((i & size) == 0);
-                    if ((a > b) == up) { ws.sel[i] = b; ws.sel[j] = a; }
-                }
-            }
-            __syncwarp();
-        }
-    }
+    warp_sort_sel(ws, k);
 }
 
 __device__ __forceinline__ unsigned long long pack_sel(float key, int i) {
@@ -176,15 +157,18 @@ __device__ __forceinline__ unsigned long long pack_sel(float key, int i) {
 }
 
 // Threshold form of the selection.  pass(T) gathers into ws.sel every point
-// whose key is <= T (entries past kStore dropped) and returns how many
-// qualified (a pass may stop counting early once far above the window).
-// T is adapted until at least k and at most kStore points qualify.  When
-// more than TO_KNN_KMAX qualified, the threshold is narrowed among the
-// stored keys alone.  The survivors are sorted by (key, index).  Every point
-// closer than the k-th is kept, so the result equals warp_select's.  The
-// update assumes a locally uniform density, count ~ T^(dim/2), kept inside
-// the bracket of thresholds already seen.  Returns false when exact ties
-// keep the count out of the window.
+// whose key is <= T and returns how many qualified.  A pass may lower T on
+// its way (the cell-grid pass does when its store fills: it keeps only the
+// stored keys under a new threshold, so the store still holds every point
+// with key <= the final T); past kStore it stops storing, and it may stop
+// counting once far above the window.  T is adapted until at least k and at
+// most kStore points qualify.  The threshold is then narrowed among the
+// stored keys alone until at most the power of two above k remain, and the
+// survivors are sorted by (key, index).  Every point closer than the k-th is
+// kept, so the result equals warp_select's.  The threshold update assumes a
+// locally uniform density, count ~ T^(dim/2), kept inside the bracket of
+// thresholds already seen.  Returns false when exact ties keep the count out
+// of the window.
 __device__ __forceinline__ bool next_threshold(int cnt, int k, float target, float expo,
                                                float& T, float& lo, float& hi) {
     if (cnt < k) lo = T; else hi = T;
@@ -201,10 +185,48 @@ __device__ __forceinline__ bool next_threshold(int cnt, int k, float target, flo
     return true;
 }
 
-template <class Pass>
-__device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass pass) {
+__device__ __forceinline__ float sel_key(const WarpScratch& ws, int i) {
+    // high word of the packed (key, index) entry
+    return __uint_as_float(reinterpret_cast<const unsigned*>(ws.sel)[2 * i + 1]);
+}
+
+// Lower T among the cnt stored candidates (all with key <= T) until between
+// lo_n and hi_n of them have key <= T, then compact those to the front in
+// their stored order (in place: a write never passes the read position).
+// Returns false, changing nothing, when ties make the window unreachable.
+__device__ bool narrow_stored(WarpScratch& ws, int& cnt, float& T, int lo_n, int hi_n,
+                              float expo) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
+    const float target = 0.5f * (float)(lo_n + hi_n);
+    float lo = -1.0f, hi = T, T2 = T;
+    int c2 = cnt;
+    bool ok = false;
+    for (int iter = 0; iter < 64; ++iter) {
+        if (!next_threshold(c2, lo_n, target, expo, T2, lo, hi)) break;
+        unsigned cl = 0;
+        for (int i = lane; i < cnt; i += 32) cl += (sel_key(ws, i) <= T2) ? 1u : 0u;
+        c2 = (int)__reduce_add_sync(kFull, cl);
+        if (c2 >= lo_n && c2 <= hi_n) { ok = true; break; }
+    }
+    if (!ok) return false;
+    int pos0 = 0;
+    for (int base = 0; base < cnt; base += 32) {
+        const int i = base + lane;
+        const unsigned long long v = (i < cnt) ? ws.sel[i] : ~0ull;
+        const bool le = (i < cnt) && __uint_as_float((unsigned)(v >> 32)) <= T2;
+        const unsigned m = __ballot_sync(kFull, le);
+        if (le) ws.sel[pos0 + __popc(m & lt_mask)] = v;
+        pos0 += __popc(m);
+    }
+    __syncwarp();
+    cnt = c2;
+    T = T2;
+    return true;
+}
+
+template <class Pass>
+__device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass pass) {
     float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > window
     const float expo = 2.0f / (float)dim;
     const float target = sqrtf((float)k * (float)kStore);
@@ -217,34 +239,13 @@ __device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass
     }
     __syncwarp();
     if (cnt < k || cnt > kStore) return false;
-    if (cnt > TO_KNN_KMAX) {
-        // narrow among the stored candidates
-        const float target2 = 0.5f * (float)(k + TO_KNN_KMAX);
-        float lo2 = -1.0f, hi2 = T, T2 = T;
-        int c2 = cnt;
-        bool ok = false;
-        for (int iter = 0; iter < 64; ++iter) {
-            if (!next_threshold(c2, k, target2, expo, T2, lo2, hi2)) break;
-            unsigned cl = 0;
-            for (int i = lane; i < cnt; i += 32)
-                cl += (__uint_as_float((unsigned)(ws.sel[i] >> 32)) <= T2) ? 1u : 0u;
-            c2 = (int)__reduce_add_sync(kFull, cl);
-            if (c2 >= k && c2 <= TO_KNN_KMAX) { ok = true; break; }
-        }
-        if (!ok) return false;
-        int pos0 = 0;
-        for (int base = 0; base < cnt; base += 32) {
-            int i = base + lane;
-            unsigned long long v = (i < cnt) ? ws.sel[i] : ~0ull;
-            bool le = (i < cnt) && __uint_as_float((unsigned)(v >> 32)) <= T2;
-            unsigned m = __ballot_sync(kFull, le);
-            if (le) ws.out[pos0 + __popc(m & lt_mask)] = v;
-            pos0 += __popc(m);
-        }
-        __syncwarp();
-        for (int i = lane; i < c2; i += 32) ws.sel[i] = ws.out[i];
-        __syncwarp();
-        cnt = c2;
+    int cap = 32;
+    while (cap < k) cap <<= 1;
+    if (cnt > cap) {
+        float T2 = T;
+        if (!narrow_stored(ws, cnt, T2, k, cap, expo) && cnt > TO_KNN_KMAX &&
+            !narrow_stored(ws, cnt, T2, k, TO_KNN_KMAX, expo))
+            return false;
     }
     warp_sort_sel(ws, cnt);
     // next query starts from a threshold a little above this k-th distance
@@ -259,7 +260,7 @@ struct ScanPass {
     int stride, n, dim;
     const float* q;
     WarpScratch* ws;
-    __device__ int operator()(float T) const {
+    __device__ int operator()(float& T) const {
         const int lane = threadIdx.x & 31;
         const unsigned lt_mask = (1u << lane) - 1u;
         int cnt = 0;
@@ -299,11 +300,16 @@ struct GridPass {
     int stride;
     const float* q;
     WarpScratch* ws;
-    __device__ int operator()(float T) const {
+    int k;
+    // T may come back lower: when the store fills, the stored keys are cut
+    // to a threshold keeping between k and kStore / 2 of them, and the rest
+    // of the pass uses it (its cells were chosen for the larger radius)
+    __device__ int operator()(float& T) const {
         const int lane = threadIdx.x & 31;
         const unsigned lt_mask = (1u << lane) - 1u;
         const float r = sqrtf(T);
-        const float Tp = T * 1.0002f + 1e-30f;
+        const float expo = 2.0f / (float)D;
+        bool over = false;                  // ties kept the store from being cut
         int cl[D], span[D];
         float tol[D];
 #pragma unroll
@@ -332,6 +338,7 @@ struct GridPass {
                     if (e > 0.0f) lb2 = lb2 + e * e;
                 }
             }
+            const float Tp = T * 1.0002f + 1e-30f;
             if (lb2 > Tp) continue;
             float r0 = sqrtf(Tp - lb2) + tol[0];
             int a0 = cell_of(q[0] - r0, g->lo[0], g->inv[0], g->G[0]);
@@ -343,11 +350,19 @@ struct GridPass {
                 float key = in ? sqdist(gs, stride, i, D, q) : INFINITY;
                 bool le = in && key <= T;
                 unsigned m = __ballot_sync(kFull, le);
+                if (!over && cnt + __popc(m) > kStore) {
+                    if (narrow_stored(*ws, cnt, T, k, kStore / 2, expo)) {
+                        le = in && key <= T;
+                        m = __ballot_sync(kFull, le);
+                    } else {
+                        over = true;
+                    }
+                }
                 int pos = cnt + __popc(m & lt_mask);
                 if (le && pos < kStore) ws->sel[pos] = pack_sel(key, gi[i]);
                 cnt += __popc(m);
             }
-            if (cnt > 4 * kStore) return cnt;   // far above the window
+            if (over && cnt > 4 * kStore) return cnt;   // far above the window
         }
         return cnt;
     }
@@ -368,6 +383,7 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     const float* xs = a.xn + (size_t)c * d * P;
     if (tid < d) { s_umin[tid] = 0xFFFFFFFFu; s_umax[tid] = 0u; }
     if (tid == 0) s_bad = 0;
+    if (c == 0 && tid == 0) *a.knn_next = 0;     // work counter of k_knn_rov
     __syncthreads();
     for (int j = 0; j < d; ++j) {
         float lo = INFINITY, hi = -INFINITY;
@@ -475,75 +491,67 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     }
 }
 
-// ROV: kNN + multiLocLinReg fused.  Grid (ceil(Q / kQ), C); a warp
-// handles kRun consecutive grid queries of control c, starting its
-// threshold from the k-th distance the same query had in the year before.  After the selection
-// every lane accumulates the normal equations of neighbours lane, lane+32,
-// ...; the butterfly sum leaves the same totals in every lane.  The CTA's
-// kQ systems are then solved one per thread of warp 0, so each FP64
-// instruction of the Cholesky solve serves kQ queries (to_lsm_math.h).
-constexpr int kRun = 1;
-constexpr int kQ = kWarps * kRun;       // queries per CTA, <= 32
+// ROV: kNN + multiLocLinReg fused.  Persistent warps take (control, grid
+// query) items from a counter, so no warp waits on another: items differ a
+// lot in cost (queries outside the point cloud need wide radii).  A query's
+// threshold starts from its k-th distance of the year before, times
+// kSeedGrow.  After the selection every lane accumulates the normal
+// equations of neighbours lane, lane+32, ...; the butterfly sum leaves the
+// same totals in every lane, and lane 0 stores them.  k_knn_solve then
+// solves one system per thread (FP64 Cholesky, to_lsm_math.h).
+constexpr float kSeedGrow = 1.6f;
 
 template <int D>
-size_t knn_rov_smem() {
-    return sizeof(WarpScratch) * kWarps + sizeof(float) * kQ * ((D + 1) + (D + 1) * (D + 1));
-}
+__host__ __device__ constexpr int knn_acc_len() { return (D + 1) + (D + 1) * (D + 1); }
+
+size_t knn_rov_smem() { return sizeof(WarpScratch) * kWarps; }
 
 template <int D>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, 4)
 k_knn_rov(to_rov_args a, int t) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    WarpScratch* wsa = reinterpret_cast<WarpScratch*>(sm_raw);
-    constexpr int M = D + 1, NA = M + M * M;
-    float* s_acc = reinterpret_cast<float*>(sm_raw + sizeof(WarpScratch) * kWarps);
-    const int c = blockIdx.y;
-    const int P = a.P, R = a.R;
-    const int n = a.npts[c], k = a.kc[c];
-    const size_t blk = (size_t)R * D + 2 * (size_t)a.Q;
-    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)R * D;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int qc = blockIdx.x * kQ;
-    if (n < 3 || k <= 0) {
-        if (threadIdx.x < kQ && qc + threadIdx.x < a.Q) yout[qc + threadIdx.x] = 0.0f;
-        return;
-    }
-    const to_knn_grid g = a.ggrid[c];
-    const float* xs = a.xn + (size_t)c * D * P;
-    const float* y = a.yv + (size_t)c * P;
-    const float* xr = a.xraw + (size_t)c * D * P;
-    WarpScratch& ws = wsa[warp];
-    float T0 = 0.0f;
-    for (int j = 0; j < D; ++j)
-        if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
-    if (!(T0 > 0.0f)) T0 = powf((float)k / (float)n, 2.0f / (float)D);
-    float T = T0;
-    float* kth_prev = a.kth + (size_t)c * a.Q;
-    for (int r = 0; r < kRun; ++r) {
-        const int ql = warp * kRun + r;
-        const int qi = qc + ql;
-        if (qi >= a.Q) break;
-        if (r == 0 && kth_prev[qi] > 0.0f) T = kth_prev[qi] * 1.3f;
+    constexpr int M = D + 1, NA = knn_acc_len<D>();
+    const int P = a.P, Q = a.Q;
+    const int lane = threadIdx.x & 31;
+    WarpScratch& ws = reinterpret_cast<WarpScratch*>(sm_raw)[threadIdx.x >> 5];
+    const int items = a.C * Q;
+    for (;;) {
+        int item = 0;
+        if (lane == 0) item = atomicAdd(a.knn_next, 1);
+        item = __shfl_sync(kFull, item, 0);
+        if (item >= items) break;
+        const int c = item / Q, qi = item - c * Q;
+        const int n = a.npts[c], k = a.kc[c];
+        if (n < 3 || k <= 0) continue;           // k_knn_solve writes 0
+        const to_knn_grid g = a.ggrid[c];
+        const float* xs = a.xn + (size_t)c * D * P;
+        const float* y = a.yv + (size_t)c * P;
+        const float* xr = a.xraw + (size_t)c * D * P;
+        float T0 = 0.0f;
+        for (int j = 0; j < D; ++j)
+            if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
+        if (!(T0 > 0.0f)) T0 = powf((float)k / (float)n, 2.0f / (float)D);
+        float* kth_prev = a.kth + (size_t)c * Q;
+        const float kp = kth_prev[qi];
+        float T = kp > 0.0f ? kp * kSeedGrow : T0;
         float qn[D], xq[D];
         to_rov_query<D>(a, qi, qn, xq);
         bool ok = false;
         if (g.ok) {
             GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
-                           a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws};
+                           a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
             ok = threshold_select(k, D, T, ws, gp);
         } else {
             ScanPass sp{xs, P, n, D, qn, &ws};
             ok = threshold_select(k, D, T, ws, sp);
         }
-        if (!ok) {
-            warp_select(xs, P, n, D, qn, k, ws);
-            T = T0;
-        }
-        if (lane == 0) kth_prev[qi] = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+        if (!ok) warp_select(xs, P, n, D, qn, k, ws);
+        const float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+        if (lane == 0) kth_prev[qi] = kth;
         // lane-strided local linear regression
         float acc[NA];
         to_lsm_acc_init(D, acc);
-        const float h = sqrtf(__uint_as_float((unsigned)(ws.sel[k - 1] >> 32)));
+        const float h = sqrtf(kth);
         for (int kk = lane; kk < k; kk += 32) {
             const unsigned long long v = ws.sel[kk];
             const int i = (int)(v & 0xFFFFFFFFu);
@@ -563,7 +571,7 @@ k_knn_rov(to_rov_args a, int t) {
             }
             to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
         }
-        float* sa = s_acc + (size_t)ql * NA;
+        float* sa = a.knn_acc + (size_t)item * NA;
 #pragma unroll
         for (int e = 0; e < M; ++e) {
             float x = acc[e];
@@ -580,9 +588,21 @@ k_knn_rov(to_rov_args a, int t) {
             }
         __syncwarp();
     }
-    __syncthreads();
-    if (threadIdx.x < kQ && qc + threadIdx.x < a.Q)
-        yout[qc + threadIdx.x] = to_lsm_solve_intercept(D, s_acc + (size_t)threadIdx.x * NA);
+}
+
+// one regression system per thread: the intercept at grid query qi of
+// control c (0 where the control has too few points)
+template <int D>
+__global__ void k_knn_solve(to_rov_args a, int t) {
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.C * a.Q) return;
+    const int c = item / a.Q, qi = item - c * a.Q;
+    const size_t blk = (size_t)a.R * D + 2 * (size_t)a.Q;
+    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)a.R * D;
+    const int n = a.npts[c], k = a.kc[c];
+    yout[qi] = (n < 3 || k <= 0)
+                   ? 0.0f
+                   : to_lsm_solve_intercept(D, a.knn_acc + (size_t)item * knn_acc_len<D>());
 }
 
 // generic: explicit dim-major queries
@@ -615,11 +635,25 @@ k_knn_generic(const float* ref_g, int n, const float* query, int Q, int dim, int
 }
 
 template <int D>
-to_status launch_knn_rov(to_ctx ctx, dim3 grid, const to_rov_args& a, int t) {
-    const size_t smem = knn_rov_smem<D>();
+to_status launch_knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
+    const size_t smem = knn_rov_smem();
     TO_CUDA(ctx, cudaFuncSetAttribute(k_knn_rov<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
+    int per_sm = 0;
+    TO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn_rov<D>,
+                                                               kWarps * 32, smem));
+    if (per_sm < 1) per_sm = 1;
+    const int items = a.C * a.Q;
+    int grid = (ctx->sm_count > 0 ? ctx->sm_count : 152) * per_sm;
+    if (grid > (items + kWarps - 1) / kWarps) grid = (items + kWarps - 1) / kWarps;
+    to_prof_begin(ctx, "knn");
     k_knn_rov<D><<<grid, kWarps * 32, smem, ctx->stream>>>(a, t);
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
+    to_prof_begin(ctx, "knn_solve");
+    k_knn_solve<D><<<(items + 127) / 128, 128, 0, ctx->stream>>>(a, t);
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
     return TO_OK;
 }
 
@@ -641,16 +675,12 @@ to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     k_knn_grid<<<a.C, 1024, 0, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
-    dim3 grid((a.Q + kQ - 1) / kQ, a.C);
-    to_prof_begin(ctx, "knn");
     switch (d) {
-        case 2: TO_TRY(launch_knn_rov<2>(ctx, grid, a, t)); break;
-        case 3: TO_TRY(launch_knn_rov<3>(ctx, grid, a, t)); break;
-        case 4: TO_TRY(launch_knn_rov<4>(ctx, grid, a, t)); break;
-        default: TO_TRY(launch_knn_rov<5>(ctx, grid, a, t)); break;
+        case 2: TO_TRY(launch_knn_rov<2>(ctx, a, t)); break;
+        case 3: TO_TRY(launch_knn_rov<3>(ctx, a, t)); break;
+        case 4: TO_TRY(launch_knn_rov<4>(ctx, a, t)); break;
+        default: TO_TRY(launch_knn_rov<5>(ctx, a, t)); break;
     }
-    to_prof_end(ctx);
-    TO_LAUNCHED(ctx);
     return TO_OK;
 }
 

@@ -328,75 +328,124 @@ __global__ void k_rov_terminal(to_rov_args a) {
 // Per year: regression states, stable compaction by the year's random
 // control (allocateXYRegressionData :1012-1069), per-control and global
 // min/max (computeStateMinMax :1073-1148), k, normalised points and the
-// axis values of the regression grid.  One CTA.
-__global__ void __launch_bounds__(1024) k_lsm_prepare(to_rov_args a, int t) {
+// axis values of the regression grid.  Three launches over chunks of
+// kLsmChunk paths: per-chunk counts by control, then the scatter in path
+// order (chunk offset + warp offset + rank in the warp) with min/max
+// folded into order-preserving integer keys, then the finish (totals, k,
+// min/max rules, normalisation) across the grid.
+
+constexpr int kLsmChunk = 1024;
+
+// the year's regression group of path p: its control when every species'
+// adjusted population clears its threshold (or the control is 0), else -1
+__device__ __forceinline__ int lsm_group(const to_rov_args& a, int p, int t) {
+    if (p >= a.P) return -1;
+    const int ctl = a.controls[(size_t)t * a.P + p];
+    if (ctl == 0) return 0;
+    for (int s = 0; s < a.S; ++s)
+        if (adj_pop(a, p, t, s, a.C - 1) < a.params[8 * s + 3]) return -1;
+    return ctl;
+}
+
+// order-preserving unsigned key of a float (min/max through integer atomics)
+__device__ __forceinline__ unsigned lsm_key(float v) {
+    unsigned k = __float_as_uint(v);
+    return (k & 0x80000000u) ? ~k : (k | 0x80000000u);
+}
+__device__ __forceinline__ float lsm_unkey(unsigned k) {
+    k = (k & 0x80000000u) ? (k & 0x7FFFFFFFu) : ~k;
+    return __uint_as_float(k);
+}
+
+__global__ void __launch_bounds__(kLsmChunk) k_lsm_count(to_rov_args a, int t) {
+    __shared__ int s_cnt[TO_ROV_MAXC];
+    const int C = a.C, d = a.S + 1, tid = threadIdx.x, lane = tid & 31;
+    if (tid < C) s_cnt[tid] = 0;
+    if (blockIdx.x == 0)
+        for (int q = tid; q < C * d; q += blockDim.x) {
+            a.lkey[2 * q] = 0xFFFFFFFFu;
+            a.lkey[2 * q + 1] = 0u;
+        }
+    __syncthreads();
+    const int grp = lsm_group(a, blockIdx.x * kLsmChunk + tid, t);
+    for (int c = 0; c < C; ++c) {
+        unsigned m = __ballot_sync(0xffffffffu, grp == c);
+        if (lane == 0 && m) atomicAdd(&s_cnt[c], __popc(m));
+    }
+    __syncthreads();
+    if (tid < C) a.lcnt[(size_t)tid * gridDim.x + blockIdx.x] = s_cnt[tid];
+}
+
+__global__ void __launch_bounds__(kLsmChunk) k_lsm_scatter(to_rov_args a, int t) {
+    const int P = a.P, S = a.S, C = a.C, d = S + 1, nb = gridDim.x;
+    __shared__ int s_off[TO_ROV_MAXC];
+    __shared__ int s_scan[TO_ROV_MAXC][32];
+    __shared__ unsigned s_key[TO_ROV_MAXC][TO_LSM_MAXD][2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // chunk offsets: warp c sums the counts of the chunks before this one
+    if (warp < C) {
+        int acc = 0;
+        for (int b = lane; b < (int)blockIdx.x; b += 32) acc += a.lcnt[(size_t)warp * nb + b];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) s_off[warp] = acc;
+    }
+    for (int q = tid; q < C * d; q += blockDim.x) {
+        s_key[q / d][q % d][0] = 0xFFFFFFFFu;
+        s_key[q / d][q % d][1] = 0u;
+    }
+    const int p = blockIdx.x * kLsmChunk + tid;
+    const int grp = lsm_group(a, p, t);
+    float xv[TO_LSM_MAXD];
+    if (grp >= 0) {
+        for (int s = 0; s < S; ++s) xv[s] = adj_pop(a, p, t, s, C - 1);
+        xv[S] = unit_profit(a, p, t, a.Y + 1, a.Y + 1);
+    }
+    int before = 0;
+    for (int c = 0; c < C; ++c) {
+        unsigned m = __ballot_sync(0xffffffffu, grp == c);
+        if (grp == c) before = __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) s_scan[c][warp] = __popc(m);
+        // per-warp min / max of the control's states
+        if (m) {
+            for (int j = 0; j < d; ++j) {
+                float lo = grp == c ? xv[j] : INFINITY, hi = grp == c ? xv[j] : -INFINITY;
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+                }
+                if (lane == 0) {
+                    atomicMin(&s_key[c][j][0], lsm_key(lo));
+                    atomicMax(&s_key[c][j][1], lsm_key(hi));
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (grp >= 0) {
+        int pos = s_off[grp] + before;
+        for (int w = 0; w < warp; ++w) pos += s_scan[grp][w];
+        a.yv[(size_t)grp * P + pos] = a.condExp[(size_t)(t + 1) * P + p];
+        for (int j = 0; j < d; ++j) a.xraw[((size_t)grp * d + j) * P + pos] = xv[j];
+    }
+    for (int q = tid; q < C * d; q += blockDim.x) {
+        const int c = q / d, j = q % d;
+        if (s_key[c][j][1] != 0u) {      // the chunk holds points of control c
+            atomicMin(&a.lkey[2 * q], s_key[c][j][0]);
+            atomicMax(&a.lkey[2 * q + 1], s_key[c][j][1]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_lsm_finish(to_rov_args a, int t, int nb) {
     const int P = a.P, S = a.S, C = a.C, d = S + 1, R = a.R;
     __shared__ int s_cnt[TO_ROV_MAXC];
-    __shared__ int s_scan[32 * TO_ROV_MAXC];
     __shared__ float s_min[TO_ROV_MAXC + 1][TO_LSM_MAXD], s_max[TO_ROV_MAXC + 1][TO_LSM_MAXD];
-    __shared__ unsigned s_umin[TO_ROV_MAXC][TO_LSM_MAXD], s_umax[TO_ROV_MAXC][TO_LSM_MAXD];
-    __shared__ float s_first[TO_ROV_MAXC][TO_LSM_MAXD];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
-    if (tid < C) s_cnt[tid] = 0;
-    __syncthreads();
-    for (int base = 0; base < P; base += blockDim.x) {
-        int p = base + tid;
-        int grp = -1;
-        float xv[TO_LSM_MAXD];
-        if (p < P) {
-            for (int s = 0; s < S; ++s) xv[s] = adj_pop(a, p, t, s, C - 1);
-            xv[S] = unit_profit(a, p, t, a.Y + 1, a.Y + 1);
-            int ctl = a.controls[(size_t)t * P + p];
-            bool valid = true;
-            for (int s = 0; s < S; ++s)
-                if (xv[s] < a.params[8 * s + 3]) { valid = false; break; }
-            if (valid || ctl == 0) grp = ctl;
-        }
-        // one CTA scan per control, in path order
-        for (int c = 0; c < C; ++c) {
-            unsigned m = __ballot_sync(0xffffffffu, grp == c);
-            int before = __popc(m & ((1u << lane) - 1u));
-            if (lane == 0) s_scan[c * 32 + warp] = __popc(m);
-            __syncthreads();
-            int wbase = 0;
-            for (int w = 0; w < warp; ++w) wbase += s_scan[c * 32 + w];
-            int total = 0;
-            for (int w = 0; w < nw; ++w) total += s_scan[c * 32 + w];
-            if (grp == c) {
-                int pos = s_cnt[c] + wbase + before;
-                a.yv[(size_t)c * P + pos] = a.condExp[(size_t)(t + 1) * P + p];
-                for (int j = 0; j < d; ++j) a.xraw[((size_t)c * d + j) * P + pos] = xv[j];
-            }
-            __syncthreads();
-            if (tid == 0) s_cnt[c] += total;
-            __syncthreads();
-        }
-    }
-    // min / max per control: the reference scans from the first point with
-    // "if (xmin > x) ... else if (xmax < x)", i.e. plain min and max
-    for (int q = tid; q < C * d; q += blockDim.x) {
-        int c = q / d, j = q - c * d;
-        s_umin[c][j] = 0xFFFFFFFFu;
-        s_umax[c][j] = 0u;
-        s_first[c][j] = s_cnt[c] > 0 ? a.xraw[((size_t)c * d + j) * P] : 0.0f;
-    }
-    __syncthreads();
-    for (int c = 0; c < C; ++c) {
-        int n = s_cnt[c];
-        for (int j = 0; j < d; ++j) {
-            const float* xs = a.xraw + ((size_t)c * d + j) * P;
-            float lo = INFINITY, hi = -INFINITY;
-            for (int m = tid; m < n; m += blockDim.x) { lo = fminf(lo, xs[m]); hi = fmaxf(hi, xs[m]); }
-            for (int o = 16; o > 0; o >>= 1) {
-                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-            }
-            // order-preserving integer keys for shared atomics
-            unsigned kl = __float_as_uint(lo), kh = __float_as_uint(hi);
-            kl = (kl & 0x80000000u) ? ~kl : (kl | 0x80000000u);
-            kh = (kh & 0x80000000u) ? ~kh : (kh | 0x80000000u);
-            if (lane == 0) { atomicMin(&s_umin[c][j], kl); atomicMax(&s_umax[c][j], kh); }
-        }
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (warp < C) {
+        int acc = 0;
+        for (int b = lane; b < nb; b += 32) acc += a.lcnt[(size_t)warp * nb + b];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) s_cnt[warp] = acc;
     }
     __syncthreads();
     if (tid == 0) {
@@ -404,14 +453,15 @@ __global__ void __launch_bounds__(1024) k_lsm_prepare(to_rov_args a, int t) {
             bool own = (c == 0) || (s_cnt[c] > d + 1);
             for (int j = 0; j < d; ++j) {
                 if (own && s_cnt[c] > 0) {
-                    unsigned kl = s_umin[c][j], kh = s_umax[c][j];
-                    kl = (kl & 0x80000000u) ? (kl & 0x7FFFFFFFu) : ~kl;
-                    kh = (kh & 0x80000000u) ? (kh & 0x7FFFFFFFu) : ~kh;
-                    float lo = __uint_as_float(kl), hi = __uint_as_float(kh);
-                    // the scan starts from the first point, so a first value
-                    // of -0/+0 keeps its sign when it is the extreme
-                    if (lo == s_first[c][j]) lo = s_first[c][j];
-                    if (hi == s_first[c][j]) hi = s_first[c][j];
+                    float lo = lsm_unkey(a.lkey[2 * (c * d + j)]);
+                    float hi = lsm_unkey(a.lkey[2 * (c * d + j) + 1]);
+                    // the reference scans from the first point with
+                    // "if (xmin > x) ... else if (xmax < x)": plain min and
+                    // max, except that a first value of -0/+0 keeps its
+                    // sign when it is the extreme
+                    const float first = a.xraw[((size_t)c * d + j) * P];
+                    if (lo == first) lo = first;
+                    if (hi == first) hi = first;
                     s_min[c][j] = lo; s_max[c][j] = hi;
                 } else if (own) {
                     s_min[c][j] = 0.0f; s_max[c][j] = 0.0f;
@@ -427,37 +477,38 @@ __global__ void __launch_bounds__(1024) k_lsm_prepare(to_rov_args a, int t) {
                 if (hi < s_max[c][j]) hi = s_max[c][j];
             }
             s_min[C][j] = lo; s_max[C][j] = hi;
-            a.gmin[j] = lo; a.gmax[j] = hi;
         }
-        for (int c = 0; c < C; ++c) {
-            int n = s_cnt[c];
+    }
+    __syncthreads();
+    if (blockIdx.x == 0) {
+        if (tid < d) { a.gmin[tid] = s_min[C][tid]; a.gmax[tid] = s_max[C][tid]; }
+        if (tid < C) {
+            const int n = s_cnt[tid];
             int k = 0;
             if (n > 3) {
                 k = (int)(10.0 * (log((double)n) + 1.0));
                 if (k > n) k = n;
             }
-            a.npts[c] = n;
-            a.kc[c] = k;
+            a.npts[tid] = n;
+            a.kc[tid] = k;
+        }
+        // axis values of the regression grid (createQueryPoints :1187-1190)
+        const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+        for (int q = tid; q < C * d * R; q += blockDim.x) {
+            int c = q / (d * R), r = q - c * d * R;
+            int j = r / R, di = r - j * R;
+            a.reg[(size_t)t * C * blk + (size_t)c * blk + (size_t)j * R + di] =
+                to_lsm_query_axis(di, s_min[C][j], s_max[C][j], R);
         }
     }
-    __syncthreads();
     // normalised points (host normalisation, SimulateGPU.cu:4591-4603)
-    for (int c = 0; c < C; ++c) {
-        int n = s_cnt[c];
-        for (int q = tid; q < n * d; q += blockDim.x) {
-            int j = q / n, m = q - j * n;
-            a.xn[((size_t)c * d + j) * P + m] = to_lsm_normalise(
-                a.xraw[((size_t)c * d + j) * P + m], s_min[C][j], s_max[C][j], j == S,
-                a.scaling);
-        }
-    }
-    // axis values of the regression grid (createQueryPoints :1187-1190)
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
-    for (int q = tid; q < C * d * R; q += blockDim.x) {
-        int c = q / (d * R), r = q - c * d * R;
-        int j = r / R, di = r - j * R;
-        a.reg[(size_t)t * C * blk + (size_t)c * blk + (size_t)j * R + di] =
-            to_lsm_query_axis(di, s_min[C][j], s_max[C][j], R);
+    const size_t total = (size_t)C * d * P;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + tid; q < total;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int cj = (int)(q / P), m = (int)(q - (size_t)cj * P);
+        const int c = cj / d, j = cj - c * d;
+        if (m >= s_cnt[c]) continue;
+        a.xn[q] = to_lsm_normalise(a.xraw[q], s_min[C][j], s_max[C][j], j == S, a.scaling);
     }
 }
 
@@ -670,9 +721,17 @@ to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
 to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb) {
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
+    if (a.lblocks != (a.P + kLsmChunk - 1) / kLsmChunk)
+        return to_set_error(ctx, TO_ERR_INVALID, "regression chunks %d", a.lblocks);
+    int fblocks = (int)(((size_t)a.C * (a.S + 1) * a.P + 255) / 256);
+    if (fblocks > 4 * 152) fblocks = 4 * 152;
     for (int t = a.Y - 2; t > 0; --t) {
         to_prof_begin(ctx, "lsm_prepare");
-        k_lsm_prepare<<<1, 1024, 0, ctx->stream>>>(a, t);
+        k_lsm_count<<<a.lblocks, kLsmChunk, 0, ctx->stream>>>(a, t);
+        TO_LAUNCHED(ctx);
+        k_lsm_scatter<<<a.lblocks, kLsmChunk, 0, ctx->stream>>>(a, t);
+        TO_LAUNCHED(ctx);
+        k_lsm_finish<<<fblocks, 256, 0, ctx->stream>>>(a, t, a.lblocks);
         to_prof_end(ctx);
         TO_LAUNCHED(ctx);
         TO_TRY(knn_rov(ctx, a, t));      // kNN and the local linear regressions

@@ -94,6 +94,10 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
     acc((size_t)C * (TO_KNN_GCELLS + 1) * 4); acc((size_t)C * sizeof(to_knn_grid));
     acc((size_t)C * Q * 4);
+    const int lblocks = (P + 1023) / 1024;
+    acc((size_t)C * lblocks * 4); acc((size_t)C * d * 2 * 4);
+    const size_t nacc = (size_t)(d + 1) * (d + 2);
+    acc(4); acc((size_t)C * Q * nacc * 4);
     acc((size_t)Y * C * blk * 4); acc((size_t)Y * P * 4); acc((size_t)Y * P * 4);
     acc((size_t)Y * P * 4); acc((size_t)Y * S * P * 4); acc(5 * 8);
     const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
@@ -136,6 +140,11 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.gcell = to_arena_take<int>(ctx, (size_t)C * (TO_KNN_GCELLS + 1));
     a.ggrid = to_arena_take<to_knn_grid>(ctx, C);
     a.kth = to_arena_take<float>(ctx, (size_t)C * Q);
+    a.lcnt = to_arena_take<int>(ctx, (size_t)C * lblocks);
+    a.lkey = to_arena_take<unsigned>(ctx, (size_t)C * d * 2);
+    a.lblocks = lblocks;
+    a.knn_next = to_arena_take<int>(ctx, 1);
+    a.knn_acc = to_arena_take<float>(ctx, (size_t)C * Q * nacc);
     a.reg = to_arena_take<float>(ctx, (size_t)Y * C * blk);
     a.condExp = to_arena_take<float>(ctx, (size_t)Y * P);
     a.optCont = to_arena_take<int>(ctx, (size_t)Y * P);

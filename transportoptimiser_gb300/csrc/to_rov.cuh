@@ -54,6 +54,11 @@ struct to_rov_args {
     int* gcell;                       // [C][TO_KNN_GCELLS + 1] cell starts
     to_knn_grid* ggrid;               // [C]
     float* kth;                       // [C][Q] k-th squared distance, year before
+    int* lcnt;                        // [C][lblocks] points per control and path chunk
+    unsigned* lkey;                   // [C][d][2] min / max keys of the states
+    int lblocks;                      // path chunks of the compaction
+    int* knn_next;                    // work counter of the kNN kernel
+    float* knn_acc;                   // [C][Q][(d+1)(d+2)] normal equations per query
     int kmax;
     // outputs (device)
     float* reg;                       // [Y][C][R*d + 2Q]
