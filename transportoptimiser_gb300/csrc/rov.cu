@@ -393,6 +393,7 @@ __global__ void __launch_bounds__(kLsmChunk) k_lsm_scatter(to_rov_args a, int t)
         s_key[q / d][q % d][0] = 0xFFFFFFFFu;
         s_key[q / d][q % d][1] = 0u;
     }
+    __syncthreads();                     // keys set before any warp folds into them
     const int p = blockIdx.x * kLsmChunk + tid;
     const int grp = lsm_group(a, p, t);
     float xv[TO_LSM_MAXD];

@@ -371,8 +371,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 }
                 if (c == C) ntot[lane] = tt;
             }
-            if (warp == 0) tot[lane] = 0.0f;   // replaced below, after the barrier
-            __syncthreads();
+            __syncthreads();                   // every warp has read tot
             if (warp == 0) tot[lane] = ntot[lane];
 #pragma unroll
             for (int gi = 0; gi < MAXG; ++gi) {
