@@ -290,7 +290,12 @@ __device__ __forceinline__ int cell_of(float x, float lo, float inv, int G) {
     return c < G - 1 ? c : G - 1;
 }
 
-// pass over the cells a ball of radius sqrt(T) around q can touch
+// Pass over the cells a ball of radius sqrt(T) around q can touch.  Cell
+// rows (runs of dimension-0 cells, contiguous in the sorted order) are set up
+// 32 at a time, one per lane: the row's lower-bound distance, its dimension-0
+// range and its point range.  The warp then walks the concatenated point
+// ranges of the batch in full chunks of 32; a lane finds the row of its point
+// in a small per-warp table (its row index only moves forward).
 template <int D>
 struct GridPass {
     const to_knn_grid* g;
@@ -310,6 +315,8 @@ struct GridPass {
         const float r = sqrtf(T);
         const float expo = 2.0f / (float)D;
         bool over = false;                  // ties kept the store from being cut
+        int* row_off = reinterpret_cast<int*>(ws->hist);   // [33] batch offsets
+        int* row_beg = row_off + 33;                         // [32] first point of a row
         int cl[D], span[D];
         float tol[D];
 #pragma unroll
@@ -322,32 +329,59 @@ struct GridPass {
 #pragma unroll
         for (int j = 1; j < D; ++j) nrows *= span[j];
         int cnt = 0;
-        for (int row = 0; row < nrows; ++row) {
-            int rem = row, cell = 0, mul = g->G[0];
-            float lb2 = 0.0f;
+        for (int rb = 0; rb < nrows; rb += 32) {
+            // this lane's row
+            const int row = rb + lane;
+            int beg = 0, len = 0;
+            if (row < nrows) {
+                int rem = row, cell = 0, mul = g->G[0];
+                float lb2 = 0.0f;
 #pragma unroll
-            for (int j = 1; j < D; ++j) {
-                int cj = cl[j] + rem % span[j];
-                rem /= span[j];
-                cell += cj * mul;
-                mul *= g->G[j];
-                if (g->inv[j] > 0.0f) {
-                    float slo = g->lo[j] + (float)cj * g->w[j];
-                    float shi = slo + g->w[j];
-                    float e = fmaxf(slo - q[j], q[j] - shi) - tol[j];
-                    if (e > 0.0f) lb2 = lb2 + e * e;
+                for (int j = 1; j < D; ++j) {
+                    const int cj = cl[j] + rem % span[j];
+                    rem /= span[j];
+                    cell += cj * mul;
+                    mul *= g->G[j];
+                    if (g->inv[j] > 0.0f) {
+                        const float slo = g->lo[j] + (float)cj * g->w[j];
+                        const float shi = slo + g->w[j];
+                        const float e = fmaxf(slo - q[j], q[j] - shi) - tol[j];
+                        if (e > 0.0f) lb2 = lb2 + e * e;
+                    }
+                }
+                const float Tp = T * 1.0002f + 1e-30f;
+                if (lb2 <= Tp) {
+                    const float r0 = sqrtf(Tp - lb2) + tol[0];
+                    const int a0 = cell_of(q[0] - r0, g->lo[0], g->inv[0], g->G[0]);
+                    const int b0 = cell_of(q[0] + r0, g->lo[0], g->inv[0], g->G[0]);
+                    beg = gc[cell + a0];
+                    len = gc[cell + b0 + 1] - beg;
                 }
             }
-            const float Tp = T * 1.0002f + 1e-30f;
-            if (lb2 > Tp) continue;
-            float r0 = sqrtf(Tp - lb2) + tol[0];
-            int a0 = cell_of(q[0] - r0, g->lo[0], g->inv[0], g->G[0]);
-            int b0 = cell_of(q[0] + r0, g->lo[0], g->inv[0], g->G[0]);
-            const int s = gc[cell + a0], e = gc[cell + b0 + 1];
-            for (int base = s; base < e; base += 32) {
-                int i = base + lane;
-                bool in = i < e;
-                float key = in ? sqdist(gs, stride, i, D, q) : INFINITY;
+            // exclusive scan of the row lengths
+            int incl = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(kFull, incl, 31);
+            __syncwarp();
+            row_off[lane] = incl - len;
+            row_beg[lane] = beg;
+            if (lane == 31) row_off[32] = total;
+            __syncwarp();
+            int my = 0;                     // row of this lane's point
+            for (int base = 0; base < total; base += 32) {
+                const int f = base + lane;
+                const bool in = f < total;
+                float key = INFINITY;
+                int i = 0;
+                if (in) {
+                    while (f >= row_off[my + 1]) ++my;
+                    i = row_beg[my] + (f - row_off[my]);
+                    key = sqdist(gs, stride, i, D, q);
+                }
                 bool le = in && key <= T;
                 unsigned m = __ballot_sync(kFull, le);
                 if (!over && cnt + __popc(m) > kStore) {
@@ -358,19 +392,21 @@ struct GridPass {
                         over = true;
                     }
                 }
-                int pos = cnt + __popc(m & lt_mask);
+                const int pos = cnt + __popc(m & lt_mask);
                 if (le && pos < kStore) ws->sel[pos] = pack_sel(key, gi[i]);
                 cnt += __popc(m);
             }
             if (over && cnt > 4 * kStore) return cnt;   // far above the window
+            __syncwarp();
         }
         return cnt;
     }
 };
 
 // Per control: bounding box of the normalised points, a cell grid of about
-// 8n/k cells (at most TO_KNN_GCELLS), and a counting sort of the points into
-// it.  One CTA per control.
+// 32n/k cells (at most TO_KNN_GCELLS; a few points per cell, since rows are
+// set up 32 at a time and cost little), and a counting sort of the points
+// into it.  One CTA per control.
 __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     const int c = blockIdx.x, d = a.S + 1, P = a.P;
     const int n = a.npts[c], k = a.kc[c];
@@ -408,7 +444,7 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     if (tid == 0) {
         to_knn_grid g;
         g.ok = (!s_bad && n >= 3 && k > 0) ? 1 : 0;
-        int target = (k > 0) ? (int)(8LL * n / k) : 1;
+        int target = (k > 0) ? (int)(32LL * n / k) : 1;
         if (target < 1) target = 1;
         int gd = (int)floorf(powf((float)target, 1.0f / (float)d));
         if (gd < 1) gd = 1;
@@ -499,7 +535,7 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 // equations of neighbours lane, lane+32, ...; the butterfly sum leaves the
 // same totals in every lane, and lane 0 stores them.  k_knn_solve then
 // solves one system per thread (FP64 Cholesky, to_lsm_math.h).
-constexpr float kSeedGrow = 1.6f;
+constexpr float kSeedGrow = 1.4f;
 
 template <int D>
 __host__ __device__ constexpr int knn_acc_len() { return (D + 1) + (D + 1) * (D + 1); }
