@@ -260,6 +260,12 @@ typedef struct {
     int demand_idx;          /* process multiplying the unit profit, -1: none */
     uint64_t seed;
     int road, sem, migration;
+    int algo;                /* 4 (or 0): ALGO4, regression values; 6: ALGO6,
+                                each year's value is the realised discounted
+                                payoff of the path re-simulated from that year
+                                under the regression-optimal controls
+                                (optimalForwardPaths, SimulateGPU.cu:1199-2206,
+                                5011-5436); sem 1 and sparse migration only */
 } to_rov_problem;
 
 typedef struct {

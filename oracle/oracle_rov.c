@@ -112,11 +112,15 @@ static float local_linear(int dim, int k, int Q, int qi, const float* dist,
 
 /* k rule of the ALGO4 loop (SimulateGPU.cu:4542-4545); 0 when n <= 3, and
  * never more than n (the reference reads past the data then). */
-int or_k_rov(int n) {
+int or_k_rov_mult(int n, int mult) {
     if (n <= 3) return 0;
-    int k = (int)(10.0 * (log((double)n) + 1.0));
+    int k = (int)((double)mult * (log((double)n) + 1.0));
     return k < n ? k : n;
 }
+
+/* k nearest neighbours of the ALGO4 regressions (SimulateGPU.cu:4517);
+ * ALGO6 uses 3 (ln n + 1) (its host loop, SimulateGPU.cu:5110) */
+int or_k_rov(int n) { return or_k_rov_mult(n, 10); }
 
 /* ------------------------------------------------------------------------ */
 /* ROV                                                                        */
@@ -128,6 +132,9 @@ typedef struct {
     float* aars;        /* [P][Y+1][S][C] */
     float* uRes;        /* [P][Y+1][U] (reference stride) */
     int* controls;      /* [P][Y] */
+    float* popY;        /* ALGO6: [P][Y][S][maxN] patch populations, start of year */
+    float* gmY;         /* ALGO6: [P][Y][S] mean growth rate of the year */
+    int maxN;
 } rov_fwd_job;
 
 static void rov_forward_paths(rov_fwd_job* j) {
@@ -170,6 +177,11 @@ static void rov_forward_paths(rov_fwd_job* j) {
                 float jsz = (pr->sem == 0) ? (zj * s5 - s5 / 2.0f) : (zj * sp[5] - s5 / 2.0f);
                 gm[s] = gm[s] + sp[4] * (sp[1] - gm[s]) * pr->dt + gm[s] * brown
                         + (to_expf(jsz) - 1.0f) * gm[s] * jump;
+                if (j->popY) {
+                    memcpy(j->popY + (((size_t)p * Y + t) * S + s) * j->maxN, ps,
+                           sizeof(float) * (size_t)N);
+                    j->gmY[((size_t)p * Y + t) * S + s] = gm[s];
+                }
                 float initial = or_grouped_sum(ps, N);
                 for (int c = 0; c < C; ++c) {
                     const float* M = pr->mmm[s] + (size_t)c * N * N;
@@ -255,10 +267,149 @@ static float unit_profit(const or_rov_problem* pr, const float* uRes, int p, int
     return prof;
 }
 
+
+/* ALGO6 decisions, the same rules as the backward induction below
+ * (SimulateGPU.cu:2375-2463 terminal, :2464-2776 interior); state holds the
+ * adjusted populations [C][S] and the unit profit at [S*C] */
+static void rov_decide(const or_rov_problem* pr, const float* reg, long blk, int t,
+                       int terminal, const float* state, float* best_out, int* bc_out) {
+    const int S = pr->n_species, C = pr->n_controls, R = pr->dim_res;
+    const float disc = 1.0f + pr->rrr * pr->dt / 100.0f;
+    float pay[TO_MAX_C_ORACLE];
+    int valid[TO_MAX_C_ORACLE];
+    for (int c = 0; c < C; ++c) {
+        valid[c] = 1;
+        for (int s = 0; s < S; ++s) {
+            float thr = (pr->sem == 0) ? pr->params_flat[S * s + 3] : pr->params[s][3];
+            if (state[c * S + s] < thr && c > 0) { valid[c] = 0; break; }
+        }
+        if (!valid[c]) { pay[c] = 0.0f; continue; }
+        if (terminal) {
+            float v = pr->flows[c] * state[S * C];
+            pay[c] = v > 0.0f ? 0.0f : v;
+        } else {
+            float cur = pr->flows[c] * state[S * C];
+            const float* rb = reg + (size_t)t * C * blk + (size_t)c * blk;
+            float v = (pr->sem == 0) ? to_lsm_interp_ref(rb, R, S, C, state)
+                                     : to_lsm_interp(rb, R, S, state + c * S, state[S * C]);
+            double ce = (double)(v / disc);
+            if (ce > 0.0) ce = 0.0;
+            pay[c] = (float)((double)cur + ce);
+        }
+    }
+    float best = pay[0];
+    int bc = 0;
+    for (int c = 1; c < C; ++c) {
+        if (!valid[c]) continue;
+        int better = terminal ? (pay[c] < best)
+                   : (pr->sem == 0 ? ((double)pay[c] < 0.975 * (double)best) : (pay[c] < best));
+        if (better) { best = pay[c]; bc = c; }
+    }
+    *best_out = best;
+    *bc_out = bc;
+}
+
+typedef struct {
+    const or_rov_problem* pr;
+    int p0, p1, t0, maxN;
+    const float* popY;
+    const float* gmY;
+    const float* uRes;
+    const float* reg;
+    float* condExp;
+    int* opt_cont;
+} rov_resim_job;
+
+/* ALGO6 (optimalForwardPaths, SimulateGPU.cu:1199-2206, as its comments
+ * describe it): each path restarts from its forward-pass patch populations
+ * at year t0, takes the decided control every year (regression of the year,
+ * terminal rule in the last), migrates and grows with the forward pass's
+ * noise and growth mean; the value is the realised payoff flows[c] * profit
+ * discounted by (1 + r dt / 100) per year. */
+static void rov_resim_paths(rov_resim_job* j) {
+    const or_rov_problem* pr = j->pr;
+    const int P = pr->n_paths, Y = pr->n_years, S = pr->n_species, C = pr->n_controls,
+              R = pr->dim_res, d = S + 1, Y1 = Y + 1, maxN = j->maxN, t0 = j->t0;
+    long Q = 1;
+    for (int i = 0; i < d; ++i) Q *= R;
+    const long blk = (long)R * d + 2L * Q;
+    const float disc = 1.0f + pr->rrr * pr->dt / 100.0f;
+    float* x = (float*)malloc(sizeof(float) * (size_t)S * maxN);
+    float* mig = (float*)malloc(sizeof(float) * (size_t)S * C * maxN);
+    float tot[TO_LSM_MAXD];
+    for (int p = j->p0; p < j->p1; ++p) {
+        for (int s = 0; s < S; ++s) {
+            const int N = pr->n_patches[s];
+            memcpy(x + (size_t)s * maxN, j->popY + (((size_t)p * Y + t0) * S + s) * maxN,
+                   sizeof(float) * (size_t)N);
+            tot[s] = or_grouped_sum(x + (size_t)s * maxN, N);
+        }
+        float val = 0.0f, df = 1.0f;
+        int c0 = 0;
+        for (int u = t0; u < Y; ++u) {
+            float state[TO_MAX_C_ORACLE * TO_LSM_MAXD + 1];
+            for (int s = 0; s < S; ++s) {
+                const int N = pr->n_patches[s];
+                const float* xs = x + (size_t)s * maxN;
+                for (int c = 0; c < C; ++c) {
+                    const float* M = pr->mmm[s] + (size_t)c * N * N;
+                    float* mg = mig + ((size_t)s * C + c) * maxN;
+                    for (int k = 0; k < N; ++k) {
+                        float acc = 0.0f;
+                        const float* col = M + (size_t)k * N;
+                        for (int l = 0; l < N; ++l) acc = fmaf(xs[l], col[l], acc);
+                        mg[k] = acc;
+                    }
+                    float tt = or_grouped_sum(mg, N);
+                    state[c * S + s] = tot[s] * (tt / tot[s]);
+                }
+            }
+            const float prof = unit_profit(pr, j->uRes, p, u, Y1, Y1);
+            state[S * C] = prof;
+            float best;
+            int bc;
+            rov_decide(pr, j->reg, blk, u, u == Y - 1, state, &best, &bc);
+            val = val + (pr->flows[bc] * prof) * df;
+            df = df / disc;
+            if (u == t0) c0 = bc;
+            if (u == Y - 1) break;
+            for (int s = 0; s < S; ++s) {
+                const int N = pr->n_patches[s], N4 = (N + 3) & ~3;
+                const float* sp = pr->params[s];
+                const float g = j->gmY[((size_t)p * Y + u) * S + s];
+                const float* mg = mig + ((size_t)s * C + bc) * maxN;
+                float* xs = x + (size_t)s * maxN;
+                for (int k = 0; k < N; ++k) {
+                    float z = to_normal1(pr->seed, TO_STREAM_GROWTH, pr->road, p, u,
+                                         (uint32_t)(s * N4 + k));
+                    float gr = (pr->sem == 0) ? g + z * sp[7] : fmaf(sp[7] * z, g, g);
+                    float m = mg[k], cp = pr->caps[s][k];
+                    xs[k] = (pr->sem == 0) ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
+                                           : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
+                }
+                tot[s] = or_grouped_sum(xs, N);
+            }
+        }
+        j->condExp[(size_t)t0 * P + p] = val;
+        j->opt_cont[(size_t)t0 * P + p] = c0;
+    }
+    free(x);
+    free(mig);
+}
+
+static void* rov_resim_thread(void* a) { rov_resim_paths((rov_resim_job*)a); return NULL; }
+
 int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
     const int P = pr->n_paths, Y = pr->n_years, S = pr->n_species, C = pr->n_controls,
               U = pr->n_uncertainties, R = pr->dim_res, d = S + 1;
     if (S < 1 || S > TO_LSM_MAXD - 1 || C < 1 || Y < 2 || P < 1 || R < 2) return -1;
+    const int algo = pr->algo == 0 ? 4 : pr->algo;
+    if ((algo != 4 && algo != 6) || (algo == 6 && pr->sem != 1)) return -1;
+    const int kmult = algo == 6 ? 3 : 10;
+    int maxN = 0;
+    for (int s = 0; s < S; ++s) if (pr->n_patches[s] > maxN) maxN = pr->n_patches[s];
+    float* popY = algo == 6 ? (float*)calloc((size_t)P * Y * S * maxN, sizeof(float)) : NULL;
+    float* gmY = algo == 6 ? (float*)calloc((size_t)P * Y * S, sizeof(float)) : NULL;
     long Qn = 1;
     for (int i = 0; i < d; ++i) Qn *= R;
     const int Q = (int)Qn;
@@ -278,7 +429,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
     for (int i = 0; i < nt; ++i) {
         int a = i * per, b = a + per > P ? P : a + per;
         if (a >= b) break;
-        rov_fwd_job jj = {pr, a, b, totalPops, aars, uRes, controls};
+        rov_fwd_job jj = {pr, a, b, totalPops, aars, uRes, controls, popY, gmY, maxN};
         jobs[used++] = jj;
     }
     for (int i = 1; i < used; ++i) pthread_create(&th[i], NULL, rov_fwd_thread, &jobs[i]);
@@ -396,7 +547,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
         for (int c = 0; c < C; ++c) {
             int n = npts[c];
             float* yout = reg + (size_t)t * C * blk + (size_t)c * blk + (size_t)R * d;
-            int k = or_k_rov(n);
+            int k = or_k_rov_mult(n, kmult);
             if (n < 3 || k == 0) {
                 for (int q = 0; q < Q; ++q) yout[q] = 0.0f;
                 continue;
@@ -463,6 +614,22 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
             }
             condExp[(size_t)t * P + p] = best;
             res->opt_cont[(size_t)t * P + p] = bc;
+        }
+        if (algo == 6) {
+            /* the year's value and control come from the re-simulated paths */
+            rov_resim_job rj[128];
+            pthread_t rth[128];
+            int rused = 0, rper = (P + nt - 1) / nt;
+            for (int i = 0; i < nt; ++i) {
+                int a0 = i * rper, b0 = a0 + rper > P ? P : a0 + rper;
+                if (a0 >= b0) break;
+                rov_resim_job jr = {pr, a0, b0, t, maxN, popY, gmY, uRes, reg, condExp,
+                                    res->opt_cont};
+                rj[rused++] = jr;
+            }
+            for (int i = 1; i < rused; ++i) pthread_create(&rth[i], NULL, rov_resim_thread, &rj[i]);
+            if (rused > 0) rov_resim_paths(&rj[0]);
+            for (int i = 1; i < rused; ++i) pthread_join(rth[i], NULL);
         }
     }
 
@@ -545,6 +712,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
         memcpy(res->u_results, uRes, sizeof(float) * (size_t)P * (Y + 1) * U);
     free(xin); free(xraw); free(xnorm); free(yv); free(qn); free(xqg); free(dist); free(ind);
     free(totalPops); free(aars); free(uRes); free(controls); free(condExp); free(reg);
+    free(popY); free(gmY);
     return 0;
 }
 

@@ -34,6 +34,8 @@ typedef struct {
     int demand_idx;                     /* process multiplying the profit, -1  */
     uint64_t seed;
     int road, sem, n_threads;
+    int algo;                           /* 4 (or 0): ALGO4; 6: ALGO6 path
+                                           re-simulation (sem 1 only)        */
 } or_rov_problem;
 
 typedef struct {
@@ -55,6 +57,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res);
 void or_knn(const float* ref, int n, const float* query, int Q, int dim, int k,
             float* dist, int* ind);
 int or_k_rov(int n);
+int or_k_rov_mult(int n, int mult);
 int or_k_surrogate_mte(int n);
 int or_k_surrogate_rov(int n);
 void or_build_surrogate_1d(int n, const float* x, const float* y, int R, float* out);

@@ -303,7 +303,8 @@ class OrRovProblem(C.Structure):
                 ("ore_content", c_float_p), ("ore_sd", c_float_p), ("unit_cost", C.c_float),
                 ("unit_revenue", C.c_float), ("dt", C.c_float), ("rrr", C.c_float),
                 ("scaling", C.c_float), ("demand_idx", C.c_int), ("seed", C.c_uint64),
-                ("road", C.c_int), ("sem", C.c_int), ("n_threads", C.c_int)]
+                ("road", C.c_int), ("sem", C.c_int), ("n_threads", C.c_int),
+                ("algo", C.c_int)]
 
 
 class OrRovResult(C.Structure):
@@ -344,7 +345,8 @@ def simulate_rov(rp, threads=1, want_paths=False):
                       _p(a["fuel_idx"], C.c_int), len(a["ore_content"]),
                       _p(a["ore_content"], C.c_float), _p(a["ore_sd"], C.c_float),
                       rp["unit_cost"], rp["unit_revenue"], rp["dt"], rp["rrr"], 2.0,
-                      rp.get("demand_idx", -1), rp["seed"], rp["road"], rp["sem"], threads)
+                      rp.get("demand_idx", -1), rp["seed"], rp["road"], rp["sem"], threads,
+                      int(rp.get("algo", 4)))
     d = S + 1
     blk = R * d + 2 * R ** d
     res = dict(cond_exp=np.zeros(P * Y, np.float32), opt_cont=np.zeros(P * Y, np.int32),

@@ -119,3 +119,26 @@ def test_rov_many_chunks_repeatable_and_exact(ctx):
     gpu = sg.simulateROVCUDA(rp, ctx=ctx)
     orc = po.simulate_rov(rp, threads=16)
     _compare_exact(gpu, orc, P, Y, 2)
+
+
+@pytest.mark.parametrize("S,R,P,Y", [(2, 8, 700, 10), (1, 16, 900, 8), (2, 8, 1100, 25)])
+def test_rov_algo6_bit_exact(ctx, S, R, P, Y):
+    """ALGO6: every path re-simulated from each year under the regression-
+    optimal controls; values, decisions and regressions equal the oracle's."""
+    sc = synth.rov_road(3, n_species=S)
+    models = [po.species_model(sc, sc.species[s], sc.roads[0], sem=1) for s in range(S)]
+    rp = rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                 n_processes=3, demand=True, seed=4, road=7, algo=6)
+    gpu = sg.simulateROVCUDA(rp, migration=MIG_SPARSE_FP32, ctx=ctx)
+    orc = po.simulate_rov(rp, threads=16)
+    assert np.isfinite(orc["stats"][0])
+    _compare_exact(gpu, orc, P, Y, S)
+
+
+def test_rov_algo6_refuses_dense_forms(ctx):
+    from transportoptimiser_gb300._capi import TransOptError
+    sc = synth.rov_road(3, n_species=1)
+    models = [po.species_model(sc, sc.species[0], sc.roads[0], sem=1)]
+    rp = rov_problem_from_models(models, sc, n_paths=200, n_years=6, dim_res=8, sem=1, algo=6)
+    with pytest.raises(TransOptError):
+        sg.simulateROVCUDA(rp, migration=MIG_SIMT_FP32, ctx=ctx)

@@ -122,7 +122,7 @@ class RovProblem(C.Structure):
                 ("ore_content", c_float_p), ("ore_sd", c_float_p), ("unit_cost", C.c_float),
                 ("unit_revenue", C.c_float), ("dt", C.c_float), ("rrr", C.c_float),
                 ("demand_idx", C.c_int), ("seed", C.c_uint64), ("road", C.c_int),
-                ("sem", C.c_int), ("migration", C.c_int)]
+                ("sem", C.c_int), ("migration", C.c_int), ("algo", C.c_int)]
 
 
 class RovResult(C.Structure):

@@ -31,9 +31,15 @@
 #include "to_internal.cuh"
 #include "to_lsm_math.h"
 #include "to_rov.cuh"
+#include "to_rov_dev.cuh"
 #include "to_sparse.cuh"
 
 namespace {
+
+using to_rovd::adj_pop;
+using to_rovd::ore_at;
+using to_rovd::threshold;
+using to_rovd::unit_profit;
 
 // ---------------------------------------------------------------------------
 // exogenous processes and random controls (forwardPathKernel :930-952,
@@ -247,82 +253,25 @@ k_rov_forward(to_rov_args a) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// shared pieces of the backward pass
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float ure(const to_rov_args& a, int p, int t, int u, int stride_y) {
-    // value at the reference's flat index (p*stride_y + t)*U + u of its
-    // [P][Y+1][U] array, read from the [U][Y+1][P] layout
-    const int U = a.U, Y1 = a.Y + 1;
-    long F = ((long)p * stride_y + t) * U + u;
-    long per = (long)Y1 * U;
-    int pp = (int)(F / per);
-    long rem = F - (long)pp * per;
-    int tt = (int)(rem / U), uu = (int)(rem - (long)tt * U);
-    return a.uRes[((size_t)uu * Y1 + tt) * a.P + pp];
-}
-
-__device__ __forceinline__ float ore_at(const to_rov_args& a, int p, int t, int c) {
-    long f, gen;
-    if (a.sem == 0) {
-        f = ((long)p * a.Y + t) * a.Cm + c;
-        gen = f / ((long)a.Y * a.P);
-    } else {
-        gen = c;
-        f = (long)c * a.Y * a.P + (long)p * a.Y + t;
-    }
-    float z = to_normal1(a.seed, TO_STREAM_ORE, (uint32_t)a.road, (uint32_t)(f >> 2), 0,
-                         (uint32_t)(f & 3));
-    return a.ore_content[gen] + a.ore_sd[gen] * z;
-}
-
-__device__ __forceinline__ float unit_profit(const to_rov_args& a, int p, int t,
-                                             int fuel_stride_y, int ore_stride_y) {
-    float uf = 0.0f, ore = 0.0f;
-    for (int f = 0; f < a.nF; ++f)
-        uf = fmaf(a.fuel_costs[f], ure(a, p, t, a.fuel_idx[f], fuel_stride_y), uf);
-    for (int c = 0; c < a.Cm; ++c)
-        ore = fmaf(ore_at(a, p, t, c), ure(a, p, t, a.nF + c, ore_stride_y), ore);
-    float prof = (a.unit_cost + uf) - a.unit_revenue * ore;
-    if (a.demand_idx >= 0)
-        prof = prof * a.uRes[((size_t)a.demand_idx * (a.Y + 1) + t) * a.P + p];
-    return prof;
-}
-
-__device__ __forceinline__ float adj_pop(const to_rov_args& a, int p, int t, int s, int c) {
-    return a.totalPops[((size_t)s * (a.Y + 1) + t) * a.P + p] *
-           a.aars[(((size_t)s * a.C + c) * a.Y + t) * a.P + p];
-}
-
-__device__ __forceinline__ float threshold(const to_rov_args& a, int s) {
-    return (a.sem == 0) ? a.params[a.S * s + 3] : a.params[8 * s + 3];
-}
 
 // terminal year (backwardInduction :2375-2463)
 __global__ void k_rov_terminal(to_rov_args a) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.P) return;
     const int t = a.Y - 1, C = a.C, S = a.S;
+    float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
+    for (int c = 0; c < C; ++c)
+        for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
     float prof = unit_profit(a, p, t, a.Y + 1, a.sem == 0 ? a.Y : a.Y + 1);
-    float best = 0.0f;
-    int bc = 0;
-    for (int c = 0; c < C; ++c) {
-        bool valid = true;
-        for (int s = 0; s < S; ++s)
-            if (adj_pop(a, p, t, s, c) < threshold(a, s) && c > 0) { valid = false; break; }
-        float pay = 0.0f;
-        if (valid) {
-            float v = a.flows[c] * prof;
-            pay = v > 0.0f ? 0.0f : v;
-        }
-        if (c == 0) best = pay;
-        else if (valid && pay < best) { best = pay; bc = c; }
-    }
+    state[S * C] = prof;
+    float best;
+    int bc;
+    to_rovd::decide_terminal(a, state, best, bc);
     a.condExp[(size_t)t * a.P + p] = best;
     a.optCont[(size_t)t * a.P + p] = bc;
     a.unitProfits[(size_t)t * a.P + p] = prof;
     for (int s = 0; s < S; ++s)
-        a.adjPops[((size_t)t * S + s) * a.P + p] = adj_pop(a, p, t, s, C - 1);
+        a.adjPops[((size_t)t * S + s) * a.P + p] = state[(C - 1) * S + s];
 }
 
 // Per year: regression states, stable compaction by the year's random
@@ -487,7 +436,7 @@ __global__ void __launch_bounds__(256) k_lsm_finish(to_rov_args a, int t, int nb
             const int n = s_cnt[tid];
             int k = 0;
             if (n > 3) {
-                k = (int)(10.0 * (log((double)n) + 1.0));
+                k = (int)((double)a.k_mult * (log((double)n) + 1.0));
                 if (k > n) k = n;
             }
             a.npts[tid] = n;
@@ -521,7 +470,7 @@ namespace {
 __global__ void k_rov_backward(to_rov_args a, int t) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= a.P) return;
-    const int C = a.C, S = a.S, d = S + 1, R = a.R;
+    const int C = a.C, S = a.S;
     float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
     for (int c = 0; c < C; ++c)
         for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
@@ -531,29 +480,9 @@ __global__ void k_rov_backward(to_rov_args a, int t) {
     float prof = unit_profit(a, p, t, sy, sy);
     state[S * C] = prof;
     a.unitProfits[(size_t)t * a.P + p] = prof;
-    const float disc = 1.0f + a.rrr * a.dt / 100.0f;
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
-    float best = 0.0f;
-    int bc = 0;
-    for (int c = 0; c < C; ++c) {
-        bool valid = true;
-        for (int s = 0; s < S; ++s)
-            if (state[c * S + s] < threshold(a, s) && c > 0) { valid = false; break; }
-        float pay = 0.0f;
-        if (valid) {
-            float cur = a.flows[c] * state[S * C];
-            const float* rb = a.reg + (size_t)t * C * blk + (size_t)c * blk;
-            float v = (a.sem == 0) ? to_lsm_interp_ref(rb, R, S, C, state)
-                                   : to_lsm_interp(rb, R, S, state + c * S, state[S * C]);
-            double ce = (double)(v / disc);
-            if (ce > 0.0) ce = 0.0;
-            pay = (float)((double)cur + ce);
-        }
-        if (c == 0) { best = pay; continue; }
-        if (!valid) continue;
-        bool better = (a.sem == 0) ? ((double)pay < 0.975 * (double)best) : (pay < best);
-        if (better) { best = pay; bc = c; }
-    }
+    float best;
+    int bc;
+    to_rovd::decide_interior(a, t, state, best, bc);
     a.condExp[(size_t)t * a.P + p] = best;
     a.optCont[(size_t)t * a.P + p] = bc;
 }
@@ -670,7 +599,8 @@ __global__ void k_rov_first(to_rov_args a) {
 
 namespace to_k {
 
-to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb);
+to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
+                       const to_csc* csc);
 
 to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
     const int P = a.P;
@@ -682,7 +612,7 @@ to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
     TO_LAUNCHED(ctx);
     if (csc) {
         TO_TRY(rov_forward_sparse(ctx, a, *csc));
-        return rov_backward(ctx, a, pblocks, tpb);
+        return rov_backward(ctx, a, pblocks, tpb, csc);
     }
     // forward tile shape
     const int NE = a.ne, KG = NE / 4;
@@ -716,10 +646,13 @@ to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
     }
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
-    return rov_backward(ctx, a, pblocks, tpb);
+    return rov_backward(ctx, a, pblocks, tpb, nullptr);
 }
 
-to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb) {
+to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
+                       const to_csc* csc) {
+    if (a.algo == 6 && (!csc || !a.popsY || !a.gmY))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "ALGO6 needs the sparse forward pass");
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
     if (a.lblocks != (a.P + kLsmChunk - 1) / kLsmChunk)
@@ -740,6 +673,9 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb) {
         k_rov_backward<<<pblocks, tpb, 0, ctx->stream>>>(a, t);
         to_prof_end(ctx);
         TO_LAUNCHED(ctx);
+        // ALGO6: the year's value becomes the realised payoff of each path
+        // re-simulated from year t under the regression-optimal controls
+        if (a.algo == 6) TO_TRY(rov_resim_sparse(ctx, a, *csc, t));
     }
     k_rov_first<<<1, 1024, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);

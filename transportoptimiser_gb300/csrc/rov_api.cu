@@ -43,6 +43,12 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     if (pr->sem == 0 && S != 1)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED,
                             "reference semantics are defined for one species only");
+    const int algo = pr->algo == 0 ? 4 : pr->algo;
+    if (algo != 4 && algo != 6) return to_set_error(ctx, TO_ERR_INVALID, "algo %d", pr->algo);
+    if (algo == 6 && (pr->sem != 1 || pr->migration == TO_MIG_SIMT_FP32 ||
+                      pr->migration == TO_MIG_TC_3XTF32))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "ALGO6 is built for sem 1 with the sparse migration form");
     if (pr->demand_idx >= U) return TO_ERR_INVALID;
     for (int f = 0; f < pr->n_fuels; ++f)
         if (pr->fuel_idx[f] < 0 || pr->fuel_idx[f] >= U) return TO_ERR_INVALID;
@@ -103,6 +109,7 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
     acc((size_t)S * C * (NP + 1) * 4); acc((size_t)S * C * cap * 2); acc((size_t)S * C * cap * 4);
     acc((size_t)S * C * 4);
+    if (algo == 6) { acc((size_t)Y * S * NP * P * 4); acc((size_t)Y * S * P * 4); }
     TO_TRY(to_arena_reserve(ctx, bytes + 4096));
     TO_CUDA(ctx, cudaMemsetAsync(ctx->arena, 0, bytes, ctx->stream));
     to_rov_args a;
@@ -112,6 +119,7 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.sem = pr->sem; a.road = pr->road; a.dt = pr->dt; a.rrr = pr->rrr;
     a.unit_cost = pr->unit_cost; a.unit_revenue = pr->unit_revenue; a.scaling = 2.0f;
     a.seed = pr->seed; a.np = NP; a.ne = NP; a.kmax = kmax;
+    a.algo = algo; a.k_mult = algo == 6 ? 3 : 10;
     float* d_mmm = to_arena_take<float>(ctx, mmm.size());
     float* d_ip = to_arena_take<float>(ctx, ip.size());
     float* d_cp = to_arena_take<float>(ctx, cp.size());
@@ -143,6 +151,10 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     a.lcnt = to_arena_take<int>(ctx, (size_t)C * lblocks);
     a.lkey = to_arena_take<unsigned>(ctx, (size_t)C * d * 2);
     a.lblocks = lblocks;
+    if (algo == 6) {
+        a.popsY = to_arena_take<float>(ctx, (size_t)Y * S * NP * P);
+        a.gmY = to_arena_take<float>(ctx, (size_t)Y * S * P);
+    }
     a.knn_next = to_arena_take<int>(ctx, 1);
     a.knn_acc = to_arena_take<float>(ctx, (size_t)C * Q * nacc);
     a.reg = to_arena_take<float>(ctx, (size_t)Y * C * blk);
@@ -185,7 +197,7 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
         for (int v : nz) { if (v < 0) ok = false; mx = v > mx ? v : mx; }
         csc.cap_smem = (mx + 7) & ~7;
         sparse = ok && to_k::rov_sparse_smem(NP, C, csc.cap_smem) <= ctx->smem_optin;
-        if (!sparse && pr->migration == TO_MIG_SPARSE_FP32)
+        if (!sparse && (pr->migration == TO_MIG_SPARSE_FP32 || algo == 6))
             return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
     }
     TO_TRY(to_k::rov_run(ctx, a, sparse ? &csc : nullptr));

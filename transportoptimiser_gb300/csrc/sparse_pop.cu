@@ -22,6 +22,7 @@
 #include "to_internal.cuh"
 #include "to_pop.cuh"
 #include "to_rov.cuh"
+#include "to_rov_dev.cuh"
 #include "to_sparse.cuh"
 
 namespace {
@@ -311,8 +312,18 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 gm[lane] = g + sp[4] * (sp[1] - g) * a.dt + g * brown
                            + (to_expf(jsz) - 1.0f) * g * jump;
                 ctl[lane] = (path < P) ? a.controls[(size_t)t * P + path] : 0;
+                if (a.gmY && path < P) a.gmY[((size_t)t * a.S + s) * P + path] = gm[lane];
             }
             __syncthreads();
+            if (a.popsY) {
+                // ALGO6 restarts paths from here: the year's starting patch
+                // populations, 32 consecutive paths per row
+                for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
+                    const int pth = blockIdx.x * kLanes + (q & (kLanes - 1));
+                    if (pth < P)
+                        a.popsY[(((size_t)t * a.S + s) * NE + (q >> 5)) * P + pth] = cur[q];
+                }
+            }
             const float g = gm[lane];
             const int my_c = ctl[lane];
             float nv[MAXG][4];
@@ -383,6 +394,166 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
             }
             __syncthreads();
         }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// ALGO6 path re-simulation (optimalForwardPaths :1199-2206, as its comments
+// describe it).  Grid ceil(P/32): a CTA re-simulates 32 paths (lane = path)
+// from year t0 to the horizon with every species together, since each
+// year's control depends on all species' states:
+//   A. all warps: every (species, control) migration of this year's
+//      populations into shared memory (CSC, ascending origins, as forward);
+//   B. warps (s, c): the grouped total and the adjusted population
+//      tot * (total / tot), the forward pass's arithmetic;
+//   C. warp 0: the decision (regression of the year, or the terminal rule
+//      in the last year) and the realised payoff flows[c] * profit,
+//      discounted by (1 + r dt / 100) per year;
+//   D. all warps: growth of the chosen control's migrated populations with
+//      the forward pass's noise and growth mean (stored by it);
+//   E. warps s: the new totals.
+// The year-t0 value replaces condExp[t0] and the year-t0 control optCont[t0].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024, 1)
+k_rov_resim_sparse(to_rov_args a, to_csc csc, int t0) {
+    extern __shared__ unsigned char sm_raw[];
+    const int NE = a.ne, NG = NE >> 2, NP = a.np, C = a.C, S = a.S, Y = a.Y, P = a.P;
+    const int SC = S * C;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int path = blockIdx.x * kLanes + lane;
+    float* cur = reinterpret_cast<float*>(sm_raw);                  // [S][NE][32]
+    float* mig = cur + (size_t)S * NE * kLanes;                     // [S][C][NE][32]
+    float* capv = mig + (size_t)SC * NE * kLanes;                   // [S][NE]
+    float* tot = capv + (size_t)S * NE;                             // [S][32]
+    float* adj = tot + (size_t)S * kLanes;                          // [S][C][32]
+    int* ctl = reinterpret_cast<int*>(adj + (size_t)SC * kLanes);   // [32]
+    int* cptr = ctl + kLanes;                                       // [S*C][NE+1]
+    float* cval = reinterpret_cast<float*>(cptr + (size_t)SC * (NE + 1));  // [S*C][cap_smem]
+    uint16_t* cidx = reinterpret_cast<uint16_t*>(cval + (size_t)SC * csc.cap_smem);
+    const uint32_t road = (uint32_t)a.road;
+
+    for (int q = threadIdx.x; q < S * NE * kLanes; q += blockDim.x) {
+        const int sk = q >> 5, pth = blockIdx.x * kLanes + (q & (kLanes - 1));
+        const int s = sk / NE, k = sk - s * NE;
+        cur[q] = (pth < P) ? a.popsY[(((size_t)t0 * S + s) * NE + k) * P + pth] : 0.0f;
+    }
+    for (int q = threadIdx.x; q < S * NE; q += blockDim.x) {
+        const int s = q / NE, k = q - s * NE;
+        capv[q] = a.caps[(size_t)s * NP + k];
+    }
+    for (int m = 0; m < SC; ++m) {
+        const int nnz = csc.nnz[m];
+        for (int k = threadIdx.x; k <= NE; k += blockDim.x)
+            cptr[m * (NE + 1) + k] = csc.ptr[(size_t)m * (NP + 1) + (k <= NP ? k : NP)];
+        for (int e = threadIdx.x; e < nnz; e += blockDim.x) {
+            cval[(size_t)m * csc.cap_smem + e] = csc.val[(size_t)m * csc.cap + e];
+            cidx[(size_t)m * csc.cap_smem + e] = csc.idx[(size_t)m * csc.cap + e];
+        }
+    }
+    __syncthreads();
+    for (int s = warp; s < S; s += W) {
+        float tt = 0.0f;
+        for (int grp = 0; grp < NG; ++grp) {
+            const float* v = cur + ((size_t)s * NE + grp * 4) * kLanes + lane;
+            tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
+        }
+        tot[s * kLanes + lane] = tt;
+    }
+    const float disc = 1.0f + a.rrr * a.dt / 100.0f;
+    float val = 0.0f, df = 1.0f;        // warp 0: realised value, discount factor
+    int c0 = 0;
+    for (int u = t0; u < Y; ++u) {
+        __syncthreads();
+        // A. migrations of every (species, control)
+        for (int s = 0; s < S; ++s) {
+            const float* cs = cur + (size_t)s * NE * kLanes + lane;
+            for (int grp = warp; grp < NG; grp += W) {
+                for (int c = 0; c < C; ++c) {
+                    const int m = s * C + c;
+                    const int* cp = cptr + m * (NE + 1);
+                    const float* cv = cval + (size_t)m * csc.cap_smem;
+                    const uint16_t* ci = cidx + (size_t)m * csc.cap_smem;
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = grp * 4 + j;
+                        float acc = 0.0f;
+                        for (int e = cp[k]; e < cp[k + 1]; ++e)
+                            acc = fmaf(cs[(int)ci[e] * kLanes], cv[e], acc);
+                        mig[((size_t)m * NE + k) * kLanes + lane] = acc;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        // B. adjusted populations tot * (migrated total / tot)
+        for (int m = warp; m < SC; m += W) {
+            const int s = m / C;
+            float tt = 0.0f;
+            for (int grp = 0; grp < NG; ++grp) {
+                const float* v = mig + ((size_t)m * NE + grp * 4) * kLanes + lane;
+                tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
+            }
+            const float ts = tot[s * kLanes + lane];
+            adj[m * kLanes + lane] = ts * (tt / ts);
+        }
+        __syncthreads();
+        // C. the decision and the realised payoff
+        if (warp == 0) {
+            int bc = 0;
+            if (path < P) {
+                float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
+                for (int c = 0; c < C; ++c)
+                    for (int s = 0; s < S; ++s) state[c * S + s] = adj[(s * C + c) * kLanes + lane];
+                const float prof = to_rovd::unit_profit(a, path, u, Y + 1, Y + 1);
+                state[S * C] = prof;
+                float best;
+                if (u == Y - 1) to_rovd::decide_terminal(a, state, best, bc);
+                else to_rovd::decide_interior(a, u, state, best, bc);
+                val = val + (a.flows[bc] * prof) * df;
+                df = df / disc;
+            }
+            if (u == t0) c0 = bc;
+            ctl[lane] = bc;
+        }
+        __syncthreads();
+        if (u == Y - 1) break;
+        // D. growth of the chosen control's migrated populations
+        const int cu = ctl[lane];
+        for (int s = 0; s < S; ++s) {
+            const float* sp = a.params + 8 * s;
+            const int N4 = (a.n_patches[s] + 3) & ~3;
+            const float g = (path < P) ? a.gmY[((size_t)u * S + s) * P + path] : 0.0f;
+            for (int grp = warp; grp < NG; grp += W) {
+                float z[4];
+                to_normal4(a.seed, TO_STREAM_GROWTH, road, path, u,
+                           (uint32_t)((s * N4) >> 2) + grp, z);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int k = grp * 4 + j;
+                    const float mv = mig[(((size_t)s * C + cu) * NE + k) * kLanes + lane];
+                    const float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
+                    const float cpk = capv[s * NE + k];
+                    cur[((size_t)s * NE + k) * kLanes + lane] =
+                        (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
+                                     : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
+                }
+            }
+        }
+        __syncthreads();
+        // E. totals of the new populations
+        for (int s = warp; s < S; s += W) {
+            float tt = 0.0f;
+            for (int grp = 0; grp < NG; ++grp) {
+                const float* v = cur + ((size_t)s * NE + grp * 4) * kLanes + lane;
+                tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
+            }
+            tot[s * kLanes + lane] = tt;
+        }
+    }
+    if (warp == 0 && path < P) {
+        a.condExp[(size_t)t0 * P + path] = val;
+        a.optCont[(size_t)t0 * P + path] = c0;
     }
 }
 
@@ -480,6 +651,27 @@ to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc) {
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_rov_forward_sparse<TO_ROV_MAXC, kMaxG><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
     }
+    to_prof_end(ctx);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
+
+size_t rov_resim_smem(int NE, int S, int C, int cap_smem) {
+    const size_t SC = (size_t)S * C;
+    return ((size_t)S * NE * kLanes + SC * NE * kLanes + (size_t)S * NE + (size_t)S * kLanes +
+            SC * kLanes) * 4 + kLanes * 4 + SC * (NE + 1) * 4 + SC * cap_smem * 6 + 16;
+}
+
+to_status rov_resim_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc, int t0) {
+    const size_t smem = rov_resim_smem(a.ne, a.S, a.C, csc.cap_smem);
+    if (smem > ctx->smem_optin)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "ALGO6 re-simulation needs %zu B", smem);
+    const int blocks = (a.P + kLanes - 1) / kLanes;
+    to_prof_begin(ctx, "rov_resim");
+    TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_resim_sparse,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_rov_resim_sparse<<<blocks, 1024, smem, ctx->stream>>>(a, csc, t0);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;

@@ -57,6 +57,10 @@ struct to_rov_args {
     int* lcnt;                        // [C][lblocks] points per control and path chunk
     unsigned* lkey;                   // [C][d][2] min / max keys of the states
     int lblocks;                      // path chunks of the compaction
+    int k_mult;                       // k = k_mult (ln n + 1): 10 ALGO4, 3 ALGO6
+    int algo;                         // 4 or 6
+    float* popsY;                     // ALGO6: [Y][S][ne][P] patch populations, start of year
+    float* gmY;                       // ALGO6: [Y][S][P] mean growth rate of the year
     int* knn_next;                    // work counter of the kNN kernel
     float* knn_acc;                   // [C][Q][(d+1)(d+2)] normal equations per query
     int kmax;

@@ -22,4 +22,7 @@ size_t mte_sparse_smem(int NE, int cap_smem);
 size_t rov_sparse_smem(int NE, int C, int cap_smem);
 to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc);
 to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc);
+// ALGO6: paths re-simulated from year t0 under the optimal policy
+size_t rov_resim_smem(int NE, int S, int C, int cap_smem);
+to_status rov_resim_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc, int t0);
 }

@@ -17,11 +17,13 @@ import numpy as np
 
 
 def rov_problem_from_models(models, scene, n_paths, n_years=50, dim_res=16, seed=0, road=0,
-                            sem=0, rrr=7.0, n_processes=3, demand=False):
+                            sem=0, rrr=7.0, n_processes=3, demand=False, algo=4):
     """Builds a ROV problem from species models (dicts with N, init_pops,
     caps, mmm) of a synthetic scene.  Processes: fuel price, commodity price
     and (corrected semantics) traffic demand, mean-reverting with theta
-    0.2/0.35/0.5 and sigma 0.1/0.2/0.3, no jumps."""
+    0.2/0.35/0.5 and sigma 0.1/0.2/0.3, no jumps.  algo 4: regression values
+    (ALGO4); 6: values of paths re-simulated under the optimal policy
+    (ALGO6, sem 1)."""
     species = []
     for m, sp in zip(models, scene.species):
         params = np.array(sp.params, np.float32).copy()
@@ -39,4 +41,4 @@ def rov_problem_from_models(models, scene, n_paths, n_years=50, dim_res=16, seed
                 uncert=np.asarray(uncert, np.float32),
                 fuel_costs=np.array([0.3], np.float32), fuel_idx=np.array([0], np.int32),
                 ore_content=np.array([0.8], np.float32), ore_sd=np.array([0.05], np.float32),
-                demand_idx=(2 if (demand and n_processes > 2) else -1))
+                demand_idx=(2 if (demand and n_processes > 2) else -1), algo=algo)

@@ -198,7 +198,8 @@ def rov_ctypes(problem: dict, migration=_capi.MIG_AUTO):
                           len(oc), ptr(oc, C.c_float), ptr(osd, C.c_float),
                           problem["unit_cost"], problem["unit_revenue"], problem["dt"],
                           problem["rrr"], problem.get("demand_idx", -1), problem["seed"],
-                          problem["road"], problem["sem"], migration)
+                          problem["road"], problem["sem"], migration,
+                          int(problem.get("algo", 4)))
     return pr, keep
 
 
