@@ -172,6 +172,13 @@ to_mte_args mte_args(to_ctx ctx, to_gen g, const to_eval_opts* o, int NE) {
     return m;
 }
 
+// the species model writes the compressed columns of the sparse migration
+// kernel directly (no dense matrices, no packing pass)
+void model_to_csc(to_gen g, to_model_args& a) {
+    a.csc_ptr = g->csc.ptr; a.csc_idx = g->csc.idx; a.csc_val = g->csc.val;
+    a.csc_nnz = g->csc.nnz; a.csc_cap = g->csc.cap;
+}
+
 to_status run_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice) {
     if (choice == CH_SPARSE) return to_k::mte_sparse(ctx, m, RS, g->csc);
     if (choice == CH_TC) return to_k::mte_tc(ctx, m, RS);
@@ -244,6 +251,8 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     }
     to_model_args a;
     model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
+    const bool fused_csc = o->migration == TO_MIG_SPARSE_FP32;
+    if (fused_csc) model_to_csc(g, a);
     TO_TRY(to_k::species_model(ctx, a, RS));
     // the widest species model decides the tile shape of the path kernel
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
@@ -251,7 +260,7 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_LAUNCHED(ctx);
     const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32);
     if (try_sparse) {
-        TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
+        if (!fused_csc) TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
         k_min_max_int<<<1, 1024, 0, ctx->stream>>>(RS * g->C, g->csc.nnz, d_max + 1);
         TO_LAUNCHED(ctx);
     }
@@ -297,8 +306,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     for (uint64_t f : fields) key = mix(key, f);
     if (g->exec && g->graph_key == key) {
         TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
-        ctx->launches += 2 + (g->plan_choice == CH_SPARSE ? 1 : 0) +
-                         (g->plan_choice == CH_TC ? 2 : 1) + 2;
+        ctx->launches += 2 + (g->plan_choice == CH_TC ? 2 : 1) + 2;
         return TO_OK;
     }
     if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
@@ -332,9 +340,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
         a.cell_off = g->d_cell_off;
         a.cells = g->d_cells;
     }
+    if (choice == CH_SPARSE) model_to_csc(g, a);
     if (st == TO_OK) st = to_k::species_model(ctx, a, RS);
-    if (st == TO_OK && choice == CH_SPARSE)
-        st = to_k::pack_csc(ctx, g->d_mmm, g->NP, g->C, g->d_np, RS, g->csc);
     if (st == TO_OK) st = tail(ctx, g, m, RS, choice, d_results_out);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);

@@ -468,8 +468,13 @@ k_species_links(to_model_args a) {
         for (int q = n4 * 4 + threadIdx.x; q < N * N; q += blockDim.x) cross[q] = 0;
     }
     const int NP = a.npad;
+    const bool to_csc = a.csc_ptr != nullptr;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
-    {
+    int* s_col = reinterpret_cast<int*>(s_surv + a.C * (SC + 1));    // [C][NP] column counts
+    double* s_sum = reinterpret_cast<double*>(s_col + ((a.C * NP + 1) & ~1));  // [NM] row sums
+    if (to_csc) {
+        for (int q = threadIdx.x; q < a.C * NP; q += blockDim.x) s_col[q] = 0;
+    } else {
         float4* m4 = reinterpret_cast<float4*>(mmm);
         const size_t n4 = (size_t)a.C * NP * NP / 4;
         for (size_t q = threadIdx.x; q < n4; q += blockDim.x) m4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -586,6 +591,7 @@ k_species_links(to_model_args a) {
         if (lane == 0)
             for (int q = 0; q < cnt; ++q) summ += rowv[q];
         summ = __shfl_sync(0xffffffffu, summ, 0);
+        if (lane == 0) s_sum[i] = summ;
         // second pass: the same in-range set, slot by slot
         int base = 0;
         for (int j0 = 0; j0 < N; j0 += 32) {
@@ -593,17 +599,123 @@ k_species_links(to_model_args a) {
             bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
             unsigned m = __ballot_sync(0xffffffffu, inr);
             if (inr) {
-                const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))] / summ;
+                const int slot = base + __popc(m & ((1u << lane) - 1u));
+                const double tr = rowv[slot] / summ;
+                if (to_csc) rowv[slot] = tr;         // the fill pass reads it back
                 const int cr = cross[(size_t)i * N + j];
                 for (int c = 0; c < a.C; ++c) {
                     float mv = (float)(tr * surv_of(c, cr));
-                    if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
+                    if ((double)mv > 0.00001) {
+                        if (to_csc) atomicAdd(&s_col[c * NP + j], 1);
+                        else mmm[((size_t)c * NP + j) * NP + i] = mv;
+                    }
                 }
                 if (trans) trans[(size_t)i * NM + j] = tr;
             }
             base += __popc(m);
         }
         __syncwarp();
+    }
+    if (to_csc) {
+        // column starts (exclusive scan per control), then the entries: a
+        // warp per origin row again, slots taken by shared atomics, and a
+        // sort of each short column by origin
+        __syncthreads();
+        for (int c = warp; c < a.C; c += nwarp) {
+            int* col = s_col + c * NP;
+            int run = 0;
+            for (int k0 = 0; k0 < NP; k0 += 32) {
+                const int k = k0 + lane;
+                const int v = k < NP ? col[k] : 0;
+                int x = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (lane >= o) x += y;
+                }
+                if (k < NP) {
+                    col[k] = run + x - v;
+                    a.csc_ptr[((size_t)rs * a.C + c) * (NP + 1) + k] = run + x - v;
+                }
+                run += __shfl_sync(0xffffffffu, x, 31);
+            }
+            if (lane == 0) {
+                a.csc_ptr[((size_t)rs * a.C + c) * (NP + 1) + NP] = run;
+                a.csc_nnz[(size_t)rs * a.C + c] = run <= a.csc_cap ? run : -1;
+            }
+        }
+        __syncthreads();
+        for (int i = warp; i < N; i += nwarp) {
+            const double* rowv = wv + (size_t)i * NM;
+            int base = 0;
+            for (int j0 = 0; j0 < N; j0 += 32) {
+                const int j = j0 + lane;
+                bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
+                unsigned m = __ballot_sync(0xffffffffu, inr);
+                if (inr) {
+                    const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))];
+                    const int cr = cross[(size_t)i * N + j];
+                    for (int c = 0; c < a.C; ++c) {
+                        float mv = (float)(tr * surv_of(c, cr));
+                        const size_t mtx = (size_t)rs * a.C + c;
+                        if ((double)mv > 0.00001) {
+                            const int pos = atomicAdd(&s_col[c * NP + j], 1);
+                            if (pos < a.csc_cap) {
+                                a.csc_idx[mtx * a.csc_cap + pos] = (uint16_t)i;
+                                a.csc_val[mtx * a.csc_cap + pos] = mv;
+                            }
+                        }
+                    }
+                }
+                base += __popc(m);
+            }
+        }
+        __syncthreads();
+        // a warp per column: every entry's rank among the column's origins
+        // (distinct) is its place; columns of up to 32 * 8 entries
+        for (int q = warp; q < a.C * N; q += nwarp) {
+            const int c = q / N, k = q - c * N;
+            const size_t mtx = (size_t)rs * a.C + c;
+            const int* pk = a.csc_ptr + mtx * (NP + 1);
+            const int e0 = pk[k], e1 = pk[k + 1], len = e1 - e0;
+            if (e1 > a.csc_cap || len < 2) continue;
+            uint16_t* ix = a.csc_idx + mtx * a.csc_cap + e0;
+            float* vv = a.csc_val + mtx * a.csc_cap + e0;
+            uint16_t key[8];
+            float val[8];
+            int rank[8];
+            const int per = (len + 31) >> 5;
+            if (per > 8) {
+                // long column: one lane, insertion sort
+                if (lane == 0)
+                    for (int e = 1; e < len; ++e) {
+                        const uint16_t kk = ix[e];
+                        const float vl = vv[e];
+                        int f = e - 1;
+                        while (f >= 0 && ix[f] > kk) { ix[f + 1] = ix[f]; vv[f + 1] = vv[f]; --f; }
+                        ix[f + 1] = kk;
+                        vv[f + 1] = vl;
+                    }
+                __syncwarp();
+                continue;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int e = lane + 32 * u;
+                key[u] = (u < per && e < len) ? ix[e] : 0xFFFFu;
+                val[u] = (u < per && e < len) ? vv[e] : 0.0f;
+                rank[u] = 0;
+            }
+            for (int f = 0; f < len; ++f) {
+                const uint16_t kf = ix[f];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) rank[u] += (u < per && kf < key[u]) ? 1 : 0;
+            }
+            __syncwarp();
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                if (u < per && lane + 32 * u < len) { ix[rank[u]] = key[u]; vv[rank[u]] = val[u]; }
+            __syncwarp();
+        }
     }
     // dense FP64 transition / survival outputs (single-road API only)
     if (trans || surv) {
@@ -691,15 +803,19 @@ to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
     // links: float centroids, segment and survival tables
     const size_t smem2 = (size_t)2 * a.max_patches * sizeof(float) +
                          (size_t)4 * TO_SURV_TABLE_SEGS * sizeof(float) +
-                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
+                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double) +
+                         (size_t)((a.C * a.npad + 1) & ~1) * sizeof(int) +
+                         (size_t)a.max_patches * sizeof(double);
     if (smem2 > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d patches exceed shared memory",
                             a.max_patches);
     TO_CUDA(ctx, cudaFuncSetAttribute(k_species_links,
                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-    to_prof_begin(ctx, "species_model");
+    to_prof_begin(ctx, "species_patches");
     k_species_patches<<<n_rs, 1024, smem, ctx->stream>>>(a);
+    to_prof_end(ctx);
     TO_LAUNCHED(ctx);
+    to_prof_begin(ctx, "species_links");
     k_species_links<<<n_rs, 512, smem2, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);

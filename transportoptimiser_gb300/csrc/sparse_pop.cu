@@ -564,8 +564,10 @@ namespace to_k {
 to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_patches,
                    int n_rs, to_csc& csc) {
     if (NP > 1024) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NP);
+    to_prof_begin(ctx, "pack_csc");
     k_pack_csc<<<n_rs * C, 1024, 0, ctx->stream>>>(mmm, NP, C, n_patches, csc.cap,
                                                  csc.ptr, csc.idx, csc.val, csc.nnz);
+    to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }

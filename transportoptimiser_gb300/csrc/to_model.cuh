@@ -41,6 +41,13 @@ struct to_model_args {
     double* trans;               // optional [RS][NM][NM]
     double* surv;                // optional [RS][C][NM][NM]
     float* mmm;                  // [RS][C][NP][NP] destination-major
+    // compressed-column output instead of mmm (when csc_ptr is set): per
+    // matrix rs*C + c, destination k's origins ascending with their values
+    int* csc_ptr;                // [RS*C][NP+1]
+    uint16_t* csc_idx;           // [RS*C][csc_cap]
+    float* csc_val;              // [RS*C][csc_cap]
+    int* csc_nnz;                // [RS*C], -1 above csc_cap
+    int csc_cap;
     float* init_pops;            // [RS][NP]
     float* caps;                 // [RS][NP] (padding 1.0)
     int* d_flags;
