@@ -259,6 +259,18 @@ def rov_adjoint_leg(ctx, rov_paths=10000, adj_paths=20000, reps=3):
     rov = {"paths": rov_paths, "ms_per_valuation": 1000.0 * statistics.median(ts),
            "value": float(out["stats"][0]), "se": float(out["value_se"]),
            "patches": [int(m["N"]) for m in models]}
+    # ALGO6: each year's value from paths re-simulated under the optimal policy
+    r6 = rov_problem_from_models(models, sc, n_paths=rov_paths, n_years=YEARS, dim_res=16,
+                                 sem=1, n_processes=3, demand=True, algo=6)
+    out6 = sg.simulateROVCUDA(r6, want=(), ctx=ctx)
+    ts6 = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out6 = sg.simulateROVCUDA(r6, want=(), ctx=ctx)
+        ts6.append(time.perf_counter() - t0)
+    rov["algo6_ms_per_valuation"] = 1000.0 * statistics.median(ts6)
+    rov["algo6_value"] = float(out6["stats"][0])
+    rov["algo6_se"] = float(out6["value_se"])
     ra = rov_problem_from_models(models, sc, n_paths=adj_paths, n_years=YEARS, dim_res=16,
                                  sem=1, n_processes=3, demand=True)
     pol = sg.simulateROVCUDA(ra, want=("opt_cont",), ctx=ctx)
