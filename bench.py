@@ -419,10 +419,11 @@ def main():
             step_device(o_prof)
         torch.cuda.synchronize()
         mte_ms, mte_n = ctx.kernel_time(mte_name)
+        lb_ms, lb_n = ctx.kernel_time("species_labels")
         pt_ms, pt_n = ctx.kernel_time("species_patches")
         lk_ms, lk_n = ctx.kernel_time("species_links")
         pk_ms, pk_n = ctx.kernel_time("pack_csc")
-        sm_ms, sm_n = pt_ms + lk_ms + pk_ms, max(pt_n, 1)
+        sm_ms, sm_n = lb_ms + pt_ms + lk_ms + pk_ms, max(pt_n, 1)
         ctx.profile(False)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = sum(step_ms) / len(step_ms)
@@ -508,6 +509,7 @@ def main():
                        "l2": "flushed (256 MB write) between steps",
                        "wall_s_timed": t_wall},
             "e2e": {"value": e2e_value, "unit": "designs/s", "h2d_bytes_per_step": h2d,
+                    "ms_steps": [round(x, 3) for x in e2e_ms],
                     "d2h_bytes_per_step": d2h},
             "plain": {"value": plain_value, "unit": "designs/s",
                       "roads": args.plain_roads, "note": "one road per call, host entry points"},
@@ -522,6 +524,7 @@ def main():
                          "useful_achieved": useful_tf,
                          "kernel_ms": mte_ms / max(mte_n, 1),
                          "species_model_ms": sm_ms / max(sm_n, 1),
+                         "species_labels_ms": lb_ms / max(lb_n, 1),
                          "species_patches_ms": pt_ms / max(pt_n, 1),
                          "species_links_ms": lk_ms / max(lk_n, 1),
                          "pack_csc_ms": pk_ms / max(pk_n, 1)},

@@ -38,6 +38,9 @@ struct to_gen_s {
     float* d_popmap = nullptr;           // [S][W*H]
     to_model_species* d_species = nullptr;
     float* d_params = nullptr;           // [S][8]
+    int n_label_types = 0;               // habitable types of any species
+    int* d_label_types = nullptr;        // [T]
+    int* d_labels = nullptr;             // [max_roads][T][W*H]
     // per-generation buffers
     char* buf = nullptr;
     size_t buf_bytes = 0;
@@ -148,6 +151,7 @@ void model_args(to_gen g, int R, const int* cell_off, const int* cells, const in
     a.crossings_scratch = g->d_cross; a.trans_scratch = g->d_tv;
     a.mmm = g->d_mmm; a.init_pops = g->d_ip; a.caps = g->d_cp;
     a.d_flags = ctx->d_flags;
+    a.n_label_types = g->n_label_types; a.label_types = g->d_label_types; a.labels = g->d_labels;
 }
 
 to_status grow_end(to_ctx ctx, to_gen g, size_t n) {
@@ -170,13 +174,6 @@ to_mte_args mte_args(to_ctx ctx, to_gen g, const to_eval_opts* o, int NE) {
     m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
     m.end_pops = g->d_end; m.flags = ctx->d_flags;
     return m;
-}
-
-// the species model writes the compressed columns of the sparse migration
-// kernel directly (no dense matrices, no packing pass)
-void model_to_csc(to_gen g, to_model_args& a) {
-    a.csc_ptr = g->csc.ptr; a.csc_idx = g->csc.idx; a.csc_val = g->csc.val;
-    a.csc_nnz = g->csc.nnz; a.csc_cap = g->csc.cap;
 }
 
 to_status run_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice) {
@@ -251,8 +248,6 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     }
     to_model_args a;
     model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
-    const bool fused_csc = o->migration == TO_MIG_SPARSE_FP32;
-    if (fused_csc) model_to_csc(g, a);
     TO_TRY(to_k::species_model(ctx, a, RS));
     // the widest species model decides the tile shape of the path kernel
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
@@ -260,7 +255,7 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_LAUNCHED(ctx);
     const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32);
     if (try_sparse) {
-        if (!fused_csc) TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
+        TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
         k_min_max_int<<<1, 1024, 0, ctx->stream>>>(RS * g->C, g->csc.nnz, d_max + 1);
         TO_LAUNCHED(ctx);
     }
@@ -306,7 +301,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     for (uint64_t f : fields) key = mix(key, f);
     if (g->exec && g->graph_key == key) {
         TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
-        ctx->launches += 2 + (g->plan_choice == CH_TC ? 2 : 1) + 2;
+        ctx->launches += 3 + (g->plan_choice == CH_SPARSE ? 1 : 0) +
+                         (g->plan_choice == CH_TC ? 2 : 1) + 2;
         return TO_OK;
     }
     if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
@@ -340,8 +336,9 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
         a.cell_off = g->d_cell_off;
         a.cells = g->d_cells;
     }
-    if (choice == CH_SPARSE) model_to_csc(g, a);
     if (st == TO_OK) st = to_k::species_model(ctx, a, RS);
+    if (st == TO_OK && choice == CH_SPARSE)
+        st = to_k::pack_csc(ctx, g->d_mmm, g->NP, g->C, g->d_np, RS, g->csc);
     if (st == TO_OK) st = tail(ctx, g, m, RS, choice, d_results_out);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
@@ -385,6 +382,16 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     const int S = g->S, C = g->C, NM = g->NM, NP = g->NP;
     std::vector<to_model_species> hs(S);
     std::vector<float> pm((size_t)S * n), prm((size_t)S * 8);
+    std::vector<int> ltypes;           // habitable types of any species, first appearance
+    for (int s = 0; s < S; ++s)
+        for (int h = 0; h < sc->species[s].n_hab && sc->species[s].habs; ++h) {
+            const int t = sc->species[s].habs[h].type;
+            if (t == 3 || t == 4) continue;
+            bool seen = false;
+            for (int v : ltypes) seen |= (v == t);
+            if (!seen) ltypes.push_back(t);
+        }
+    g->n_label_types = (int)ltypes.size();
     for (int s = 0; s < S; ++s) {
         const to_species_desc& d = sc->species[s];
         if (d.n_hab <= 0 || d.n_hab > TO_MAX_HAB || !d.habs || !d.pop_map || !d.hazard ||
@@ -413,6 +420,11 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     if ((e = cudaMalloc(&g->d_popmap, pm.size() * sizeof(float))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&g->d_species, S * sizeof(to_model_species))) != cudaSuccess) return fail(e);
     if ((e = cudaMalloc(&g->d_params, prm.size() * sizeof(float))) != cudaSuccess) return fail(e);
+    if ((e = cudaMalloc(&g->d_label_types, (ltypes.size() + 1) * sizeof(int))) != cudaSuccess)
+        return fail(e);
+    if (!ltypes.empty())
+        cudaMemcpy(g->d_label_types, ltypes.data(), ltypes.size() * sizeof(int),
+                   cudaMemcpyHostToDevice);
     cudaMemcpy(g->d_base, sc->base_map, n * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(g->d_popmap, pm.data(), pm.size() * sizeof(float), cudaMemcpyHostToDevice);
     cudaMemcpy(g->d_species, hs.data(), S * sizeof(to_model_species), cudaMemcpyHostToDevice);
@@ -434,6 +446,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     acc((RS * TO_RESULT_STRIDE + 64) * 8);
     acc((R + 1) * 4);
     acc(R * 16 * 4);
+    acc(R * g->n_label_types * n * 4);
     const size_t cap = (size_t)NP * 32;
     acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
     if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
@@ -460,6 +473,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->d_results = carve<double>(p, RS * TO_RESULT_STRIDE + 64);
     g->d_counts = carve<int>(p, R + 1);
     g->d_feat = carve<float>(p, R * 16);
+    g->d_labels = carve<int>(p, R * g->n_label_types * n);
     g->csc.ptr = carve<int>(p, RS * C * (NP + 1));
     g->csc.idx = carve<uint16_t>(p, RS * C * cap);
     g->csc.val = carve<float>(p, RS * C * cap);
@@ -480,6 +494,7 @@ to_status to_scene_destroy(to_gen g) {
     cudaFree(g->d_popmap);
     cudaFree(g->d_species);
     cudaFree(g->d_params);
+    cudaFree(g->d_label_types);
     cudaFree(g->buf);
     cudaFree(g->d_end);
     delete g;

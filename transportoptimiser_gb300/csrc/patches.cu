@@ -399,6 +399,85 @@ k_species_patches(to_model_args a) {
     if (threadIdx.x == 0) a.n_patches[rs] = N;
 }
 
+
+// Labels of one (road, habitable type): the type's cells less the road's
+// cells, labelled as LabelImage numbers into global memory.  The labels do
+// not depend on the species, so every species of the road reads them.
+__global__ void __launch_bounds__(1024)
+k_road_labels(to_model_args a) {
+    extern __shared__ int smem[];
+    const int T = a.n_label_types;
+    const int road = blockIdx.x / T, ti = blockIdx.x - road * T;
+    const int W = a.W, n = W * a.H;
+    int* s_tmp = smem;                         // 33 ints
+    int* par = smem + 64;
+    const int typ = a.label_types[ti];
+    const int* hab = a.hab_map;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) par[i] = (hab[i] == typ) ? i : -1;
+    __syncthreads();
+    const int c0 = a.cell_off ? a.cell_off[road] : 0;
+    const int c1 = a.cell_off ? a.cell_off[road + 1] : 0;
+    for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) par[a.cells[q]] = -1;
+    __syncthreads();
+    cta_label(n, W, par, s_tmp, a.d_flags);
+    int* out = a.labels + ((size_t)road * T + ti) * n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = par[i];
+}
+
+// The patch pass of k_species_patches on labels from k_road_labels: same
+// habitat order, same per-(block, region) sums, so the same patch list.
+__global__ void __launch_bounds__(512)
+k_species_patches_lab(to_model_args a) {
+    extern __shared__ int smem[];
+    const int rs = blockIdx.x;
+    const int road = rs / a.S, sp = rs - road * a.S;
+    const int W = a.W, H = a.H, n = W * H, T = a.n_label_types;
+    int* s_tmp = smem;                         // 33 ints
+    int* s_misc = s_tmp + 40;                  // counters
+    int* s_list = smem + 64;                   // block region lists
+    const to_model_species& S = a.species[sp];
+    const int NM = a.max_patches;
+    double* area = a.area + (size_t)rs * NM;
+    double* cap = a.cap + (size_t)rs * NM;
+    double* popd = a.pop + (size_t)rs * NM;
+    double* cx = a.cx + (size_t)rs * NM;
+    double* cy = a.cy + (size_t)rs * NM;
+    int* ptype = a.type + (size_t)rs * NM;
+    const float* popmap = a.pop_map + (size_t)sp * n;
+
+    if (threadIdx.x == 0) { s_misc[0] = 0; s_misc[1] = -1; }
+    __syncthreads();
+    bool ok = true;
+    for (int h = 0; h < S.n_hab; ++h) {
+        int typ = S.hab_type[h];
+        if (typ == 3 || typ == 4) continue;      // CLEAR, ROAD
+        int ti = 0;
+        while (ti < T && a.label_types[ti] != typ) ++ti;
+        if (ti == T) { ok = false; continue; }    // not planned for: flagged
+        const int* L = a.labels + ((size_t)road * T + ti) * n;
+        float maxpop = (float)S.hab_max_pop[h];
+        auto lab = [&](int c) { return L[c]; };
+        auto popf = [&](int c) { return popmap[c]; };
+        auto emit = [&](int o, int cnt, float pop, float sx, float sy, int bx, int by) {
+            float v[5];
+            finish_patch(cnt, pop, sx, sy, bx, by, a.skpx, a.skpy, a.xs, a.ys, a.spa, maxpop, v);
+            area[o] = (double)v[0];
+            cap[o] = (double)v[1];
+            popd[o] = (double)v[2];
+            cx[o] = (double)v[3];
+            cy[o] = (double)v[4];
+            ptype[o] = h;
+        };
+        ok &= cta_block_patches(W, H, a.skpx, a.skpy, a.xres, a.yres, NM, &s_misc[0], s_tmp,
+                                s_list, lab, popf, emit);
+        __syncthreads();
+    }
+    if (!ok && a.d_flags) atomicExch(a.d_flags, TO_DEVERR_PATCHES);
+    __syncthreads();
+    const int N = min(s_misc[0], NM);
+    if (threadIdx.x == 0) a.n_patches[rs] = N;
+}
+
 // Second half of the species-road model, one CTA per (road, species):
 // patch-pair distances, road crossings, transition and survival
 // probabilities and the migration matrices.  Small shared memory, so two
@@ -468,13 +547,8 @@ k_species_links(to_model_args a) {
         for (int q = n4 * 4 + threadIdx.x; q < N * N; q += blockDim.x) cross[q] = 0;
     }
     const int NP = a.npad;
-    const bool to_csc = a.csc_ptr != nullptr;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
-    int* s_col = reinterpret_cast<int*>(s_surv + a.C * (SC + 1));    // [C][NP] column counts
-    double* s_sum = reinterpret_cast<double*>(s_col + ((a.C * NP + 1) & ~1));  // [NM] row sums
-    if (to_csc) {
-        for (int q = threadIdx.x; q < a.C * NP; q += blockDim.x) s_col[q] = 0;
-    } else {
+    {
         float4* m4 = reinterpret_cast<float4*>(mmm);
         const size_t n4 = (size_t)a.C * NP * NP / 4;
         for (size_t q = threadIdx.x; q < n4; q += blockDim.x) m4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -591,7 +665,6 @@ k_species_links(to_model_args a) {
         if (lane == 0)
             for (int q = 0; q < cnt; ++q) summ += rowv[q];
         summ = __shfl_sync(0xffffffffu, summ, 0);
-        if (lane == 0) s_sum[i] = summ;
         // second pass: the same in-range set, slot by slot
         int base = 0;
         for (int j0 = 0; j0 < N; j0 += 32) {
@@ -599,123 +672,17 @@ k_species_links(to_model_args a) {
             bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
             unsigned m = __ballot_sync(0xffffffffu, inr);
             if (inr) {
-                const int slot = base + __popc(m & ((1u << lane) - 1u));
-                const double tr = rowv[slot] / summ;
-                if (to_csc) rowv[slot] = tr;         // the fill pass reads it back
+                const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))] / summ;
                 const int cr = cross[(size_t)i * N + j];
                 for (int c = 0; c < a.C; ++c) {
                     float mv = (float)(tr * surv_of(c, cr));
-                    if ((double)mv > 0.00001) {
-                        if (to_csc) atomicAdd(&s_col[c * NP + j], 1);
-                        else mmm[((size_t)c * NP + j) * NP + i] = mv;
-                    }
+                    if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
                 }
                 if (trans) trans[(size_t)i * NM + j] = tr;
             }
             base += __popc(m);
         }
         __syncwarp();
-    }
-    if (to_csc) {
-        // column starts (exclusive scan per control), then the entries: a
-        // warp per origin row again, slots taken by shared atomics, and a
-        // sort of each short column by origin
-        __syncthreads();
-        for (int c = warp; c < a.C; c += nwarp) {
-            int* col = s_col + c * NP;
-            int run = 0;
-            for (int k0 = 0; k0 < NP; k0 += 32) {
-                const int k = k0 + lane;
-                const int v = k < NP ? col[k] : 0;
-                int x = v;
-                for (int o = 1; o < 32; o <<= 1) {
-                    const int y = __shfl_up_sync(0xffffffffu, x, o);
-                    if (lane >= o) x += y;
-                }
-                if (k < NP) {
-                    col[k] = run + x - v;
-                    a.csc_ptr[((size_t)rs * a.C + c) * (NP + 1) + k] = run + x - v;
-                }
-                run += __shfl_sync(0xffffffffu, x, 31);
-            }
-            if (lane == 0) {
-                a.csc_ptr[((size_t)rs * a.C + c) * (NP + 1) + NP] = run;
-                a.csc_nnz[(size_t)rs * a.C + c] = run <= a.csc_cap ? run : -1;
-            }
-        }
-        __syncthreads();
-        for (int i = warp; i < N; i += nwarp) {
-            const double* rowv = wv + (size_t)i * NM;
-            int base = 0;
-            for (int j0 = 0; j0 < N; j0 += 32) {
-                const int j = j0 + lane;
-                bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
-                unsigned m = __ballot_sync(0xffffffffu, inr);
-                if (inr) {
-                    const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))];
-                    const int cr = cross[(size_t)i * N + j];
-                    for (int c = 0; c < a.C; ++c) {
-                        float mv = (float)(tr * surv_of(c, cr));
-                        const size_t mtx = (size_t)rs * a.C + c;
-                        if ((double)mv > 0.00001) {
-                            const int pos = atomicAdd(&s_col[c * NP + j], 1);
-                            if (pos < a.csc_cap) {
-                                a.csc_idx[mtx * a.csc_cap + pos] = (uint16_t)i;
-                                a.csc_val[mtx * a.csc_cap + pos] = mv;
-                            }
-                        }
-                    }
-                }
-                base += __popc(m);
-            }
-        }
-        __syncthreads();
-        // a warp per column: every entry's rank among the column's origins
-        // (distinct) is its place; columns of up to 32 * 8 entries
-        for (int q = warp; q < a.C * N; q += nwarp) {
-            const int c = q / N, k = q - c * N;
-            const size_t mtx = (size_t)rs * a.C + c;
-            const int* pk = a.csc_ptr + mtx * (NP + 1);
-            const int e0 = pk[k], e1 = pk[k + 1], len = e1 - e0;
-            if (e1 > a.csc_cap || len < 2) continue;
-            uint16_t* ix = a.csc_idx + mtx * a.csc_cap + e0;
-            float* vv = a.csc_val + mtx * a.csc_cap + e0;
-            uint16_t key[8];
-            float val[8];
-            int rank[8];
-            const int per = (len + 31) >> 5;
-            if (per > 8) {
-                // long column: one lane, insertion sort
-                if (lane == 0)
-                    for (int e = 1; e < len; ++e) {
-                        const uint16_t kk = ix[e];
-                        const float vl = vv[e];
-                        int f = e - 1;
-                        while (f >= 0 && ix[f] > kk) { ix[f + 1] = ix[f]; vv[f + 1] = vv[f]; --f; }
-                        ix[f + 1] = kk;
-                        vv[f + 1] = vl;
-                    }
-                __syncwarp();
-                continue;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int e = lane + 32 * u;
-                key[u] = (u < per && e < len) ? ix[e] : 0xFFFFu;
-                val[u] = (u < per && e < len) ? vv[e] : 0.0f;
-                rank[u] = 0;
-            }
-            for (int f = 0; f < len; ++f) {
-                const uint16_t kf = ix[f];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) rank[u] += (u < per && kf < key[u]) ? 1 : 0;
-            }
-            __syncwarp();
-#pragma unroll
-            for (int u = 0; u < 8; ++u)
-                if (u < per && lane + 32 * u < len) { ix[rank[u]] = key[u]; vv[rank[u]] = val[u]; }
-            __syncwarp();
-        }
     }
     // dense FP64 transition / survival outputs (single-road API only)
     if (trans || surv) {
@@ -803,18 +770,38 @@ to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
     // links: float centroids, segment and survival tables
     const size_t smem2 = (size_t)2 * a.max_patches * sizeof(float) +
                          (size_t)4 * TO_SURV_TABLE_SEGS * sizeof(float) +
-                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double) +
-                         (size_t)((a.C * a.npad + 1) & ~1) * sizeof(int) +
-                         (size_t)a.max_patches * sizeof(double);
+                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
     if (smem2 > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d patches exceed shared memory",
                             a.max_patches);
     TO_CUDA(ctx, cudaFuncSetAttribute(k_species_links,
                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-    to_prof_begin(ctx, "species_patches");
-    k_species_patches<<<n_rs, 1024, smem, ctx->stream>>>(a);
-    to_prof_end(ctx);
-    TO_LAUNCHED(ctx);
+    if (a.n_label_types > 0) {
+        // labels once per (road, habitable type), then each species' patches
+        const size_t smem_l = (size_t)(64 + a.W * a.H) * sizeof(int);
+        const size_t smem_p = (size_t)(64 + a.xres * a.yres + 1 + a.max_patches) * sizeof(int);
+        if (smem_l > ctx->smem_optin || smem_p > ctx->smem_optin)
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED, "grid of %d x %d exceeds shared memory",
+                                a.W, a.H);
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_road_labels,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_l));
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_species_patches_lab,
+                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p));
+        const int roads = n_rs / a.S;
+        to_prof_begin(ctx, "species_labels");
+        k_road_labels<<<roads * a.n_label_types, 1024, smem_l, ctx->stream>>>(a);
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+        to_prof_begin(ctx, "species_patches");
+        k_species_patches_lab<<<n_rs, 512, smem_p, ctx->stream>>>(a);
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+    } else {
+        to_prof_begin(ctx, "species_patches");
+        k_species_patches<<<n_rs, 1024, smem, ctx->stream>>>(a);
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+    }
     to_prof_begin(ctx, "species_links");
     k_species_links<<<n_rs, 512, smem2, ctx->stream>>>(a);
     to_prof_end(ctx);

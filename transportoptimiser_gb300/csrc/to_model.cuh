@@ -41,13 +41,12 @@ struct to_model_args {
     double* trans;               // optional [RS][NM][NM]
     double* surv;                // optional [RS][C][NM][NM]
     float* mmm;                  // [RS][C][NP][NP] destination-major
-    // compressed-column output instead of mmm (when csc_ptr is set): per
-    // matrix rs*C + c, destination k's origins ascending with their values
-    int* csc_ptr;                // [RS*C][NP+1]
-    uint16_t* csc_idx;           // [RS*C][csc_cap]
-    float* csc_val;              // [RS*C][csc_cap]
-    int* csc_nnz;                // [RS*C], -1 above csc_cap
-    int csc_cap;
+    // labels shared by the species of a road: one labelling per (road,
+    // habitable type) into global memory, read by every species' patch
+    // pass (n_label_types 0: each CTA labels in its own shared memory)
+    int n_label_types;           // T
+    const int* label_types;      // [T] habitat codes
+    int* labels;                 // [R][T][W*H] LabelImage numbers, 0 background
     float* init_pops;            // [RS][NP]
     float* caps;                 // [RS][NP] (padding 1.0)
     int* d_flags;
