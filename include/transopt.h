@@ -287,6 +287,17 @@ typedef struct {
 to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* prob,
                           to_rov_result* res);
 
+/* A batch of roads valued together (the batched form of simulateROVCUDA for
+ * a GA generation; no reference counterpart): n_roads problems with the same
+ * dimensions, processes, costs, seed and species parameters, each with its
+ * own species models (patches, capacities, migration matrices) and road id.
+ * One launch per stage serves every road; the regressions are per (road,
+ * control).  Each road's result equals to_simulate_rov on that road alone.
+ * Corrected semantics (sem 1), ALGO4, sparse migration, >= 128 paths per
+ * road when n_roads > 1. */
+to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* probs,
+                                to_rov_result* results);
+
 /* knn_cuda_with_indexes::knn, knn_cuda_with_indexes.h:4-47: ref (dim x n)
  * and query (dim x Q) dim-major, host pointers; dist / ind are k x Q
  * (dist[kk*Q + q], ind 1-based) in ascending (distance, index) order. */

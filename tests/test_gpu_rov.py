@@ -142,3 +142,27 @@ def test_rov_algo6_refuses_dense_forms(ctx):
     rp = rov_problem_from_models(models, sc, n_paths=200, n_years=6, dim_res=8, sem=1, algo=6)
     with pytest.raises(TransOptError):
         sg.simulateROVCUDA(rp, migration=MIG_SIMT_FP32, ctx=ctx)
+
+
+def test_rov_batch_equals_single_roads(ctx):
+    """Three roads of one scene valued in one batch (chunks of the
+    compaction straddle roads: 700 paths each) give each road exactly the
+    single-road results."""
+    sc = synth.rov_road(3, n_species=2)
+    rng = np.random.Generator(np.random.Philox(5))
+    roads = [sc.roads[0]] + [synth.random_road(sc.W, sc.H, n, rng) for n in (6, 12)]
+    probs = []
+    for i, rd in enumerate(roads):
+        models = [po.species_model(sc, sc.species[s], rd, sem=1) for s in range(2)]
+        probs.append(rov_problem_from_models(models, sc, n_paths=700, n_years=12, dim_res=8,
+                                             sem=1, n_processes=3, demand=True, seed=4,
+                                             road=10 + i))
+    assert len({p["species"][0]["N"] for p in probs}) > 1      # different patch sets
+    want = ("cond_exp", "opt_cont", "regression", "unit_profits", "adj_pops")
+    batch = sg.simulateROVCUDA_batch(probs, want=want, ctx=ctx)
+    for p, b in zip(probs, batch):
+        one = sg.simulateROVCUDA(p, want=want, ctx=ctx)
+        for k in want:
+            assert np.array_equal(b[k], one[k]), k
+        assert np.array_equal(b["stats"], one["stats"])
+        assert b["value_se"] == one["value_se"]

@@ -403,10 +403,10 @@ struct GridPass {
     }
 };
 
-// Per control: bounding box of the normalised points, a cell grid of about
-// 32n/k cells (at most TO_KNN_GCELLS; a few points per cell, since rows are
-// set up 32 at a time and cost little), and a counting sort of the points
-// into it.  One CTA per control.
+// Per regression group (road, control): bounding box of the normalised
+// points, a cell grid of about 32n/k cells (at most TO_KNN_GCELLS; a few
+// points per cell, since rows are set up 32 at a time and cost little), and
+// a counting sort of the points into it.  One CTA per group.
 __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
     const int c = blockIdx.x, d = a.S + 1, P = a.P;
     const int n = a.npts[c], k = a.kc[c];
@@ -536,6 +536,8 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 // same totals in every lane, and lane 0 stores them.  k_knn_solve then
 // solves one system per thread (FP64 Cholesky, to_lsm_math.h).
 constexpr float kSeedGrow = 1.4f;
+// groups of at most this many points skip the threshold search
+constexpr int kBrute = 128;
 
 template <int D>
 __host__ __device__ constexpr int knn_acc_len() { return (D + 1) + (D + 1) * (D + 1); }
@@ -550,7 +552,7 @@ k_knn_rov(to_rov_args a, int t) {
     const int P = a.P, Q = a.Q;
     const int lane = threadIdx.x & 31;
     WarpScratch& ws = reinterpret_cast<WarpScratch*>(sm_raw)[threadIdx.x >> 5];
-    const int items = a.C * Q;
+    const int items = a.G * Q;                 // (group, query), group g = road*C + control
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.knn_next, 1);
@@ -571,9 +573,17 @@ k_knn_rov(to_rov_args a, int t) {
         const float kp = kth_prev[qi];
         float T = kp > 0.0f ? kp * kSeedGrow : T0;
         float qn[D], xq[D];
-        to_rov_query<D>(a, qi, qn, xq);
+        to_rov_query<D>(a, c / a.C, qi, qn, xq);
         bool ok = false;
-        if (g.ok) {
+        if (n <= kBrute) {
+            // few points (small batches of paths): every point's key, one
+            // sort by (key, index) - the same k nearest in the same order
+            for (int i = lane; i < kBrute; i += 32)
+                ws.sel[i] = (i < n) ? pack_sel(sqdist(xs, P, i, D, qn), i) : ~0ull;
+            __syncwarp();
+            warp_sort_sel(ws, n);
+            ok = true;
+        } else if (g.ok) {
             GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
                            a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
             ok = threshold_select(k, D, T, ws, gp);
@@ -627,14 +637,14 @@ k_knn_rov(to_rov_args a, int t) {
 }
 
 // one regression system per thread: the intercept at grid query qi of
-// control c (0 where the control has too few points)
+// group c (0 where the group has too few points)
 template <int D>
 __global__ void k_knn_solve(to_rov_args a, int t) {
     const int item = blockIdx.x * blockDim.x + threadIdx.x;
-    if (item >= a.C * a.Q) return;
+    if (item >= a.G * a.Q) return;
     const int c = item / a.Q, qi = item - c * a.Q;
     const size_t blk = (size_t)a.R * D + 2 * (size_t)a.Q;
-    float* yout = a.reg + (size_t)t * a.C * blk + (size_t)c * blk + (size_t)a.R * D;
+    float* yout = a.reg + ((size_t)t * a.G + c) * blk + (size_t)a.R * D;
     const int n = a.npts[c], k = a.kc[c];
     yout[qi] = (n < 3 || k <= 0)
                    ? 0.0f
@@ -679,7 +689,7 @@ to_status launch_knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     TO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_knn_rov<D>,
                                                                kWarps * 32, smem));
     if (per_sm < 1) per_sm = 1;
-    const int items = a.C * a.Q;
+    const int items = a.G * a.Q;
     int grid = (ctx->sm_count > 0 ? ctx->sm_count : 152) * per_sm;
     if (grid > (items + kWarps - 1) / kWarps) grid = (items + kWarps - 1) / kWarps;
     to_prof_begin(ctx, "knn");
@@ -708,7 +718,7 @@ to_status knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     if (d < 2 || d > TO_LSM_MAXD)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "regression dimension %d", d);
     to_prof_begin(ctx, "knn_grid");
-    k_knn_grid<<<a.C, 1024, 0, ctx->stream>>>(a);
+    k_knn_grid<<<a.G, 1024, 0, ctx->stream>>>(a);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     switch (d) {

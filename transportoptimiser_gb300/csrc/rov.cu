@@ -47,20 +47,21 @@ using to_rovd::unit_profit;
 // ---------------------------------------------------------------------------
 __global__ void k_rov_exog(to_rov_args a) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.P) return;
-    const int Y = a.Y, U = a.U, P = a.P;
-    const uint32_t road = (uint32_t)a.road;
+    if (p >= a.PT) return;
+    const int Y = a.Y, U = a.U, P = a.PT;
+    const int r = p / a.P, pl = p - r * a.P;      // road, path within it
+    const uint32_t road = (uint32_t)a.road_ids[r];
     for (int u = 0; u < U; ++u) a.uRes[((size_t)u * (Y + 1)) * P + p] = a.uncert[6 * u];
     for (int t = 0; t < Y; ++t) {
-        float uc = to_uniform1(a.seed, TO_STREAM_CONTROL, road, p, t, 0);
+        float uc = to_uniform1(a.seed, TO_STREAM_CONTROL, road, pl, t, 0);
         int control = (int)(uc * (float)a.C);
         if (control == a.C) control--;
         a.controls[(size_t)t * P + p] = control;
         for (int u = 0; u < U; ++u) {
             const float* up = a.uncert + 6 * u;
-            float uj = to_uniform1(a.seed, TO_STREAM_EX_JUMP, road, p, t, u);
-            float zb = to_normal1(a.seed, TO_STREAM_EX_BROWNIAN, road, p, t, u);
-            float zj = to_normal1(a.seed, TO_STREAM_EX_JUMPSIZE, road, p, t, u);
+            float uj = to_uniform1(a.seed, TO_STREAM_EX_JUMP, road, pl, t, u);
+            float zb = to_normal1(a.seed, TO_STREAM_EX_BROWNIAN, road, pl, t, u);
+            float zj = to_normal1(a.seed, TO_STREAM_EX_JUMPSIZE, road, pl, t, u);
             float jump = (uj < up[5]) ? 1.0f : 0.0f;
             float curr = a.uRes[((size_t)u * (Y + 1) + t) * P + p];
             float brown = zb * up[2];
@@ -257,7 +258,7 @@ k_rov_forward(to_rov_args a) {
 // terminal year (backwardInduction :2375-2463)
 __global__ void k_rov_terminal(to_rov_args a) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.P) return;
+    if (p >= a.PT) return;
     const int t = a.Y - 1, C = a.C, S = a.S;
     float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
     for (int c = 0; c < C; ++c)
@@ -267,33 +268,50 @@ __global__ void k_rov_terminal(to_rov_args a) {
     float best;
     int bc;
     to_rovd::decide_terminal(a, state, best, bc);
-    a.condExp[(size_t)t * a.P + p] = best;
-    a.optCont[(size_t)t * a.P + p] = bc;
-    a.unitProfits[(size_t)t * a.P + p] = prof;
+    a.condExp[(size_t)t * a.PT + p] = best;
+    a.optCont[(size_t)t * a.PT + p] = bc;
+    a.unitProfits[(size_t)t * a.PT + p] = prof;
     for (int s = 0; s < S; ++s)
-        a.adjPops[((size_t)t * S + s) * a.P + p] = state[(C - 1) * S + s];
+        a.adjPops[((size_t)t * S + s) * a.PT + p] = state[(C - 1) * S + s];
 }
 
 // Per year: regression states, stable compaction by the year's random
 // control (allocateXYRegressionData :1012-1069), per-control and global
 // min/max (computeStateMinMax :1073-1148), k, normalised points and the
-// axis values of the regression grid.  Three launches over chunks of
-// kLsmChunk paths: per-chunk counts by control, then the scatter in path
-// order (chunk offset + warp offset + rank in the warp) with min/max
-// folded into order-preserving integer keys, then the finish (totals, k,
-// min/max rules, normalisation) across the grid.
+// axis values of the regression grid.  Points are grouped by (road,
+// control), g = r*C + c.  Launches over chunks of kLsmChunk paths:
+// per-chunk counts by group, then the scatter in path order (earlier
+// chunks of the road + earlier warps + rank among the warp's lanes of the
+// same group) with min/max folded into order-preserving integer keys; then
+// one thread per road for its totals, k, min/max rules and grid axes, and
+// the normalisation across the grid.
 
 constexpr int kLsmChunk = 1024;
+// roads of a batch have at least this many paths, so a chunk touches at
+// most kLsmChunk / kLsmMinPaths + 2 roads
+constexpr int kLsmMinPaths = 128;
+constexpr int kLsmLocal = (kLsmChunk / kLsmMinPaths + 2) * TO_ROV_MAXC;
 
-// the year's regression group of path p: its control when every species'
-// adjusted population clears its threshold (or the control is 0), else -1
+// the year's regression group of path p: (road, control) when every
+// species' adjusted population clears its threshold (or the control is 0),
+// else -1
 __device__ __forceinline__ int lsm_group(const to_rov_args& a, int p, int t) {
-    if (p >= a.P) return -1;
-    const int ctl = a.controls[(size_t)t * a.P + p];
-    if (ctl == 0) return 0;
+    if (p >= a.PT) return -1;
+    const int ctl = a.controls[(size_t)t * a.PT + p];
+    const int g = (p / a.P) * a.C + ctl;
+    if (ctl == 0) return g;
     for (int s = 0; s < a.S; ++s)
         if (adj_pop(a, p, t, s, a.C - 1) < a.params[8 * s + 3]) return -1;
-    return ctl;
+    return g;
+}
+
+// first group of chunk b and how many groups it can hold
+__device__ __forceinline__ void lsm_chunk_groups(const to_rov_args& a, int b, int& g0, int& nloc) {
+    const int p0 = b * kLsmChunk;
+    const int p1 = min(p0 + kLsmChunk, a.PT) - 1;
+    const int r0 = p0 / a.P, r1 = p1 / a.P;
+    g0 = r0 * a.C;
+    nloc = (r1 - r0 + 1) * a.C;
 }
 
 // order-preserving unsigned key of a float (min/max through integer atomics)
@@ -307,42 +325,48 @@ __device__ __forceinline__ float lsm_unkey(unsigned k) {
 }
 
 __global__ void __launch_bounds__(kLsmChunk) k_lsm_count(to_rov_args a, int t) {
-    __shared__ int s_cnt[TO_ROV_MAXC];
-    const int C = a.C, d = a.S + 1, tid = threadIdx.x, lane = tid & 31;
-    if (tid < C) s_cnt[tid] = 0;
+    __shared__ int s_cnt[kLsmLocal];
+    const int d = a.S + 1, tid = threadIdx.x, lane = tid & 31;
+    int g0, nloc;
+    lsm_chunk_groups(a, blockIdx.x, g0, nloc);
+    for (int q = tid; q < nloc; q += blockDim.x) s_cnt[q] = 0;
     if (blockIdx.x == 0)
-        for (int q = tid; q < C * d; q += blockDim.x) {
+        for (int q = tid; q < a.G * d; q += blockDim.x) {
             a.lkey[2 * q] = 0xFFFFFFFFu;
             a.lkey[2 * q + 1] = 0u;
         }
     __syncthreads();
     const int grp = lsm_group(a, blockIdx.x * kLsmChunk + tid, t);
-    for (int c = 0; c < C; ++c) {
-        unsigned m = __ballot_sync(0xffffffffu, grp == c);
-        if (lane == 0 && m) atomicAdd(&s_cnt[c], __popc(m));
-    }
+    const unsigned peers = __match_any_sync(0xffffffffu, grp);
+    if (grp >= 0 && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[grp - g0], __popc(peers));
     __syncthreads();
-    if (tid < C) a.lcnt[(size_t)tid * gridDim.x + blockIdx.x] = s_cnt[tid];
+    for (int q = tid; q < nloc; q += blockDim.x)
+        a.lcnt[(size_t)(g0 + q) * gridDim.x + blockIdx.x] = s_cnt[q];
 }
 
 __global__ void __launch_bounds__(kLsmChunk) k_lsm_scatter(to_rov_args a, int t) {
     const int P = a.P, S = a.S, C = a.C, d = S + 1, nb = gridDim.x;
-    __shared__ int s_off[TO_ROV_MAXC];
-    __shared__ int s_scan[TO_ROV_MAXC][32];
-    __shared__ unsigned s_key[TO_ROV_MAXC][TO_LSM_MAXD][2];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    // chunk offsets: warp c sums the counts of the chunks before this one
-    if (warp < C) {
+    __shared__ int s_off[kLsmLocal];
+    __shared__ int s_scan[kLsmLocal][32];
+    __shared__ unsigned s_key[kLsmLocal][TO_LSM_MAXD][2];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    int g0, nloc;
+    lsm_chunk_groups(a, blockIdx.x, g0, nloc);
+    // chunk offsets: warp q sums group q's counts in the road's earlier chunks
+    for (int q = warp; q < nloc; q += nw) {
+        const int g = g0 + q;
+        const int bfirst = (int)(((size_t)(g / C) * P) / kLsmChunk);
         int acc = 0;
-        for (int b = lane; b < (int)blockIdx.x; b += 32) acc += a.lcnt[(size_t)warp * nb + b];
+        for (int b = bfirst + lane; b < (int)blockIdx.x; b += 32) acc += a.lcnt[(size_t)g * nb + b];
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) s_off[warp] = acc;
+        if (lane == 0) s_off[q] = acc;
     }
-    for (int q = tid; q < C * d; q += blockDim.x) {
+    for (int q = tid; q < nloc * 32; q += blockDim.x) s_scan[q >> 5][q & 31] = 0;
+    for (int q = tid; q < nloc * d; q += blockDim.x) {
         s_key[q / d][q % d][0] = 0xFFFFFFFFu;
         s_key[q / d][q % d][1] = 0u;
     }
-    __syncthreads();                     // keys set before any warp folds into them
+    __syncthreads();                     // zeroed before any warp adds to them
     const int p = blockIdx.x * kLsmChunk + tid;
     const int grp = lsm_group(a, p, t);
     float xv[TO_LSM_MAXD];
@@ -350,115 +374,120 @@ __global__ void __launch_bounds__(kLsmChunk) k_lsm_scatter(to_rov_args a, int t)
         for (int s = 0; s < S; ++s) xv[s] = adj_pop(a, p, t, s, C - 1);
         xv[S] = unit_profit(a, p, t, a.Y + 1, a.Y + 1);
     }
-    int before = 0;
-    for (int c = 0; c < C; ++c) {
-        unsigned m = __ballot_sync(0xffffffffu, grp == c);
-        if (grp == c) before = __popc(m & ((1u << lane) - 1u));
-        if (lane == 0) s_scan[c][warp] = __popc(m);
-        // per-warp min / max of the control's states
-        if (m) {
-            for (int j = 0; j < d; ++j) {
-                float lo = grp == c ? xv[j] : INFINITY, hi = grp == c ? xv[j] : -INFINITY;
-                for (int o = 16; o > 0; o >>= 1) {
-                    lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-                    hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-                }
-                if (lane == 0) {
-                    atomicMin(&s_key[c][j][0], lsm_key(lo));
-                    atomicMax(&s_key[c][j][1], lsm_key(hi));
-                }
+    // lanes of the same group: rank, count and min / max of the states
+    const unsigned peers = __match_any_sync(0xffffffffu, grp);
+    const int before = __popc(peers & ((1u << lane) - 1u));
+    const bool leader = lane == __ffs(peers) - 1;
+    if (grp >= 0) {
+        const int lq = grp - g0;
+        if (leader) s_scan[lq][warp] = __popc(peers);
+        for (int j = 0; j < d; ++j) {
+            const unsigned lo = __reduce_min_sync(peers, lsm_key(xv[j]));
+            const unsigned hi = __reduce_max_sync(peers, lsm_key(xv[j]));
+            if (leader) {
+                atomicMin(&s_key[lq][j][0], lo);
+                atomicMax(&s_key[lq][j][1], hi);
             }
         }
     }
     __syncthreads();
     if (grp >= 0) {
-        int pos = s_off[grp] + before;
-        for (int w = 0; w < warp; ++w) pos += s_scan[grp][w];
-        a.yv[(size_t)grp * P + pos] = a.condExp[(size_t)(t + 1) * P + p];
+        const int lq = grp - g0;
+        int pos = s_off[lq] + before;
+        for (int w = 0; w < warp; ++w) pos += s_scan[lq][w];
+        a.yv[(size_t)grp * P + pos] = a.condExp[(size_t)(t + 1) * a.PT + p];
         for (int j = 0; j < d; ++j) a.xraw[((size_t)grp * d + j) * P + pos] = xv[j];
     }
-    for (int q = tid; q < C * d; q += blockDim.x) {
-        const int c = q / d, j = q % d;
-        if (s_key[c][j][1] != 0u) {      // the chunk holds points of control c
-            atomicMin(&a.lkey[2 * q], s_key[c][j][0]);
-            atomicMax(&a.lkey[2 * q + 1], s_key[c][j][1]);
+    for (int q = tid; q < nloc * d; q += blockDim.x) {
+        const int lq = q / d, j = q % d;
+        if (s_key[lq][j][1] != 0u) {     // the chunk holds points of the group
+            const size_t gq = (size_t)(g0 + lq) * d + j;
+            atomicMin(&a.lkey[2 * gq], s_key[lq][j][0]);
+            atomicMax(&a.lkey[2 * gq + 1], s_key[lq][j][1]);
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_lsm_finish(to_rov_args a, int t, int nb) {
+// one thread per road: group totals, the reference's min/max rules, the
+// road's combined range, k and the regression grid axes
+__global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nr) return;
     const int P = a.P, S = a.S, C = a.C, d = S + 1, R = a.R;
-    __shared__ int s_cnt[TO_ROV_MAXC];
-    __shared__ float s_min[TO_ROV_MAXC + 1][TO_LSM_MAXD], s_max[TO_ROV_MAXC + 1][TO_LSM_MAXD];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (warp < C) {
-        int acc = 0;
-        for (int b = lane; b < nb; b += 32) acc += a.lcnt[(size_t)warp * nb + b];
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) s_cnt[warp] = acc;
+    const int bfirst = (int)(((size_t)r * P) / kLsmChunk);
+    const int blast = (int)(((size_t)r * P + P - 1) / kLsmChunk);
+    int cnt[TO_ROV_MAXC];
+    float mn[TO_ROV_MAXC + 1][TO_LSM_MAXD], mx[TO_ROV_MAXC + 1][TO_LSM_MAXD];
+    for (int c = 0; c < C; ++c) {
+        const size_t g = (size_t)r * C + c;
+        int n = 0;
+        for (int b = bfirst; b <= blast; ++b) n += a.lcnt[g * nb + b];
+        cnt[c] = n;
     }
-    __syncthreads();
-    if (tid == 0) {
-        for (int c = 0; c < C; ++c) {
-            bool own = (c == 0) || (s_cnt[c] > d + 1);
-            for (int j = 0; j < d; ++j) {
-                if (own && s_cnt[c] > 0) {
-                    float lo = lsm_unkey(a.lkey[2 * (c * d + j)]);
-                    float hi = lsm_unkey(a.lkey[2 * (c * d + j) + 1]);
-                    // the reference scans from the first point with
-                    // "if (xmin > x) ... else if (xmax < x)": plain min and
-                    // max, except that a first value of -0/+0 keeps its
-                    // sign when it is the extreme
-                    const float first = a.xraw[((size_t)c * d + j) * P];
-                    if (lo == first) lo = first;
-                    if (hi == first) hi = first;
-                    s_min[c][j] = lo; s_max[c][j] = hi;
-                } else if (own) {
-                    s_min[c][j] = 0.0f; s_max[c][j] = 0.0f;
-                } else {
-                    s_min[c][j] = s_min[0][j]; s_max[c][j] = s_max[0][j];
-                }
-            }
-        }
+    for (int c = 0; c < C; ++c) {
+        const size_t g = (size_t)r * C + c;
+        const bool own = (c == 0) || (cnt[c] > d + 1);
         for (int j = 0; j < d; ++j) {
-            float lo = s_min[0][j], hi = s_max[0][j];
-            for (int c = 1; c < C; ++c) {
-                if (lo > s_min[c][j]) lo = s_min[c][j];
-                if (hi < s_max[c][j]) hi = s_max[c][j];
+            if (own && cnt[c] > 0) {
+                float lo = lsm_unkey(a.lkey[2 * (g * d + j)]);
+                float hi = lsm_unkey(a.lkey[2 * (g * d + j) + 1]);
+                // the reference scans from the first point with
+                // "if (xmin > x) ... else if (xmax < x)": plain min and
+                // max, except that a first value of -0/+0 keeps its sign
+                // when it is the extreme
+                const float first = a.xraw[(g * d + j) * P];
+                if (lo == first) lo = first;
+                if (hi == first) hi = first;
+                mn[c][j] = lo; mx[c][j] = hi;
+            } else if (own) {
+                mn[c][j] = 0.0f; mx[c][j] = 0.0f;
+            } else {
+                mn[c][j] = mn[0][j]; mx[c][j] = mx[0][j];
             }
-            s_min[C][j] = lo; s_max[C][j] = hi;
         }
     }
-    __syncthreads();
-    if (blockIdx.x == 0) {
-        if (tid < d) { a.gmin[tid] = s_min[C][tid]; a.gmax[tid] = s_max[C][tid]; }
-        if (tid < C) {
-            const int n = s_cnt[tid];
-            int k = 0;
-            if (n > 3) {
-                k = (int)((double)a.k_mult * (log((double)n) + 1.0));
-                if (k > n) k = n;
-            }
-            a.npts[tid] = n;
-            a.kc[tid] = k;
+    for (int j = 0; j < d; ++j) {
+        float lo = mn[0][j], hi = mx[0][j];
+        for (int c = 1; c < C; ++c) {
+            if (lo > mn[c][j]) lo = mn[c][j];
+            if (hi < mx[c][j]) hi = mx[c][j];
         }
+        mn[C][j] = lo; mx[C][j] = hi;
+        a.gmin[(size_t)r * d + j] = lo;
+        a.gmax[(size_t)r * d + j] = hi;
+    }
+    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+    for (int c = 0; c < C; ++c) {
+        const size_t g = (size_t)r * C + c;
+        const int n = cnt[c];
+        int k = 0;
+        if (n > 3) {
+            k = (int)((double)a.k_mult * (log((double)n) + 1.0));
+            if (k > n) k = n;
+        }
+        a.npts[g] = n;
+        a.kc[g] = k;
         // axis values of the regression grid (createQueryPoints :1187-1190)
-        const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
-        for (int q = tid; q < C * d * R; q += blockDim.x) {
-            int c = q / (d * R), r = q - c * d * R;
-            int j = r / R, di = r - j * R;
-            a.reg[(size_t)t * C * blk + (size_t)c * blk + (size_t)j * R + di] =
-                to_lsm_query_axis(di, s_min[C][j], s_max[C][j], R);
-        }
+        float* ax = a.reg + ((size_t)t * a.G + g) * blk;
+        for (int j = 0; j < d; ++j)
+            for (int di = 0; di < R; ++di)
+                ax[(size_t)j * R + di] = to_lsm_query_axis(di, mn[C][j], mx[C][j], R);
     }
-    // normalised points (host normalisation, SimulateGPU.cu:4591-4603)
-    const size_t total = (size_t)C * d * P;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + tid; q < total;
+}
+
+// normalised points (host normalisation, SimulateGPU.cu:4591-4603)
+__global__ void __launch_bounds__(256) k_lsm_norm(to_rov_args a) {
+    const int P = a.P, S = a.S, C = a.C, d = S + 1;
+    const size_t total = (size_t)a.G * d * P;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (size_t)gridDim.x * blockDim.x) {
-        const int cj = (int)(q / P), m = (int)(q - (size_t)cj * P);
-        const int c = cj / d, j = cj - c * d;
-        if (m >= s_cnt[c]) continue;
-        a.xn[q] = to_lsm_normalise(a.xraw[q], s_min[C][j], s_max[C][j], j == S, a.scaling);
+        const size_t gj = q / P;
+        const int m = (int)(q - gj * P);
+        const int g = (int)(gj / d), j = (int)(gj - (size_t)g * d);
+        if (m >= a.npts[g]) continue;
+        const size_t r = (size_t)(g / C);
+        a.xn[q] = to_lsm_normalise(a.xraw[q], a.gmin[r * d + j], a.gmax[r * d + j], j == S,
+                                   a.scaling);
     }
 }
 
@@ -469,27 +498,29 @@ namespace {
 // backwardInduction for 0 < t < Y-1 (:2464-2776)
 __global__ void k_rov_backward(to_rov_args a, int t) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= a.P) return;
+    if (p >= a.PT) return;
     const int C = a.C, S = a.S;
     float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
     for (int c = 0; c < C; ++c)
         for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
     for (int s = 0; s < S; ++s)
-        a.adjPops[((size_t)t * S + s) * a.P + p] = state[(C - 1) * S + s];
+        a.adjPops[((size_t)t * S + s) * a.PT + p] = state[(C - 1) * S + s];
     int sy = (a.sem == 0) ? a.Y : a.Y + 1;
     float prof = unit_profit(a, p, t, sy, sy);
     state[S * C] = prof;
-    a.unitProfits[(size_t)t * a.P + p] = prof;
+    a.unitProfits[(size_t)t * a.PT + p] = prof;
     float best;
     int bc;
-    to_rovd::decide_interior(a, t, state, best, bc);
-    a.condExp[(size_t)t * a.P + p] = best;
-    a.optCont[(size_t)t * a.P + p] = bc;
+    to_rovd::decide_interior(a, t, p / a.P, state, best, bc);
+    a.condExp[(size_t)t * a.PT + p] = best;
+    a.optCont[(size_t)t * a.PT + p] = bc;
 }
 
 // firstPeriodInduction (:2210-2330) with FP64 reductions; one CTA.
 __global__ void k_rov_first(to_rov_args a) {
+    // one CTA per road; its paths are base .. base+P-1 of the batch
     const int P = a.P, C = a.C, S = a.S, Y = a.Y;
+    const size_t PT = (size_t)a.PT, base = (size_t)blockIdx.x * P;
     __shared__ double s_sum[TO_ROV_MAXC][32], s_cnt[TO_ROV_MAXC][32];
     __shared__ double s_best;
     __shared__ int s_bc;
@@ -497,8 +528,8 @@ __global__ void k_rov_first(to_rov_args a) {
     double sum[TO_ROV_MAXC], cnt[TO_ROV_MAXC];
     for (int c = 0; c < C; ++c) { sum[c] = 0.0; cnt[c] = 0.0; }
     for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        int c = a.controls[p];
-        sum[c] += (double)a.condExp[(size_t)P + p];
+        int c = a.controls[base + p];
+        sum[c] += (double)a.condExp[PT + base + p];
         cnt[c] += 1.0;
     }
     for (int c = 0; c < C; ++c) {
@@ -512,11 +543,13 @@ __global__ void k_rov_first(to_rov_args a) {
     if (threadIdx.x == 0) {
         float uf = 0.0f, ore = 0.0f;
         for (int f = 0; f < a.nF; ++f)
-            uf = fmaf(a.fuel_costs[f], a.uRes[((size_t)a.fuel_idx[f] * (Y + 1)) * P], uf);
+            uf = fmaf(a.fuel_costs[f], a.uRes[((size_t)a.fuel_idx[f] * (Y + 1)) * PT + base], uf);
         for (int c = 0; c < a.Cm; ++c)
-            ore = fmaf(ore_at(a, 0, 0, c), a.uRes[((size_t)(a.nF + c) * (Y + 1)) * P], ore);
+            ore = fmaf(ore_at(a, (int)base, 0, c),
+                       a.uRes[((size_t)(a.nF + c) * (Y + 1)) * PT + base], ore);
         float prof0 = (a.unit_cost + uf) - a.unit_revenue * ore;
-        if (a.demand_idx >= 0) prof0 = prof0 * a.uRes[((size_t)a.demand_idx * (Y + 1)) * P];
+        if (a.demand_idx >= 0)
+            prof0 = prof0 * a.uRes[((size_t)a.demand_idx * (Y + 1)) * PT + base];
         const double discd = (double)(1.0f + a.rrr * a.dt / 100.0f);
         double pay[TO_ROV_MAXC];
         int stop = C;
@@ -527,8 +560,8 @@ __global__ void k_rov_first(to_rov_args a) {
             else { stop = c; break; }
             bool valid = true;
             for (int s = 0; s < S; ++s) {
-                float adj = a.totalPops[((size_t)s * (Y + 1)) * P] *
-                            a.aars[(((size_t)s * C + c) * Y) * P];
+                float adj = a.totalPops[((size_t)s * (Y + 1)) * PT + base] *
+                            a.aars[(((size_t)s * C + c) * Y) * PT + base];
                 if (adj < threshold(a, s) && c > 0) { valid = false; break; }
             }
             if (valid) {
@@ -549,8 +582,8 @@ __global__ void k_rov_first(to_rov_args a) {
     const int bc = s_bc;
     double ss = 0.0, m1 = 0.0, n1 = 0.0;
     for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        if (a.controls[p] == bc) {
-            double v = (double)a.condExp[(size_t)P + p];
+        if (a.controls[base + p] == bc) {
+            double v = (double)a.condExp[PT + base + p];
             ss += (v - best) * (v - best);
             m1 += v;
             n1 += 1.0;
@@ -571,8 +604,8 @@ __global__ void k_rov_first(to_rov_args a) {
     double mean = N1 > 0.0 ? M1 / N1 : 0.0;
     double vv = 0.0;
     for (int p = threadIdx.x; p < P; p += blockDim.x)
-        if (a.controls[p] == bc) {
-            double v = (double)a.condExp[(size_t)P + p] - mean;
+        if (a.controls[base + p] == bc) {
+            double v = (double)a.condExp[PT + base + p] - mean;
             vv += v * v;
         }
     for (int o = 16; o > 0; o >>= 1) vv += __shfl_xor_sync(0xffffffffu, vv, o);
@@ -580,18 +613,19 @@ __global__ void k_rov_first(to_rov_args a) {
     if (lane == 0) s_sum[2 % TO_ROV_MAXC][warp] = vv;
     __syncthreads();
     for (int p = threadIdx.x; p < P; p += blockDim.x) {
-        a.condExp[p] = (float)best;
-        a.optCont[p] = bc;
+        a.condExp[base + p] = (float)best;
+        a.optCont[base + p] = bc;
     }
     if (threadIdx.x == 0) {
         double V = 0.0;
         for (int w = 0; w < nw; ++w) V += s_sum[2 % TO_ROV_MAXC][w];
         double sdfac = (a.sem == 0) ? (1.0 + (double)a.rrr / (100.0 * (double)a.dt)) : discd;
-        a.stats[0] = (double)(float)best;
-        a.stats[1] = (double)bc;
-        a.stats[2] = (N1 > 0.0) ? sqrt(SS / (N1 * sdfac)) : 0.0;
-        a.stats[3] = (N1 > 1.0) ? sqrt(V / (N1 - 1.0)) / sqrt(N1) / discd : 0.0;
-        a.stats[4] = N1;
+        double* st = a.stats + 5 * (size_t)blockIdx.x;
+        st[0] = (double)(float)best;
+        st[1] = (double)bc;
+        st[2] = (N1 > 0.0) ? sqrt(SS / (N1 * sdfac)) : 0.0;
+        st[3] = (N1 > 1.0) ? sqrt(V / (N1 - 1.0)) / sqrt(N1) / discd : 0.0;
+        st[4] = N1;
     }
 }
 
@@ -603,7 +637,7 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
                        const to_csc* csc);
 
 to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
-    const int P = a.P;
+    const int P = a.PT;                        // every path of the batch
     const int tpb = 128;
     const int pblocks = (P + tpb - 1) / tpb;
     to_prof_begin(ctx, "rov_exog");
@@ -614,6 +648,8 @@ to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
         TO_TRY(rov_forward_sparse(ctx, a, *csc));
         return rov_backward(ctx, a, pblocks, tpb, csc);
     }
+    if (a.nr != 1)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "batched roads need the sparse migration form");
     // forward tile shape
     const int NE = a.ne, KG = NE / 4;
     int pgroups = 256 / KG;
@@ -651,13 +687,13 @@ to_status rov_run(to_ctx ctx, to_rov_args a, const to_csc* csc) {
 
 to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
                        const to_csc* csc) {
-    if (a.algo == 6 && (!csc || !a.popsY || !a.gmY))
-        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "ALGO6 needs the sparse forward pass");
+    if (a.algo == 6 && (!csc || !a.popsY || !a.gmY || a.nr != 1))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "ALGO6 needs the sparse forward pass, one road");
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
-    if (a.lblocks != (a.P + kLsmChunk - 1) / kLsmChunk)
+    if (a.lblocks != (a.PT + kLsmChunk - 1) / kLsmChunk || (a.nr > 1 && a.P < kLsmMinPaths))
         return to_set_error(ctx, TO_ERR_INVALID, "regression chunks %d", a.lblocks);
-    int fblocks = (int)(((size_t)a.C * (a.S + 1) * a.P + 255) / 256);
+    int fblocks = (int)(((size_t)a.G * (a.S + 1) * a.P + 255) / 256);
     if (fblocks > 4 * 152) fblocks = 4 * 152;
     for (int t = a.Y - 2; t > 0; --t) {
         to_prof_begin(ctx, "lsm_prepare");
@@ -665,7 +701,9 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
         TO_LAUNCHED(ctx);
         k_lsm_scatter<<<a.lblocks, kLsmChunk, 0, ctx->stream>>>(a, t);
         TO_LAUNCHED(ctx);
-        k_lsm_finish<<<fblocks, 256, 0, ctx->stream>>>(a, t, a.lblocks);
+        k_lsm_stats<<<(a.nr + 127) / 128, 128, 0, ctx->stream>>>(a, t, a.lblocks);
+        TO_LAUNCHED(ctx);
+        k_lsm_norm<<<fblocks, 256, 0, ctx->stream>>>(a);
         to_prof_end(ctx);
         TO_LAUNCHED(ctx);
         TO_TRY(knn_rov(ctx, a, t));      // kNN and the local linear regressions
@@ -677,7 +715,7 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
         // re-simulated from year t under the regression-optimal controls
         if (a.algo == 6) TO_TRY(rov_resim_sparse(ctx, a, *csc, t));
     }
-    k_rov_first<<<1, 1024, 0, ctx->stream>>>(a);
+    k_rov_first<<<a.nr, 1024, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }

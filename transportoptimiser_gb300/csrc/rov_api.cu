@@ -31,12 +31,20 @@ int k_rule(int n) {
 extern "C" {
 
 to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* res) {
-    if (!ctx || !pr || !res || pr->n_species <= 0 || pr->n_paths <= 0 ||
+    return to_simulate_rov_batch(ctx, 1, pr, res);
+}
+
+to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* prs,
+                                to_rov_result* results) {
+    if (!ctx || !prs || !results || n_roads <= 0) return TO_ERR_INVALID;
+    const to_rov_problem* pr = &prs[0];
+    if (pr->n_species <= 0 || pr->n_paths <= 0 ||
         pr->n_years < 3 || pr->n_controls <= 0 || pr->n_controls > TO_ROV_MAXC ||
         pr->dim_res < 2 || !pr->species || !pr->flows || pr->n_uncertainties < 0 ||
         (pr->n_uncertainties > 0 && !pr->uncert) || pr->n_fuels < 0 ||
         pr->n_commodities < 0 || pr->n_fuels + pr->n_commodities > pr->n_uncertainties)
         return TO_ERR_INVALID;
+    const int NR = n_roads;
     const int S = pr->n_species, P = pr->n_paths, Y = pr->n_years, C = pr->n_controls;
     const int U = pr->n_uncertainties, R = pr->dim_res, d = S + 1;
     if (d > TO_LSM_MAXD) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d species", S);
@@ -49,6 +57,34 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
                       pr->migration == TO_MIG_TC_3XTF32))
         return to_set_error(ctx, TO_ERR_UNSUPPORTED,
                             "ALGO6 is built for sem 1 with the sparse migration form");
+    if (NR > 1) {
+        // one batch: the same dimensions, processes, costs and seed; each
+        // road brings its own species models and road id
+        if (pr->sem != 1 || algo != 4 || P < 128 || pr->migration == TO_MIG_SIMT_FP32 ||
+            pr->migration == TO_MIG_TC_3XTF32)
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                                "batched roads: sem 1, ALGO4, sparse migration, >= 128 paths");
+        for (int r = 1; r < NR; ++r) {
+            const to_rov_problem& q = prs[r];
+            bool same = q.n_species == S && q.n_paths == P && q.n_years == Y &&
+                        q.n_controls == C && q.dim_res == R && q.n_uncertainties == U &&
+                        q.n_fuels == pr->n_fuels && q.n_commodities == pr->n_commodities &&
+                        q.unit_cost == pr->unit_cost && q.unit_revenue == pr->unit_revenue &&
+                        q.dt == pr->dt && q.rrr == pr->rrr && q.demand_idx == pr->demand_idx &&
+                        q.seed == pr->seed && q.sem == pr->sem && q.migration == pr->migration &&
+                        (q.algo == 0 ? 4 : q.algo) == algo && q.species && q.flows;
+            for (int c = 0; same && c < C; ++c) same = q.flows[c] == pr->flows[c];
+            for (int i = 0; same && i < 6 * U; ++i) same = q.uncert[i] == pr->uncert[i];
+            for (int f = 0; same && f < pr->n_fuels; ++f)
+                same = q.fuel_costs[f] == pr->fuel_costs[f] && q.fuel_idx[f] == pr->fuel_idx[f];
+            for (int c = 0; same && c < pr->n_commodities; ++c)
+                same = q.ore_content[c] == pr->ore_content[c] && q.ore_sd[c] == pr->ore_sd[c];
+            for (int s = 0; same && s < S; ++s)
+                for (int k = 0; same && k < 8; ++k)
+                    same = q.species[s].params && q.species[s].params[k] == pr->species[s].params[k];
+            if (!same) return to_set_error(ctx, TO_ERR_INVALID, "road %d differs from road 0", r);
+        }
+    }
     if (pr->demand_idx >= U) return TO_ERR_INVALID;
     for (int f = 0; f < pr->n_fuels; ++f)
         if (pr->fuel_idx[f] < 0 || pr->fuel_idx[f] >= U) return TO_ERR_INVALID;
@@ -56,65 +92,77 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     for (int j = 0; j < d; ++j) Ql *= R;
     if (Ql > (1L << 22)) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "grid %ld", Ql);
     const int Q = (int)Ql;
+    const long PTl = (long)NR * P;
+    if (PTl > (1L << 30)) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%ld paths", PTl);
+    const int PT = (int)PTl, G = NR * C, RS = NR * S;
     cudaSetDevice(ctx->device);
     int maxN = 0;
-    for (int s = 0; s < S; ++s) {
-        const to_rov_species& sp = pr->species[s];
-        if (sp.n_patches <= 0 || !sp.params || !sp.init_pops || !sp.caps || !sp.mmm)
-            return TO_ERR_INVALID;
-        maxN = sp.n_patches > maxN ? sp.n_patches : maxN;
-        for (int k = 0; k < sp.n_patches; ++k)
-            if (!std::isfinite(sp.init_pops[k]) || !(sp.caps[k] > 0.0f) ||
-                !std::isfinite(sp.caps[k]))
-                return to_set_error(ctx, TO_ERR_NONFINITE, "species %d patch %d", s, k);
-    }
+    for (int r = 0; r < NR; ++r)
+        for (int s = 0; s < S; ++s) {
+            const to_rov_species& sp = prs[r].species[s];
+            if (sp.n_patches <= 0 || !sp.params || !sp.init_pops || !sp.caps || !sp.mmm)
+                return TO_ERR_INVALID;
+            maxN = sp.n_patches > maxN ? sp.n_patches : maxN;
+            for (int k = 0; k < sp.n_patches; ++k)
+                if (!std::isfinite(sp.init_pops[k]) || !(sp.caps[k] > 0.0f) ||
+                    !std::isfinite(sp.caps[k]))
+                    return to_set_error(ctx, TO_ERR_NONFINITE, "road %d species %d patch %d",
+                                        r, s, k);
+        }
     for (int i = 0; i < 6 * U; ++i)
         if (!std::isfinite(pr->uncert[i])) return to_set_error(ctx, TO_ERR_NONFINITE, "uncert %d", i);
     const int NP = (maxN + 3) & ~3;
     if (NP > 1020) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d patches", maxN);
-    std::vector<float> mmm((size_t)S * C * NP * NP, 0.0f), ip((size_t)S * NP, 0.0f),
-        cp((size_t)S * NP, 1.0f), prm((size_t)S * 8);
-    std::vector<int> np(S);
-    for (int s = 0; s < S; ++s) {
-        const to_rov_species& sp = pr->species[s];
-        int N = sp.n_patches;
-        np[s] = N;
-        for (int k = 0; k < N; ++k) { ip[(size_t)s * NP + k] = sp.init_pops[k]; cp[(size_t)s * NP + k] = sp.caps[k]; }
-        for (int c = 0; c < C; ++c)
-            for (int k = 0; k < N; ++k)
-                for (int l = 0; l < N; ++l)
-                    mmm[(((size_t)s * C + c) * NP + k) * NP + l] = sp.mmm[((size_t)c * N + k) * N + l];
-        for (int q = 0; q < 8; ++q) prm[(size_t)s * 8 + q] = sp.params[q];
+    std::vector<float> mmm((size_t)RS * C * NP * NP, 0.0f), ip((size_t)RS * NP, 0.0f),
+        cp((size_t)RS * NP, 1.0f), prm((size_t)S * 8);
+    std::vector<int> np(RS), rid(NR);
+    for (int r = 0; r < NR; ++r) {
+        rid[r] = prs[r].road;
+        for (int s = 0; s < S; ++s) {
+            const to_rov_species& sp = prs[r].species[s];
+            const size_t rs = (size_t)r * S + s;
+            int N = sp.n_patches;
+            np[rs] = N;
+            for (int k = 0; k < N; ++k) { ip[rs * NP + k] = sp.init_pops[k]; cp[rs * NP + k] = sp.caps[k]; }
+            for (int c = 0; c < C; ++c)
+                for (int k = 0; k < N; ++k)
+                    for (int l = 0; l < N; ++l)
+                        mmm[((rs * C + c) * NP + k) * NP + l] = sp.mmm[((size_t)c * N + k) * N + l];
+        }
     }
+    for (int s = 0; s < S; ++s)
+        for (int q = 0; q < 8; ++q) prm[(size_t)s * 8 + q] = pr->species[s].params[q];
     const int kmax = k_rule(P) > 0 ? k_rule(P) : 1;
     if (kmax > TO_KNN_KMAX) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d", kmax);
     const size_t blk = (size_t)R * d + 2 * (size_t)Q;
+    const int lblocks = (PT + 1023) / 1024;
+    const size_t nacc = (size_t)(d + 1) * (d + 2);
+    const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
     size_t bytes = 0;
     auto acc = [&](size_t b) { bytes += to_align256(b); };
-    acc(mmm.size() * 4); acc(ip.size() * 4); acc(cp.size() * 4); acc(prm.size() * 4); acc(S * 4);
+    acc(mmm.size() * 4); acc(ip.size() * 4); acc(cp.size() * 4); acc(prm.size() * 4); acc(RS * 4);
+    acc(NR * 4);
     acc(C * 4); acc(6 * (size_t)(U > 0 ? U : 1) * 4); acc(16 * 4); acc(16 * 4); acc(16 * 4); acc(16 * 4);
-    acc((size_t)Y * P * 4); acc((size_t)(U > 0 ? U : 1) * (Y + 1) * P * 4);
-    acc((size_t)S * (Y + 1) * P * 4); acc((size_t)S * C * Y * P * 4);
-    acc((size_t)C * d * P * 4); acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
-    acc(C * 4); acc(C * 4); acc(d * 4); acc(d * 4);
-    acc((size_t)C * d * P * 4); acc((size_t)C * P * 4);
-    acc((size_t)C * (TO_KNN_GCELLS + 1) * 4); acc((size_t)C * sizeof(to_knn_grid));
-    acc((size_t)C * Q * 4);
-    const int lblocks = (P + 1023) / 1024;
-    acc((size_t)C * lblocks * 4); acc((size_t)C * d * 2 * 4);
-    const size_t nacc = (size_t)(d + 1) * (d + 2);
-    acc(4); acc((size_t)C * Q * nacc * 4);
-    acc((size_t)Y * C * blk * 4); acc((size_t)Y * P * 4); acc((size_t)Y * P * 4);
-    acc((size_t)Y * P * 4); acc((size_t)Y * S * P * 4); acc(5 * 8);
-    const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
-    acc((size_t)S * C * (NP + 1) * 4); acc((size_t)S * C * cap * 2); acc((size_t)S * C * cap * 4);
-    acc((size_t)S * C * 4);
+    acc((size_t)Y * PT * 4); acc((size_t)(U > 0 ? U : 1) * (Y + 1) * PT * 4);
+    acc((size_t)S * (Y + 1) * PT * 4); acc((size_t)S * C * Y * PT * 4);
+    acc((size_t)G * d * P * 4); acc((size_t)G * d * P * 4); acc((size_t)G * P * 4);
+    acc(G * 4); acc(G * 4); acc((size_t)NR * d * 4); acc((size_t)NR * d * 4);
+    acc((size_t)G * d * P * 4); acc((size_t)G * P * 4);
+    acc((size_t)G * (TO_KNN_GCELLS + 1) * 4); acc((size_t)G * sizeof(to_knn_grid));
+    acc((size_t)G * Q * 4);
+    acc((size_t)G * lblocks * 4); acc((size_t)G * d * 2 * 4);
+    acc(4); acc((size_t)G * Q * nacc * 4);
+    acc((size_t)Y * G * blk * 4); acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4);
+    acc((size_t)Y * PT * 4); acc((size_t)Y * S * PT * 4); acc((size_t)NR * 5 * 8);
+    acc((size_t)RS * C * (NP + 1) * 4); acc((size_t)RS * C * cap * 2); acc((size_t)RS * C * cap * 4);
+    acc((size_t)RS * C * 4);
     if (algo == 6) { acc((size_t)Y * S * NP * P * 4); acc((size_t)Y * S * P * 4); }
     TO_TRY(to_arena_reserve(ctx, bytes + 4096));
     TO_CUDA(ctx, cudaMemsetAsync(ctx->arena, 0, bytes, ctx->stream));
     to_rov_args a;
     memset(&a, 0, sizeof(a));
     a.P = P; a.Y = Y; a.S = S; a.C = C; a.U = U; a.R = R; a.Q = Q;
+    a.nr = NR; a.PT = PT; a.G = G;
     a.nF = pr->n_fuels; a.Cm = pr->n_commodities; a.demand_idx = pr->demand_idx;
     a.sem = pr->sem; a.road = pr->road; a.dt = pr->dt; a.rrr = pr->rrr;
     a.unit_cost = pr->unit_cost; a.unit_revenue = pr->unit_revenue; a.scaling = 2.0f;
@@ -124,7 +172,8 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     float* d_ip = to_arena_take<float>(ctx, ip.size());
     float* d_cp = to_arena_take<float>(ctx, cp.size());
     float* d_prm = to_arena_take<float>(ctx, prm.size());
-    int* d_np = to_arena_take<int>(ctx, S);
+    int* d_np = to_arena_take<int>(ctx, RS);
+    int* d_rid = to_arena_take<int>(ctx, NR);
     float* d_flows = to_arena_take<float>(ctx, C);
     float* d_unc = to_arena_take<float>(ctx, 6 * (size_t)(U > 0 ? U : 1));
     float* d_fc = to_arena_take<float>(ctx, 16);
@@ -132,50 +181,51 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     float* d_oc = to_arena_take<float>(ctx, 16);
     float* d_os = to_arena_take<float>(ctx, 16);
     if (pr->n_fuels > 16 || pr->n_commodities > 16) return TO_ERR_UNSUPPORTED;
-    a.controls = to_arena_take<int>(ctx, (size_t)Y * P);
-    a.uRes = to_arena_take<float>(ctx, (size_t)(U > 0 ? U : 1) * (Y + 1) * P);
-    a.totalPops = to_arena_take<float>(ctx, (size_t)S * (Y + 1) * P);
-    a.aars = to_arena_take<float>(ctx, (size_t)S * C * Y * P);
-    a.xraw = to_arena_take<float>(ctx, (size_t)C * d * P);
-    a.xn = to_arena_take<float>(ctx, (size_t)C * d * P);
-    a.yv = to_arena_take<float>(ctx, (size_t)C * P);
-    a.npts = to_arena_take<int>(ctx, C);
-    a.kc = to_arena_take<int>(ctx, C);
-    a.gmin = to_arena_take<float>(ctx, d);
-    a.gmax = to_arena_take<float>(ctx, d);
-    a.gsx = to_arena_take<float>(ctx, (size_t)C * d * P);
-    a.gsi = to_arena_take<int>(ctx, (size_t)C * P);
-    a.gcell = to_arena_take<int>(ctx, (size_t)C * (TO_KNN_GCELLS + 1));
-    a.ggrid = to_arena_take<to_knn_grid>(ctx, C);
-    a.kth = to_arena_take<float>(ctx, (size_t)C * Q);
-    a.lcnt = to_arena_take<int>(ctx, (size_t)C * lblocks);
-    a.lkey = to_arena_take<unsigned>(ctx, (size_t)C * d * 2);
+    a.controls = to_arena_take<int>(ctx, (size_t)Y * PT);
+    a.uRes = to_arena_take<float>(ctx, (size_t)(U > 0 ? U : 1) * (Y + 1) * PT);
+    a.totalPops = to_arena_take<float>(ctx, (size_t)S * (Y + 1) * PT);
+    a.aars = to_arena_take<float>(ctx, (size_t)S * C * Y * PT);
+    a.xraw = to_arena_take<float>(ctx, (size_t)G * d * P);
+    a.xn = to_arena_take<float>(ctx, (size_t)G * d * P);
+    a.yv = to_arena_take<float>(ctx, (size_t)G * P);
+    a.npts = to_arena_take<int>(ctx, G);
+    a.kc = to_arena_take<int>(ctx, G);
+    a.gmin = to_arena_take<float>(ctx, (size_t)NR * d);
+    a.gmax = to_arena_take<float>(ctx, (size_t)NR * d);
+    a.gsx = to_arena_take<float>(ctx, (size_t)G * d * P);
+    a.gsi = to_arena_take<int>(ctx, (size_t)G * P);
+    a.gcell = to_arena_take<int>(ctx, (size_t)G * (TO_KNN_GCELLS + 1));
+    a.ggrid = to_arena_take<to_knn_grid>(ctx, G);
+    a.kth = to_arena_take<float>(ctx, (size_t)G * Q);
+    a.lcnt = to_arena_take<int>(ctx, (size_t)G * lblocks);
+    a.lkey = to_arena_take<unsigned>(ctx, (size_t)G * d * 2);
     a.lblocks = lblocks;
+    a.knn_next = to_arena_take<int>(ctx, 1);
+    a.knn_acc = to_arena_take<float>(ctx, (size_t)G * Q * nacc);
+    a.reg = to_arena_take<float>(ctx, (size_t)Y * G * blk);
+    a.condExp = to_arena_take<float>(ctx, (size_t)Y * PT);
+    a.optCont = to_arena_take<int>(ctx, (size_t)Y * PT);
+    a.unitProfits = to_arena_take<float>(ctx, (size_t)Y * PT);
+    a.adjPops = to_arena_take<float>(ctx, (size_t)Y * S * PT);
+    a.stats = to_arena_take<double>(ctx, (size_t)NR * 5);
+    to_csc csc;
+    csc.ptr = to_arena_take<int>(ctx, (size_t)RS * C * (NP + 1));
+    csc.idx = to_arena_take<uint16_t>(ctx, (size_t)RS * C * cap);
+    csc.val = to_arena_take<float>(ctx, (size_t)RS * C * cap);
+    csc.nnz = to_arena_take<int>(ctx, (size_t)RS * C);
+    csc.cap = cap;
+    csc.cap_smem = 0;
     if (algo == 6) {
         a.popsY = to_arena_take<float>(ctx, (size_t)Y * S * NP * P);
         a.gmY = to_arena_take<float>(ctx, (size_t)Y * S * P);
     }
-    a.knn_next = to_arena_take<int>(ctx, 1);
-    a.knn_acc = to_arena_take<float>(ctx, (size_t)C * Q * nacc);
-    a.reg = to_arena_take<float>(ctx, (size_t)Y * C * blk);
-    a.condExp = to_arena_take<float>(ctx, (size_t)Y * P);
-    a.optCont = to_arena_take<int>(ctx, (size_t)Y * P);
-    a.unitProfits = to_arena_take<float>(ctx, (size_t)Y * P);
-    a.adjPops = to_arena_take<float>(ctx, (size_t)Y * S * P);
-    a.stats = to_arena_take<double>(ctx, 5);
-    to_csc csc;
-    csc.ptr = to_arena_take<int>(ctx, (size_t)S * C * (NP + 1));
-    csc.idx = to_arena_take<uint16_t>(ctx, (size_t)S * C * cap);
-    csc.val = to_arena_take<float>(ctx, (size_t)S * C * cap);
-    csc.nnz = to_arena_take<int>(ctx, (size_t)S * C);
-    csc.cap = cap;
-    csc.cap_smem = 0;
-    if (!a.stats) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
+    if (!csc.nnz || (algo == 6 && !a.gmY)) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
     TO_TRY(up(ctx, d_mmm, mmm.data(), mmm.size()));
     TO_TRY(up(ctx, d_ip, ip.data(), ip.size()));
     TO_TRY(up(ctx, d_cp, cp.data(), cp.size()));
     TO_TRY(up(ctx, d_prm, prm.data(), prm.size()));
     TO_TRY(up(ctx, d_np, np.data(), np.size()));
+    TO_TRY(up(ctx, d_rid, rid.data(), rid.size()));
     TO_TRY(up(ctx, d_flows, pr->flows, C));
     TO_TRY(up(ctx, d_unc, pr->uncert, 6 * (size_t)U));
     TO_TRY(up(ctx, d_fc, pr->fuel_costs, pr->n_fuels));
@@ -184,11 +234,11 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
     TO_TRY(up(ctx, d_os, pr->ore_sd, pr->n_commodities));
     a.n_patches = d_np; a.params = d_prm; a.init_pops = d_ip; a.caps = d_cp;
     a.mmm = d_mmm; a.flows = d_flows; a.uncert = d_unc; a.fuel_costs = d_fc;
-    a.fuel_idx = d_fi; a.ore_content = d_oc; a.ore_sd = d_os;
+    a.fuel_idx = d_fi; a.ore_content = d_oc; a.ore_sd = d_os; a.road_ids = d_rid;
     bool sparse = false;
     if (pr->migration == TO_MIG_AUTO || pr->migration == TO_MIG_SPARSE_FP32) {
-        TO_TRY(to_k::pack_csc(ctx, d_mmm, NP, C, d_np, S, csc));
-        std::vector<int> nz((size_t)S * C);
+        TO_TRY(to_k::pack_csc(ctx, d_mmm, NP, C, d_np, RS, csc));
+        std::vector<int> nz((size_t)RS * C);
         TO_CUDA(ctx, cudaMemcpyAsync(nz.data(), csc.nnz, nz.size() * sizeof(int),
                                      cudaMemcpyDeviceToHost, ctx->stream));
         TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -197,33 +247,76 @@ to_status to_simulate_rov(to_ctx ctx, const to_rov_problem* pr, to_rov_result* r
         for (int v : nz) { if (v < 0) ok = false; mx = v > mx ? v : mx; }
         csc.cap_smem = (mx + 7) & ~7;
         sparse = ok && to_k::rov_sparse_smem(NP, C, csc.cap_smem) <= ctx->smem_optin;
-        if (!sparse && (pr->migration == TO_MIG_SPARSE_FP32 || algo == 6))
+        if (!sparse && (pr->migration == TO_MIG_SPARSE_FP32 || algo == 6 || NR > 1))
             return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
     }
     TO_TRY(to_k::rov_run(ctx, a, sparse ? &csc : nullptr));
-    double st[5];
-    TO_TRY(down(ctx, st, a.stats, 5));
+    std::vector<double> st((size_t)NR * 5);
+    TO_TRY(down(ctx, st.data(), a.stats, (size_t)NR * 5));
+    // road-major device arrays -> each road's [Y][P] (or [Y][S][P]) output
     std::vector<float> f;
     std::vector<int> iv;
-    auto fetch_f = [&](double* out, const float* dptr, size_t n) -> to_status {
-        if (!out) return TO_OK;
-        f.resize(n);
-        TO_TRY(down(ctx, f.data(), dptr, n));
+    auto fetch_rows = [&](int which, const float* dptr, size_t rows) -> to_status {
+        bool any = false;
+        for (int r = 0; r < NR; ++r) {
+            double* o = which == 0 ? results[r].cond_exp
+                      : which == 1 ? results[r].unit_profits : results[r].adj_pops;
+            any |= o != nullptr;
+        }
+        if (!any) return TO_OK;
+        f.resize(rows * PT);
+        TO_TRY(down(ctx, f.data(), dptr, rows * PT));
         TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-        for (size_t i = 0; i < n; ++i) out[i] = (double)f[i];
+        for (int r = 0; r < NR; ++r) {
+            double* o = which == 0 ? results[r].cond_exp
+                      : which == 1 ? results[r].unit_profits : results[r].adj_pops;
+            if (!o) continue;
+            for (size_t row = 0; row < rows; ++row)
+                for (int p = 0; p < P; ++p)
+                    o[row * P + p] = (double)f[row * PT + (size_t)r * P + p];
+        }
         return TO_OK;
     };
-    TO_TRY(fetch_f(res->cond_exp, a.condExp, (size_t)Y * P));
-    TO_TRY(fetch_f(res->unit_profits, a.unitProfits, (size_t)Y * P));
-    TO_TRY(fetch_f(res->adj_pops, a.adjPops, (size_t)Y * S * P));
-    TO_TRY(fetch_f(res->regression, a.reg, (size_t)Y * C * blk));
-    if (res->opt_cont) TO_TRY(down(ctx, res->opt_cont, a.optCont, (size_t)Y * P));
+    TO_TRY(fetch_rows(0, a.condExp, (size_t)Y));
+    TO_TRY(fetch_rows(1, a.unitProfits, (size_t)Y));
+    TO_TRY(fetch_rows(2, a.adjPops, (size_t)Y * S));
+    bool want_reg = false, want_oc = false;
+    for (int r = 0; r < NR; ++r) {
+        want_reg |= results[r].regression != nullptr;
+        want_oc |= results[r].opt_cont != nullptr;
+    }
+    if (want_reg) {
+        f.resize((size_t)Y * G * blk);
+        TO_TRY(down(ctx, f.data(), a.reg, (size_t)Y * G * blk));
+        TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int r = 0; r < NR; ++r) {
+            double* o = results[r].regression;
+            if (!o) continue;
+            for (int t = 0; t < Y; ++t)
+                for (size_t q = 0; q < (size_t)C * blk; ++q)
+                    o[((size_t)t * C) * blk + q] = (double)f[((size_t)t * G + (size_t)r * C) * blk + q];
+        }
+    }
+    if (want_oc) {
+        iv.resize((size_t)Y * PT);
+        TO_TRY(down(ctx, iv.data(), a.optCont, (size_t)Y * PT));
+        TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int r = 0; r < NR; ++r) {
+            int* o = results[r].opt_cont;
+            if (!o) continue;
+            for (int t = 0; t < Y; ++t)
+                for (int p = 0; p < P; ++p) o[(size_t)t * P + p] = iv[(size_t)t * PT + (size_t)r * P + p];
+        }
+    }
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    res->value = st[0];
-    res->control = st[1];
-    res->sd = st[2];
-    res->se = st[3];
-    res->n_best = (int)st[4];
+    for (int r = 0; r < NR; ++r) {
+        const double* sr = st.data() + 5 * (size_t)r;
+        results[r].value = sr[0];
+        results[r].control = sr[1];
+        results[r].sd = sr[2];
+        results[r].se = sr[3];
+        results[r].n_best = (int)sr[4];
+    }
     return TO_OK;
 }
 

@@ -250,9 +250,13 @@ template <int CMAX, int MAXG>
 __global__ void __launch_bounds__(1024, 1)
 k_rov_forward_sparse(to_rov_args a, to_csc csc) {
     extern __shared__ unsigned char sm_raw[];
+    // grid (path tiles of a road, roads): lane = path of road blockIdx.y
     const int NE = a.ne, NG = NE >> 2, NP = a.np, C = a.C, Y = a.Y, P = a.P;
+    const size_t PT = (size_t)a.PT;
+    const int rd = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int path = blockIdx.x * kLanes + lane;
+    const size_t gp = (size_t)rd * P + path;                    // path of the batch
     float* cur = reinterpret_cast<float*>(sm_raw);                 // [NE][32]
     float* part = cur + (size_t)NE * kLanes;                       // [C+1][NG][32]
     float* capv = part + (size_t)(C + 1) * NG * kLanes;            // [NE]
@@ -263,21 +267,22 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
     int* cptr = ctl + kLanes;                                      // [C][NE+1]
     float* cval = reinterpret_cast<float*>(cptr + (size_t)C * (NE + 1));  // [C][cap_smem]
     uint16_t* cidx = reinterpret_cast<uint16_t*>(cval + (size_t)C * csc.cap_smem);
-    const uint32_t road = (uint32_t)a.road;
+    const uint32_t road = (uint32_t)a.road_ids[rd];
 
     for (int s = 0; s < a.S; ++s) {
-        const int N = a.n_patches[s];
+        const int rs = rd * a.S + s;
+        const int N = a.n_patches[rs];
         const int N4 = (N + 3) & ~3;
         const float* sp = a.params + 8 * s;
-        const float* ip = a.init_pops + (size_t)s * NP;
+        const float* ip = a.init_pops + (size_t)rs * NP;
         __syncthreads();
         for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
             int k = q / kLanes;
             cur[q] = (k < N) ? ip[k] : 0.0f;
         }
-        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)s * NP + k];
+        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)rs * NP + k];
         for (int c = 0; c < C; ++c) {
-            const int mtx = s * C + c;
+            const int mtx = rs * C + c;
             const int nnz = csc.nnz[mtx];
             for (int k = threadIdx.x; k <= NE; k += blockDim.x)
                 cptr[c * (NE + 1) + k] = csc.ptr[(size_t)mtx * (NP + 1) + (k <= NP ? k : NP)];
@@ -295,7 +300,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
             }
             tot[lane] = tt;
             gm[lane] = sp[0];
-            if (path < P) a.totalPops[((size_t)s * (Y + 1)) * P + path] = tt;
+            if (path < P) a.totalPops[((size_t)s * (Y + 1)) * PT + gp] = tt;
         }
         __syncthreads();
         for (int t = 0; t < Y; ++t) {
@@ -311,7 +316,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 float g = gm[lane];
                 gm[lane] = g + sp[4] * (sp[1] - g) * a.dt + g * brown
                            + (to_expf(jsz) - 1.0f) * g * jump;
-                ctl[lane] = (path < P) ? a.controls[(size_t)t * P + path] : 0;
+                ctl[lane] = (path < P) ? a.controls[(size_t)t * PT + gp] : 0;
                 if (a.gmY && path < P) a.gmY[((size_t)t * a.S + s) * P + path] = gm[lane];
             }
             __syncthreads();
@@ -377,8 +382,8 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
                 for (int grp = 0; grp < NG; ++grp)
                     tt = tt + part[((size_t)c * NG + grp) * kLanes + lane];
                 if (path < P) {
-                    if (c < C) a.aars[(((size_t)s * C + c) * Y + t) * P + path] = tt / tot[lane];
-                    else a.totalPops[((size_t)s * (Y + 1) + t + 1) * P + path] = tt;
+                    if (c < C) a.aars[(((size_t)s * C + c) * Y + t) * PT + gp] = tt / tot[lane];
+                    else a.totalPops[((size_t)s * (Y + 1) + t + 1) * PT + gp] = tt;
                 }
                 if (c == C) ntot[lane] = tt;
             }
@@ -509,7 +514,7 @@ k_rov_resim_sparse(to_rov_args a, to_csc csc, int t0) {
                 state[S * C] = prof;
                 float best;
                 if (u == Y - 1) to_rovd::decide_terminal(a, state, best, bc);
-                else to_rovd::decide_interior(a, u, state, best, bc);
+                else to_rovd::decide_interior(a, u, 0, state, best, bc);
                 val = val + (a.flows[bc] * prof) * df;
                 df = df / disc;
             }
@@ -642,7 +647,7 @@ to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc) {
     int warps = warps_for(a.ne, a.C + 1 > 4 ? a.C + 1 : 4);
     if ((a.ne / 4 + warps - 1) / warps > kMaxG)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", a.ne);
-    const int blocks = (a.P + kLanes - 1) / kLanes;
+    const dim3 blocks((a.P + kLanes - 1) / kLanes, a.nr);
     to_prof_begin(ctx, "rov_forward_sparse");
     if (a.C <= 3) {
         TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_sparse<3, kMaxG>,

@@ -17,19 +17,24 @@ struct to_knn_grid {
     int ok;
 };
 
+// A batch of nr roads with the same dimensions: path arrays are road-major
+// ([..][PT], road r's paths at r*P .. r*P+P-1) and the regressions are
+// grouped by (road, control), group g = r*C + c.
 struct to_rov_args {
-    int P, Y, S, C, U, R, Q;          // paths, years, species, controls, processes, dimRes, R^d
+    int P, Y, S, C, U, R, Q;          // paths per road, years, species, controls, processes, dimRes, R^d
+    int nr, PT, G;                    // roads, paths of all roads (nr*P), groups (nr*C)
+    const int* road_ids;              // [nr] road id of each road (random streams)
     int nF, Cm, demand_idx, sem, road;
     float dt, rrr, unit_cost, unit_revenue, scaling;
     uint64_t seed;
     int np, ne;                       // stride / effective width of patch arrays
     int tile_paths, l_chunk;          // forward tile (launcher)
     // inputs (device)
-    const int* n_patches;             // [S]
+    const int* n_patches;             // [nr][S]
     const float* params;              // [S*8]
-    const float* init_pops;           // [S][np]
-    const float* caps;                // [S][np] (padding 1)
-    const float* mmm;                 // [S][C][np][np] destination-major
+    const float* init_pops;           // [nr][S][np]
+    const float* caps;                // [nr][S][np] (padding 1)
+    const float* mmm;                 // [nr][S][C][np][np] destination-major
     const float* flows;               // [C]
     const float* uncert;              // [U*6]
     const float* fuel_costs;          // [nF]
@@ -37,49 +42,51 @@ struct to_rov_args {
     const float* ore_content;         // [Cm]
     const float* ore_sd;              // [Cm]
     // path state (device)
-    int* controls;                    // [Y][P]
-    float* uRes;                      // [U][Y+1][P]
-    float* totalPops;                 // [S][Y+1][P]
-    float* aars;                      // [S][C][Y][P]
-    // regression scratch (device)
-    float* xraw;                      // [C][d][P] compacted raw states
-    float* xn;                        // [C][d][P] normalised
-    float* yv;                        // [C][P]
-    int* npts;                        // [C]
-    int* kc;                          // [C]
-    float* gmin;                      // [d]
-    float* gmax;                      // [d]
-    float* gsx;                       // [C][d][P] points in cell order
-    int* gsi;                         // [C][P] their original indices
-    int* gcell;                       // [C][TO_KNN_GCELLS + 1] cell starts
-    to_knn_grid* ggrid;               // [C]
-    float* kth;                       // [C][Q] k-th squared distance, year before
-    int* lcnt;                        // [C][lblocks] points per control and path chunk
-    unsigned* lkey;                   // [C][d][2] min / max keys of the states
+    int* controls;                    // [Y][PT]
+    float* uRes;                      // [U][Y+1][PT]
+    float* totalPops;                 // [S][Y+1][PT]
+    float* aars;                      // [S][C][Y][PT]
+    // regression scratch (device), per group g = r*C + c
+    float* xraw;                      // [G][d][P] compacted raw states
+    float* xn;                        // [G][d][P] normalised
+    float* yv;                        // [G][P]
+    int* npts;                        // [G]
+    int* kc;                          // [G]
+    float* gmin;                      // [nr][d]
+    float* gmax;                      // [nr][d]
+    float* gsx;                       // [G][d][P] points in cell order
+    int* gsi;                         // [G][P] their original indices
+    int* gcell;                       // [G][TO_KNN_GCELLS + 1] cell starts
+    to_knn_grid* ggrid;               // [G]
+    float* kth;                       // [G][Q] k-th squared distance, year before
+    int* lcnt;                        // [G][lblocks] points per group and path chunk
+    unsigned* lkey;                   // [G][d][2] min / max keys of the states
     int lblocks;                      // path chunks of the compaction
     int k_mult;                       // k = k_mult (ln n + 1): 10 ALGO4, 3 ALGO6
     int algo;                         // 4 or 6
     float* popsY;                     // ALGO6: [Y][S][ne][P] patch populations, start of year
     float* gmY;                       // ALGO6: [Y][S][P] mean growth rate of the year
     int* knn_next;                    // work counter of the kNN kernel
-    float* knn_acc;                   // [C][Q][(d+1)(d+2)] normal equations per query
+    float* knn_acc;                   // [G][Q][(d+1)(d+2)] normal equations per query
     int kmax;
     // outputs (device)
-    float* reg;                       // [Y][C][R*d + 2Q]
-    float* condExp;                   // [Y][P]
-    int* optCont;                     // [Y][P]
-    float* unitProfits;               // [Y][P]
-    float* adjPops;                   // [Y][S][P]
-    double* stats;                    // [5]: value, control, SD, SE, n
+    float* reg;                       // [Y][G][R*d + 2Q]
+    float* condExp;                   // [Y][PT]
+    int* optCont;                     // [Y][PT]
+    float* unitProfits;               // [Y][PT]
+    float* adjPops;                   // [Y][S][PT]
+    double* stats;                    // [nr][5]: value, control, SD, SE, n
 };
 
 // grid query q of the current year: normalised coordinates (for kNN) and
 // the coordinates the regression centres on (createQueryPoints + host
 // normalisation; sem 0 centres on the unit grid, SimulateGPU.cu:2964-2966)
 template <int D>
-__device__ __forceinline__ void to_rov_query(const to_rov_args& a, int q, float* qn,
+__device__ __forceinline__ void to_rov_query(const to_rov_args& a, int road, int q, float* qn,
                                              float* xq) {
     const int R = a.R;
+    const float* lo = a.gmin + (size_t)road * D;
+    const float* hi = a.gmax + (size_t)road * D;
     int rem = q;
     int div = a.Q / R;
 #pragma unroll
@@ -87,8 +94,8 @@ __device__ __forceinline__ void to_rov_query(const to_rov_args& a, int q, float*
         int di = rem / div;
         rem -= di * div;
         div /= R;
-        float raw = to_lsm_query_axis(di, a.gmin[j], a.gmax[j], R);
-        float nv = to_lsm_normalise(raw, a.gmin[j], a.gmax[j], j == a.S, a.scaling);
+        float raw = to_lsm_query_axis(di, lo[j], hi[j], R);
+        float nv = to_lsm_normalise(raw, lo[j], hi[j], j == a.S, a.scaling);
         qn[j] = nv;
         xq[j] = (a.sem == 0) ? to_lsm_unit_axis(di, R) : nv;
     }

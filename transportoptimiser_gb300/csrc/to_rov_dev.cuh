@@ -11,26 +11,28 @@ namespace to_rovd {
 
 __device__ __forceinline__ float ure(const to_rov_args& a, int p, int t, int u, int stride_y) {
     // value at the reference's flat index (p*stride_y + t)*U + u of its
-    // [P][Y+1][U] array, read from the [U][Y+1][P] layout
+    // [P][Y+1][U] array, read from the [U][Y+1][PT] layout (p: path of the
+    // batch; the stride Y quirk only arises for one road)
     const int U = a.U, Y1 = a.Y + 1;
     long F = ((long)p * stride_y + t) * U + u;
     long per = (long)Y1 * U;
     int pp = (int)(F / per);
     long rem = F - (long)pp * per;
     int tt = (int)(rem / U), uu = (int)(rem - (long)tt * U);
-    return a.uRes[((size_t)uu * Y1 + tt) * a.P + pp];
+    return a.uRes[((size_t)uu * Y1 + tt) * a.PT + pp];
 }
 
 __device__ __forceinline__ float ore_at(const to_rov_args& a, int p, int t, int c) {
+    const int r = p / a.P, pl = p - r * a.P;      // road, path within it
     long f, gen;
     if (a.sem == 0) {
-        f = ((long)p * a.Y + t) * a.Cm + c;
+        f = ((long)pl * a.Y + t) * a.Cm + c;
         gen = f / ((long)a.Y * a.P);
     } else {
         gen = c;
-        f = (long)c * a.Y * a.P + (long)p * a.Y + t;
+        f = (long)c * a.Y * a.P + (long)pl * a.Y + t;
     }
-    float z = to_normal1(a.seed, TO_STREAM_ORE, (uint32_t)a.road, (uint32_t)(f >> 2), 0,
+    float z = to_normal1(a.seed, TO_STREAM_ORE, (uint32_t)a.road_ids[r], (uint32_t)(f >> 2), 0,
                          (uint32_t)(f & 3));
     return a.ore_content[gen] + a.ore_sd[gen] * z;
 }
@@ -44,13 +46,13 @@ __device__ __forceinline__ float unit_profit(const to_rov_args& a, int p, int t,
         ore = fmaf(ore_at(a, p, t, c), ure(a, p, t, a.nF + c, ore_stride_y), ore);
     float prof = (a.unit_cost + uf) - a.unit_revenue * ore;
     if (a.demand_idx >= 0)
-        prof = prof * a.uRes[((size_t)a.demand_idx * (a.Y + 1) + t) * a.P + p];
+        prof = prof * a.uRes[((size_t)a.demand_idx * (a.Y + 1) + t) * a.PT + p];
     return prof;
 }
 
 __device__ __forceinline__ float adj_pop(const to_rov_args& a, int p, int t, int s, int c) {
-    return a.totalPops[((size_t)s * (a.Y + 1) + t) * a.P + p] *
-           a.aars[(((size_t)s * a.C + c) * a.Y + t) * a.P + p];
+    return a.totalPops[((size_t)s * (a.Y + 1) + t) * a.PT + p] *
+           a.aars[(((size_t)s * a.C + c) * a.Y + t) * a.PT + p];
 }
 
 __device__ __forceinline__ float threshold(const to_rov_args& a, int s) {
@@ -81,9 +83,10 @@ __device__ __forceinline__ void decide_terminal(const to_rov_args& a, const floa
 }
 
 // Interior-year decision (backwardInduction :2464-2776): current payoff plus
-// the discounted regression value of year t (capped at zero), least wins.
-__device__ __forceinline__ void decide_interior(const to_rov_args& a, int t, const float* state,
-                                                float& best, int& bc) {
+// the discounted regression value of year t (capped at zero), least wins;
+// road r's regressions.
+__device__ __forceinline__ void decide_interior(const to_rov_args& a, int t, int r,
+                                                const float* state, float& best, int& bc) {
     const int C = a.C, S = a.S, d = S + 1, R = a.R;
     const float disc = 1.0f + a.rrr * a.dt / 100.0f;
     const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
@@ -96,7 +99,7 @@ __device__ __forceinline__ void decide_interior(const to_rov_args& a, int t, con
         float pay = 0.0f;
         if (valid) {
             float cur = a.flows[c] * state[S * C];
-            const float* rb = a.reg + (size_t)t * C * blk + (size_t)c * blk;
+            const float* rb = a.reg + ((size_t)t * a.G + (size_t)r * C + c) * blk;
             float v = (a.sem == 0) ? to_lsm_interp_ref(rb, R, S, C, state)
                                    : to_lsm_interp(rb, R, S, state + c * S, state[S * C]);
             double ce = (double)(v / disc);

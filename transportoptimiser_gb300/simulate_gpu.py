@@ -236,6 +236,47 @@ def simulateROVCUDA(problem: dict, want=("cond_exp", "opt_cont", "unit_profits",
     return out
 
 
+def simulateROVCUDA_batch(problems, want=("cond_exp", "opt_cont", "regression"),
+                          migration=_capi.MIG_AUTO, ctx: Context | None = None) -> list:
+    """Several roads valued in one batch (to_simulate_rov_batch): problems
+    with the same dimensions, processes, costs, seed and species parameters,
+    each with its own species models and road id.  Returns one dict per road,
+    as simulateROVCUDA does."""
+    ctx = ctx or context()
+    n = len(problems)
+    prs = (_capi.RovProblem * n)()
+    ress = (_capi.RovResult * n)()
+    keep, outs = [], []
+    for i, problem in enumerate(problems):
+        S = len(problem["species"])
+        P, Y, R = problem["n_paths"], problem["n_years"], problem["dim_res"]
+        Cn = len(problem["flows"])
+        pr, k = rov_ctypes(problem, migration)
+        keep.append(k)
+        prs[i] = pr
+        d = S + 1
+        out = {}
+        if "cond_exp" in want: out["cond_exp"] = np.zeros(Y * P)
+        if "opt_cont" in want: out["opt_cont"] = np.zeros(Y * P, np.int32)
+        if "unit_profits" in want: out["unit_profits"] = np.zeros(Y * P)
+        if "adj_pops" in want: out["adj_pops"] = np.zeros(Y * S * P)
+        if "regression" in want: out["regression"] = np.zeros(Y * Cn * (R * d + 2 * R ** d))
+        r = ress[i]
+        r.cond_exp = ptr(out.get("cond_exp"), C.c_double)
+        r.opt_cont = ptr(out.get("opt_cont"), C.c_int)
+        r.unit_profits = ptr(out.get("unit_profits"), C.c_double)
+        r.adj_pops = ptr(out.get("adj_pops"), C.c_double)
+        r.regression = ptr(out.get("regression"), C.c_double)
+        outs.append(out)
+    ctx.check(ctx.lib.to_simulate_rov_batch(ctx.handle, n, prs, ress), "to_simulate_rov_batch")
+    for i, out in enumerate(outs):
+        r = ress[i]
+        out["stats"] = np.array([r.value, r.control, r.sd])
+        out["value_se"] = r.se
+        out["n_best"] = r.n_best
+    return outs
+
+
 def knn(ref_pts: np.ndarray, query: np.ndarray, k: int, ctx: Context | None = None):
     """knn_cuda_with_indexes::knn: ref (dim x n), query (dim x Q), dim-major.
     Returns dist, ind (k x Q, ind 1-based)."""
