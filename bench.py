@@ -293,6 +293,52 @@ def rov_adjoint_leg(ctx, rov_paths=10000, adj_paths=20000, reps=3):
     return {"rov": rov, "adjoint": adj}
 
 
+def rov_generation_leg(ctx, n_roads=256, reps=3, plain_roads=16):
+    """ROV valuation of a GA generation of roads in one batch
+    (to_simulate_rov_batch) at N* paths per road from a 512-path pilot, next
+    to one road per call (the reference's way)."""
+    import numpy as np
+    from transportoptimiser_gb300 import synth
+    from transportoptimiser_gb300 import simulate_gpu as sg
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    sc = synth.rov_road(0, n_species=2)
+    rng = np.random.Generator(np.random.Philox(11))
+    roads = [sc.roads[0]] + [synth.random_road(sc.W, sc.H, int(rng.integers(8, 65)), rng)
+                             for _ in range(n_roads - 1)]
+    models = []
+    for rd in roads:
+        hab = sc.hab_map(rd)
+        models.append([sg.createSpeciesModel(hab, sc.pop_map(sp, hab), sc.W, sc.H, sc.res,
+                                             sp.habitats, rd.colmajor(), rd.G, sp.hazard,
+                                             sp.lambda_mean, sem=1, max_patches=512, ctx=ctx)
+                       for sp in sc.species])
+
+    def problems(P):
+        return [rov_problem_from_models(m, sc, n_paths=P, n_years=YEARS, dim_res=16, sem=1,
+                                        n_processes=3, demand=True, road=i)
+                for i, m in enumerate(models)]
+    pilot = sg.simulateROVCUDA_batch(problems(512), want=(), ctx=ctx)
+    need = max((o["value_se"] * math.sqrt(512) / (0.01 * abs(o["stats"][0]))) ** 2
+               for o in pilot if o["stats"][0] != 0.0)
+    P = int(min(max(128, math.ceil(need / 128.0) * 128), 4096))
+    probs = problems(P)
+    sg.simulateROVCUDA_batch(probs, want=(), ctx=ctx)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        sg.simulateROVCUDA_batch(probs, want=(), ctx=ctx)
+        ts.append(time.perf_counter() - t0)
+    tb = statistics.median(ts)
+    t0 = time.perf_counter()
+    for p in probs[:plain_roads]:
+        sg.simulateROVCUDA(p, want=(), ctx=ctx)
+    t1 = (time.perf_counter() - t0) / plain_roads
+    return {"roads": n_roads, "paths_per_road": P, "pilot_paths": 512, "years": YEARS,
+            "batch_ms": 1000.0 * tb, "designs_per_s": n_roads / tb,
+            "plain_ms_per_road": 1000.0 * t1, "plain_designs_per_s": 1.0 / t1,
+            "note": "2 species, 3 controls, 16^3 regression grid; batch = to_simulate_rov_batch"}
+
+
 def profile_rov(args):
     """One ROV valuation (ALGO4) of a 128 x 128 one-road scene with 2 species on the GPU."""
     from transportoptimiser_gb300 import synth
@@ -482,6 +528,7 @@ def main():
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
 
     rov_adj = rov_adjoint_leg(ctx) if rank == 0 and args.rov_leg else None
+    rov_gen = rov_generation_leg(ctx) if rank == 0 and args.rov_leg else None
 
     surrogate = None
     if rank == 0 and args.surrogate_samples > 0:
@@ -530,6 +577,7 @@ def main():
                          "pack_csc_ms": pk_ms / max(pk_n, 1)},
             "surrogate": surrogate,
             "rov_one_road": rov_adj["rov"] if rov_adj else None,
+            "rov_generation": rov_gen,
             "adjoint": rov_adj["adjoint"] if rov_adj else None,
             "cpu_baseline": cpu,
             "gpu_launches": int(launches),
