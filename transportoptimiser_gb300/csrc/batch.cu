@@ -63,6 +63,7 @@ struct to_gen_s {
     cudaGraphExec_t exec = nullptr;
     uint64_t graph_key = 0;
     int plan_ne = 0, plan_cap = 0, plan_choice = -1;
+    uint64_t graph_launches = 0;         // kernels in the captured generation
 };
 
 namespace {
@@ -301,8 +302,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     for (uint64_t f : fields) key = mix(key, f);
     if (g->exec && g->graph_key == key) {
         TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
-        ctx->launches += 3 + (g->plan_choice == CH_SPARSE ? 1 : 0) +
-                         (g->plan_choice == CH_TC ? 2 : 1) + 2;
+        ctx->launches += g->graph_launches;
         return TO_OK;
     }
     if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
@@ -328,6 +328,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     to_mte_args m = mte_args(ctx, g, o, ne);
     const bool prof = ctx->profile;
     ctx->profile = false;                      // no event records inside the capture
+    const uint64_t l0 = ctx->launches;
     TO_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     to_status st = TO_OK;
     if (!cell_off) {
@@ -350,6 +351,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_CUDA(ctx, ce);
     g->graph_key = key;
     g->plan_ne = ne; g->plan_cap = cap; g->plan_choice = choice;
+    g->graph_launches = ctx->launches - l0;
     return TO_OK;
 }
 

@@ -22,7 +22,7 @@ k_mte_simt(to_mte_args a) {
     extern __shared__ float smem[];
     const int NP = a.npad, NE = a.npe, KG = NE >> 2;
     const int TP = a.tile_paths;
-    const int rs = blockIdx.y;
+    const int rs = a.rs0 + blockIdx.y;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int tid = threadIdx.x;
     const int pg = tid / KG, kg = tid - pg * KG;

@@ -343,7 +343,7 @@ __device__ __forceinline__ bool within(double d2, double md, double md2lo, doubl
 __global__ void __launch_bounds__(1024)
 k_species_patches(to_model_args a) {
     extern __shared__ int smem[];
-    const int rs = blockIdx.x;                 // road*S + species
+    const int rs = a.rs0 + blockIdx.x;         // road*S + species
     const int road = rs / a.S, sp = rs - road * a.S;
     const int W = a.W, H = a.H, n = W * H;
     int* s_tmp = smem;                         // 33 ints
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(1024)
 k_road_labels(to_model_args a) {
     extern __shared__ int smem[];
     const int T = a.n_label_types;
-    const int road = blockIdx.x / T, ti = blockIdx.x - road * T;
+    const int road = a.rs0 / a.S + (int)blockIdx.x / T, ti = (int)blockIdx.x % T;
     const int W = a.W, n = W * a.H;
     int* s_tmp = smem;                         // 33 ints
     int* par = smem + 64;
@@ -429,7 +429,7 @@ k_road_labels(to_model_args a) {
 __global__ void __launch_bounds__(512)
 k_species_patches_lab(to_model_args a) {
     extern __shared__ int smem[];
-    const int rs = blockIdx.x;
+    const int rs = a.rs0 + blockIdx.x;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int W = a.W, H = a.H, n = W * H, T = a.n_label_types;
     int* s_tmp = smem;                         // 33 ints
@@ -487,7 +487,7 @@ __global__ void __launch_bounds__(512, 2)
 k_species_links(to_model_args a) {
     extern __shared__ __align__(16) unsigned char sml[];
     __shared__ int s_last, s_cnt, s_npair;
-    const int rs = blockIdx.x;
+    const int rs = a.rs0 + blockIdx.x;
     const int road = rs / a.S, sp = rs - road * a.S;
     const to_model_species& S = a.species[sp];
     const int NM = a.max_patches;

@@ -36,8 +36,8 @@ constexpr int kLanes = 32;
 __global__ void __launch_bounds__(1024)
 k_pack_csc(const float* __restrict__ mmm, int NP, int C, const int* __restrict__ n_patches,
            int cap, int* __restrict__ ptr, uint16_t* __restrict__ idx, float* __restrict__ val,
-           int* __restrict__ nnz) {
-    const int mtx = blockIdx.x;
+           int* __restrict__ nnz, int mtx0) {
+    const int mtx = mtx0 + blockIdx.x;
     const int rs = mtx / C;
     const int N = n_patches[rs];
     const float* M = mmm + (size_t)mtx * NP * NP;
@@ -110,7 +110,7 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     constexpr int PW = kLanes * PPL;                           // paths per CTA
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int NE = a.npe, NG = NE >> 2, NP = a.npad;
-    const int rs = blockIdx.y;
+    const int rs = a.rs0 + blockIdx.y;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int mtx = rs * a.C + a.c_use;
@@ -567,11 +567,11 @@ k_rov_resim_sparse(to_rov_args a, to_csc csc, int t0) {
 namespace to_k {
 
 to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_patches,
-                   int n_rs, to_csc& csc) {
+                   int n_rs, to_csc& csc, int rs0) {
     if (NP > 1024) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NP);
     to_prof_begin(ctx, "pack_csc");
     k_pack_csc<<<n_rs * C, 1024, 0, ctx->stream>>>(mmm, NP, C, n_patches, csc.cap,
-                                                 csc.ptr, csc.idx, csc.val, csc.nnz);
+                                                 csc.ptr, csc.idx, csc.val, csc.nnz, rs0 * C);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;

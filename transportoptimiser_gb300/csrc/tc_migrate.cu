@@ -44,7 +44,7 @@ __device__ __forceinline__ float tf32_hi(float x) {
 }
 
 __global__ void k_tc_pack(to_mte_args a, int MT, int KGN, float* __restrict__ packed) {
-    const int rs = blockIdx.y, blk = blockIdx.x;
+    const int rs = a.rs0 + blockIdx.y, blk = blockIdx.x;
     const int m = blk / KGN, g = blk - m * KGN;
     const int N = a.n_patches[rs], NP = a.npad;
     const float* M = a.mmm + ((size_t)rs * a.C + a.c_use) * NP * NP;
@@ -99,7 +99,7 @@ k_mte_tc(to_mte_args a, TcShape sh, const float* __restrict__ packed, int* __res
     float* endp = reinterpret_cast<float*>(sm + off_end(sh));
     float* zs = reinterpret_cast<float*>(sm + off_z(sh));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int rs = blockIdx.y;
+    const int rs = a.rs0 + blockIdx.y;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int N = a.n_patches[rs], NP = a.npad;
     if (N > KGN * KGRP || N > MT * 128) {

@@ -28,6 +28,7 @@ struct to_model_args {
     const int* seg_off;          // [R+1] road segments CSR
     const double* segs;          // 4 doubles (x1, y1, x2, y2) per segment
     int sem;
+    int rs0;                     // first (road, species) of the launch (rs = road*S + species)
     int max_patches;             // NM: stride of per-(road,species) arrays
     int npad;                    // NP: padded patch count of the matrices
     // outputs, all indexed by rs = road*S + species

@@ -8,6 +8,7 @@ struct to_mte_args {
     uint64_t seed;
     int sem;
     int road0;                   // stream id of road 0 of the batch
+    int rs0;                     // first (road, species) of the launch
     int npad;                    // NP: stride of the per-road arrays
     int npe;                     // effective width (multiple of 4, >= every N)
     int tile_paths, l_chunk;     // filled by the launcher

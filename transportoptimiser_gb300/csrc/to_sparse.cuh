@@ -17,7 +17,7 @@ struct to_rov_args;
 
 namespace to_k {
 to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_patches,
-                   int n_rs, to_csc& csc);
+                   int n_rs, to_csc& csc, int rs0 = 0);
 size_t mte_sparse_smem(int NE, int cap_smem);
 size_t rov_sparse_smem(int NE, int C, int cap_smem);
 to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc);
