@@ -265,6 +265,9 @@ __global__ void k_adj_pop_fwd(AdjArgs a, int TP) {
 __global__ void k_adj_pop_bwd(AdjArgs a, int TP, int ntheta) {
     extern __shared__ float sm[];
     const int s = blockIdx.y, lane = threadIdx.x, p = blockIdx.x * TP + lane;
+    // the sweep is linear in the species' output weight: a zero weight
+    // contributes exactly zero (the per-path gradients start zeroed)
+    if (a.gout[1 + s] == 0.0f) return;
     const int N = a.n_patches[s];
     const bool live = p < a.P;
     const int pp = live ? p : 0;
@@ -530,8 +533,10 @@ to_status to_adjoint_backward(to_ctx ctx, to_tape t, const double* grad_outputs,
     TO_CUDA(ctx, cudaMemcpyAsync(const_cast<float*>(a.gout), go, (size_t)(1 + S) * 4,
                                  cudaMemcpyHostToDevice, ctx->stream));
     TO_CUDA(ctx, cudaMemsetAsync(a.gpath, 0, (size_t)P * ntheta * 8, ctx->stream));
-    k_adj_pv_grad<<<(P + 127) / 128, 128, 0, ctx->stream>>>(a, ntheta);
-    TO_LAUNCHED(ctx);
+    if (grad_outputs[0] != 0.0) {           // the PV part is linear in its weight too
+        k_adj_pv_grad<<<(P + 127) / 128, 128, 0, ctx->stream>>>(a, ntheta);
+        TO_LAUNCHED(ctx);
+    }
     const int TP = tile_paths(t->maxN);
     const size_t smb = (size_t)3 * t->maxN * TP * 4;
     TO_CUDA(ctx, cudaFuncSetAttribute(k_adj_pop_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize,
