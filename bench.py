@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--profile-rov", action="store_true",
                     help="one ROV valuation of a one-road scene (2 species, ~115 "
                          "patches, 3 controls, 16 bins per dimension), for profilers")
+    ap.add_argument("--profile-rov-batch", type=int, default=0, metavar="PATHS",
+                    help="one batched ROV valuation of 256 roads at PATHS paths each, for "
+                         "profilers")
     ap.add_argument("--rov-paths", type=int, default=10000)
     ap.add_argument("--surrogate-samples", type=int, default=50000,
                     help="training pairs for the learned surrogate (0: skip that leg)")
@@ -152,6 +155,26 @@ def cpu_baseline_port(scene, roads, P, seconds=20.0, threads=None):
     return done / dt, threads, done
 
 
+def reference_n_star(scene, roads, threads=None):
+    """Paths per road for a 1% standard error, by the same rule as the GPU
+    arm (largest need over roads and species, rounded up to 64, at least 64),
+    from a CPU pilot at PILOT_PATHS paths on the given roads."""
+    import numpy as np
+    from oracle import pyoracle as po
+    threads = threads or os.cpu_count() or 1
+    need = 64
+    for r, rd in enumerate(roads):
+        for s, sp in enumerate(scene.species):
+            m = po.species_model(scene, sp, rd, sem=0, max_patches=1024)
+            e = po.simulate_mte(PILOT_PATHS, YEARS, m["N"], 1.0, sp.params, m["init_pops"],
+                                m["caps"], m["mmm"][-1], 1, r, s, 0, threads).astype(np.float64)
+            mean = e.mean()
+            if mean > 0:
+                sigma = e.std(ddof=1)
+                need = max(need, math.ceil((sigma / (0.01 * abs(mean))) ** 2))
+    return int(min(math.ceil(need / 64.0) * 64, 16384))
+
+
 # --------------------------------------------------------------------------
 def run_reference(args):
     """--impl reference: the CPU port of the reference on the host cores."""
@@ -163,7 +186,8 @@ def run_reference(args):
     from transportoptimiser_gb300 import build as b
     b.build_oracle()
     scene = synth.generation(0, n_roads=args.roads)
-    P = PILOT_PATHS
+    # the paths the metric needs (1% standard error), from a bounded pilot
+    P = reference_n_star(scene, scene.roads[:8])
     for _ in range(args.warmup):
         cpu_baseline_port(scene, scene.roads[:1], 64, seconds=1.0)
     vals = []
@@ -177,7 +201,8 @@ def run_reference(args):
             "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "paths": P, "note": "per step: roads valued "
-                       "in an 8 s sample"},
+                       "in an 8 s sample; paths per road N* from a %d-path CPU pilot on "
+                       "8 roads" % PILOT_PATHS},
             "cpu_baseline": {"value": value, "unit": "designs/s", "cores": cores,
                              "kind": "port", "sample": "roads valued in 8 s per step, "
                              "%d paths, all species" % P},
@@ -293,7 +318,7 @@ def rov_adjoint_leg(ctx, rov_paths=10000, adj_paths=20000, reps=3):
     return {"rov": rov, "adjoint": adj}
 
 
-def rov_generation_leg(ctx, n_roads=256, reps=3, plain_roads=16):
+def rov_generation_leg(ctx, n_roads=256, reps=3, plain_roads=16, paths=None):
     """ROV valuation of a GA generation of roads in one batch
     (to_simulate_rov_batch) at N* paths per road from a 512-path pilot, next
     to one road per call (the reference's way)."""
@@ -317,12 +342,17 @@ def rov_generation_leg(ctx, n_roads=256, reps=3, plain_roads=16):
         return [rov_problem_from_models(m, sc, n_paths=P, n_years=YEARS, dim_res=16, sem=1,
                                         n_processes=3, demand=True, road=i)
                 for i, m in enumerate(models)]
-    pilot = sg.simulateROVCUDA_batch(problems(512), want=(), ctx=ctx)
-    need = max((o["value_se"] * math.sqrt(512) / (0.01 * abs(o["stats"][0]))) ** 2
-               for o in pilot if o["stats"][0] != 0.0)
-    P = int(min(max(128, math.ceil(need / 128.0) * 128), 4096))
+    if paths is None:
+        pilot = sg.simulateROVCUDA_batch(problems(512), want=(), ctx=ctx)
+        need = max((o["value_se"] * math.sqrt(512) / (0.01 * abs(o["stats"][0]))) ** 2
+                   for o in pilot if o["stats"][0] != 0.0)
+        P = int(min(max(128, math.ceil(need / 128.0) * 128), 4096))
+    else:
+        P = paths
     probs = problems(P)
     sg.simulateROVCUDA_batch(probs, want=(), ctx=ctx)
+    if reps == 0:
+        return {"roads": n_roads, "paths_per_road": P}
     ts = []
     for _ in range(reps):
         t0 = time.perf_counter()
@@ -332,7 +362,7 @@ def rov_generation_leg(ctx, n_roads=256, reps=3, plain_roads=16):
     t0 = time.perf_counter()
     for p in probs[:plain_roads]:
         sg.simulateROVCUDA(p, want=(), ctx=ctx)
-    t1 = (time.perf_counter() - t0) / plain_roads
+    t1 = (time.perf_counter() - t0) / max(plain_roads, 1)
     return {"roads": n_roads, "paths_per_road": P, "pilot_paths": 512, "years": YEARS,
             "batch_ms": 1000.0 * tb, "designs_per_s": n_roads / tb,
             "plain_ms_per_road": 1000.0 * t1, "plain_designs_per_s": 1.0 / t1,
@@ -365,6 +395,11 @@ def main():
         return run_reference(args)
     if args.profile_rov:
         return profile_rov(args)
+    if args.profile_rov_batch:
+        from transportoptimiser_gb300._capi import Context
+        print(json.dumps(rov_generation_leg(Context(0), reps=0, plain_roads=0,
+                                            paths=args.profile_rov_batch)))
+        return 0
 
     import numpy as np
     import torch
