@@ -166,3 +166,32 @@ def test_rov_batch_equals_single_roads(ctx):
             assert np.array_equal(b[k], one[k]), k
         assert np.array_equal(b["stats"], one["stats"])
         assert b["value_se"] == one["value_se"]
+
+
+def test_rov_batch_edges(ctx):
+    """Ragged path tiles (130 paths per road), a batch of one road, and the
+    refusals: roads that differ in a shared setting, too few paths per road."""
+    from transportoptimiser_gb300._capi import TransOptError
+    sc = synth.rov_road(3, n_species=1)
+    rng = np.random.Generator(np.random.Philox(9))
+    roads = [sc.roads[0], synth.random_road(sc.W, sc.H, 9, rng)]
+    models = [[po.species_model(sc, sc.species[0], rd, sem=1)] for rd in roads]
+
+    def prob(m, P, Y=8, road=0):
+        return rov_problem_from_models(m, sc, n_paths=P, n_years=Y, dim_res=8, sem=1,
+                                       n_processes=3, demand=True, seed=2, road=road)
+    want = ("cond_exp", "opt_cont", "regression")
+    probs = [prob(m, 130, road=i) for i, m in enumerate(models)]
+    for p, b in zip(probs, sg.simulateROVCUDA_batch(probs, want=want, ctx=ctx)):
+        one = sg.simulateROVCUDA(p, want=want, ctx=ctx)
+        for k in want:
+            assert np.array_equal(b[k], one[k]), k
+        assert np.array_equal(b["stats"], one["stats"])
+    single = sg.simulateROVCUDA_batch([prob(models[0], 60)], want=want, ctx=ctx)[0]
+    one = sg.simulateROVCUDA(prob(models[0], 60), want=want, ctx=ctx)
+    for k in want:
+        assert np.array_equal(single[k], one[k]), k
+    with pytest.raises(TransOptError):
+        sg.simulateROVCUDA_batch([prob(models[0], 130), prob(models[1], 130, Y=9)], ctx=ctx)
+    with pytest.raises(TransOptError):
+        sg.simulateROVCUDA_batch([prob(models[0], 64), prob(models[1], 64, road=1)], ctx=ctx)

@@ -538,6 +538,47 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 constexpr float kSeedGrow = 1.4f;
 // groups of at most this many points skip the threshold search
 constexpr int kBrute = 128;
+// groups of at most this many points keep every key in registers (12 per
+// lane) and search the threshold on them, without the cell grid
+constexpr int kRegKeys = 12;
+constexpr int kReg = 32 * kRegKeys;
+
+// Threshold selection on keys held in registers (lane l holds points l,
+// l+32, ...): T moves until between k and cap keys qualify, then they are
+// compacted into ws.sel and sorted by (key, index).  Every key <= T is
+// kept, so the k nearest come out exact.  False when ties keep the count
+// out of the window.
+__device__ bool reg_select(const float (&key)[kRegKeys], int k, int dim, float T,
+                          WarpScratch& ws) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int cap = 32;
+    while (cap < k) cap <<= 1;
+    const float expo = 2.0f / (float)dim;
+    const float target = 0.5f * (float)(k + cap);
+    float lo = -1.0f, hi = -1.0f;
+    int cnt = -1;
+    for (int iter = 0; iter < 64; ++iter) {
+        if (!(T < INFINITY) || !(T >= 0.0f)) return false;
+        cnt = 0;
+#pragma unroll
+        for (int u = 0; u < kRegKeys; ++u) cnt += __popc(__ballot_sync(kFull, key[u] <= T));
+        if (cnt >= k && cnt <= cap) break;
+        if (!next_threshold(cnt, k, target, expo, T, lo, hi)) return false;
+    }
+    if (cnt < k || cnt > cap) return false;
+    int pos = 0;
+#pragma unroll
+    for (int u = 0; u < kRegKeys; ++u) {
+        const bool le = key[u] <= T;
+        const unsigned m = __ballot_sync(kFull, le);
+        if (le) ws.sel[pos + __popc(m & lt_mask)] = pack_sel(key[u], lane + 32 * u);
+        pos += __popc(m);
+    }
+    __syncwarp();
+    warp_sort_sel(ws, cnt);
+    return true;
+}
 
 template <int D>
 __host__ __device__ constexpr int knn_acc_len() { return (D + 1) + (D + 1) * (D + 1); }
@@ -583,6 +624,14 @@ k_knn_rov(to_rov_args a, int t) {
             __syncwarp();
             warp_sort_sel(ws, n);
             ok = true;
+        } else if (n <= kReg) {
+            float key[kRegKeys];
+#pragma unroll
+            for (int u = 0; u < kRegKeys; ++u) {
+                const int i = lane + 32 * u;
+                key[u] = (i < n) ? sqdist(xs, P, i, D, qn) : INFINITY;
+            }
+            ok = reg_select(key, k, D, T, ws);
         } else if (g.ok) {
             GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
                            a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
