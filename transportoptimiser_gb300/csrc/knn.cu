@@ -5,13 +5,14 @@
 // insertion sort over it, a sqrt pass, with host copies around each call)
 // and multiLocLinReg (SimulateGPU.cu:2934-3053).
 //
-// A warp owns a run of neighbouring grid queries.  For each query it
-// gathers every point within a squared-distance threshold T by ballot
-// compaction; T adapts until between k and 256 points qualify (and is
-// carried to the next, neighbouring, query).  The survivors are
-// bitonic-sorted by (squared distance, index): exactly the set and order the
-// reference's stable insertion sort returns.  When exact ties keep the count
-// out of that window, a 4 x 8-bit radix select on the same keys takes over.
+// A warp handles one query at a time.  It gathers every point within a
+// squared-distance threshold T by ballot compaction; T adapts until between
+// k and the store size qualify, then the survivors are narrowed to the power
+// of two above k and bitonic-sorted by (squared distance, index): exactly
+// the set and order the reference's stable insertion sort returns.  Small
+// point sets are handled whole (all keys sorted, or the threshold searched
+// on keys held in registers).  When exact ties keep the count out of the
+// window, a 4 x 8-bit radix select on the same keys takes over.
 //
 // For the ROV the points of each control are first binned into a uniform
 // cell grid (k_knn_grid, a counting sort), so a threshold pass visits only

@@ -15,13 +15,14 @@
 //    the populations; the random streams are regenerated from Philox where
 //    they are consumed (nothing of size P*Y*N is stored);
 //  * the reference's serial <<<1,1>>> compaction and min/max kernels become
-//    one CTA-wide stable scan per year;
-//  * kNN runs on the device with a warp per query: radix select of the k-th
-//    smallest (squared distance, index) key, then a bitonic sort of the k
-//    survivors - the same neighbour set and order as the reference's stable
-//    insertion sort, without its P x Q distance matrix or host round trips;
+//    per-chunk counts, an ordered scatter and a per-road finish over all SMs;
+//  * kNN runs on the device (knn.cu): persistent warps, one query at a time,
+//    the same neighbour set and order as the reference's stable insertion
+//    sort without its P x Q distance matrix or host round trips;
 //  * the local linear systems are accumulated in FP32 and solved in FP64
-//    (Cholesky); expectations are reduced in FP64.
+//    (Cholesky); expectations are reduced in FP64;
+//  * several roads can be valued in one batch: paths are road-major and the
+//    regressions are grouped by (road, control).
 // Every per-query / per-path formula comes from to_lsm_math.h so the SIMT
 // path reproduces the oracle bit for bit.
 #include <cmath>
