@@ -136,6 +136,18 @@ __device__ __forceinline__ int seg_hit(double x1, double y1, double x2, double y
     return (ua >= 0.0 && ua <= 1.0 && ub >= 0.0 && ub <= 1.0) ? 1 : 0;
 }
 
+// the same test in FP32 on a segment given as origin + direction
+__device__ __forceinline__ int seg_hit_f(float x1, float y1, float dx, float dy, float x3,
+                                         float y3, float ex, float ey) {
+    const float d = dx * ey - dy * ex;
+    if (d == 0.0f) return 0;
+    const float ua = ((x3 - x1) * ey - (y3 - y1) * ex) / d;
+    const float ub = ((x3 - x1) * dy - (y3 - y1) * dx) / d;
+    return (ua >= 0.0f && ua <= 1.0f && ub >= 0.0f && ub <= 1.0f) ? 1 : 0;
+}
+
+constexpr int kFeatSegs = 256;           // segments staged in shared memory
+
 // 16 features per road (surrogate inputs):
 //  0 length / W, 1 segments / 64, 2 road cells / W, 3 / 4 crossing
 //  exposure: road crossings per animal of species 0 moving 5 / 12 cells
@@ -177,8 +189,23 @@ __global__ void k_road_features(int R, int W, int H, const int* __restrict__ bas
     atomicAdd(&s_acc[8], loss);
     for (int b = 2; b < 5; ++b) atomicAdd(&s_acc[3 + b], hist[b]);
     const int g0 = seg_off[r], g1 = seg_off[r + 1];
+    __shared__ float s_seg[4][kFeatSegs];    // x3, y3, x4 - x3, y4 - y3
+    const bool seg_smem = g1 - g0 <= kFeatSegs;
+    if (seg_smem)
+        for (int g = threadIdx.x; g < g1 - g0; g += blockDim.x) {
+            const double* sg = segs + 4 * (size_t)(g0 + g);
+            s_seg[0][g] = (float)sg[0];
+            s_seg[1][g] = (float)sg[1];
+            s_seg[2][g] = (float)(sg[2] - sg[0]);
+            s_seg[3][g] = (float)(sg[3] - sg[1]);
+        }
+    __syncthreads();
     {
-        // crossing exposure of animals moving 5 and 12 cells
+        // crossing exposure of animals moving 5 and 12 cells in 8 directions
+        // (FP32: surrogate inputs, compared only through the network)
+        const float kc = 0.70710678f;
+        const float dir_x[8] = {1.0f, kc, 0.0f, -kc, -1.0f, -kc, 0.0f, kc};
+        const float dir_y[8] = {0.0f, kc, 1.0f, kc, 0.0f, -kc, -1.0f, -kc};
         const int nx = (W + 4) / 5, ny = (H + 4) / 5;
         const int nprobe = nx * ny * 16;
         double ex[2] = {0.0, 0.0}, ew[2] = {0.0, 0.0};
@@ -187,17 +214,22 @@ __global__ void k_road_features(int R, int W, int H, const int* __restrict__ bas
             const int ix = cell % nx, iy = cell / nx;
             const int x0 = 5 * ix + 2, y0 = 5 * iy + 2;
             if (x0 >= W || y0 >= H) continue;
-            const double dist = di ? 12.0 : 5.0;
-            const double ang = 0.7853981633974483 * dir;
-            const double x1 = x0 + dist * cos(ang), y1 = y0 + dist * sin(ang);
-            const int cx1 = (int)rint(x1), cy1 = (int)rint(y1);
+            const float dist = di ? 12.0f : 5.0f;
+            const float dx = dist * dir_x[dir], dy = dist * dir_y[dir];
+            const int cx1 = (int)rintf((float)x0 + dx), cy1 = (int)rintf((float)y0 + dy);
             if (cx1 < 0 || cx1 >= W || cy1 < 0 || cy1 >= H) continue;
             const double w = (double)popmap[x0 + y0 * W] * (double)popmap[cx1 + cy1 * W];
             if (!(w > 0.0)) continue;
             int hits = 0;
-            for (int g = g0; g < g1; ++g) {
-                const double* sg = segs + 4 * (size_t)g;
-                hits += seg_hit(x0, y0, x1, y1, sg[0], sg[1], sg[2], sg[3]);
+            if (seg_smem) {
+                for (int g = 0; g < g1 - g0; ++g)
+                    hits += seg_hit_f((float)x0, (float)y0, dx, dy, s_seg[0][g], s_seg[1][g],
+                                      s_seg[2][g], s_seg[3][g]);
+            } else {
+                for (int g = g0; g < g1; ++g) {
+                    const double* sg = segs + 4 * (size_t)g;
+                    hits += seg_hit(x0, y0, x0 + dx, y0 + dy, sg[0], sg[1], sg[2], sg[3]);
+                }
             }
             ex[di] += w * hits;
             ew[di] += w;

@@ -126,16 +126,20 @@ def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.01, top=0
 
 
 def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: Ensemble | None,
-           tol=0.01, top=0.1):
+           tol=0.01, top=0.1, timings: dict | None = None):
     """A small GA (tournament selection, crossover, mutation, elitism).  With
     an ensemble the generation is screened; without, every design is valued
     by Monte Carlo.  Returns (best road, its fitness by Monte Carlo, number of
-    Monte Carlo valuations, seconds)."""
+    Monte Carlo valuations, seconds).  `timings`, when given, receives the
+    seconds spent valuing generations (features, network, Monte Carlo) and
+    in the host-side GA operators."""
     roads = random_roads(scene, pop, rng)
     n_mc = 0
     t0 = time.perf_counter()
+    t_val = 0.0
     best, best_fit = None, -np.inf
     for _ in range(generations):
+        tv = time.perf_counter()
         if ens is None:
             packed = pack_segments(roads)
             feats = gen.features(packed)
@@ -144,6 +148,7 @@ def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: E
             mc = np.ones(len(roads), bool)
         else:
             y, fit, mc, feats = screened_values(gen, ens, roads, opts, tol, top)
+        t_val += time.perf_counter() - tv
         n_mc += int(mc.sum())
         # only Monte Carlo values may become the incumbent
         cand = np.flatnonzero(mc)
@@ -158,4 +163,8 @@ def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: E
             child = crossover(a, b, rng) if rng.random() < 0.5 else a
             children.append(mutate(child, scene, rng))
         roads = children
-    return best, best_fit, n_mc, time.perf_counter() - t0
+    total = time.perf_counter() - t0
+    if timings is not None:
+        timings["valuation_s"] = t_val
+        timings["ga_ops_s"] = total - t_val
+    return best, best_fit, n_mc, total
