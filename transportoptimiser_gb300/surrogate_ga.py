@@ -5,10 +5,12 @@ include/main/RoadGA.cpp:2040, 1553) values every design by Monte Carlo, or
 by local-linear grid surrogates of one or two aggregate predictors
 (buildSurrogateMTECUDA / buildSurrogateROVCUDA).  Here an ensemble of two
 MLPs (transportoptimiser_gb300.mlp, own tensor-core kernels) trained on
-pairs the batched simulator generates screens each generation: the plain
-Monte Carlo re-values every design whose ensemble members disagree by more
-than the tolerance (1%) and the top 10% by predicted fitness, and stays the
-judge of the surrogate's error.
+pairs the batched simulator generates screens each generation (surrogate
+pre-selection): the plain Monte Carlo values the most promising designs -
+the top fraction (25%) by an optimistic score, the predicted fitness plus
+the members' spread - and every design whose members disagree by more than
+the tolerance (10%); it stays the judge of the surrogate's error, and only
+Monte Carlo values become the incumbent.
 
 Per road the surrogate predicts:
     0 mean over species of E[end population] / initial population
@@ -108,13 +110,15 @@ class Ensemble:
         return mean, spread
 
 
-def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.01, top=0.1):
+def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.10, top=0.25):
     """Values of a generation with surrogate screening.  Returns (y [R][3],
     fitness [R], mask of the designs re-valued by Monte Carlo, features)."""
     packed = pack_segments(roads)
     feats = gen.features(packed)
     y, spread = ens.predict(feats, gen.ctx)
-    score = fitness(y, feats)
+    # optimistic: the predicted fitness plus the members' relative spread
+    # on the fitness term, so uncertain designs get a chance
+    score = fitness(y, feats) + spread[:, 2] * np.abs(y[:, 2])
     sel = (spread[:, 0] > tol) | (spread[:, 2] > tol)
     k = max(1, int(round(top * len(roads))))
     sel[np.argsort(-score)[:k]] = True
@@ -126,7 +130,7 @@ def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.01, top=0
 
 
 def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: Ensemble | None,
-           tol=0.01, top=0.1, timings: dict | None = None):
+           tol=0.10, top=0.25, timings: dict | None = None):
     """A small GA (tournament selection, crossover, mutation, elitism).  With
     an ensemble the generation is screened; without, every design is valued
     by Monte Carlo.  Returns (best road, its fitness by Monte Carlo, number of
