@@ -51,6 +51,7 @@ struct to_gen_s {
     int* d_type;
     int* d_cross;
     double* d_tv;
+    uint16_t* d_tdest;
     float *d_mmm, *d_ip, *d_cp;
     float* d_end = nullptr;              // grown on demand [RS][P]
     size_t end_cap = 0;
@@ -149,7 +150,7 @@ void model_args(to_gen g, int R, const int* cell_off, const int* cells, const in
     a.n_patches = g->d_np; a.n_transitions = g->d_nt;
     a.area = g->d_area; a.cap = g->d_cap; a.pop = g->d_pop;
     a.cx = g->d_cx; a.cy = g->d_cy; a.type = g->d_type;
-    a.crossings_scratch = g->d_cross; a.trans_scratch = g->d_tv;
+    a.crossings_scratch = g->d_cross; a.trans_scratch = g->d_tv; a.trans_dest = g->d_tdest;
     a.mmm = g->d_mmm; a.init_pops = g->d_ip; a.caps = g->d_cp;
     a.d_flags = ctx->d_flags;
     a.n_label_types = g->n_label_types; a.label_types = g->d_label_types; a.labels = g->d_labels;
@@ -442,6 +443,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     acc(RS * NM * 4);
     acc(RS * NM * NM * 4);
     acc(RS * NM * NM * 8);
+    acc(RS * NM * NM * 2);
     acc(RS * C * NP * NP * 4);
     acc(RS * NP * 4); acc(RS * NP * 4);
     acc(RS * 5 * 8);
@@ -468,6 +470,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->d_type = carve<int>(p, RS * NM);
     g->d_cross = carve<int>(p, RS * NM * NM);
     g->d_tv = carve<double>(p, RS * NM * NM);
+    g->d_tdest = carve<uint16_t>(p, RS * NM * NM);
     g->d_mmm = carve<float>(p, RS * C * NP * NP);
     g->d_ip = carve<float>(p, RS * NP);
     g->d_cp = carve<float>(p, RS * NP);

@@ -382,6 +382,7 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
                    to_align256((size_t)NM * 8) * 5 + to_align256((size_t)NM * 4) +
                    to_align256((size_t)NM * NM * 4) * 2 +
                    to_align256((size_t)NM * NM * 8) * 2 +
+                   to_align256((size_t)NM * NM * 2) +
                    to_align256((size_t)C * NM * NM * 8) +
                    to_align256((size_t)C * NP * NP * 4) + to_align256((size_t)NP * 4) * 2 +
                    4096;
@@ -402,6 +403,7 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
     a.crossings_scratch = to_arena_take<int>(ctx, (size_t)NM * NM);
     a.crossings_out = to_arena_take<int>(ctx, (size_t)NM * NM);
     a.trans_scratch = to_arena_take<double>(ctx, (size_t)NM * NM);
+    a.trans_dest = to_arena_take<uint16_t>(ctx, (size_t)NM * NM);
     a.trans = to_arena_take<double>(ctx, (size_t)NM * NM);
     a.surv = to_arena_take<double>(ctx, (size_t)C * NM * NM);
     a.mmm = to_arena_take<float>(ctx, (size_t)C * NP * NP);

@@ -487,6 +487,7 @@ __global__ void __launch_bounds__(512, 2)
 k_species_links(to_model_args a) {
     extern __shared__ __align__(16) unsigned char sml[];
     __shared__ int s_last, s_cnt, s_npair;
+    __shared__ int s_tmp[33];
     const int rs = a.rs0 + blockIdx.x;
     const int road = rs / a.S, sp = rs - road * a.S;
     const to_model_species& S = a.species[sp];
@@ -516,7 +517,9 @@ k_species_links(to_model_args a) {
     float* cyf = cxf + NM;                                      // [NM]
     float* sgf = cyf + NM;                                      // [4][SC]
     double* s_attr = reinterpret_cast<double*>(sgf + 4 * SC);   // [TO_MAX_HAB]
-    double* s_surv = s_attr + TO_MAX_HAB;                       // [C][G+1]
+    double* s_surv = s_attr + TO_MAX_HAB;                       // [C][SC+1]
+    double* s_sum = s_surv + a.C * (SC + 1);                    // [NM] row sums
+    int* s_off = reinterpret_cast<int*>(s_sum + NM);            // [NM+1] row offsets
     const double lda = S.lambda_mult * S.lambda_sd + S.lambda_mean;
     for (int k = threadIdx.x; k < N; k += blockDim.x) { cxf[k] = (float)cx[k]; cyf[k] = (float)cy[k]; }
     if (seg_tab)
@@ -628,10 +631,18 @@ k_species_links(to_model_args a) {
     __syncthreads();
 
     // Transition probabilities (SpeciesRoadPatches.cpp:383-426) and the
-    // migration matrices.  A warp per origin row i: lanes test the
-    // destinations j in parallel, the in-range terms are summed in j order
-    // by one lane (the reference's order), and only non-zero entries are
-    // divided, multiplied by survival and written.
+    // migration matrices.  FP64 issues at a small fraction of the FP32 rate
+    // here, and a warp pays for a whole FP64 instruction however few lanes
+    // are active, so the in-range pairs (a few per row) are listed first and
+    // the FP64 work then runs over the list on full warps:
+    //   T1  a warp per origin row i lists its in-range destinations j in
+    //       ascending order (float tests; FP64 only within 1e-6 of the cut-off)
+    //   T2  one thread per listed pair: the unnormalised weight
+    //   T3  one thread per row: the row sum in j order (the reference's order)
+    //   T4  one thread per listed pair: division by the row sum, survival,
+    //       the migration matrices
+    // Every value goes through the same operations in the same order as a
+    // row-at-a-time evaluation, so the bits do not depend on the schedule.
     const double max_dist_t = (a.sem == 0)
         ? log(0.05) / (-(S.lambda_mean + S.lambda_sd * lda))
         : log(0.05) / (-lda);
@@ -640,49 +651,78 @@ k_species_links(to_model_args a) {
     const float ft_lo = (float)(mt2 * (1.0 - 1e-6)), ft_hi = (float)(mt2 * (1.0 + 1e-6));
     double* trans = a.trans ? a.trans + (size_t)rs * NM * NM : nullptr;
     double* surv = a.surv ? a.surv + (size_t)rs * a.C * NM * NM : nullptr;
-    double* wv = a.trans_scratch + (size_t)rs * NM * NM;        // per-row values, [i][slot]
+    double* wv = a.trans_scratch + (size_t)rs * NM * NM;        // weights, [i][slot]
+    uint16_t* dj = a.trans_dest + (size_t)rs * NM * NM;         // destinations, [i][slot]
+    // T1
     for (int i = warp; i < N; i += nwarp) {
-        double* rowv = wv + (size_t)i * NM;
+        uint16_t* rowj = dj + (size_t)i * NM;
         int cnt = 0;
         for (int j0 = 0; j0 < N; j0 += 32) {
             const int j = j0 + lane;
-            bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
-            unsigned m = __ballot_sync(0xffffffffu, inr);
-            if (inr) {
-                double w = area[j] * lda * s_attr[ptype[j]];
-                double v = w;
-                if (i != j) {
-                    double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
-                    double d = sqrt(dx * dx + dy * dy);
-                    v = (a.sem == 0) ? w / exp(-lda * d) : w * exp(-lda * d);
-                }
-                rowv[cnt + __popc(m & ((1u << lane) - 1u))] = v;
-            }
+            const bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
+            const unsigned m = __ballot_sync(0xffffffffu, inr);
+            if (inr) rowj[cnt + __popc(m & ((1u << lane) - 1u))] = (uint16_t)j;
             cnt += __popc(m);
         }
-        __syncwarp();
-        double summ = 0.0;
-        if (lane == 0)
-            for (int q = 0; q < cnt; ++q) summ += rowv[q];
-        summ = __shfl_sync(0xffffffffu, summ, 0);
-        // second pass: the same in-range set, slot by slot
-        int base = 0;
-        for (int j0 = 0; j0 < N; j0 += 32) {
-            const int j = j0 + lane;
-            bool inr = (j < N) && in_range(i, j, ft_lo, ft_hi, max_dist_t, mt2lo, mt2hi);
-            unsigned m = __ballot_sync(0xffffffffu, inr);
-            if (inr) {
-                const double tr = rowv[base + __popc(m & ((1u << lane) - 1u))] / summ;
-                const int cr = cross[(size_t)i * N + j];
-                for (int c = 0; c < a.C; ++c) {
-                    float mv = (float)(tr * surv_of(c, cr));
-                    if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
-                }
-                if (trans) trans[(size_t)i * NM + j] = tr;
-            }
-            base += __popc(m);
+        if (lane == 0) s_off[i] = cnt;
+    }
+    __syncthreads();
+    {   // row offsets: exclusive scan of the counts, s_off[N] = total
+        const int chunk = (N + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int lo = (int)threadIdx.x * chunk, hi = min(N, lo + chunk);
+        int c = 0;
+        for (int i = lo; i < hi; ++i) c += s_off[i];
+        int total = 0;
+        int base = cta_exclusive_scan(c, s_tmp, &total);
+        for (int i = lo; i < hi; ++i) { const int v = s_off[i]; s_off[i] = base; base += v; }
+        if (threadIdx.x == 0) s_off[N] = total;
+    }
+    __syncthreads();
+    const int n_listed = s_off[N];
+    auto row_of = [&](int f) {                 // s_off[i] <= f < s_off[i + 1]
+        int lo = 0, hi = N;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_off[mid] <= f) lo = mid; else hi = mid;
         }
-        __syncwarp();
+        return lo;
+    };
+    // T2
+    for (int f = threadIdx.x; f < n_listed; f += blockDim.x) {
+        const int i = row_of(f);
+        const size_t at = (size_t)i * NM + (f - s_off[i]);
+        const int j = dj[at];
+        const double w = area[j] * lda * s_attr[ptype[j]];
+        double v = w;
+        if (i != j) {
+            const double dx = cx[i] - cx[j], dy = cy[i] - cy[j];
+            const double d = sqrt(dx * dx + dy * dy);
+            v = (a.sem == 0) ? w / exp(-lda * d) : w * exp(-lda * d);
+        }
+        wv[at] = v;
+    }
+    __syncthreads();
+    // T3
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const double* rowv = wv + (size_t)i * NM;
+        const int n = s_off[i + 1] - s_off[i];
+        double summ = 0.0;
+        for (int q = 0; q < n; ++q) summ += rowv[q];
+        s_sum[i] = summ;
+    }
+    __syncthreads();
+    // T4
+    for (int f = threadIdx.x; f < n_listed; f += blockDim.x) {
+        const int i = row_of(f);
+        const size_t at = (size_t)i * NM + (f - s_off[i]);
+        const int j = dj[at];
+        const double tr = wv[at] / s_sum[i];
+        const int cr = cross[(size_t)i * N + j];
+        for (int c = 0; c < a.C; ++c) {
+            const float mv = (float)(tr * surv_of(c, cr));
+            if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
+        }
+        if (trans) trans[(size_t)i * NM + j] = tr;
     }
     // dense FP64 transition / survival outputs (single-road API only)
     if (trans || surv) {
@@ -770,8 +810,10 @@ to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
     // links: float centroids, segment and survival tables
     const size_t smem2 = (size_t)2 * a.max_patches * sizeof(float) +
                          (size_t)4 * TO_SURV_TABLE_SEGS * sizeof(float) +
-                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double);
-    if (smem2 > ctx->smem_optin)
+                         (size_t)(TO_MAX_HAB + a.C * (TO_SURV_TABLE_SEGS + 1)) * sizeof(double) +
+                         (size_t)a.max_patches * sizeof(double) +
+                         (size_t)(a.max_patches + 1) * sizeof(int);
+    if (smem2 > ctx->smem_optin || a.max_patches > 65535)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "%d patches exceed shared memory",
                             a.max_patches);
     TO_CUDA(ctx, cudaFuncSetAttribute(k_species_links,

@@ -39,6 +39,7 @@ struct to_model_args {
     int* crossings_scratch;      // [RS][NM*NM] (N*N packed)
     int* crossings_out;          // optional [RS][NM][NM]
     double* trans_scratch;       // [RS][NM][NM]
+    uint16_t* trans_dest;        // [RS][NM][NM] in-range destinations per origin row
     double* trans;               // optional [RS][NM][NM]
     double* surv;                // optional [RS][C][NM][NM]
     float* mmm;                  // [RS][C][NP][NP] destination-major
