@@ -131,6 +131,11 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 
     const int N = a.n_patches[rs];
     const int N4 = (N + 3) & ~3;
+    // groups of this (road, species); the launch is shaped for the widest
+    // model, and the groups past N4 would only ever hold zeros (no
+    // non-zeros reach them, the growth of 0 is 0) so they are not visited.
+    // Their totals are +0, which leaves a sum that started at +0 unchanged.
+    const int NGr = N4 >> 2;
     const float* ip = a.init_pops + (size_t)rs * NP;
     const float* sp8 = a.params + 8 * sp;
     const float p0 = sp8[0], p1 = sp8[1], p2 = sp8[2], p4 = sp8[4], p5 = sp8[5],
@@ -176,7 +181,7 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 #pragma unroll
         for (int gi = 0; gi < MAXG; ++gi) {
             const int grp = warp + gi * W;
-            if (grp < NG) {
+            if (grp < NGr) {
                 float z[PPL][4];
 #pragma unroll
                 for (int i = 0; i < PPL; ++i)
@@ -217,7 +222,7 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 #pragma unroll
         for (int gi = 0; gi < MAXG; ++gi) {
             const int grp = warp + gi * W;
-            if (grp < NG) {
+            if (grp < NGr) {
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -232,9 +237,9 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
         if (path >= a.n_paths) continue;
         float e = 0.0f;
         if (a.n_years > 0 && a.sem == 0) {
-            for (int grp = 0; grp < NG; ++grp) e = e + part[grp * PW + i];
+            for (int grp = 0; grp < NGr; ++grp) e = e + part[grp * PW + i];
         } else {
-            for (int grp = 0; grp < NG; ++grp) {
+            for (int grp = 0; grp < NGr; ++grp) {
                 const float* v = cur + (size_t)grp * 4 * PW + i;
                 e = e + grouped4(v[0], v[PW], v[2 * PW], v[3 * PW]);
             }
@@ -273,6 +278,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
         const int rs = rd * a.S + s;
         const int N = a.n_patches[rs];
         const int N4 = (N + 3) & ~3;
+        const int NGr = N4 >> 2;           // this road's groups (see k_mte_sparse)
         const float* sp = a.params + 8 * s;
         const float* ip = a.init_pops + (size_t)rs * NP;
         __syncthreads();
@@ -294,7 +300,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
         __syncthreads();
         if (warp == 0) {
             float tt = 0.0f;
-            for (int grp = 0; grp < NG; ++grp) {
+            for (int grp = 0; grp < NGr; ++grp) {
                 const float* v = cur + (size_t)grp * 4 * kLanes + lane;
                 tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
             }
@@ -335,7 +341,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
 #pragma unroll
             for (int gi = 0; gi < MAXG; ++gi) {
                 const int grp = warp + gi * W;
-                if (grp < NG) {
+                if (grp < NGr) {
                 float z[4];
                 to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
                            (uint32_t)((s * N4) >> 2) + grp, z);
@@ -379,7 +385,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
             // populations (groups ascending)
             for (int c = warp; c <= C; c += W) {
                 float tt = 0.0f;
-                for (int grp = 0; grp < NG; ++grp)
+                for (int grp = 0; grp < NGr; ++grp)
                     tt = tt + part[((size_t)c * NG + grp) * kLanes + lane];
                 if (path < P) {
                     if (c < C) a.aars[(((size_t)s * C + c) * Y + t) * PT + gp] = tt / tot[lane];
@@ -392,7 +398,7 @@ k_rov_forward_sparse(to_rov_args a, to_csc csc) {
 #pragma unroll
             for (int gi = 0; gi < MAXG; ++gi) {
                 const int grp = warp + gi * W;
-                if (grp < NG) {
+                if (grp < NGr) {
 #pragma unroll
                     for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
                 }

@@ -225,11 +225,15 @@ TO_HD void to_normal4(uint64_t seed, uint32_t stream, uint32_t road,
     to_box_muller(w.v[2], w.v[3], &out[2], &out[3]);
 }
 
+/* normal number (lane & 3) of the group's four: only its Box-Muller pair is
+   evaluated, with the same operations as in to_normal4 */
 TO_HD float to_normal1(uint64_t seed, uint32_t stream, uint32_t road,
                        uint32_t path, uint32_t year, uint32_t lane) {
-    float o[4];
-    to_normal4(seed, stream, road, path, year, lane >> 2, o);
-    return o[lane & 3];
+    to_u32x4 w = to_stream_block(seed, stream, road, path, year, lane >> 2);
+    const int hi = (lane & 2) != 0;
+    float z0, z1;
+    to_box_muller(hi ? w.v[2] : w.v[0], hi ? w.v[3] : w.v[1], &z0, &z1);
+    return (lane & 1) ? z1 : z0;
 }
 
 TO_HD float to_uniform1(uint64_t seed, uint32_t stream, uint32_t road,
