@@ -103,7 +103,7 @@ __device__ __forceinline__ float grouped4(float a, float b, float c, float d) {
 constexpr int kMaxG = 4;
 
 template <int MAXG, int PPL>
-__global__ void __launch_bounds__(PPL == 1 ? 1024 : 768, 1)
+__global__ void __launch_bounds__(1024, 1)
 k_mte_sparse(to_mte_args a, to_csc csc) {
     // PPL paths per lane: lane owns paths lane + 32 i; every non-zero read
     // from shared memory serves all of them
@@ -127,7 +127,8 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     float* part = cur + (size_t)NE * PW;                       // [NG][PW]
     float* capv = part + (size_t)NG * PW;                      // [NE]
     float* gm = capv + NE;                                     // [PW]
-    int* cptr = reinterpret_cast<int*>(gm + PW);               // [NE+1]
+    float* xs = gm + PW;                                       // [3][PW] year's draws
+    int* cptr = reinterpret_cast<int*>(xs + 3 * PW);           // [NE+1]
 
     const int N = a.n_patches[rs];
     const int N4 = (N + 3) & ~3;
@@ -161,16 +162,28 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     __syncthreads();
 
     for (int t = 0; t < a.n_years; ++t) {
-        for (int i = threadIdx.x; i < PW; i += blockDim.x) {
+        // the growth mean's three draws per path, one thread each: jump
+        // indicator, Brownian term, jump factor minus one
+        for (int q = threadIdx.x; q < 3 * PW; q += blockDim.x) {
+            const int which = q / PW, i = q - which * PW;
             const uint32_t path = (uint32_t)(blockIdx.x * PW + i);
-            float uj = to_uniform1(a.seed, TO_STREAM_SP_JUMP, road_id, path, t, sp);
-            float zb = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road_id, path, t, sp);
-            float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road_id, path, t, sp);
-            float jump = (uj < p6) ? 1.0f : 0.0f;
-            float brown = zb * p2;
-            float jsz = (a.sem == 0) ? (zj * sj2 - sj2 / 2.0f) : (zj * p5 - sj2 / 2.0f);
-            float g = gm[i];
-            gm[i] = g + p4 * (p1 - g) * a.dt + g * brown + (to_expf(jsz) - 1.0f) * g * jump;
+            float v;
+            if (which == 0) {
+                v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road_id, path, t, sp) < p6) ? 1.0f : 0.0f;
+            } else if (which == 1) {
+                v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road_id, path, t, sp) * p2;
+            } else {
+                const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road_id, path, t, sp);
+                const float jsz = (a.sem == 0) ? (zj * sj2 - sj2 / 2.0f) : (zj * p5 - sj2 / 2.0f);
+                v = to_expf(jsz) - 1.0f;
+            }
+            xs[q] = v;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < PW; i += blockDim.x) {
+            const float jump = xs[i], brown = xs[PW + i], em1 = xs[2 * PW + i];
+            const float g = gm[i];
+            gm[i] = g + p4 * (p1 - g) * a.dt + g * brown + em1 * g * jump;
         }
         __syncthreads();
         float g[PPL];
@@ -588,10 +601,10 @@ to_status pack_csc(to_ctx ctx, const float* mmm, int NP, int C, const int* n_pat
 static int mte_ppl(int NE, int cap_smem, size_t smem_cap);
 
 size_t mte_sparse_smem_ppl(int NE, int cap_smem, int ppl) {
-    const int maxg = kMaxG, maxw = ppl == 1 ? 32 : 24;
-    if (NE > maxw * maxg * 4) return ~size_t(0);
+    const int maxg = ppl == 1 ? kMaxG : 3;      // 32 warps of maxg groups of four
+    if (NE > 32 * maxg * 4) return ~size_t(0);
     const int NG = NE / 4, PW = kLanes * ppl;
-    return (size_t)cap_smem * 8 + (size_t)(NE * PW + NG * PW + NE + PW) * 4 +
+    return (size_t)cap_smem * 8 + (size_t)(NE * PW + NG * PW + NE + 4 * PW) * 4 +
            (size_t)(NE + 1) * 4 + 16;
 }
 
@@ -626,9 +639,12 @@ to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
     dim3 grid((a.n_paths + PW - 1) / PW, n_rs);
     to_prof_begin(ctx, "mte_sparse");
     if (ppl == 2) {
-        TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG, 2>,
+        // 32 warps of at most three groups (NE <= 384): a shorter chain of
+        // groups per warp between the year's barriers than 24 warps of four,
+        // and within 64 registers a thread
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<3, 2>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_mte_sparse<kMaxG, 2><<<grid, warps * 32, smem, ctx->stream>>>(a, csc);
+        k_mte_sparse<3, 2><<<grid, 1024, smem, ctx->stream>>>(a, csc);
     } else {
         TO_CUDA(ctx, cudaFuncSetAttribute(k_mte_sparse<kMaxG, 1>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
