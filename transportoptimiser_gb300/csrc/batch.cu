@@ -156,6 +156,12 @@ void model_args(to_gen g, int R, const int* cell_off, const int* cells, const in
     a.n_label_types = g->n_label_types; a.label_types = g->d_label_types; a.labels = g->d_labels;
 }
 
+// the model kernel writes the packed migration matrices (no dense ones)
+void csc_direct(to_gen g, to_model_args& a) {
+    a.csc_ptr = g->csc.ptr; a.csc_idx = g->csc.idx; a.csc_val = g->csc.val;
+    a.csc_nnz = g->csc.nnz; a.csc_cap = g->csc.cap;
+}
+
 to_status grow_end(to_ctx ctx, to_gen g, size_t n) {
     if (n > g->end_cap) {
         if (g->d_end) TO_CUDA(ctx, cudaFree(g->d_end));
@@ -250,6 +256,10 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     }
     to_model_args a;
     model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
+    // sparse migration asked for: the model kernel writes the packed
+    // matrices itself (the tuner's dense candidates need the dense form)
+    const bool packed = (o->migration == TO_MIG_SPARSE_FP32);
+    if (packed) csc_direct(g, a);
     TO_TRY(to_k::species_model(ctx, a, RS));
     // the widest species model decides the tile shape of the path kernel
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
@@ -257,7 +267,7 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_LAUNCHED(ctx);
     const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32);
     if (try_sparse) {
-        TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
+        if (!packed) TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
         k_min_max_int<<<1, 1024, 0, ctx->stream>>>(RS * g->C, g->csc.nnz, d_max + 1);
         TO_LAUNCHED(ctx);
     }
@@ -338,9 +348,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
         a.cell_off = g->d_cell_off;
         a.cells = g->d_cells;
     }
+    if (choice == CH_SPARSE) csc_direct(g, a);  // packed matrices straight from the model
     if (st == TO_OK) st = to_k::species_model(ctx, a, RS);
-    if (st == TO_OK && choice == CH_SPARSE)
-        st = to_k::pack_csc(ctx, g->d_mmm, g->NP, g->C, g->d_np, RS, g->csc);
     if (st == TO_OK) st = tail(ctx, g, m, RS, choice, d_results_out);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);

@@ -551,7 +551,8 @@ k_species_links(to_model_args a) {
     }
     const int NP = a.npad;
     float* mmm = a.mmm + (size_t)rs * a.C * NP * NP;
-    {
+    const bool direct = a.csc_ptr != nullptr;
+    if (!direct) {
         float4* m4 = reinterpret_cast<float4*>(mmm);
         const size_t n4 = (size_t)a.C * NP * NP / 4;
         for (size_t q = threadIdx.x; q < n4; q += blockDim.x) m4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -718,11 +719,84 @@ k_species_links(to_model_args a) {
         const int j = dj[at];
         const double tr = wv[at] / s_sum[i];
         const int cr = cross[(size_t)i * N + j];
-        for (int c = 0; c < a.C; ++c) {
-            const float mv = (float)(tr * surv_of(c, cr));
-            if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
+        if (direct) {
+            // the pair's place in destination j's list (in range is
+            // symmetric, so row j lists its origins, ascending)
+            const uint16_t* rj = dj + (size_t)j * NM;
+            int lo = 0, hi = s_off[j + 1] - s_off[j];
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if ((int)rj[mid] < i) lo = mid + 1; else hi = mid;
+            }
+            const size_t ft = (size_t)s_off[j] + lo;
+            for (int c = 0; c < a.C; ++c)
+                mmm[(size_t)c * NP * NP + ft] = (float)(tr * surv_of(c, cr));
+        } else {
+            for (int c = 0; c < a.C; ++c) {
+                const float mv = (float)(tr * surv_of(c, cr));
+                if ((double)mv > 0.00001) mmm[((size_t)c * NP + j) * NP + i] = mv;
+            }
         }
         if (trans) trans[(size_t)i * NM + j] = tr;
+    }
+    if (direct) {
+        // packed matrices: destination j's entries are the listed origins
+        // whose value passes the reference's 1e-5 cut, ascending - the dense
+        // matrix's non-zeros of row j in k_pack_csc's order
+        __syncthreads();
+        const unsigned lt = (1u << lane) - 1u;
+        for (int c = 0; c < a.C; ++c) {
+            const int mtx = rs * a.C + c;
+            int* cp = a.csc_ptr + (size_t)mtx * (NP + 1);
+            const float* mvT = mmm + (size_t)c * NP * NP;
+            for (int j = warp; j < NP; j += nwarp) {
+                int cnt = 0;
+                if (j < N) {
+                    const int f0 = s_off[j], n = s_off[j + 1] - f0;
+                    for (int q0 = 0; q0 < n; q0 += 32) {
+                        const bool keep = q0 + lane < n && (double)mvT[f0 + q0 + lane] > 0.00001;
+                        cnt += __popc(__ballot_sync(0xffffffffu, keep));
+                    }
+                }
+                if (lane == 0) cp[j] = cnt;
+            }
+            __syncthreads();
+            {
+                const int chunk = (NP + (int)blockDim.x - 1) / (int)blockDim.x;
+                const int lo = (int)threadIdx.x * chunk, hi = min(NP, lo + chunk);
+                int c0 = 0;
+                for (int k = lo; k < hi; ++k) c0 += cp[k];
+                int total = 0;
+                int base = cta_exclusive_scan(c0, s_tmp, &total);
+                for (int k = lo; k < hi; ++k) { const int v = cp[k]; cp[k] = base; base += v; }
+                if (threadIdx.x == 0) {
+                    cp[NP] = total;
+                    a.csc_nnz[mtx] = (total <= a.csc_cap) ? total : -1;
+                }
+            }
+            __syncthreads();
+            if (cp[NP] <= a.csc_cap) {
+                uint16_t* ix = a.csc_idx + (size_t)mtx * a.csc_cap;
+                float* vv = a.csc_val + (size_t)mtx * a.csc_cap;
+                for (int j = warp; j < N; j += nwarp) {
+                    int o = cp[j];
+                    const int f0 = s_off[j], n = s_off[j + 1] - f0;
+                    for (int q0 = 0; q0 < n; q0 += 32) {
+                        const bool in = q0 + lane < n;
+                        const float mv = in ? mvT[f0 + q0 + lane] : 0.0f;
+                        const bool keep = in && (double)mv > 0.00001;
+                        const unsigned b = __ballot_sync(0xffffffffu, keep);
+                        if (keep) {
+                            const int q = o + __popc(b & lt);
+                            ix[q] = dj[(size_t)j * NM + q0 + lane];
+                            vv[q] = mv;
+                        }
+                        o += __popc(b);
+                    }
+                }
+            }
+            __syncthreads();
+        }
     }
     // dense FP64 transition / survival outputs (single-road API only)
     if (trans || surv) {

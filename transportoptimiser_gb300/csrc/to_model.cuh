@@ -43,6 +43,14 @@ struct to_model_args {
     double* trans;               // optional [RS][NM][NM]
     double* surv;                // optional [RS][C][NM][NM]
     float* mmm;                  // [RS][C][NP][NP] destination-major
+    // csc_ptr non-null: the migration matrices go straight into the packed
+    // form (what k_pack_csc makes of the dense ones) and the dense [C][NP][NP]
+    // block of each (road, species) is only scratch, never zeroed
+    int* csc_ptr;                // [RS*C][NP+1]
+    uint16_t* csc_idx;           // [RS*C][csc_cap]
+    float* csc_val;              // [RS*C][csc_cap]
+    int* csc_nnz;                // [RS*C], -1 above csc_cap
+    int csc_cap;
     // labels shared by the species of a road: one labelling per (road,
     // habitable type) into global memory, read by every species' patch
     // pass (n_label_types 0: each CTA labels in its own shared memory)
