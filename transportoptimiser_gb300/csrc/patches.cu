@@ -425,57 +425,121 @@ k_road_labels(to_model_args a) {
 }
 
 // The patch pass of k_species_patches on labels from k_road_labels: same
-// habitat order, same per-(block, region) sums, so the same patch list.
-__global__ void __launch_bounds__(512)
+// patch list (habitats in order, then coarse blocks, regions ascending,
+// the same per-(block, region) sums).  All habitable types are worked on at
+// once: warps over (type, block) items for the two region passes, one scan
+// over the items in that order, and a thread per patch for the sums, so a
+// CTA is not a chain of small per-type phases with a few threads busy.
+__global__ void __launch_bounds__(512, 3)
 k_species_patches_lab(to_model_args a) {
     extern __shared__ int smem[];
     const int rs = a.rs0 + blockIdx.x;
     const int road = rs / a.S, sp = rs - road * a.S;
     const int W = a.W, H = a.H, n = W * H, T = a.n_label_types;
     int* s_tmp = smem;                         // 33 ints
-    int* s_misc = s_tmp + 40;                  // counters
-    int* s_list = smem + 64;                   // block region lists
+    int* s_hab = smem + 40;                    // [TO_MAX_HAB] habitat index of item type
+    int* s_lt = s_hab + TO_MAX_HAB;            // [TO_MAX_HAB] its label type
+    int* s_misc = s_lt + TO_MAX_HAB;           // [0] habitable types, [1] flag
+    const int nblocks = a.xres * a.yres;
+    int* s_off = smem + 64;                    // [TO_MAX_HAB * nblocks + 1]
+    int* s_lab = s_off + TO_MAX_HAB * nblocks + 1;   // [max_patches]
     const to_model_species& S = a.species[sp];
     const int NM = a.max_patches;
-    double* area = a.area + (size_t)rs * NM;
-    double* cap = a.cap + (size_t)rs * NM;
-    double* popd = a.pop + (size_t)rs * NM;
-    double* cx = a.cx + (size_t)rs * NM;
-    double* cy = a.cy + (size_t)rs * NM;
-    int* ptype = a.type + (size_t)rs * NM;
     const float* popmap = a.pop_map + (size_t)sp * n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int skpx = a.skpx, skpy = a.skpy, xres = a.xres;
 
-    if (threadIdx.x == 0) { s_misc[0] = 0; s_misc[1] = -1; }
-    __syncthreads();
-    bool ok = true;
-    for (int h = 0; h < S.n_hab; ++h) {
-        int typ = S.hab_type[h];
-        if (typ == 3 || typ == 4) continue;      // CLEAR, ROAD
-        int ti = 0;
-        while (ti < T && a.label_types[ti] != typ) ++ti;
-        if (ti == T) { ok = false; continue; }    // not planned for: flagged
-        const int* L = a.labels + ((size_t)road * T + ti) * n;
-        float maxpop = (float)S.hab_max_pop[h];
-        auto lab = [&](int c) { return L[c]; };
-        auto popf = [&](int c) { return popmap[c]; };
-        auto emit = [&](int o, int cnt, float pop, float sx, float sy, int bx, int by) {
-            float v[5];
-            finish_patch(cnt, pop, sx, sy, bx, by, a.skpx, a.skpy, a.xs, a.ys, a.spa, maxpop, v);
-            area[o] = (double)v[0];
-            cap[o] = (double)v[1];
-            popd[o] = (double)v[2];
-            cx[o] = (double)v[3];
-            cy[o] = (double)v[4];
-            ptype[o] = h;
-        };
-        ok &= cta_block_patches(W, H, a.skpx, a.skpy, a.xres, a.yres, NM, &s_misc[0], s_tmp,
-                                s_list, lab, popf, emit);
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        int nh = 0, bad = 0;
+        for (int h = 0; h < S.n_hab; ++h) {
+            const int typ = S.hab_type[h];
+            if (typ == 3 || typ == 4) continue;      // CLEAR, ROAD
+            int ti = 0;
+            while (ti < T && a.label_types[ti] != typ) ++ti;
+            if (ti == T) { bad = 1; continue; }       // not planned for: flagged
+            s_hab[nh] = h;
+            s_lt[nh] = ti;
+            ++nh;
+        }
+        s_misc[0] = nh;
+        s_misc[1] = bad;
     }
-    if (!ok && a.d_flags) atomicExch(a.d_flags, TO_DEVERR_PATCHES);
     __syncthreads();
-    const int N = min(s_misc[0], NM);
-    if (threadIdx.x == 0) a.n_patches[rs] = N;
+    const int nitems = s_misc[0] * nblocks;
+    const int* labels = a.labels + (size_t)road * T * n;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int it = warp; it < nitems; it += nw) {
+            const int hi = it / nblocks, b = it - hi * nblocks;
+            const int* L = labels + (size_t)s_lt[hi] * n;
+            const int by = b / xres, bx = b - by * xres;
+            int bsx, bsy;
+            block_extent(bx, by, W, H, skpx, skpy, bsx, bsy);
+            const int ncell = (bsx > 0 && bsy > 0) ? bsx * bsy : 0;
+            const int out = pass ? s_off[it] : 0;
+            int lastr = 0, cnt = 0;
+            for (;;) {
+                int mn = 0x7fffffff;
+                for (int e = lane; e < ncell; e += 32) {
+                    const int ii = e / bsy, jj = e - ii * bsy;
+                    const int r = L[(bx * skpx + ii) + (by * skpy + jj) * W];
+                    if (r > lastr && r < mn) mn = r;
+                }
+                mn = __reduce_min_sync(0xffffffffu, mn);
+                if (mn == 0x7fffffff) break;
+                if (pass && lane == 0 && out + cnt < NM) s_lab[out + cnt] = mn;
+                ++cnt;
+                lastr = mn;
+            }
+            if (!pass && lane == 0) s_off[it] = cnt;
+        }
+        __syncthreads();
+        if (!pass) {
+            const int total = cta_scan_array(s_off, nitems, s_tmp);
+            if (threadIdx.x == 0) s_off[nitems] = total;
+            __syncthreads();
+        }
+    }
+    const int total = s_off[nitems];
+    const int nemit = min(total, NM);
+    for (int t = threadIdx.x; t < nemit; t += blockDim.x) {
+        int lo = 0, hi = nitems;                  // item: last one with s_off <= t
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_off[mid] <= t) lo = mid; else hi = mid;
+        }
+        const int it = lo, ht = it / nblocks, b = it - ht * nblocks;
+        const int h = s_hab[ht];
+        const int* L = labels + (size_t)s_lt[ht] * n;
+        const int by = b / xres, bx = b - by * xres;
+        int bsx, bsy;
+        block_extent(bx, by, W, H, skpx, skpy, bsx, bsy);
+        const int r = s_lab[t];
+        int cnt = 0;
+        float pop = 0.0f, sx = 0.0f, sy = 0.0f;
+        for (int ii = 0; ii < bsx; ++ii)
+            for (int jj = 0; jj < bsy; ++jj) {
+                const int c = (bx * skpx + ii) + (by * skpy + jj) * W;
+                if (L[c] != r) continue;
+                cnt += 1;
+                pop = pop + popmap[c];
+                sx = sx + (float)ii;
+                sy = sy + (float)jj;
+            }
+        float v[5];
+        finish_patch(cnt, pop, sx, sy, bx, by, skpx, skpy, a.xs, a.ys, a.spa,
+                     (float)S.hab_max_pop[h], v);
+        const size_t o = (size_t)rs * NM + t;
+        a.area[o] = (double)v[0];
+        a.cap[o] = (double)v[1];
+        a.pop[o] = (double)v[2];
+        a.cx[o] = (double)v[3];
+        a.cy[o] = (double)v[4];
+        a.type[o] = h;
+    }
+    if (threadIdx.x == 0) {
+        if ((s_misc[1] || total > NM) && a.d_flags) atomicExch(a.d_flags, TO_DEVERR_PATCHES);
+        a.n_patches[rs] = nemit;
+    }
 }
 
 // Second half of the species-road model, one CTA per (road, species):
@@ -895,7 +959,8 @@ to_status species_model(to_ctx ctx, const to_model_args& a, int n_rs) {
     if (a.n_label_types > 0) {
         // labels once per (road, habitable type), then each species' patches
         const size_t smem_l = (size_t)(64 + a.W * a.H) * sizeof(int);
-        const size_t smem_p = (size_t)(64 + a.xres * a.yres + 1 + a.max_patches) * sizeof(int);
+        const size_t smem_p =
+            (size_t)(64 + TO_MAX_HAB * a.xres * a.yres + 1 + a.max_patches) * sizeof(int);
         if (smem_l > ctx->smem_optin || smem_p > ctx->smem_optin)
             return to_set_error(ctx, TO_ERR_UNSUPPORTED, "grid of %d x %d exceeds shared memory",
                                 a.W, a.H);
