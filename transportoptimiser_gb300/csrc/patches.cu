@@ -516,15 +516,30 @@ k_species_patches_lab(to_model_args a) {
         const int r = s_lab[t];
         int cnt = 0;
         float pop = 0.0f, sx = 0.0f, sy = 0.0f;
-        for (int ii = 0; ii < bsx; ++ii)
-            for (int jj = 0; jj < bsy; ++jj) {
-                const int c = (bx * skpx + ii) + (by * skpy + jj) * W;
-                if (L[c] != r) continue;
-                cnt += 1;
-                pop = pop + popmap[c];
-                sx = sx + (float)ii;
-                sy = sy + (float)jj;
+        // cells in the reference's order (x offset outer, y offset inner),
+        // their loads issued four at a time before the in-order sums
+        for (int ii = 0; ii < bsx; ++ii) {
+            const int* Lc = L + (bx * skpx + ii) + (size_t)(by * skpy) * W;
+            const float* Pc = popmap + (bx * skpx + ii) + (size_t)(by * skpy) * W;
+            for (int j0 = 0; j0 < bsy; j0 += 4) {
+                int lv[4];
+                float pv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const bool in = j0 + u < bsy;
+                    lv[u] = in ? Lc[(size_t)(j0 + u) * W] : -1;
+                    pv[u] = in ? Pc[(size_t)(j0 + u) * W] : 0.0f;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (lv[u] == r) {
+                        cnt += 1;
+                        pop = pop + pv[u];
+                        sx = sx + (float)ii;
+                        sy = sy + (float)(j0 + u);
+                    }
             }
+        }
         float v[5];
         finish_patch(cnt, pop, sx, sy, bx, by, skpx, skpy, a.xs, a.ys, a.spa,
                      (float)S.hab_max_pop[h], v);
