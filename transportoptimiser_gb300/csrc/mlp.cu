@@ -3,7 +3,7 @@
 // own kernels.  The reference has no learned surrogate (its GA fitness uses
 // the local-linear grid surrogates, SimulateGPU.cu:5533-5917); this is the
 // learned alternative used for GA screening, with the plain Monte Carlo as
-// the fallback and the judge of its error.
+// the fallback and the measure of its error.
 //
 // One CTA owns a tile of 128 rows (TMEM lane = row) and runs the whole
 // forward and, for training, the whole backward pass on it:

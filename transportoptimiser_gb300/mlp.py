@@ -6,7 +6,7 @@ accumulation) in this library's own forward and backward kernels
 The reference's GA fitness uses local-linear grid surrogates
 (SimulateGPU.cu:5533-5917, ``buildSurrogate*CUDA``); it has no learned
 model.  Here the MLP screens designs, and the plain Monte Carlo stays the
-fallback and the judge of its error.
+fallback and the measure of its error.
 
 Parameter vector layout (FP32, ``NPARAM``): W1[128][16], b1[128],
 W2[128][128], b2[128], W3[3][128], b3[3].

@@ -9,7 +9,7 @@ pairs the batched simulator generates screens each generation (surrogate
 pre-selection): the plain Monte Carlo values the most promising designs -
 the top fraction (25%) by an optimistic score, the predicted fitness plus
 the members' spread - and every design whose members disagree by more than
-the tolerance (10%); it stays the judge of the surrogate's error, and only
+the tolerance (10%); it stays the measure of the surrogate's error, and only
 Monte Carlo values become the incumbent.
 
 Per road the surrogate predicts:
