@@ -216,7 +216,7 @@ to_status tuned_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int N
     cudaEvent_t e0, e1;
     TO_CUDA(ctx, cudaEventCreate(&e0));
     TO_CUDA(ctx, cudaEventCreate(&e1));
-    int best = -1, last = -1;
+    int best = -1;
     const bool feas[3] = {sparse_ok, true, tc_ok};
     for (int c = 0; c < 3; ++c) {
         if (!feas[c]) continue;
@@ -228,7 +228,6 @@ to_status tuned_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int N
         float ms = 0.0f;
         TO_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
         te.ms[c] = ms;
-        last = c;
         if (best < 0 || ms < te.ms[best]) best = c;
     }
     cudaEventDestroy(e0);
@@ -236,7 +235,6 @@ to_status tuned_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int N
     if (best < 0) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "no feasible migration kernel");
     te.choice = best;
     ctx->tune.push_back(te);
-    (void)last;
     *choice = best;
     return TO_OK;
 }
