@@ -561,7 +561,8 @@ def main():
     # contraction's, 2 * P * N^2 * Y per (road, species); the sparse kernel
     # skips the zeros, so its useful (non-zero) FLOPs are reported beside it.
     # DRAM traffic per launch: an ncu capture (dram__bytes_read/write.sum) of
-    # the same kernel on 32 roads read 1.59 MB (the CSC matrices, initial
+    # the same kernel at the generation shape on 64 roads (192 road-species,
+    # 64 paths) read 3.27 MB and wrote nothing (the CSC matrices, initial
     # populations and capacities, proportional to road-species count, not to
     # paths); scaled to this launch's road-species count.
     Nsum2 = float((Ns.astype(np.float64) ** 2).sum())
@@ -571,7 +572,7 @@ def main():
     mte_avg_s = (mte_ms / max(mte_n, 1)) / 1000.0
     achieved_tf = dense_equiv_flops / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
     useful_tf = (useful_flops / mte_avg_s / 1e12) if (useful_flops and mte_avg_s > 0) else None
-    traffic = 1.594368e6 * (args.roads * len(scene.species)) / 96.0
+    traffic = 3.265024e6 * (args.roads * len(scene.species)) / 192.0
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
 
     rov_adj = rov_adjoint_leg(ctx) if rank == 0 and args.rov_leg else None
@@ -612,7 +613,7 @@ def main():
                          "frac": achieved_tf / bf16_peak,
                          "peak_kind": peak_kind + " bf16 dense (TF32 is half, 3xTF32 a sixth)",
                          "traffic": traffic, "traffic_note": "bytes per launch, ncu on "
-                         "32 roads scaled by road-species count",
+                         "64 roads scaled by road-species count",
                          "flops_per_launch": dense_equiv_flops,
                          "useful_flops_per_launch": useful_flops,
                          "useful_achieved": useful_tf,
