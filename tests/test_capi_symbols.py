@@ -74,3 +74,45 @@ int main(void) {
         assert r.returncode == 0, (cc, r.returncode, r.stderr)
         built += 1
     assert built >= 1
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every ctypes mirror of a struct in include/transopt.h has the C
+    compiler's size and field offsets (a mismatch would pass garbage across
+    the boundary without any error)."""
+    import shutil
+    import subprocess
+    from transportoptimiser_gb300 import _capi
+    from transportoptimiser_gb300.adjoint import AdjointProblem
+    pairs = {"to_habitat": _capi.Habitat, "to_species_in": _capi.SpeciesIn,
+             "to_species_out": _capi.SpeciesOut, "to_mte_species": _capi.MteSpecies,
+             "to_mte_problem": _capi.MteProblem, "to_mte_stats": _capi.MteStats,
+             "to_mte_device_problem": _capi.MteDeviceProblem,
+             "to_exp_pv_params": _capi.ExpPvParams, "to_species_desc": _capi.SpeciesDesc,
+             "to_scene": _capi.Scene, "to_eval_opts": _capi.EvalOpts,
+             "to_rov_species": _capi.RovSpecies, "to_rov_problem": _capi.RovProblem,
+             "to_rov_result": _capi.RovResult, "to_adjoint_problem": AdjointProblem}
+    cc = shutil.which("gcc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "transopt.h"', 'int main(void) {']
+    for cname, py in pairs.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", str(ROOT / "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                               text=True).stdout.splitlines():
+        name, field, val = line.split()
+        got[(name, field)] = int(val)
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
