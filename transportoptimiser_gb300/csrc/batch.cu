@@ -22,6 +22,7 @@
 #include <cstring>
 #include <vector>
 
+#include "to_grid.h"
 #include "to_internal.cuh"
 #include "to_model.cuh"
 #include "to_pop.cuh"
@@ -374,6 +375,16 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
         sc->max_patches <= 0 || sc->max_roads <= 0 || sc->max_cells < 0 ||
         sc->max_segments <= 0)
         return TO_ERR_INVALID;
+    {
+        const int r = sc->res;
+        const int xr = (sc->W % r == 0) ? r : r + 1, yr = (sc->H % r == 0) ? r : r + 1;
+        const int sx = (int)std::floor((double)(sc->W - 1) / (double)r);
+        const int sy = (int)std::floor((double)(sc->H - 1) / (double)r);
+        if (!to_blocks_inside(sc->W, sc->H, sx, sy, xr, yr))
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                                "coarse blocks of a %d x %d grid at resolution %d run past it",
+                                sc->W, sc->H, r);
+    }
     cudaSetDevice(ctx->device);
     to_gen g = new to_gen_s();
     g->ctx = ctx;

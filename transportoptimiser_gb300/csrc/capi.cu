@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "to_grid.h"
 #include "to_internal.cuh"
 #include "to_model.cuh"
 #include "to_pop.cuh"
@@ -275,6 +276,10 @@ to_status to_build_patches(to_ctx ctx, int W, int H, int skpx, int skpy,
     if (!ctx || !labels || !pops || !n_patches || W <= 0 || H <= 0 ||
         skpx <= 0 || skpy <= 0 || xres <= 0 || yres <= 0 || max_patches < 0)
         return TO_ERR_INVALID;
+    if (!to_blocks_inside(W, H, skpx, skpy, xres, yres))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "coarse blocks of %d x %d cells run past the %d x %d grid",
+                            skpx, skpy, W, H);
     if (n_regions <= 0) return TO_OK;
     cudaSetDevice(ctx->device);
     size_t n = (size_t)W * H;
@@ -361,6 +366,10 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
     a.skpx = (int)std::floor((double)(W - 1) / (double)res);
     a.skpy = (int)std::floor((double)(H - 1) / (double)res);
     if (a.skpx <= 0 || a.skpy <= 0) return TO_ERR_INVALID;
+    if (!to_blocks_inside(W, H, a.skpx, a.skpy, a.xres, a.yres))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "coarse blocks of a %d x %d grid at resolution %d run past it",
+                            W, H, res);
     a.xs = (float)in->xspacing; a.ys = (float)in->yspacing;
     a.spa = (float)(in->xspacing * in->yspacing);
     a.sem = in->sem; a.max_patches = NM; a.npad = NP;
