@@ -84,6 +84,7 @@ static to_status check_device_flags(to_ctx ctx) {
                          : f == TO_DEVERR_UNION ? "union-find did not converge"
                          : f == TO_DEVERR_PATCHES ? "patch capacity exceeded"
                          : f == TO_DEVERR_SPIN ? "bounded wait expired"
+                         : f == TO_DEVERR_CELL ? "road cell outside the grid"
                          : "device check failed";
         return to_set_error(ctx, f == TO_DEVERR_SPIN ? TO_ERR_TIMEOUT
                                                       : TO_ERR_UNSUPPORTED,

@@ -372,7 +372,11 @@ k_species_patches(to_model_args a) {
         for (int i = threadIdx.x; i < n; i += blockDim.x)
             par[i] = (hab[i] == typ) ? i : -1;
         __syncthreads();
-        for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) par[a.cells[q]] = -1;
+        for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) {
+            const int cc = a.cells[q];        // device inputs: checked here
+            if ((unsigned)cc < (unsigned)n) par[cc] = -1;
+            else if (a.d_flags) atomicExch(a.d_flags, TO_DEVERR_CELL);
+        }
         __syncthreads();
         int nreg = cta_label(n, W, par, s_tmp, a.d_flags);
         if (nreg == 0) continue;
@@ -417,7 +421,11 @@ k_road_labels(to_model_args a) {
     __syncthreads();
     const int c0 = a.cell_off ? a.cell_off[road] : 0;
     const int c1 = a.cell_off ? a.cell_off[road + 1] : 0;
-    for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) par[a.cells[q]] = -1;
+    for (int q = c0 + threadIdx.x; q < c1; q += blockDim.x) {
+        const int cc = a.cells[q];            // device inputs: checked here
+        if ((unsigned)cc < (unsigned)n) par[cc] = -1;
+        else if (a.d_flags) atomicExch(a.d_flags, TO_DEVERR_CELL);
+    }
     __syncthreads();
     cta_label(n, W, par, s_tmp, a.d_flags);
     int* out = a.labels + ((size_t)road * T + ti) * n;

@@ -53,7 +53,8 @@ struct to_ctx_s {
 
 // device-side error codes written to ctx->d_flags[0]
 enum { TO_DEVERR_NONE = 0, TO_DEVERR_REGIONS = 1, TO_DEVERR_UNION = 2,
-       TO_DEVERR_PATCHES = 3, TO_DEVERR_SPIN = 4, TO_DEVERR_PLAN = 5 };
+       TO_DEVERR_PATCHES = 3, TO_DEVERR_SPIN = 4, TO_DEVERR_PLAN = 5,
+       TO_DEVERR_CELL = 6 };
 
 to_status to_set_error(to_ctx ctx, to_status s, const char* fmt, ...);
 to_status to_check_cuda(to_ctx ctx, cudaError_t e, const char* what);
