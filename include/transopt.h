@@ -193,7 +193,14 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
  * it before any stream capture.  All calls share the array: calls that
  * overlap on the GPU race on it.  Work is enqueued on `stream`
  * (cudaStream_t, may be 0); d_stats receives [n_species][5] doubles: mean,
- * SD, standard error, P(end < 0.2 x initial), initial population. */
+ * SD, standard error, P(end < 0.2 x initial), initial population.
+ * n_patches lives in device memory, so the host cannot check it: a species
+ * whose n_patches[s] is negative or above npad gets NaN in all five of its
+ * statistics (nothing is read past its rows) while the call still returns
+ * TO_OK; NaN statistics therefore mean a patch count outside [0, npad].
+ * n_species is at most 65535 (TO_ERR_UNSUPPORTED above).  A CUDA error
+ * already pending on the calling thread is reported as TO_ERR_CUDA before
+ * anything is enqueued, and left pending for its owner. */
 typedef struct {
     int n_species, n_paths, n_years;
     int npad;                /* row stride of the arrays below, multiple of 4 */
@@ -465,6 +472,23 @@ to_status to_evaluate_roads_d(to_ctx ctx, to_gen gen, int n_roads,
                               const int* cell_off, const int* cells,
                               const int* seg_off, const double* segs,
                               const to_eval_opts* opts, double* results);
+
+/* Inspection of the last evaluation of a scene (no reference counterpart;
+ * for tests and tools that check a generation road by road).  Both wait for
+ * the context stream.  to_gen_end_pops: the n_paths per-path end
+ * populations of (road, species) (n_paths must be the last call's
+ * mte_paths).  to_gen_species_model: that road's species model as the
+ * migration kernel read it - patch count, initial populations and
+ * capacities [N], and the migration matrices expanded to dense
+ * destination-major [C][N][N] floats (from the packed columns when the
+ * sparse kernel ran, else from the dense form); nnz[C] (optional) gets the
+ * packed non-zero counts, -1 where none were packed.  Arrays may be NULL;
+ * N > max_patches is TO_ERR_INVALID with *n_patches set. */
+to_status to_gen_end_pops(to_ctx ctx, to_gen gen, int road, int species, int n_paths,
+                          float* end_pops);
+to_status to_gen_species_model(to_ctx ctx, to_gen gen, int road, int species, int max_patches,
+                               int* n_patches, float* init_pops, float* caps, float* mmm,
+                               int* nnz);
 
 /* ------------------------------------------------------------------------
  * Learned surrogate (no counterpart in the reference, whose GA fitness uses

@@ -318,26 +318,38 @@ float or_grouped_sum(const float* v, int N) {
 typedef struct {
     int p0, p1, n_years, N, species, road, sem;
     float dt;
-    const float *params, *init, *caps, *mmm;
+    const float *params, *init, *caps;
+    /* compressed columns of the destination-major matrix: destination k's
+     * non-zeros are origins idx[ptr[k] .. ptr[k+1]) ascending, with values */
+    const int* ptr;
+    const int* idx;
+    const float* val;
     uint64_t seed;
     float* out;
 } mte_job;
 
+/* One path at a time, as mteKernel does (one thread per path,
+ * SimulateGPU.cu:595-717): the migration walks destination k's compressed
+ * column (mteKernel :628-635 reads the dense2Sparse CSC lists) in ascending
+ * origin order with fused multiply-adds; the growth normals come four per
+ * Philox call (the patch group's block), which are the same bits as one
+ * to_normal1 per patch. */
 static void mte_paths(const mte_job* j) {
     int N = j->N;
     int N4 = (N + 3) & ~3;
-    float* pop = (float*)malloc(sizeof(float) * (size_t)N);
-    float* mig = (float*)malloc(sizeof(float) * (size_t)N);
+    float* pop = (float*)malloc(sizeof(float) * (size_t)N4);
+    float* mig = (float*)malloc(sizeof(float) * (size_t)N4);
     const float* sp = j->params;
     float sj2 = sp[5] * sp[5];
+    const uint32_t grp0 = (uint32_t)((j->species * N4) >> 2);
     for (int p = j->p0; p < j->p1; ++p) {
         for (int k = 0; k < N; ++k) pop[k] = j->init[k];
         float gm = sp[0];
         for (int t = 0; t < j->n_years; ++t) {
             for (int k = 0; k < N; ++k) {
-                const float* col = j->mmm + (size_t)k * N;
                 float acc = 0.0f;
-                for (int l = 0; l < N; ++l) acc = fmaf(pop[l], col[l], acc);
+                for (int e = j->ptr[k]; e < j->ptr[k + 1]; ++e)
+                    acc = fmaf(pop[j->idx[e]], j->val[e], acc);
                 mig[k] = acc;
             }
             float uj = to_uniform1(j->seed, TO_STREAM_SP_JUMP, j->road, p, t, j->species);
@@ -349,13 +361,16 @@ static void mte_paths(const mte_job* j) {
                                       : (zj * sp[5] - sj2 / 2.0f);
             gm = gm + sp[4] * (sp[1] - gm) * j->dt + gm * brown
                  + (to_expf(jsz) - 1.0f) * gm * jump;
-            int lane0 = j->species * N4;
-            for (int k = 0; k < N; ++k) {
-                float z = to_normal1(j->seed, TO_STREAM_GROWTH, j->road, p, t, lane0 + k);
-                float gr = fmaf(sp[7] * z, gm, gm);
-                float m = mig[k];
-                float c = j->caps[k];
-                pop[k] = m * (1.0f + gr * (c - m) / c);
+            for (int k0 = 0; k0 < N; k0 += 4) {
+                float z[4];
+                to_normal4(j->seed, TO_STREAM_GROWTH, j->road, p, t, grp0 + (k0 >> 2), z);
+                for (int q = 0; q < 4 && k0 + q < N; ++q) {
+                    const int k = k0 + q;
+                    float gr = fmaf(sp[7] * z[q], gm, gm);
+                    float m = mig[k];
+                    float c = j->caps[k];
+                    pop[k] = m * (1.0f + gr * (c - m) / c);
+                }
             }
         }
         float e = (j->n_years == 0) ? or_grouped_sum(j->init, N)
@@ -368,6 +383,25 @@ static void mte_paths(const mte_job* j) {
 
 static void* mte_thread(void* a) { mte_paths((const mte_job*)a); return NULL; }
 
+/* dense2Sparse (SimulateGPU.cu:5973-5996) of a destination-major N x N
+ * matrix: entries > 0 of row k (destination k) in ascending origin order.
+ * The skipped entries are exact zeros, so fmaf over the list gives the bits
+ * of fmaf over the whole dense row.  Returns the non-zero count. */
+int or_pack_csc(int N, const float* mmm, int* ptr, int* idx, float* val) {
+    int n = 0;
+    for (int k = 0; k < N; ++k) {
+        ptr[k] = n;
+        const float* row = mmm + (size_t)k * N;
+        for (int l = 0; l < N; ++l)
+            if (row[l] > 0.0f) {
+                if (idx) { idx[n] = l; val[n] = row[l]; }
+                ++n;
+            }
+    }
+    ptr[N] = n;
+    return n;
+}
+
 void or_simulate_mte(int n_paths, int n_years, int N, float dt,
                      const float* params8, const float* init_pops,
                      const float* caps, const float* mmm, uint64_t seed,
@@ -375,6 +409,11 @@ void or_simulate_mte(int n_paths, int n_years, int N, float dt,
                      float* end_pops) {
     if (n_threads < 1) n_threads = 1;
     if (n_threads > 256) n_threads = 256;
+    int* ptr = (int*)malloc(sizeof(int) * (size_t)(N + 1));
+    int nnz = or_pack_csc(N, mmm, ptr, NULL, NULL);
+    int* idx = (int*)malloc(sizeof(int) * (size_t)(nnz > 0 ? nnz : 1));
+    float* val = (float*)malloc(sizeof(float) * (size_t)(nnz > 0 ? nnz : 1));
+    or_pack_csc(N, mmm, ptr, idx, val);
     mte_job jobs[256];
     pthread_t th[256];
     int per = (n_paths + n_threads - 1) / n_threads;
@@ -384,12 +423,18 @@ void or_simulate_mte(int n_paths, int n_years, int N, float dt,
         if (p1 > n_paths) p1 = n_paths;
         if (p0 >= p1) break;
         mte_job j = {p0, p1, n_years, N, species, road, sem, dt, params8,
-                     init_pops, caps, mmm, seed, end_pops};
+                     init_pops, caps, ptr, idx, val, seed, end_pops};
         jobs[used++] = j;
     }
-    if (used == 1) { mte_paths(&jobs[0]); return; }
-    for (int i = 0; i < used; ++i) pthread_create(&th[i], NULL, mte_thread, &jobs[i]);
-    for (int i = 0; i < used; ++i) pthread_join(th[i], NULL);
+    if (used == 1) {
+        mte_paths(&jobs[0]);
+    } else {
+        for (int i = 0; i < used; ++i) pthread_create(&th[i], NULL, mte_thread, &jobs[i]);
+        for (int i = 0; i < used; ++i) pthread_join(th[i], NULL);
+    }
+    free(ptr);
+    free(idx);
+    free(val);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -86,6 +86,9 @@ int or_species_model(const or_species_in* in, or_species_out* out);
 
 /* SimulateGPU.cu:595-717 + 3650-3864.  mmm: N*N destination-major for the
  * highest-flow control.  end_pops: n_paths floats. */
+/* compressed columns of a destination-major N x N matrix (entries > 0,
+ * ascending origin order); idx / val may be NULL to count only */
+int or_pack_csc(int N, const float* mmm, int* ptr, int* idx, float* val);
 void or_simulate_mte(int n_paths, int n_years, int N, float dt,
                      const float* params8, const float* init_pops,
                      const float* caps, const float* mmm, uint64_t seed,

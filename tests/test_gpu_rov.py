@@ -195,3 +195,46 @@ def test_rov_batch_edges(ctx):
         sg.simulateROVCUDA_batch([prob(models[0], 130), prob(models[1], 130, Y=9)], ctx=ctx)
     with pytest.raises(TransOptError):
         sg.simulateROVCUDA_batch([prob(models[0], 64), prob(models[1], 64, road=1)], ctx=ctx)
+
+
+@pytest.mark.parametrize("S,R,P,Y", [(2, 16, 3000, 50), (1, 8, 900, 20)])
+def test_rov_touched_queries_match_full_grid(ctx, S, R, P, Y):
+    """Without the regression surfaces in the output, each year's regressions
+    are fitted only at the grid queries the backward pass reads.  Decisions,
+    continuation values, the road value and its statistics stay identical
+    to the run that fits (and returns) the whole grid, and to the oracle."""
+    sc = synth.rov_road(1, n_species=S)
+    models = [po.species_model(sc, sc.species[s], sc.roads[0], sem=1) for s in range(S)]
+    rp = rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                 n_processes=3, demand=True, seed=21, road=3)
+    full = sg.simulateROVCUDA(rp, migration=MIG_SPARSE_FP32, ctx=ctx)
+    part = sg.simulateROVCUDA(rp, want=("cond_exp", "opt_cont", "unit_profits", "adj_pops"),
+                              migration=MIG_SPARSE_FP32, ctx=ctx)
+    for k in ("cond_exp", "opt_cont", "unit_profits", "adj_pops"):
+        assert np.array_equal(full[k], part[k]), k
+    assert np.array_equal(full["stats"], part["stats"])
+    assert full["value_se"] == part["value_se"] and full["n_best"] == part["n_best"]
+    orc = po.simulate_rov(rp, threads=16)
+    assert np.array_equal(part["opt_cont"], orc["opt_cont"])
+    assert np.array_equal(part["cond_exp"].astype(np.float32), orc["cond_exp"])
+
+
+def test_rov_batch_touched_queries_match_full_grid(ctx):
+    """The batched form (one road per (road, control) regression group) with
+    and without the surfaces: identical results for every road."""
+    sc = synth.rov_road(0, n_species=2)
+    rng = np.random.Generator(np.random.Philox(5))
+    roads = [sc.roads[0]] + [synth.random_road(sc.W, sc.H, int(rng.integers(8, 40)), rng)
+                             for _ in range(5)]
+    probs = []
+    for i, rd in enumerate(roads):
+        ms = [po.species_model(sc, sp, rd, sem=1) for sp in sc.species]
+        probs.append(rov_problem_from_models(ms, sc, n_paths=640, n_years=30, dim_res=16, sem=1,
+                                             n_processes=3, demand=True, road=10 + i))
+    full = sg.simulateROVCUDA_batch(probs, ctx=ctx)
+    part = sg.simulateROVCUDA_batch(probs, want=("cond_exp", "opt_cont"), ctx=ctx)
+    for f, p in zip(full, part):
+        assert np.array_equal(f["cond_exp"], p["cond_exp"])
+        assert np.array_equal(f["opt_cont"], p["opt_cont"])
+        assert np.array_equal(f["stats"], p["stats"])
+        assert f["value_se"] == p["value_se"]

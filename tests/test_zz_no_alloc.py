@@ -71,3 +71,30 @@ def test_noalloc_rejects_oversized_problem(ctx):
     d_stats = torch.zeros(5, dtype=torch.float64, device="cuda")
     st = lib.to_simulate_mte_noalloc_d(None, C.byref(prob), C.c_void_p(d_stats.data_ptr()))
     assert st == 6          # TO_ERR_UNSUPPORTED, nothing launched
+
+
+def test_noalloc_patch_count_above_npad_gives_nan_statistics(ctx):
+    """n_patches lives in the caller's device memory, so only the kernels can
+    see that it exceeds npad: that species' statistics are NaN (nothing is
+    read past its rows), the call returns TO_OK, and the other species are
+    unaffected."""
+    torch = pytest.importorskip("torch")
+    lib = _capi.load()
+    sc = synth.rov_road(0, n_species=2)
+    models = [po.species_model(sc, sc.species[s], sc.roads[0], sem=0) for s in range(2)]
+    params = [sc.species[s].params for s in range(2)]
+    P, Y = 256, 20
+    prob, keep = _device_problem(torch, models, params, P, Y, 3, 7, 0)
+    n_dev = keep[0]
+    n_dev[1] = prob.npad + 4          # the last species claims more patches than its rows hold
+    torch.cuda.synchronize()
+    d_stats = torch.zeros(2 * 5, dtype=torch.float64, device="cuda")
+    st = lib.to_simulate_mte_noalloc_d(None, C.byref(prob), C.c_void_p(d_stats.data_ptr()))
+    assert st == 0
+    torch.cuda.synchronize()
+    got = d_stats.cpu().numpy().reshape(2, 5)
+    assert np.isnan(got[1]).all(), got[1]
+    _, want = sg.simulateMTECUDA(models, params, P, Y, seed=3, road=7, sem=0,
+                                 migration=_capi.MIG_SIMT_FP32, ctx=ctx)
+    exp = [want[0][k] for k in ("mean", "sd", "se", "p_below", "init_total")]
+    assert list(got[0]) == exp

@@ -177,6 +177,10 @@ SIGNATURES = {
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
     "to_ctx_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "to_gen_end_pops": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                  c_float_p]),
+    "to_gen_species_model": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                       c_int_p, c_float_p, c_float_p, c_float_p, c_int_p]),
     "to_select_samples": (C.c_int, [C.c_void_p, C.c_int, c_double_p, C.c_int, c_double_p,
                                     C.c_int, C.c_int, c_int_p]),
     "to_interpolate_surrogate": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, c_double_p,

@@ -85,14 +85,20 @@ def build_oracle(force: bool = False) -> Path:
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     if force or _stale(ORACLE_LIB, deps):
         cc = shutil.which("gcc") or "cc"
-        _run([cc, "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
+        _run([cc, "-O3", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared",
               "-pthread", *map(str, srcs), "-o", str(ORACLE_LIB), "-lm"])
     return ORACLE_LIB
 
 
+def reference_dir() -> Path:
+    """Where the reference tree is mounted (TO_REFERENCE_DIR, the same
+    variable oracle/build_ref.sh reads)."""
+    return Path(os.environ.get("TO_REFERENCE_DIR", "/root/reference"))
+
+
 def build_reference_pin() -> None:
     script = ORACLE_DIR / "build_ref.sh"
-    if Path("/root/reference").exists() and script.exists():
+    if reference_dir().exists() and script.exists():
         _run(["sh", str(script)])
 
 

@@ -66,6 +66,11 @@ struct to_gen_s {
     uint64_t graph_key = 0;
     int plan_ne = 0, plan_cap = 0, plan_choice = -1;
     uint64_t graph_launches = 0;         // kernels in the captured generation
+    // what the last evaluation left readable (to_gen_species_model /
+    // to_gen_end_pops): its shape and which migration-matrix forms it wrote
+    int last_R = 0, last_paths = 0;
+    bool last_dense = false, last_csc = false;
+    bool graph_dense = false, graph_csc = false;
 };
 
 namespace {
@@ -291,6 +296,8 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     else TO_TRY(tuned_choice(ctx, g, m, RS, NE, sparse_ok, NE <= 512, &choice));
     TO_TRY(tail(ctx, g, m, RS, choice, d_results_out));
     if (plan) { plan[0] = NE; plan[1] = g->csc.cap_smem; plan[2] = choice; }
+    g->last_R = R; g->last_paths = o->mte_paths;
+    g->last_dense = !packed; g->last_csc = try_sparse;
     return TO_OK;
 }
 
@@ -313,6 +320,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     if (g->exec && g->graph_key == key) {
         TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
         ctx->launches += g->graph_launches;
+        g->last_R = R; g->last_paths = o->mte_paths;
+        g->last_dense = g->graph_dense; g->last_csc = g->graph_csc;
         return TO_OK;
     }
     if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
@@ -361,6 +370,10 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     g->graph_key = key;
     g->plan_ne = ne; g->plan_cap = cap; g->plan_choice = choice;
     g->graph_launches = ctx->launches - l0;
+    // the capture ran nothing: the planning pass above left the buffers; a
+    // replay leaves the forms the captured kernels write
+    g->graph_dense = (choice != CH_SPARSE);
+    g->graph_csc = (choice == CH_SPARSE);
     return TO_OK;
 }
 
@@ -640,6 +653,83 @@ to_status to_road_features(to_ctx ctx, to_gen g, int R, const int* seg_off, cons
     if (f != 0) {
         cudaMemsetAsync(ctx->d_flags, 0, sizeof(int), ctx->stream);
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "road cells exceed the scene capacity");
+    }
+    return TO_OK;
+}
+
+to_status to_gen_end_pops(to_ctx ctx, to_gen g, int road, int species, int n_paths,
+                          float* out) {
+    if (!ctx || !g || !out || road < 0 || road >= g->last_R || species < 0 ||
+        species >= g->S || n_paths != g->last_paths || !g->d_end)
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const size_t rs = (size_t)road * g->S + species;
+    TO_CUDA(ctx, cudaMemcpy(out, g->d_end + rs * n_paths, (size_t)n_paths * sizeof(float),
+                            cudaMemcpyDeviceToHost));
+    return TO_OK;
+}
+
+to_status to_gen_species_model(to_ctx ctx, to_gen g, int road, int species, int max_patches,
+                               int* n_patches, float* init_pops, float* caps, float* mmm,
+                               int* nnz) {
+    if (!ctx || !g || !n_patches || road < 0 || road >= g->last_R || species < 0 ||
+        species >= g->S || max_patches <= 0)
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const size_t rs = (size_t)road * g->S + species;
+    const int C = g->C, NP = g->NP;
+    int N = 0;
+    TO_CUDA(ctx, cudaMemcpy(&N, g->d_np + rs, sizeof(int), cudaMemcpyDeviceToHost));
+    *n_patches = N;
+    if (N > max_patches || N > NP) return to_set_error(ctx, TO_ERR_INVALID, "%d patches", N);
+    if (init_pops)
+        TO_CUDA(ctx, cudaMemcpy(init_pops, g->d_ip + rs * NP, (size_t)N * sizeof(float),
+                                cudaMemcpyDeviceToHost));
+    if (caps)
+        TO_CUDA(ctx, cudaMemcpy(caps, g->d_cp + rs * NP, (size_t)N * sizeof(float),
+                                cudaMemcpyDeviceToHost));
+    std::vector<int> nz(C, -1);
+    if (g->last_csc)
+        TO_CUDA(ctx, cudaMemcpy(nz.data(), g->csc.nnz + rs * C, C * sizeof(int),
+                                cudaMemcpyDeviceToHost));
+    if (nnz) for (int c = 0; c < C; ++c) nnz[c] = nz[c];
+    if (!mmm) return TO_OK;
+    std::vector<float> dense((size_t)NP * NP);
+    std::vector<int> ptr(NP + 1);
+    std::vector<uint16_t> idx;
+    std::vector<float> val;
+    for (int c = 0; c < C; ++c) {
+        const size_t mtx = rs * C + c;
+        float* o = mmm + (size_t)c * N * N;
+        if (g->last_csc && nz[c] >= 0) {
+            // the packed form the sparse kernel read, expanded
+            TO_CUDA(ctx, cudaMemcpy(ptr.data(), g->csc.ptr + mtx * (NP + 1),
+                                    (NP + 1) * sizeof(int), cudaMemcpyDeviceToHost));
+            idx.resize(nz[c] > 0 ? nz[c] : 1);
+            val.resize(nz[c] > 0 ? nz[c] : 1);
+            if (nz[c] > 0) {
+                TO_CUDA(ctx, cudaMemcpy(idx.data(), g->csc.idx + mtx * g->csc.cap,
+                                        nz[c] * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+                TO_CUDA(ctx, cudaMemcpy(val.data(), g->csc.val + mtx * g->csc.cap,
+                                        nz[c] * sizeof(float), cudaMemcpyDeviceToHost));
+            }
+            memset(o, 0, (size_t)N * N * sizeof(float));
+            for (int k = 0; k < N; ++k)
+                for (int e = ptr[k]; e < ptr[k + 1]; ++e) {
+                    if (e < 0 || e >= nz[c] || idx[e] >= N)
+                        return to_set_error(ctx, TO_ERR_INVALID, "packed matrix %d", c);
+                    o[(size_t)k * N + idx[e]] = val[e];
+                }
+        } else if (g->last_dense) {
+            TO_CUDA(ctx, cudaMemcpy(dense.data(), g->d_mmm + mtx * NP * NP,
+                                    (size_t)NP * NP * sizeof(float), cudaMemcpyDeviceToHost));
+            for (int k = 0; k < N; ++k)
+                memcpy(o + (size_t)k * N, dense.data() + (size_t)k * NP, N * sizeof(float));
+        } else {
+            return to_set_error(ctx, TO_ERR_INVALID, "no matrix form of control %d", c);
+        }
     }
     return TO_OK;
 }

@@ -594,12 +594,15 @@ k_knn_rov(to_rov_args a, int t) {
     const int P = a.P, Q = a.Q;
     const int lane = threadIdx.x & 31;
     WarpScratch& ws = reinterpret_cast<WarpScratch*>(sm_raw)[threadIdx.x >> 5];
-    const int items = a.G * Q;                 // (group, query), group g = road*C + control
+    // (group, query) items, group g = road*C + control: every grid query, or
+    // the year's list of the queries the backward pass reads
+    const int items = a.touched ? *a.qcount : a.G * Q;
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.knn_next, 1);
         item = __shfl_sync(kFull, item, 0);
         if (item >= items) break;
+        if (a.touched) item = a.qlist[item];
         const int c = item / Q, qi = item - c * Q;
         const int n = a.npts[c], k = a.kc[c];
         if (n < 3 || k <= 0) continue;           // k_knn_solve writes 0
@@ -690,7 +693,11 @@ k_knn_rov(to_rov_args a, int t) {
 // group c (0 where the group has too few points)
 template <int D>
 __global__ void k_knn_solve(to_rov_args a, int t) {
-    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.touched) {
+        if (item >= *a.qcount) return;
+        item = a.qlist[item];
+    }
     if (item >= a.G * a.Q) return;
     const int c = item / a.Q, qi = item - c * a.Q;
     const size_t blk = (size_t)a.R * D + 2 * (size_t)a.Q;

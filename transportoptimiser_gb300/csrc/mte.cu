@@ -150,7 +150,9 @@ k_mte_simt(to_mte_args a) {
 }
 
 // Per (road, species) statistics in FP64: mean, population SD
-// (Simulator.cpp:184-191), standard error and P(end < 0.2 init).
+// (Simulator.cpp:184-191), standard error and P(end < 0.2 init).  A patch
+// count outside [0, NP] (a caller's device input that the host could not
+// check) gives NaN in all five and reads nothing past the species' row.
 __global__ void k_mte_stats(int P, const float* __restrict__ end_pops,
                             const float* __restrict__ init_pops, int NP,
                             const int* __restrict__ n_patches,
@@ -159,10 +161,14 @@ __global__ void k_mte_stats(int P, const float* __restrict__ end_pops,
     const float* e = end_pops + (size_t)rs * P;
     __shared__ double s_sum[32], s_sq[32], s_cnt[32];
     __shared__ double s_init;
+    const int N = n_patches[rs];
+    if (N < 0 || N > NP) {
+        if (threadIdx.x < 5) stats[5 * (size_t)rs + threadIdx.x] = (double)NAN;
+        return;
+    }
     if (threadIdx.x == 0) {
         double t = 0.0;
         const float* ip = init_pops + (size_t)rs * NP;
-        int N = n_patches[rs];
         for (int k = 0; k < N; ++k) t += (double)ip[k];
         s_init = t;
     }
@@ -279,8 +285,12 @@ extern "C" to_status to_simulate_mte_noalloc_d(void* stream,
         pr->npad <= 0 || pr->npad % 4 != 0 || pr->npad > 1020 || !pr->n_patches ||
         !pr->params || !pr->init_pops || !pr->caps || !pr->mmm)
         return TO_ERR_INVALID;
-    if ((long long)pr->n_species * pr->n_paths > TO_NOALLOC_MTE_MAX_VALUES)
+    if ((long long)pr->n_species * pr->n_paths > TO_NOALLOC_MTE_MAX_VALUES ||
+        pr->n_species > 65535)      // species are the grid's y dimension
         return TO_ERR_UNSUPPORTED;
+    // an error left pending by the caller's own work is not this call's:
+    // report it without clearing it, and launch nothing
+    if (cudaPeekAtLastError() != cudaSuccess) return TO_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
         cudaGetLastError();
@@ -323,7 +333,7 @@ extern "C" to_status to_simulate_mte_noalloc_d(void* stream,
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (cudaFuncSetAttribute(k_mte_simt, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem) != cudaSuccess) {
-        cudaGetLastError();
+        cudaGetLastError();   // this call's own error (none was pending)
         return TO_ERR_CUDA;
     }
     dim3 grid((a.n_paths + a.tile_paths - 1) / a.tile_paths, a.S);

@@ -492,6 +492,70 @@ __global__ void __launch_bounds__(256) k_lsm_norm(to_rov_args a) {
     }
 }
 
+// Touched-query mode, corrected semantics: k_rov_backward at year t reads
+// control c's regression block of the path's road at the 2^d corners of
+// the cell holding the path's own state for c (to_lsm_interp), for every
+// control valid for the path (decide_interior).  Mark exactly those grid
+// queries; k_lsm_list compacts the marks into the year's work list and
+// clears them again.  The reads happen after this year's axes are written
+// (k_lsm_stats), so the corners are the ones the backward pass will read.
+__global__ void __launch_bounds__(256) k_lsm_mark(to_rov_args a, int t) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p == 0) *a.qcount = 0;
+    if (p >= a.PT) return;
+    const int C = a.C, S = a.S, d = S + 1, R = a.R;
+    const int r = p / a.P;
+    float state[TO_ROV_MAXC * (TO_LSM_MAXD - 1) + 1];
+    for (int c = 0; c < C; ++c)
+        for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
+    const int sy = a.Y + 1;
+    const float prof = unit_profit(a, p, t, sy, sy);
+    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
+    for (int c = 0; c < C; ++c) {
+        bool valid = true;
+        for (int s = 0; s < S; ++s)
+            if (state[c * S + s] < threshold(a, s) && c > 0) { valid = false; break; }
+        if (!valid) continue;
+        const size_t g = (size_t)r * C + c;
+        const float* rb = a.reg + ((size_t)t * a.G + g) * blk;
+        int li[TO_LSM_MAXD];
+        for (int j = 0; j < d; ++j) {
+            const float v = (j < S) ? state[c * S + j] : prof;
+            li[j] = to_lsm_lower_index(v, rb[j * R], rb[j * R + R - 1], R);
+        }
+        unsigned char* mk = a.qmark + g * a.Q;
+        for (int corner = 0; corner < (1 << d); ++corner) {
+            int idx = 0;
+            for (int j = 0; j < d; ++j) idx = idx * R + li[j] + ((corner >> (d - 1 - j)) & 1);
+            mk[idx] = 1;
+        }
+    }
+}
+
+// compaction of the year's marks into flat items g*Q + q (any order: each
+// item writes only its own outputs), clearing them for the next year
+__global__ void __launch_bounds__(1024) k_lsm_list(to_rov_args a) {
+    __shared__ int s_w[32];
+    __shared__ int s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const size_t total = (size_t)a.G * a.Q;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool on = i < total && a.qmark[i] != 0;
+    const unsigned b = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) s_w[warp] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int w = 0; w < nw; ++w) { const int v = s_w[w]; s_w[w] = tot; tot += v; }
+        s_base = tot > 0 ? atomicAdd(a.qcount, tot) : 0;
+    }
+    __syncthreads();
+    if (on) {
+        a.qlist[s_base + s_w[warp] + __popc(b & ((1u << lane) - 1u))] = (int)i;
+        a.qmark[i] = 0;
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -690,6 +754,11 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
                        const to_csc* csc) {
     if (a.algo == 6 && (!csc || !a.popsY || !a.gmY || a.nr != 1))
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "ALGO6 needs the sparse forward pass, one road");
+    if (a.touched && (a.sem != 1 || a.algo != 4 || !a.qmark || !a.qlist || !a.qcount ||
+                      (size_t)a.G * a.Q > (size_t)0x7fffffff))
+        return to_set_error(ctx, TO_ERR_INVALID, "touched-query mode: sem 1, ALGO4, scratch");
+    if (a.touched)
+        TO_CUDA(ctx, cudaMemsetAsync(a.qmark, 0, (size_t)a.G * a.Q, ctx->stream));
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
     if (a.lblocks != (a.PT + kLsmChunk - 1) / kLsmChunk || (a.nr > 1 && a.P < kLsmMinPaths))
@@ -705,8 +774,14 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
         k_lsm_stats<<<(a.nr + 127) / 128, 128, 0, ctx->stream>>>(a, t, a.lblocks);
         TO_LAUNCHED(ctx);
         k_lsm_norm<<<fblocks, 256, 0, ctx->stream>>>(a);
-        to_prof_end(ctx);
         TO_LAUNCHED(ctx);
+        if (a.touched) {
+            k_lsm_mark<<<(a.PT + 255) / 256, 256, 0, ctx->stream>>>(a, t);
+            TO_LAUNCHED(ctx);
+            k_lsm_list<<<(int)(((size_t)a.G * a.Q + 1023) / 1024), 1024, 0, ctx->stream>>>(a);
+            TO_LAUNCHED(ctx);
+        }
+        to_prof_end(ctx);
         TO_TRY(knn_rov(ctx, a, t));      // kNN and the local linear regressions
         to_prof_begin(ctx, "rov_backward");
         k_rov_backward<<<pblocks, tpb, 0, ctx->stream>>>(a, t);

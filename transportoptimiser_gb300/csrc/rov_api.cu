@@ -157,6 +157,12 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     acc((size_t)RS * C * (NP + 1) * 4); acc((size_t)RS * C * cap * 2); acc((size_t)RS * C * cap * 4);
     acc((size_t)RS * C * 4);
     if (algo == 6) { acc((size_t)Y * S * NP * P * 4); acc((size_t)Y * S * P * 4); }
+    // regressions fitted only where the backward pass reads them, unless
+    // the caller asks for the surfaces (corrected semantics, ALGO4)
+    bool want_reg = false;
+    for (int r = 0; r < NR; ++r) want_reg |= results[r].regression != nullptr;
+    const bool touched = pr->sem == 1 && algo == 4 && !want_reg;
+    if (touched) { acc((size_t)G * Q); acc((size_t)G * Q * 4); acc(4); }
     TO_TRY(to_arena_reserve(ctx, bytes + 4096));
     TO_CUDA(ctx, cudaMemsetAsync(ctx->arena, 0, bytes, ctx->stream));
     to_rov_args a;
@@ -219,6 +225,13 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
         a.popsY = to_arena_take<float>(ctx, (size_t)Y * S * NP * P);
         a.gmY = to_arena_take<float>(ctx, (size_t)Y * S * P);
     }
+    if (touched) {
+        a.touched = 1;
+        a.qmark = to_arena_take<unsigned char>(ctx, (size_t)G * Q);
+        a.qlist = to_arena_take<int>(ctx, (size_t)G * Q);
+        a.qcount = to_arena_take<int>(ctx, 1);
+        if (!a.qcount) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
+    }
     if (!csc.nnz || (algo == 6 && !a.gmY)) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
     TO_TRY(up(ctx, d_mmm, mmm.data(), mmm.size()));
     TO_TRY(up(ctx, d_ip, ip.data(), ip.size()));
@@ -280,11 +293,8 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     TO_TRY(fetch_rows(0, a.condExp, (size_t)Y));
     TO_TRY(fetch_rows(1, a.unitProfits, (size_t)Y));
     TO_TRY(fetch_rows(2, a.adjPops, (size_t)Y * S));
-    bool want_reg = false, want_oc = false;
-    for (int r = 0; r < NR; ++r) {
-        want_reg |= results[r].regression != nullptr;
-        want_oc |= results[r].opt_cont != nullptr;
-    }
+    bool want_oc = false;
+    for (int r = 0; r < NR; ++r) want_oc |= results[r].opt_cont != nullptr;
     if (want_reg) {
         f.resize((size_t)Y * G * blk);
         TO_TRY(down(ctx, f.data(), a.reg, (size_t)Y * G * blk));

@@ -69,6 +69,13 @@ struct to_rov_args {
     int* knn_next;                    // work counter of the kNN kernel
     float* knn_acc;                   // [G][Q][(d+1)(d+2)] normal equations per query
     int kmax;
+    // touched-query mode (corrected semantics, ALGO4, surfaces not
+    // returned): a year's regressions are fitted only at the grid queries
+    // some path's interpolation reads; the others are never read
+    int touched;
+    unsigned char* qmark;             // [G][Q] marks of the current year (kept zero between years)
+    int* qlist;                       // [G*Q] flat items g*Q + q of the marked queries
+    int* qcount;                      // number of entries in qlist
     // outputs (device)
     float* reg;                       // [Y][G][R*d + 2Q]
     float* condExp;                   // [Y][PT]

@@ -114,6 +114,35 @@ class Generation:
             C.c_void_p(d_seg_off), C.c_void_p(d_segs), C.byref(opts),
             C.c_void_p(d_results)), "to_evaluate_roads_d")
 
+    def end_pops(self, road: int, species: int, n_paths: int) -> np.ndarray:
+        """Per-path end populations of (road, species) from the last call."""
+        out = np.zeros(n_paths, np.float32)
+        self.ctx.check(self.ctx.lib.to_gen_end_pops(self.ctx.handle, self.handle, road, species,
+                                                    n_paths, ptr(out, C.c_float)),
+                       "to_gen_end_pops")
+        return out
+
+    def species_model(self, road: int, species: int, max_patches: int = 1024) -> dict:
+        """The species model the last call's migration kernel read: N, initial
+        populations, capacities, dense destination-major matrices [C][N][N]
+        and the packed non-zero counts (-1: none packed)."""
+        n = C.c_int(0)
+        ip = np.zeros(max_patches, np.float32)
+        cp = np.zeros(max_patches, np.float32)
+        Cn = self.scene.n_controls
+        nnz = np.zeros(Cn, np.int32)
+        self.ctx.check(self.ctx.lib.to_gen_species_model(
+            self.ctx.handle, self.handle, road, species, max_patches, C.byref(n),
+            ptr(ip, C.c_float), ptr(cp, C.c_float), None, ptr(nnz, C.c_int)),
+            "to_gen_species_model")
+        N = n.value
+        mmm = np.zeros(Cn * N * N, np.float32)
+        self.ctx.check(self.ctx.lib.to_gen_species_model(
+            self.ctx.handle, self.handle, road, species, max_patches, C.byref(n), None, None,
+            ptr(mmm, C.c_float), None), "to_gen_species_model")
+        return dict(N=N, init_pops=ip[:N].copy(), caps=cp[:N].copy(),
+                    mmm=mmm.reshape(Cn, N, N), nnz=nnz)
+
     def close(self):
         if getattr(self, "handle", None):
             self.ctx.lib.to_scene_destroy(self.handle)
