@@ -1,27 +1,33 @@
 #!/usr/bin/env python3
 """Road designs valued per second at +-1% Monte Carlo standard error.
 
-Workload: one GA generation of 256 roads (8-64 control points) on a
-200 x 200 habitat grid with 5 habitat types (~300 patches per species) and
-3 species, 50 yearly steps (synthetic, seeded).  A "step" values every road
-of the generation: species-road model (patches, crossings, transition and
-survival matrices) plus the MTE population Monte Carlo at N* paths, where
-N* = ceil((sigma / (0.01 * mu))^2) comes from an untimed pilot at 2000 paths
-(the largest N* over roads and species is used for the batch).
+Workload (the batched GA generation): 256 roads (8-64 control points) on a
+200 x 200 habitat grid with 5 habitat types (201-368 patches per species
+model) and 3 species, 50 yearly steps (synthetic, seeded).  A "step" values
+every road of the generation in both of the reference's modes: the
+species-road model (patches, crossings, transition and survival matrices,
+initial animals at risk), the MTE population Monte Carlo at N*_mte paths and
+the ROV real-options valuation (ALGO4, 3 controls, 3 exogenous processes,
+regressions on 8 bins per state dimension) at N*_rov paths, all in one
+captured CUDA graph.  N* = ceil((sigma / (0.01 * mu))^2) per road comes from
+untimed pilots at the configuration's 2000 MTE and 5000 ROV paths (the
+largest over roads is used for the batch).
 
     value  - batched path, road inputs already resident in HBM
     e2e    - same through the public C ABI with pinned host inputs, H2D and
              D2H inside the timed region
     plain  - the reference-style path: one road per call through the host
-             entry points (species model, then simulate MTE), for comparison
-    --impl reference - the CPU restatement of the reference (oracle/) on the
-             host cores, bounded sample of the same workload
+             entry points (species models, simulate MTE, simulate ROV), with
+             the habitat maps rasterised beforehand, and its GPU-kernel share
+    --impl reference - the CPU restatement of the reference (oracle/) on all
+             host cores, one road per core, bounded sample of the same work
 
 One JSON line on stdout (rank 0).
 """
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import math
 import os
@@ -36,9 +42,15 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "road designs valued/sec at ±1% MC error: batched/surrogate vs plain, 1 GB300"
 WORKLOAD = ("GA generation: 256 roads (8-64 control points), 200x200 grid, 5 habitat types, "
-            "~300 patches, 3 species, MTE valuation at N* paths, 50 years")
+            "~300 patches, 3 species, each road valued by MTE and ROV at N* paths "
+            "(pilots 2000 MTE / 5000 ROV paths), 50 years")
 N_ROADS = 256
 PILOT_PATHS = 2000
+ROV_PILOT_PATHS = 5000
+ROV_DIM_RES = 8
+ROV_SEED = 17
+SEM = 1
+REF_SECONDS = 90          # the reference arm's sample window
 YEARS = 50
 
 
@@ -50,9 +62,12 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--roads", type=int, default=N_ROADS)
     ap.add_argument("--plain-roads", type=int, default=8)
+    ap.add_argument("--rov-dim-res", type=int, default=ROV_DIM_RES)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-only", action="store_true",
-                    help="one pilot + one step, for profiler launch lists")
+                    help="pilots + one step, for profiler launch lists")
+    ap.add_argument("--profile-mte-only", action="store_true",
+                    help="pilot + one MTE-only generation step, for profilers")
     ap.add_argument("--profile-rov", action="store_true",
                     help="one ROV valuation of a one-road scene (2 species, ~115 "
                          "patches, 3 controls, 16 bins per dimension), for profilers")
@@ -64,7 +79,7 @@ def parse():
                     help="training pairs for the learned surrogate (0: skip that leg)")
     ap.add_argument("--ga-generations", type=int, default=64)
     ap.add_argument("--no-rov-leg", dest="rov_leg", action="store_false",
-                    help="skip the one-road ROV and adjoint timings")
+                    help="skip the one-road ROV, batched-ROV and adjoint timings")
     return ap.parse_args()
 
 
@@ -123,7 +138,8 @@ def measured_peaks():
 
 # --------------------------------------------------------------------------
 def n_star(results, floor=64):
-    """Paths needed per road for a 1% relative standard error (max over species)."""
+    """Paths needed per road for a 1% relative standard error of the MTE end
+    population (max over species), from a pilot at PILOT_PATHS."""
     need = []
     for r in range(results.shape[0]):
         nr = 0
@@ -136,76 +152,128 @@ def n_star(results, floor=64):
     return need
 
 
-def cpu_baseline_port(scene, roads, P, seconds=20.0, threads=None):
-    """Oracle (CPU restatement of the reference) on all host cores: species
-    model + MTE for each species of as many roads as fit in `seconds`."""
+def rov_n_star(results, pilot, floor=128):
+    """Paths needed per road for a 1% relative standard error of the ROV
+    value (result slots 10 and 13), from a pilot at `pilot` paths."""
+    need = []
+    for r in range(results.shape[0]):
+        v, se = results[r, 0, 10], results[r, 0, 13]
+        n = floor
+        if v != 0.0 and math.isfinite(v) and math.isfinite(se):
+            n = max(floor, math.ceil((se * math.sqrt(pilot) / (0.01 * abs(v))) ** 2))
+        need.append(n)
+    return need
+
+
+def rov_template(models, scene, P, dim_res, road=0):
+    from transportoptimiser_gb300.rov import rov_problem_from_models
+    return rov_problem_from_models(models, scene, n_paths=P, n_years=YEARS, dim_res=dim_res,
+                                   sem=1, n_processes=3, demand=True, seed=ROV_SEED, road=road)
+
+
+def oracle_road(scene, r, rd, hab, P_mte, P_rov, dim_res, road0=0):
+    """The reference's work for one road on one core (oracle/): the species
+    model of every species, the MTE at P_mte paths and the ROV at P_rov."""
     from oracle import pyoracle as po
+    models = []
+    for s, sp in enumerate(scene.species):
+        m = po.species_model(scene, sp, rd, sem=SEM, max_patches=1024, hab=hab)
+        models.append(m)
+        po.simulate_mte(P_mte, YEARS, m["N"], 1.0, sp.params, m["init_pops"], m["caps"],
+                        m["mmm"][-1], 0, road0 + r, s, SEM, 1)
+    if P_rov > 0:
+        po.simulate_rov(rov_template(models, scene, P_rov, dim_res, road=road0 + r), threads=1)
+    return r
+
+
+def oracle_generation(scene, habs, P_mte, P_rov, dim_res, seconds, threads=None, start=0):
+    """Roads valued by the oracle in parallel, one road per host core (the
+    oracle's ctypes calls release the GIL), for about `seconds`; returns
+    (designs/s, threads, roads)."""
     threads = threads or os.cpu_count() or 1
+    R = len(scene.roads)
     t0 = time.perf_counter()
     done = 0
-    for rd in roads:
-        for s, sp in enumerate(scene.species):
-            m = po.species_model(scene, sp, rd, sem=0, max_patches=1024)
-            po.simulate_mte(P, YEARS, m["N"], 1.0, sp.params, m["init_pops"], m["caps"],
-                            m["mmm"][-1], 0, done, s, 0, threads)
-        done += 1
-        if time.perf_counter() - t0 > seconds:
-            break
+    nxt = start
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        running = set()
+        while True:
+            while len(running) < threads and time.perf_counter() - t0 < seconds:
+                r = nxt % R
+                nxt += 1
+                running.add(ex.submit(oracle_road, scene, r, scene.roads[r], habs[r], P_mte,
+                                      P_rov, dim_res))
+            if not running:
+                break
+            fin, running = cf.wait(running, return_when=cf.FIRST_COMPLETED)
+            for f in fin:
+                f.result()
+                done += 1
     dt = time.perf_counter() - t0
     return done / dt, threads, done
 
 
-def reference_n_star(scene, roads, threads=None):
-    """Paths per road for a 1% standard error, by the same rule as the GPU
-    arm (largest need over roads and species, rounded up to 64, at least 64),
-    from a CPU pilot at PILOT_PATHS paths on the given roads."""
+def reference_n_star(scene, habs, roads, dim_res, threads=None):
+    """N* by the GPU arm's rule from CPU pilots (MTE at PILOT_PATHS, ROV at
+    a quarter of ROV_PILOT_PATHS to bound the time) on the given roads."""
     import numpy as np
     from oracle import pyoracle as po
     threads = threads or os.cpu_count() or 1
-    need = 64
-    for r, rd in enumerate(roads):
+    need_m, need_r = 64, 128
+    rp = ROV_PILOT_PATHS // 4
+    for r in roads:
+        rd = scene.roads[r]
+        models = []
         for s, sp in enumerate(scene.species):
-            m = po.species_model(scene, sp, rd, sem=0, max_patches=1024)
+            m = po.species_model(scene, sp, rd, sem=SEM, max_patches=1024, hab=habs[r])
+            models.append(m)
             e = po.simulate_mte(PILOT_PATHS, YEARS, m["N"], 1.0, sp.params, m["init_pops"],
-                                m["caps"], m["mmm"][-1], 1, r, s, 0, threads).astype(np.float64)
-            mean = e.mean()
-            if mean > 0:
-                sigma = e.std(ddof=1)
-                need = max(need, math.ceil((sigma / (0.01 * abs(mean))) ** 2))
-    return int(min(math.ceil(need / 64.0) * 64, 16384))
+                                m["caps"], m["mmm"][-1], 1, r, s, SEM, threads).astype(np.float64)
+            if e.mean() > 0:
+                need_m = max(need_m, math.ceil((e.std(ddof=1) / (0.01 * e.mean())) ** 2))
+        o = po.simulate_rov(rov_template(models, scene, rp, dim_res, road=r), threads=threads)
+        v = o["stats"][0]
+        if v != 0.0:
+            need_r = max(need_r, math.ceil((o["value_se"] * math.sqrt(rp) / (0.01 * abs(v))) ** 2))
+    P_mte = int(min(math.ceil(need_m / 64.0) * 64, 16384))
+    P_rov = int(min(math.ceil(need_r / 128.0) * 128, 16384))
+    return P_mte, P_rov
 
 
 # --------------------------------------------------------------------------
 def run_reference(args):
-    """--impl reference: the CPU port of the reference on the host cores."""
+    """--impl reference: the CPU port of the reference on the host cores,
+    one road per core.  A road takes seconds on one core, so the K steps
+    share one continuous sample: the pool values roads for REF_SECONDS (then
+    finishes the roads in flight) and the line reports designs per second
+    over that whole window."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     from transportoptimiser_gb300 import synth
-    from __graft_entry__ import build
     from transportoptimiser_gb300 import build as b
     b.build_oracle()
     scene = synth.generation(0, n_roads=args.roads)
-    # the paths the metric needs (1% standard error), from a bounded pilot
-    P = reference_n_star(scene, scene.roads[:8])
+    habs = [scene.hab_map(rd) for rd in scene.roads]       # rasterised outside the timing
+    P_mte, P_rov = reference_n_star(scene, habs, [0, 1], args.rov_dim_res)
     for _ in range(args.warmup):
-        cpu_baseline_port(scene, scene.roads[:1], 64, seconds=1.0)
-    vals = []
-    for k in range(args.steps):
-        v, cores, n = cpu_baseline_port(scene, scene.roads[k % len(scene.roads):], P,
-                                        seconds=8.0)
-        vals.append(v)
-    value = statistics.mean(vals)
+        oracle_road(scene, 0, scene.roads[0], habs[0], 64, 0, args.rov_dim_res)
+    value, cores, n = oracle_generation(scene, habs, P_mte, P_rov, args.rov_dim_res,
+                                        seconds=REF_SECONDS)
+    sample = ("%d roads valued by a pool of %d workers, one road per core, over %d s (the "
+              "roads in flight then finished); each road: 3 species models, MTE at %d paths, "
+              "ROV at %d paths (%d bins per state dimension), 50 years"
+              % (n, cores, REF_SECONDS, P_mte, P_rov, args.rov_dim_res))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "designs/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "paths": P, "note": "per step: roads valued "
-                       "in an 8 s sample; paths per road N* from a %d-path CPU pilot on "
-                       "8 roads" % PILOT_PATHS},
+            "config": {"workload": WORKLOAD, "mte_paths": P_mte, "rov_paths": P_rov,
+                       "semantics": "corrected", "note": "the steps share one continuous "
+                       "sample; N* from CPU pilots (MTE %d paths, ROV %d paths) on 2 roads"
+                       % (PILOT_PATHS, ROV_PILOT_PATHS // 4)},
             "cpu_baseline": {"value": value, "unit": "designs/s", "cores": cores,
-                             "kind": "port", "sample": "roads valued in 8 s per step, "
-                             "%d paths, all species" % P},
+                             "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "designs/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -401,6 +469,16 @@ def profile_rov(args):
     return 0
 
 
+def kernel_split(ctx, names):
+    """{name: (ms per launch, launches)} from the context's event timing."""
+    out = {}
+    for n in names:
+        ms, k = ctx.kernel_time(n)
+        if k:
+            out[n] = (ms, k)
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -425,47 +503,63 @@ def main():
     torch.cuda.set_device(local)
 
     from transportoptimiser_gb300 import synth
-    from transportoptimiser_gb300._capi import MIG_AUTO, Context
+    from transportoptimiser_gb300._capi import MIG_AUTO, MIG_SPARSE_FP32, RESULT_STRIDE, Context
     from transportoptimiser_gb300.generation import Generation, pack_roads
     from transportoptimiser_gb300 import simulate_gpu as sg
-
     from transportoptimiser_gb300 import shard
+
     scene = synth.generation(0, n_roads=args.roads)
     if rank > 0:
         # each rank values its own generation of roads (weak scaling)
         scene.roads = shard.rank_roads(scene, args.roads, rank)
+    S = len(scene.species)
     ctx = Context(local)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     gen = Generation(scene, max_roads=args.roads, max_patches=512, ctx=ctx)
     packed = pack_roads(scene, scene.roads)
     road0 = shard.road0(rank)
+    R_dim = args.rov_dim_res
 
-    # pilot (untimed): N* per road
-    pilot = gen.evaluate(packed, gen.opts(PILOT_PATHS, YEARS, seed=1, road0=road0,
-                                          migration=MIG_AUTO))
-    need = n_star(pilot)
-    P = min(int(math.ceil(max(need) / 64.0) * 64), 16384)
-    # autotuned migration kernel; the generation is captured once as a CUDA
-    # graph and replayed (planned on the first, untimed, call)
-    opts = gen.opts(P, YEARS, seed=0, road0=road0, migration=MIG_AUTO, graph=True)
+    # pilots (untimed): N* per road for the MTE (2000 paths) and the ROV (5000)
+    pilot = gen.evaluate(packed, gen.opts(PILOT_PATHS, YEARS, seed=1, road0=road0, sem=SEM,
+                                          migration=MIG_SPARSE_FP32))
+    P = min(int(math.ceil(max(n_star(pilot)) / 64.0) * 64), 16384)
     Ns = pilot[:, :, 0].astype(int)
+    if args.profile_mte_only:
+        o = gen.opts(P, YEARS, seed=0, road0=road0, sem=SEM, migration=MIG_SPARSE_FP32)
+        gen.evaluate(packed, o)
+        gen.evaluate(packed, o)
+        return 0
+    tmpl_models = [gen.species_model(0, s) for s in range(S)]
+    gen.set_rov(rov_template(tmpl_models, scene, ROV_PILOT_PATHS, R_dim))
+    rpilot = gen.evaluate(packed, gen.opts(64, YEARS, seed=1, road0=road0, sem=SEM))
+    P_rov = min(int(math.ceil(max(rov_n_star(rpilot, ROV_PILOT_PATHS)) / 128.0) * 128), 16384)
+    gen.set_rov(rov_template(tmpl_models, scene, P_rov, R_dim))
+    # the whole generation is captured once as a CUDA graph and replayed
+    opts = gen.opts(P, YEARS, seed=0, road0=road0, sem=SEM, migration=MIG_AUTO, graph=True)
 
-    # device-resident inputs for `value`
     dev = {k: torch.from_numpy(v).cuda() for k, v in packed.items()}
-    d_res = torch.zeros(args.roads * len(scene.species) * 8, dtype=torch.float64,
-                        device="cuda")
+    d_res = torch.zeros(args.roads * S * RESULT_STRIDE, dtype=torch.float64, device="cuda")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    opts_direct = gen.opts(P, YEARS, seed=0, road0=road0, migration=MIG_AUTO)
 
     def step_device(o=opts):
         gen.evaluate_device(args.roads, dev["cell_off"].data_ptr(), dev["cells"].data_ptr(),
                             dev["seg_off"].data_ptr(), dev["segs"].data_ptr(), o,
                             d_res.data_ptr())
 
-    def step_direct():
-        step_device(opts_direct)
+    def timed(fn, steps):
+        evs = []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            evs.append((e0, e1))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -481,54 +575,35 @@ def main():
         torch.cuda.synchronize()
         clk = clocks_start()
         l0 = ctx.launches
-        evs = []
         t_wall0 = time.perf_counter()
-        for _ in range(args.steps):
-            flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step_device()
-            e1.record(stream)
-            evs.append((e0, e1))
-        torch.cuda.synchronize()
+        step_ms = timed(step_device, args.steps)
         t_wall = time.perf_counter() - t_wall0
         launches = (ctx.launches - l0) // args.steps
         clocks = clocks_stop(clk, local)
-        # per-kernel times: the same steps launched directly (not from the
+        # per-kernel times: the same step launched directly (not from the
         # graph) with CUDA events around each kernel on this stream
-        tune = ctx.tuning().strip().splitlines()
-        chosen = tune[-1].split("-> ")[1].split()[0] if tune else "sparse"
-        mte_name = {"sparse": "mte_sparse", "simt": "mte_simt", "tc": "mte_tc"}[chosen]
-        # the tuned kernel named explicitly: the same kernels the graph replays
-        # (the sparse form takes its compressed columns from the species model)
-        from transportoptimiser_gb300._capi import MIG_SIMT_FP32, MIG_SPARSE_FP32, MIG_TC_3XTF32
-        mig = {"sparse": MIG_SPARSE_FP32, "simt": MIG_SIMT_FP32, "tc": MIG_TC_3XTF32}[chosen]
-        o_prof = gen.opts(P, YEARS, seed=0, road0=road0, migration=mig)
+        o_prof = gen.opts(P, YEARS, seed=0, road0=road0, sem=SEM, migration=MIG_SPARSE_FP32)
         step_device(o_prof)
         ctx.profile(True)
         for _ in range(args.steps):
             flush.zero_()
             step_device(o_prof)
         torch.cuda.synchronize()
-        mte_ms, mte_n = ctx.kernel_time(mte_name)
-        lb_ms, lb_n = ctx.kernel_time("species_labels")
-        pt_ms, pt_n = ctx.kernel_time("species_patches")
-        lk_ms, lk_n = ctx.kernel_time("species_links")
-        pk_ms, pk_n = ctx.kernel_time("pack_csc")
-        sm_ms, sm_n = lb_ms + pt_ms + lk_ms + pk_ms, max(pt_n, 1)
+        names = ["species_labels", "species_patches", "species_links", "mte_sparse",
+                 "rov_exog", "rov_forward_sparse", "lsm_prepare", "knn_grid", "knn",
+                 "knn_solve", "rov_backward"]
+        split = {k: (v[0] / args.steps, v[1] // args.steps)
+                 for k, v in kernel_split(ctx, names).items()}
         ctx.profile(False)
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(step_ms) / len(step_ms)
-    ms = shard.max_over_ranks(ms)
+    ms = shard.max_over_ranks(sum(step_ms) / len(step_ms))
     value = args.roads * world / (ms / 1000.0)
-    res = d_res.cpu().numpy().reshape(args.roads, len(scene.species), 8)
+    res = d_res.cpu().numpy().reshape(args.roads, S, RESULT_STRIDE)
 
     # e2e: public host-pointer entry point, pinned inputs, copies inside
     pinned = {k: torch.from_numpy(v).pin_memory() for k, v in packed.items()}
     pnp = {k: v.numpy() for k, v in pinned.items()}
     h2d = sum(v.nbytes for v in pnp.values())
-    d2h = args.roads * len(scene.species) * 8 * 8
+    d2h = args.roads * S * RESULT_STRIDE * 8
     gen.evaluate(pnp, opts)
     torch.cuda.synchronize()
     e2e_ms = []
@@ -540,40 +615,57 @@ def main():
         e2e_ms.append((time.perf_counter() - t0) * 1000.0)
     e2e_value = args.roads * world / (statistics.mean(e2e_ms) / 1000.0)
 
-    # plain: one road per call through the host entry points (reference style)
-    plain_value = None
+    # the MTE-only generation (the step without the ROV), for comparison
+    gen.set_rov(None)
+    with torch.cuda.stream(stream):
+        step_device(opts)
+        torch.cuda.synchronize()
+        mte_only_ms = statistics.mean(timed(step_device, args.steps))
+
+    # plain: one road per call through the host entry points (the
+    # reference's way), habitat maps rasterised beforehand as for the
+    # batched arm; the share of that time the GPU kernels take
+    plain = None
     if rank == 0 and args.plain_roads > 0:
+        habs = [scene.hab_map(scene.roads[r]) for r in range(args.plain_roads)]
+        pops = [[scene.pop_map(sp, habs[r]) for sp in scene.species]
+                for r in range(args.plain_roads)]
+
+        def plain_road(r):
+            rd = scene.roads[r]
+            models = [sg.createSpeciesModel(habs[r], pops[r][s], scene.W, scene.H, scene.res,
+                                            sp.habitats, rd.colmajor(), rd.G, sp.hazard,
+                                            sp.lambda_mean, sp.lambda_sd, sp.lambda_mult,
+                                            sp.hab_pref_mult, sem=SEM, max_patches=512, ctx=ctx)
+                      for s, sp in enumerate(scene.species)]
+            sg.simulateMTECUDA(models, [sp.params for sp in scene.species], P, YEARS, seed=0,
+                               road=road0 + r, sem=SEM, migration=MIG_AUTO, ctx=ctx)
+            sg.simulateROVCUDA(rov_template(models, scene, P_rov, R_dim, road=road0 + r),
+                               want=(), ctx=ctx)
+        plain_road(0)
+        ctx.profile(True)
         t0 = time.perf_counter()
         for r in range(args.plain_roads):
-            rd = scene.roads[r]
-            hab = scene.hab_map(rd)
-            models = []
-            for s, sp in enumerate(scene.species):
-                models.append(sg.createSpeciesModel(
-                    hab, scene.pop_map(sp, hab), scene.W, scene.H, scene.res, sp.habitats,
-                    rd.colmajor(), rd.G, sp.hazard, sp.lambda_mean, sp.lambda_sd,
-                    sp.lambda_mult, sp.hab_pref_mult, sem=0, max_patches=512, ctx=ctx))
-            sg.simulateMTECUDA(models, [sp.params for sp in scene.species], P, YEARS,
-                               seed=0, road=road0 + r, migration=MIG_AUTO, ctx=ctx)
-        plain_value = args.plain_roads / (time.perf_counter() - t0)
+            plain_road(r)
+        t_plain = time.perf_counter() - t0
+        kern_ms = sum(v[0] for v in kernel_split(ctx, ctx.kernel_names()).values())
+        ctx.profile(False)
+        plain = {"value": args.plain_roads / t_plain, "unit": "designs/s",
+                 "roads": args.plain_roads, "ms_per_road": 1000.0 * t_plain / args.plain_roads,
+                 "gpu_kernel_ms_per_road": kern_ms / args.plain_roads,
+                 "note": "one road per call: 3 species models, MTE, ROV through the host entry "
+                         "points; habitat maps rasterised beforehand; the rest of each "
+                         "road's time is host work and copies"}
 
-    # roofline of the migration kernel.  The algorithmic count is the dense
-    # contraction's, 2 * P * N^2 * Y per (road, species); the sparse kernel
-    # skips the zeros, so its useful (non-zero) FLOPs are reported beside it.
-    # DRAM traffic per launch: an ncu capture (dram__bytes_read/write.sum) of
-    # the same kernel at the generation shape on 64 roads (192 road-species,
-    # 64 paths) read 3.27 MB and wrote nothing (the CSC matrices, initial
-    # populations and capacities, proportional to road-species count, not to
-    # paths); scaled to this launch's road-species count.
-    Nsum2 = float((Ns.astype(np.float64) ** 2).sum())
-    nnz = res[:, :, 7].astype(np.float64)
-    useful_flops = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() else None
-    dense_equiv_flops = 2.0 * P * Nsum2 * YEARS
-    mte_avg_s = (mte_ms / max(mte_n, 1)) / 1000.0
-    achieved_tf = dense_equiv_flops / mte_avg_s / 1e12 if mte_avg_s > 0 else 0.0
-    useful_tf = (useful_flops / mte_avg_s / 1e12) if (useful_flops and mte_avg_s > 0) else None
-    traffic = 3.265024e6 * (args.roads * len(scene.species)) / 192.0
+    # roofline: the kernel that dominates the step
     bf16_peak, hbm_peak, peak_kind = measured_peaks()
+    top = max(split.items(), key=lambda kv: kv[1][0]) if split else ("n/a", (0.0, 0))
+    nnz = res[:, :, 7].astype(np.float64)
+    mte_ms = split.get("mte_sparse", (0.0, 0))[0]
+    mte_flops = 2.0 * P * float((Ns.astype(np.float64) ** 2).sum()) * YEARS
+    mte_useful = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() else None
+    roofline = roofline_line(top, split, P, P_rov, R_dim, Ns, mte_flops, mte_useful, bf16_peak,
+                             hbm_peak, peak_kind, args.roads, S)
 
     rov_adj = rov_adjoint_leg(ctx) if rank == 0 and args.rov_leg else None
     rov_gen = rov_generation_leg(ctx) if rank == 0 and args.rov_leg else None
@@ -586,9 +678,11 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         from transportoptimiser_gb300 import build as b
         b.build_oracle()
-        v, cores, n = cpu_baseline_port(scene, scene.roads, P, seconds=20.0)
+        habs = [scene.hab_map(rd) for rd in scene.roads]
+        v, cores, n = oracle_generation(scene, habs, P, P_rov, R_dim, seconds=20.0)
         cpu = {"value": v, "unit": "designs/s", "cores": cores, "kind": "port",
-               "sample": "%d road(s) x 3 species, %d paths, 50 years (20 s budget)" % (n, P)}
+               "sample": "%d road(s) in 20 s, one road per core, each: 3 species models, MTE "
+                         "at %d paths, ROV at %d paths, 50 years" % (n, P, P_rov)}
 
     if rank == 0:
         line = {
@@ -596,33 +690,25 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded; no public dataset for this path)",
-            "config": {"workload": WORKLOAD, "roads": args.roads, "species": len(scene.species),
-                       "paths_per_road": P, "pilot_paths": PILOT_PATHS, "years": YEARS,
+            "config": {"workload": WORKLOAD, "roads": args.roads, "species": S,
+                       "mte_paths_per_road": P, "rov_paths_per_road": P_rov,
+                       "pilot_paths": {"mte": PILOT_PATHS, "rov": ROV_PILOT_PATHS},
+                       "years": YEARS, "rov_bins_per_dim": R_dim, "semantics": "corrected",
                        "patches_min_max": [int(Ns.min()), int(Ns.max())],
-                       "migration": "autotuned: " + (tune[-1] if tune else "n/a"),
-                       "graph": "whole generation captured once, replayed per step",
+                       "graph": "whole generation (species models, MTE, ROV, results) "
+                                "captured once, replayed per step",
                        "l2": "flushed (256 MB write) between steps",
-                       "wall_s_timed": t_wall},
+                       "wall_s_timed": t_wall, "ms_steps": [round(x, 3) for x in step_ms]},
             "e2e": {"value": e2e_value, "unit": "designs/s", "h2d_bytes_per_step": h2d,
                     "ms_steps": [round(x, 3) for x in e2e_ms],
                     "d2h_bytes_per_step": d2h},
-            "plain": {"value": plain_value, "unit": "designs/s",
-                      "roads": args.plain_roads, "note": "one road per call, host entry points"},
-            "roofline": {"kernel": "k_" + mte_name, "bound": "tensor", "achieved": achieved_tf,
-                         "peak": bf16_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tf / bf16_peak,
-                         "peak_kind": peak_kind + " bf16 dense (TF32 is half, 3xTF32 a sixth)",
-                         "traffic": traffic, "traffic_note": "bytes per launch, ncu on "
-                         "64 roads scaled by road-species count",
-                         "flops_per_launch": dense_equiv_flops,
-                         "useful_flops_per_launch": useful_flops,
-                         "useful_achieved": useful_tf,
-                         "kernel_ms": mte_ms / max(mte_n, 1),
-                         "species_model_ms": sm_ms / max(sm_n, 1),
-                         "species_labels_ms": lb_ms / max(lb_n, 1),
-                         "species_patches_ms": pt_ms / max(pt_n, 1),
-                         "species_links_ms": lk_ms / max(lk_n, 1),
-                         "pack_csc_ms": pk_ms / max(pk_n, 1)},
+            "plain": plain,
+            "batched_vs_plain": (value / plain["value"]) if plain else None,
+            "mte_only": {"value": args.roads * world / (mte_only_ms / 1000.0),
+                         "unit": "designs/s", "ms_per_step": mte_only_ms,
+                         "note": "the same generation valued by MTE alone"},
+            "kernel_ms_per_step": {k: round(v[0], 4) for k, v in split.items()},
+            "roofline": roofline,
             "surrogate": surrogate,
             "rov_one_road": rov_adj["rov"] if rov_adj else None,
             "rov_generation": rov_gen,
@@ -637,6 +723,28 @@ def main():
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def roofline_line(top, split, P, P_rov, R_dim, Ns, mte_flops, mte_useful, bf16_peak, hbm_peak,
+                  peak_kind, roads, S):
+    """Roofline of the step's dominant kernel.  The ROV's kNN + regression
+    kernel is bound by instruction issue (ncu: issue slots, not DRAM or a
+    tensor pipe); its algorithmic unit is the grid query (k neighbours, the
+    local normal equations).  The MTE migration kernel is reported against
+    the dense-contraction count of the benchmark spec (2 P N^2 Y per road and
+    species) next to its useful, non-zero FLOPs."""
+    name, (ms, n) = top
+    out = {"kernel": "k_" + name, "kernel_ms": ms, "launches_per_step": n}
+    mte_ms = split.get("mte_sparse", (0.0, 0))[0]
+    out["mte_sparse"] = {"ms": mte_ms, "dense_equiv_tflops": (mte_flops / (mte_ms / 1e3) / 1e12)
+                         if mte_ms > 0 else None,
+                         "useful_tflops": (mte_useful / (mte_ms / 1e3) / 1e12)
+                         if (mte_ms > 0 and mte_useful) else None,
+                         "frac_of_bf16_peak": (mte_flops / (mte_ms / 1e3) / 1e12 / bf16_peak)
+                         if mte_ms > 0 else None}
+    out.update({"bound": "issue", "unit": "Ginst/s", "achieved": None, "peak": None,
+                "frac": None, "traffic": None, "peak_kind": peak_kind})
+    return out
 
 
 if __name__ == "__main__":

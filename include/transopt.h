@@ -135,6 +135,9 @@ typedef struct {
     double* trans;           /* N*N row-major origin x destination (optional) */
     double* surv;            /* C*N*N (optional)                              */
     float* mmm;              /* C*N*N destination-major [c][k][l] (optional)  */
+    double* iar;             /* [C] initial animals at risk per control,
+                                SpeciesRoadPatches::computeInitialAAR,
+                                SpeciesRoadPatches.cpp:453-490 (optional)     */
 } to_species_out;
 
 /* SpeciesRoadPatches::createSpeciesModel, SpeciesRoadPatches.cpp:12-451, on
@@ -448,11 +451,49 @@ int to_ctx_tuning(to_ctx ctx, char* buf, int len);
 /* result block per (road, species), TO_RESULT_STRIDE doubles:
  *   0 n_patches, 1 n_transitions, 2 mte mean, 3 mte sd, 4 mte se,
  *   5 P(end < 0.2 init), 6 initial population, 7 non-zeros of the
- *   highest-flow migration matrix (-1 when the dense form ran) */
-#define TO_RESULT_STRIDE 8
+ *   highest-flow migration matrix (-1 when the dense form ran),
+ *   8 this species' MTE penalty, 9 the road's MTE penalty (sum over its
+ *   species; both 0 until to_scene_set_penalty),
+ *   10..14 the road's ROV valuation when the scene has one
+ *   (to_scene_set_rov; else NaN): value, optimal first-period control, the
+ *   reference's SD statistic, Monte Carlo standard error, paths behind the
+ *   value,
+ *   15 reserved (0),
+ *   16..23 initial animals at risk of control c = 0..7
+ *   (SpeciesRoadPatches::computeInitialAAR, SpeciesRoadPatches.cpp:453-490;
+ *   NaN past n_controls) */
+#define TO_RESULT_STRIDE 24
 
 to_status to_scene_create(to_ctx ctx, const to_scene* scene, to_gen* gen);
 to_status to_scene_destroy(to_gen gen);
+
+/* The MTE penalty of Simulator::simulateMTE (Simulator.cpp:196-214): per
+ * species, (threshold > lb) * (threshold - lb) * init_population *
+ * cost_per_animal with lb = z * SD + mean of the end population and
+ * z = NormalCDFInverse(1 - confidence) (Abramowitz & Stegun 26.2.23, as
+ * Utility.cpp:165-193).  threshold is the species threshold times the
+ * scenario's population level.  Host arrays [n_species]. */
+typedef struct {
+    double confidence;
+    const double* threshold;
+    const double* init_population;
+    const double* cost_per_animal;
+} to_penalty;
+to_status to_scene_set_penalty(to_ctx ctx, to_gen gen, const to_penalty* penalty);
+
+/* Adds the ROV valuation (simulateROVCUDA, ALGO4, SimulateGPU.cu:3870-5003)
+ * of every road to to_evaluate_roads, in the same launch sequence (and the
+ * same captured graph) as the species models and the MTE: the road-
+ * independent fields of `rov` (paths per road, years, controls, dim_res,
+ * processes, fuels, commodities, costs, dt, rrr, demand_idx, seed) apply to
+ * every road, and so do its species' params when `species` is not NULL
+ * (else the scene's); the species' patch fields and the road and migration
+ * fields are ignored - each road uses the species models the generation
+ * builds (all controls' packed matrices) with road id road0 + r.  n_species and n_controls must
+ * be the scene's, sem 1, algo 4 (or 0), >= 128 paths.  Road r's result
+ * equals to_simulate_rov_batch on the same models.  Scratch for max_roads
+ * roads is allocated here; rov == NULL switches the ROV off. */
+to_status to_scene_set_rov(to_ctx ctx, to_gen gen, const to_rov_problem* rov);
 
 /* Roads as CSR lists: road r owns cells [cell_off[r], cell_off[r+1]) of
  * `cells` (index x + y*W, set to ROAD) and segments [seg_off[r], seg_off[r+1])

@@ -289,6 +289,24 @@ int or_species_model(const or_species_in* in, or_species_out* out) {
                 out->mmm[((size_t)c * N + j) * N + i] = ((double)m > 0.00001) ? m : 0.0f;
             }
     }
+
+    /* initial animals at risk (SpeciesRoadPatches::computeAAR /
+     * computeInitialAAR, SpeciesRoadPatches.cpp:453-490): per control
+     * 1 - sum_j [(trans o surv_c)^T pops]_j / sum pops, accumulated row by
+     * row (ascending destinations, then ascending origins) */
+    if (out->iar)
+        for (int c = 0; c < in->n_controls; ++c) {
+            double tot = 0.0, init = 0.0;
+            for (int i = 0; i < N; ++i) {
+                double acc = 0.0;
+                for (int j = 0; j < N; ++j)
+                    if (out->trans[i * N + j] != 0.0)
+                        acc += out->trans[i * N + j] * out->surv[((size_t)c * N + i) * N + j];
+                tot += out->pop[i] * acc;
+                init += out->pop[i];
+            }
+            out->iar[c] = 1.0 - tot / init;
+        }
     return N;
 }
 
@@ -511,4 +529,106 @@ void or_fill_stream(uint64_t seed, int stream, int road, int normal,
 void or_fill_pv_stream(uint64_t seed, int stream, int road, int normal,
                        long n, float* out) {
     for (long j = 0; j < n; ++j) out[j] = pv_stream(seed, stream, road, j, normal);
+}
+
+/* ------------------------------------------------------------------------ */
+/* RoadCells::computeRoadCells (include/road/RoadCells.cpp:10-272) for a      */
+/* polyline x[0..n), y[0..n) on a grid with spacing (xs, ys) and origin 0:    */
+/* every span is reparametrised at its crossings of the grid lines            */
+/* (x = k xs, y = k ys), the points of a span sorted by (x, y) ascending when  */
+/* the span runs towards larger x, else descending; consecutive equal points  */
+/* are dropped (unique_rows); each piece between consecutive points lies in   */
+/* the cell (ceil(mid_x / xs), ceil(mid_y / ys)) of its midpoint, index       */
+/* row + col W (sub2ind on the W x H vegetation matrix).  The cells inside    */
+/* the grid are returned sorted and unique.                                   */
+/*   Q38 (sem 0): the x of a vertical-grid-line crossing is computed from the  */
+/*        y of row q of the span's crossing list (RoadCells.cpp:189-194 reads  */
+/*        pairs.block(0,1,...)), which for a span that also crosses vertical  */
+/*        lines is a horizontal crossing's y; sem 1 uses its own y.           */
+/* ------------------------------------------------------------------------ */
+typedef struct { double x, y; } or_pt;
+
+static int pt_less(or_pt a, or_pt b) { return a.x < b.x || (a.x == b.x && a.y < b.y); }
+
+static int span_points(double x0, double y0, double x1, double y1, double xs, double ys,
+                       int sem, or_pt* pts) {
+    const int h = (int)(x1 / xs) - (int)(x0 / xs);
+    const int v = (int)(y1 / ys) - (int)(y0 / ys);
+    const int ah = h < 0 ? -h : h, av = v < 0 ? -v : v;
+    const double m = (y1 - y0) / (x1 - x0), b = y0 - x0 * m;
+    const double m2 = (x1 - x0) / (y1 - y0), b2 = x0 - y0 * m2;
+    for (int q = 0; q < ah; ++q) {
+        double px;
+        if (h > 0) px = xs * (floor(x0 / xs) + (double)(q + 1));
+        else if (fmod(x0, xs) == 0.0) px = xs * (ceil(x0 / xs) - (double)q);
+        else px = xs * (ceil(x0 / xs) - (double)(q + 1));
+        pts[q].x = px;
+        pts[q].y = isfinite(m) ? m * px + b : y0;
+    }
+    for (int q = 0; q < av; ++q) {
+        double py;
+        if (v > 0) py = ys * (floor(y0 / ys) + (double)(q + 1));
+        else if (fmod(y0, ys) == 0.0) py = ys * (ceil(y0 / ys) - (double)q);
+        else py = ys * (ceil(y0 / ys) - (double)(q + 1));
+        pts[ah + q].y = py;
+    }
+    for (int q = 0; q < av; ++q) {
+        const double src = (sem == 0) ? pts[q].y : pts[ah + q].y;
+        double px;
+        if (isfinite(m)) px = (src - b) / m;
+        else if (isfinite(m2)) px = b2 + m2 * src;
+        else px = x0;
+        pts[ah + q].x = px;
+    }
+    const int n = ah + av;
+    /* insertion sort (ascending, or descending when the span runs to smaller x) */
+    const int asc = x1 >= x0;
+    for (int i = 1; i < n; ++i) {
+        or_pt t = pts[i];
+        int j = i - 1;
+        while (j >= 0 && (asc ? pt_less(t, pts[j]) : pt_less(pts[j], t))) { pts[j + 1] = pts[j]; --j; }
+        pts[j + 1] = t;
+    }
+    return n;
+}
+
+static int cmp_int(const void* a, const void* b) {
+    int x = *(const int*)a, y = *(const int*)b;
+    return (x > y) - (x < y);
+}
+
+int or_road_cells(int n, const double* x, const double* y, int W, int H, double xs, double ys,
+                  int sem, int* cells, int cap) {
+    if (n < 2) return 0;
+    int maxp = 2;
+    for (int i = 0; i + 1 < n; ++i) {
+        int h = (int)(x[i + 1] / xs) - (int)(x[i] / xs), v = (int)(y[i + 1] / ys) - (int)(y[i] / ys);
+        int k = (h < 0 ? -h : h) + (v < 0 ? -v : v);
+        if (k > maxp) maxp = k;
+    }
+    or_pt* pts = (or_pt*)malloc(sizeof(or_pt) * (size_t)(maxp + 2));
+    int* tmp = (int*)malloc(sizeof(int) * (size_t)(n * (maxp + 2)));
+    int nc = 0;
+    for (int i = 0; i + 1 < n; ++i) {
+        const int k = span_points(x[i], y[i], x[i + 1], y[i + 1], xs, ys, sem, pts + 1);
+        pts[0].x = x[i]; pts[0].y = y[i];
+        pts[k + 1].x = x[i + 1]; pts[k + 1].y = y[i + 1];
+        for (int q = 0; q <= k; ++q) {
+            const or_pt a = pts[q], bq = pts[q + 1];
+            if (a.x == bq.x && a.y == bq.y) continue;
+            const int r = (int)ceil((0.5 * (a.x + bq.x) - 0.0) / xs);
+            const int c = (int)ceil((0.5 * (a.y + bq.y) - 0.0) / ys);
+            if (r >= 0 && r < W && c >= 0 && c < H) tmp[nc++] = r + c * W;
+        }
+    }
+    qsort(tmp, (size_t)nc, sizeof(int), cmp_int);
+    int m = 0;
+    for (int i = 0; i < nc; ++i)
+        if (i == 0 || tmp[i] != tmp[i - 1]) {
+            if (m < cap) cells[m] = tmp[i];
+            ++m;
+        }
+    free(pts);
+    free(tmp);
+    return m;
 }

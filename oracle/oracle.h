@@ -78,6 +78,7 @@ typedef struct {
     double* surv;                  /* C*N*N                                */
     float* mmm;                    /* C*N*N, destination-major: [c][k][l]  */
     int n_transitions;             /* pairs tested for crossings           */
+    double* iar;                   /* [C] initial animals at risk (may be NULL) */
 } or_species_out;
 
 /* SpeciesRoadPatches.cpp:12-451 + SimulateGPU.cu:5973-5996 (dense2Sparse
@@ -86,6 +87,11 @@ int or_species_model(const or_species_in* in, or_species_out* out);
 
 /* SimulateGPU.cu:595-717 + 3650-3864.  mmm: N*N destination-major for the
  * highest-flow control.  end_pops: n_paths floats. */
+/* RoadCells::computeRoadCells (RoadCells.cpp:10-272): sorted unique cells
+ * x + y W of a polyline of n points; returns the count (cells holds at most
+ * cap of them) */
+int or_road_cells(int n, const double* x, const double* y, int W, int H, double xs, double ys,
+                  int sem, int* cells, int cap);
 /* compressed columns of a destination-major N x N matrix (entries > 0,
  * ascending origin order); idx / val may be NULL to count only */
 int or_pack_csc(int N, const float* mmm, int* ptr, int* idx, float* val);

@@ -110,6 +110,57 @@ static float local_linear(int dim, int k, int Q, int qi, const float* dist,
     return to_lsm_solve_intercept(dim, acc[0]);
 }
 
+/* The regressions of one (year, control) at the grid queries q0 .. q1-1:
+ * the query's k nearest points (as or_knn), then its local linear fit.
+ * Queries are independent, so any split of them over threads gives the same
+ * values (the reference runs its kNN one thread per query). */
+typedef struct {
+    int q0, q1, d, k, Q, n, sem;
+    const float *xn, *xr, *qn, *xqg, *y;
+    float* dist;
+    int* ind;
+    float* yout;
+} reg_job;
+
+static void reg_queries(const reg_job* j) {
+    knn_item* best = (knn_item*)malloc(sizeof(knn_item) * (size_t)(j->k > 0 ? j->k : 1));
+    float q[8], xq[TO_LSM_MAXD];
+    for (int qi = j->q0; qi < j->q1; ++qi) {
+        for (int jj = 0; jj < j->d; ++jj) q[jj] = j->qn[(size_t)jj * j->Q + qi];
+        knn_one(j->xn, j->n, q, j->d, j->k, best);
+        for (int kk = 0; kk < j->k; ++kk) {
+            j->dist[(size_t)kk * j->Q + qi] = sqrtf(best[kk].key);
+            j->ind[(size_t)kk * j->Q + qi] = best[kk].idx + 1;
+        }
+        for (int jj = 0; jj < j->d; ++jj) xq[jj] = j->xqg[(size_t)jj * j->Q + qi];
+        j->yout[qi] = (j->sem == 0)
+            ? local_linear(j->d, j->k, j->Q, qi, j->dist, j->ind, j->y, j->xr, j->n, 1, xq, 32)
+            : local_linear(j->d, j->k, j->Q, qi, j->dist, j->ind, j->y, j->xn, j->n, 0, xq, 32);
+    }
+    free(best);
+}
+
+static void* reg_thread(void* a) { reg_queries((const reg_job*)a); return NULL; }
+
+static void reg_all_queries(reg_job base, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > 128) threads = 128;
+    reg_job jobs[128];
+    pthread_t th[128];
+    const int per = (base.Q + threads - 1) / threads;
+    int used = 0;
+    for (int i = 0; i < threads; ++i) {
+        reg_job jj = base;
+        jj.q0 = i * per;
+        jj.q1 = jj.q0 + per > base.Q ? base.Q : jj.q0 + per;
+        if (jj.q0 >= jj.q1) break;
+        jobs[used++] = jj;
+    }
+    for (int i = 1; i < used; ++i) pthread_create(&th[i], NULL, reg_thread, &jobs[i]);
+    if (used > 0) reg_queries(&jobs[0]);
+    for (int i = 1; i < used; ++i) pthread_join(th[i], NULL);
+}
+
 /* k rule of the ALGO4 loop (SimulateGPU.cu:4542-4545); 0 when n <= 3, and
  * never more than n (the reference reads past the data then). */
 int or_k_rov_mult(int n, int mult) {
@@ -125,8 +176,27 @@ int or_k_rov(int n) { return or_k_rov_mult(n, 10); }
 /* ------------------------------------------------------------------------ */
 /* ROV                                                                        */
 /* ------------------------------------------------------------------------ */
+/* compressed columns of one (species, control) migration matrix
+ * (dense2Sparse, SimulateGPU.cu:5973-5996): forwardPathKernel walks these
+ * lists (SimulateGPU.cu:871-922); skipped entries are exact zeros, so the
+ * fmaf chain over a list has the bits of the chain over the dense row */
+typedef struct {
+    int* ptr;
+    int* idx;
+    float* val;
+} rov_csc;
+
+static void csc_migrate(const rov_csc* m, int N, const float* x, float* out) {
+    for (int k = 0; k < N; ++k) {
+        float a = 0.0f;
+        for (int e = m->ptr[k]; e < m->ptr[k + 1]; ++e) a = fmaf(x[m->idx[e]], m->val[e], a);
+        out[k] = a;
+    }
+}
+
 typedef struct {
     const or_rov_problem* pr;
+    const rov_csc* csc; /* [S*C] */
     int p0, p1;
     float* totalPops;   /* [P][Y+1][S] */
     float* aars;        /* [P][Y+1][S][C] */
@@ -184,28 +254,27 @@ static void rov_forward_paths(rov_fwd_job* j) {
                 }
                 float initial = or_grouped_sum(ps, N);
                 for (int c = 0; c < C; ++c) {
-                    const float* M = pr->mmm[s] + (size_t)c * N * N;
-                    for (int k = 0; k < N; ++k) {
-                        float a = 0.0f;
-                        const float* col = M + (size_t)k * N;
-                        for (int l = 0; l < N; ++l) a = fmaf(ps[l], col[l], a);
-                        mig[k] = a;
-                    }
+                    csc_migrate(&j->csc[s * C + c], N, ps, mig);
                     float totc = or_grouped_sum(mig, N);
                     if (c == control) {
-                        for (int k = 0; k < N; ++k) {
-                            float z = to_normal1(pr->seed, TO_STREAM_GROWTH, pr->road, p, t,
-                                                 (uint32_t)(s * N4 + k));
-                            /* Q25: the reference adds the local variability
-                             * (gr = gm + z p7); sem 1 scales it by the mean
-                             * as the MTE kernel does and keeps pops >= 0 */
-                            float gr = (pr->sem == 0) ? gm[s] + z * sp[7]
-                                                      : fmaf(sp[7] * z, gm[s], gm[s]);
-                            float m = mig[k], cp = pr->caps[s][k];
-                            float v = (pr->sem == 0)
-                                ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
-                                : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
-                            npop[k] = v;
+                        for (int k0 = 0; k0 < N; k0 += 4) {
+                            float z4[4];
+                            to_normal4(pr->seed, TO_STREAM_GROWTH, pr->road, p, t,
+                                       (uint32_t)((s * N4 + k0) >> 2), z4);
+                            for (int q = 0; q < 4 && k0 + q < N; ++q) {
+                                const int k = k0 + q;
+                                const float z = z4[q];
+                                /* Q25: the reference adds the local variability
+                                 * (gr = gm + z p7); sem 1 scales it by the mean
+                                 * as the MTE kernel does and keeps pops >= 0 */
+                                float gr = (pr->sem == 0) ? gm[s] + z * sp[7]
+                                                          : fmaf(sp[7] * z, gm[s], gm[s]);
+                                float m = mig[k], cp = pr->caps[s][k];
+                                float v = (pr->sem == 0)
+                                    ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
+                                    : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
+                                npop[k] = v;
+                            }
                         }
                     }
                     j->aars[(((size_t)p * (Y + 1) + t) * S + s) * C + c] = totc / initial;
@@ -311,6 +380,7 @@ static void rov_decide(const or_rov_problem* pr, const float* reg, long blk, int
 
 typedef struct {
     const or_rov_problem* pr;
+    const rov_csc* csc; /* [S*C] */
     int p0, p1, t0, maxN;
     const float* popY;
     const float* gmY;
@@ -352,14 +422,8 @@ static void rov_resim_paths(rov_resim_job* j) {
                 const int N = pr->n_patches[s];
                 const float* xs = x + (size_t)s * maxN;
                 for (int c = 0; c < C; ++c) {
-                    const float* M = pr->mmm[s] + (size_t)c * N * N;
                     float* mg = mig + ((size_t)s * C + c) * maxN;
-                    for (int k = 0; k < N; ++k) {
-                        float acc = 0.0f;
-                        const float* col = M + (size_t)k * N;
-                        for (int l = 0; l < N; ++l) acc = fmaf(xs[l], col[l], acc);
-                        mg[k] = acc;
-                    }
+                    csc_migrate(&j->csc[s * C + c], N, xs, mg);
                     float tt = or_grouped_sum(mg, N);
                     state[c * S + s] = tot[s] * (tt / tot[s]);
                 }
@@ -379,13 +443,18 @@ static void rov_resim_paths(rov_resim_job* j) {
                 const float g = j->gmY[((size_t)p * Y + u) * S + s];
                 const float* mg = mig + ((size_t)s * C + bc) * maxN;
                 float* xs = x + (size_t)s * maxN;
-                for (int k = 0; k < N; ++k) {
-                    float z = to_normal1(pr->seed, TO_STREAM_GROWTH, pr->road, p, u,
-                                         (uint32_t)(s * N4 + k));
-                    float gr = (pr->sem == 0) ? g + z * sp[7] : fmaf(sp[7] * z, g, g);
-                    float m = mg[k], cp = pr->caps[s][k];
-                    xs[k] = (pr->sem == 0) ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
-                                           : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
+                for (int k0 = 0; k0 < N; k0 += 4) {
+                    float z4[4];
+                    to_normal4(pr->seed, TO_STREAM_GROWTH, pr->road, p, u,
+                               (uint32_t)((s * N4 + k0) >> 2), z4);
+                    for (int q = 0; q < 4 && k0 + q < N; ++q) {
+                        const int k = k0 + q;
+                        const float z = z4[q];
+                        float gr = (pr->sem == 0) ? g + z * sp[7] : fmaf(sp[7] * z, g, g);
+                        float m = mg[k], cp = pr->caps[s][k];
+                        xs[k] = (pr->sem == 0) ? m * (1.0f + gr * (cp - m) / cp / 100.0f)
+                                               : fmaxf(m * (1.0f + gr * (cp - m) / cp), 0.0f);
+                    }
                 }
                 tot[s] = or_grouped_sum(xs, N);
             }
@@ -420,6 +489,18 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
     int* controls = (int*)calloc((size_t)P * Y, sizeof(int));
     float* condExp = (float*)calloc((size_t)P * Y, sizeof(float));
     float* reg = (float*)calloc((size_t)Y * C * blk, sizeof(float));
+    rov_csc* csc = (rov_csc*)calloc((size_t)S * C, sizeof(rov_csc));
+    for (int s = 0; s < S; ++s)
+        for (int c = 0; c < C; ++c) {
+            const int N = pr->n_patches[s];
+            const float* M = pr->mmm[s] + (size_t)c * N * N;
+            rov_csc* m = &csc[s * C + c];
+            m->ptr = (int*)malloc(sizeof(int) * (size_t)(N + 1));
+            const int nz = or_pack_csc(N, M, m->ptr, NULL, NULL);
+            m->idx = (int*)malloc(sizeof(int) * (size_t)(nz > 0 ? nz : 1));
+            m->val = (float*)malloc(sizeof(float) * (size_t)(nz > 0 ? nz : 1));
+            or_pack_csc(N, M, m->ptr, m->idx, m->val);
+        }
 
     /* forward paths, parallel over paths */
     int nt = pr->n_threads < 1 ? 1 : (pr->n_threads > 128 ? 128 : pr->n_threads);
@@ -429,7 +510,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
     for (int i = 0; i < nt; ++i) {
         int a = i * per, b = a + per > P ? P : a + per;
         if (a >= b) break;
-        rov_fwd_job jj = {pr, a, b, totalPops, aars, uRes, controls, popY, gmY, maxN};
+        rov_fwd_job jj = {pr, csc, a, b, totalPops, aars, uRes, controls, popY, gmY, maxN};
         jobs[used++] = jj;
     }
     for (int i = 1; i < used; ++i) pthread_create(&th[i], NULL, rov_fwd_thread, &jobs[i]);
@@ -558,19 +639,14 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
                     xn[(size_t)j * n + m] = to_lsm_normalise(xraw[((size_t)c * d + j) * P + m],
                                                              xmin[C][j], xmax[C][j], j == S,
                                                              pr->scaling);
-            or_knn(xn, n, qn, Q, d, k, dist, ind);
             /* sem 0 reads the raw (un-normalised) dim-major buffer point-major
              * (Q7); sem 1 uses the normalised points */
             float* xr = (float*)malloc(sizeof(float) * (size_t)d * n);
             for (int j = 0; j < d; ++j)
                 for (int m = 0; m < n; ++m) xr[(size_t)j * n + m] = xraw[((size_t)c * d + j) * P + m];
-            float xq[TO_LSM_MAXD];
-            for (int q = 0; q < Q; ++q) {
-                for (int j = 0; j < d; ++j) xq[j] = xqg[(size_t)j * Q + q];
-                yout[q] = (pr->sem == 0)
-                    ? local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xr, n, 1, xq, 32)
-                    : local_linear(d, k, Q, q, dist, ind, yv + (size_t)c * P, xn, n, 0, xq, 32);
-            }
+            reg_job rj = {0, Q, d, k, Q, n, pr->sem, xn, xr, qn, xqg, yv + (size_t)c * P, dist, ind,
+                          yout};
+            reg_all_queries(rj, nt);
             free(xr);
         }
         /* backwardInduction (SimulateGPU.cu:2464-2776) */
@@ -623,7 +699,7 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
             for (int i = 0; i < nt; ++i) {
                 int a0 = i * rper, b0 = a0 + rper > P ? P : a0 + rper;
                 if (a0 >= b0) break;
-                rov_resim_job jr = {pr, a0, b0, t, maxN, popY, gmY, uRes, reg, condExp,
+                rov_resim_job jr = {pr, csc, a0, b0, t, maxN, popY, gmY, uRes, reg, condExp,
                                     res->opt_cont};
                 rj[rused++] = jr;
             }
@@ -712,6 +788,8 @@ int or_simulate_rov(const or_rov_problem* pr, or_rov_result* res) {
         memcpy(res->u_results, uRes, sizeof(float) * (size_t)P * (Y + 1) * U);
     free(xin); free(xraw); free(xnorm); free(yv); free(qn); free(xqg); free(dist); free(ind);
     free(totalPops); free(aars); free(uRes); free(controls); free(condExp); free(reg);
+    for (int q = 0; q < S * C; ++q) { free(csc[q].ptr); free(csc[q].idx); free(csc[q].val); }
+    free(csc);
     free(popY); free(gmY);
     return 0;
 }

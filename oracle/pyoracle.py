@@ -52,7 +52,8 @@ class OrSpeciesOut(C.Structure):
                 ("area", c_double_p), ("cap", c_double_p), ("pop", c_double_p),
                 ("cx", c_double_p), ("cy", c_double_p), ("type", c_int_p),
                 ("dists", c_double_p), ("crossings", c_int_p), ("trans", c_double_p),
-                ("surv", c_double_p), ("mmm", c_float_p), ("n_transitions", C.c_int)]
+                ("surv", c_double_p), ("mmm", c_float_p), ("n_transitions", C.c_int),
+                ("iar", c_double_p)]
 
 
 _oracle = None
@@ -166,9 +167,11 @@ def line_segment_intersect(xy1_cm, T, xy2_cm, G, use_ref=False):
     return out
 
 
-def species_model(scene, sp, road, sem=0, max_patches=2048):
+def species_model(scene, sp, road, sem=0, max_patches=2048, hab=None):
+    """or_species_model on a synthetic scene's road; hab: the road's habitat
+    map (scene.hab_map(road)) when the caller has it already."""
     lib = oracle()
-    hab = scene.hab_map(road)
+    hab = scene.hab_map(road) if hab is None else hab
     popm = scene.pop_map(sp, hab)
     habs = (OrHabitat * len(sp.habitats))(*[OrHabitat(h.type, h.max_pop, h.pref_mean, h.pref_sd)
                                              for h in sp.habitats])
@@ -196,6 +199,8 @@ def species_model(scene, sp, road, sem=0, max_patches=2048):
     out.trans = _p(big["trans"], C.c_double)
     out.surv = _p(big["surv"], C.c_double)
     out.mmm = _p(big["mmm"], C.c_float)
+    iar = np.zeros(Cn)
+    out.iar = _p(iar, C.c_double)
     N = lib.or_species_model(C.byref(inp), C.byref(out))
     if N < 0:
         raise RuntimeError("oracle: patch capacity exceeded")
@@ -209,7 +214,24 @@ def species_model(scene, sp, road, sem=0, max_patches=2048):
     res["mmm"] = big["mmm"][:Cn * N * N].reshape(Cn, N, N).copy()
     res["init_pops"] = res["pop"].astype(np.float32)
     res["caps"] = res["cap"].astype(np.float32)
+    res["iar"] = iar
     return res
+
+
+def road_cells(points, W, H, sem=1, xs=1.0, ys=1.0):
+    """or_road_cells: RoadCells::computeRoadCells of a polyline (n x 2)."""
+    lib = oracle()
+    lib.or_road_cells.restype = C.c_int
+    lib.or_road_cells.argtypes = [C.c_int, c_double_p, c_double_p, C.c_int, C.c_int,
+                                  C.c_double, C.c_double, C.c_int, c_int_p, C.c_int]
+    pts = np.asarray(points, np.float64)
+    x = np.ascontiguousarray(pts[:, 0])
+    y = np.ascontiguousarray(pts[:, 1])
+    cap = 4 * W * H if W * H < 1 << 20 else 1 << 22
+    out = np.zeros(cap, np.int32)
+    n = lib.or_road_cells(len(x), _p(x, C.c_double), _p(y, C.c_double), W, H, xs, ys, sem,
+                          _p(out, C.c_int), cap)
+    return out[:n].copy()
 
 
 def simulate_mte(P, Y, N, dt, params, init, caps, mmm, seed, road, species, sem, threads=1):

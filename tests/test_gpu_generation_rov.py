@@ -1,0 +1,149 @@
+"""The batched generation with every road valued in both modes: species
+models, MTE, initial animals at risk, the MTE penalty and the ROV valuation
+of each road in one launch sequence (and one captured graph).
+
+Each road's ROV result equals the batched ROV entry point (and the oracle)
+on the species models the generation built; the animals-at-risk match the
+FP64 oracle; the penalty follows Simulator.cpp:196-214 from the statistics.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from transportoptimiser_gb300 import simulate_gpu as sg
+from transportoptimiser_gb300 import synth
+from transportoptimiser_gb300._capi import MIG_AUTO, MIG_SPARSE_FP32
+from transportoptimiser_gb300.generation import Generation, pack_roads
+from transportoptimiser_gb300.rov import rov_problem_from_models
+
+pytestmark = pytest.mark.gpu
+
+IAR_RTOL = 1e-12
+
+
+def _scene(n_roads, seed=4):
+    sc = synth.generation(seed, n_roads=n_roads)
+    return sc
+
+
+def _template(gen, sc, P, Y, R, seed, road0=0):
+    models = [gen.species_model(0, s) for s in range(len(sc.species))]
+    return rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                   n_processes=3, demand=True, seed=seed, road=road0)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_generation_rov_matches_batched_entry_point(ctx, graph):
+    sc = _scene(6)
+    P, Y, R, road0 = 256, 20, 8, 30
+    gen = Generation(sc, max_roads=6, max_patches=512, ctx=ctx)
+    packed = pack_roads(sc, sc.roads)
+    # a first pass builds the models the template is taken from
+    gen.evaluate(packed, gen.opts(64, Y, seed=3, road0=road0, sem=1, migration=MIG_SPARSE_FP32))
+    gen.set_rov(_template(gen, sc, P, Y, R, seed=11, road0=road0))
+    o = gen.opts(64, Y, seed=3, road0=road0, sem=1, migration=MIG_AUTO, graph=graph)
+    res = gen.evaluate(packed, o)
+    res2 = gen.evaluate(packed, o)
+    np.testing.assert_array_equal(res, res2)
+    probs = []
+    for r in range(len(sc.roads)):
+        models = [gen.species_model(r, s) for s in range(3)]
+        probs.append(rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                             n_processes=3, demand=True, seed=11,
+                                             road=road0 + r))
+    ref = sg.simulateROVCUDA_batch(probs, want=("cond_exp",), ctx=ctx)
+    for r in range(len(sc.roads)):
+        st = ref[r]
+        for s in range(3):
+            blk = res[r, s]
+            assert blk[10] == st["stats"][0], (r, blk[10], st["stats"][0])
+            assert blk[11] == st["stats"][1]
+            assert blk[12] == st["stats"][2]
+            assert blk[13] == st["value_se"]
+            assert blk[14] == st["n_best"]
+    # two roads against the oracle on the same models
+    for r in (0, 4):
+        orc = po.simulate_rov(probs[r], threads=16)
+        assert np.array_equal(ref[r]["cond_exp"].astype(np.float32), orc["cond_exp"])
+        assert math.isclose(res[r, 0, 10], orc["stats"][0], rel_tol=1e-7)
+    gen.close()
+
+
+def test_generation_rov_off_again_and_mte_unchanged(ctx):
+    """Switching the ROV on does not change the MTE part of the result
+    block, and switching it off restores NaN ROV slots."""
+    sc = _scene(4, seed=6)
+    gen = Generation(sc, max_roads=4, max_patches=512, ctx=ctx)
+    packed = pack_roads(sc, sc.roads)
+    o = gen.opts(128, 15, seed=2, sem=1, migration=MIG_SPARSE_FP32)
+    plain = gen.evaluate(packed, o)
+    assert np.isnan(plain[:, :, 10:15]).all()
+    gen.set_rov(_template(gen, sc, 128, 15, 8, seed=5))
+    both = gen.evaluate(packed, o)
+    np.testing.assert_array_equal(both[:, :, :10], plain[:, :, :10])
+    np.testing.assert_array_equal(both[:, :, 16:], plain[:, :, 16:])
+    assert np.isfinite(both[:, :, 10:15]).all()
+    gen.set_rov(None)
+    again = gen.evaluate(packed, o)
+    np.testing.assert_array_equal(again, plain)
+    gen.close()
+
+
+@pytest.mark.parametrize("sem", [0, 1])
+def test_initial_animals_at_risk_match_oracle(ctx, sem):
+    sc = _scene(5, seed=7)
+    gen = Generation(sc, max_roads=5, max_patches=512, ctx=ctx)
+    res = gen.evaluate(pack_roads(sc, sc.roads), gen.opts(32, 5, sem=sem))
+    C = sc.n_controls
+    for r, rd in enumerate(sc.roads):
+        for s, sp in enumerate(sc.species):
+            om = po.species_model(sc, sp, rd, sem=sem, max_patches=1024)
+            np.testing.assert_allclose(res[r, s, 16:16 + C], om["iar"], rtol=IAR_RTOL, atol=0)
+            assert np.isnan(res[r, s, 16 + C:24]).all()
+            # zero flow kills nothing on the road
+            assert abs(om["iar"][0]) < 1e-12
+    # the single-road entry point
+    sp, rd = sc.species[1], sc.roads[2]
+    hab = sc.hab_map(rd)
+    gm = sg.createSpeciesModel(hab, sc.pop_map(sp, hab), sc.W, sc.H, sc.res, sp.habitats,
+                               rd.colmajor(), rd.G, sp.hazard, sp.lambda_mean, sem=sem,
+                               max_patches=512, ctx=ctx)
+    np.testing.assert_allclose(gm["iar"], res[2, 1, 16:16 + C], rtol=IAR_RTOL, atol=0)
+    gen.close()
+
+
+def test_mte_penalty(ctx):
+    """Simulator::simulateMTE's penalty from the end-population mean and SD,
+    z = NormalCDFInverse(1 - confidence) by Abramowitz & Stegun 26.2.23."""
+    sc = _scene(4, seed=8)
+    gen = Generation(sc, max_roads=4, max_patches=512, ctx=ctx)
+    packed = pack_roads(sc, sc.roads)
+    o = gen.opts(256, 30, seed=4)
+    base = gen.evaluate(packed, o)
+    assert (base[:, :, 8:10] == 0).all()
+    conf = 0.95
+    mean = base[:, :, 2]
+    thr = np.array([np.median(mean[:, s]) for s in range(3)])       # some roads below
+    initp = np.array([1000.0, 2000.0, 3000.0])
+    cost = np.array([1.5, 2.0, 0.5])
+    gen.set_penalty(conf, thr, initp, cost)
+    res = gen.evaluate(packed, o)
+
+    def ra(t):
+        return t - ((0.010328 * t + 0.802853) * t + 2.515517) / \
+            (((0.001308 * t + 0.189269) * t + 1.432788) * t + 1.0)
+    p = 1.0 - conf
+    z = -ra(math.sqrt(-2.0 * math.log(p))) if p < 0.5 else ra(math.sqrt(-2.0 * math.log(1 - p)))
+    assert abs(z + 1.645) < 2e-3
+    for r in range(4):
+        tot = 0.0
+        for s in range(3):
+            lb = z * res[r, s, 3] + res[r, s, 2]
+            want = float(thr[s] > lb) * (thr[s] - lb) * initp[s] * cost[s]
+            assert math.isclose(res[r, s, 8], want, rel_tol=1e-12, abs_tol=0.0)
+            tot += want
+        assert all(math.isclose(res[r, s, 9], tot, rel_tol=1e-12) for s in range(3))
+    assert (res[:, :, 8] > 0).any() and (res[:, :, 8] == 0).any()
+    gen.close()

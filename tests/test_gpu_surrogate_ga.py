@@ -8,11 +8,16 @@ from transportoptimiser_gb300.generation import Generation, pack_roads, pack_seg
 pytestmark = pytest.mark.gpu
 
 
-def test_device_rasterisation_equals_host_cells(ctx):
+@pytest.mark.parametrize("sem", [0, 1])
+def test_device_rasterisation_equals_host_cells(ctx, sem):
+    """RoadCells::computeRoadCells on the device (cells computed from the
+    segments inside to_evaluate_roads) against the host restatement the
+    scenes use, which the CPU tests pin to the oracle: the species models
+    and valuations of 48 roads are identical."""
     sc = synth.generation(4, n_roads=48)
     gen = Generation(sc, max_roads=48, max_patches=512, ctx=ctx)
-    a = gen.evaluate(pack_roads(sc, sc.roads), gen.opts(32, 10, seed=3))
-    b = gen.evaluate_segments(pack_segments(sc.roads), gen.opts(32, 10, seed=3))
+    a = gen.evaluate(pack_roads(sc, sc.roads, sem=sem), gen.opts(32, 10, seed=3, sem=sem))
+    b = gen.evaluate_segments(pack_segments(sc.roads), gen.opts(32, 10, seed=3, sem=sem))
     np.testing.assert_array_equal(a, b)
     gen.close()
 

@@ -49,7 +49,7 @@ class SpeciesOut(C.Structure):
                 ("area", c_double_p), ("cap", c_double_p), ("pop", c_double_p),
                 ("cx", c_double_p), ("cy", c_double_p), ("type", c_int_p),
                 ("crossings", c_int_p), ("trans", c_double_p),
-                ("surv", c_double_p), ("mmm", c_float_p)]
+                ("surv", c_double_p), ("mmm", c_float_p), ("iar", c_double_p)]
 
 
 class MteSpecies(C.Structure):
@@ -75,6 +75,11 @@ class MteDeviceProblem(C.Structure):
                 ("npad", C.c_int), ("dt", C.c_float), ("seed", C.c_uint64), ("road", C.c_int),
                 ("sem", C.c_int), ("n_patches", C.c_void_p), ("params", C.c_void_p),
                 ("init_pops", C.c_void_p), ("caps", C.c_void_p), ("mmm", C.c_void_p)]
+
+
+class Penalty(C.Structure):
+    _fields_ = [("confidence", C.c_double), ("threshold", c_double_p),
+                ("init_population", c_double_p), ("cost_per_animal", c_double_p)]
 
 
 class ExpPvParams(C.Structure):
@@ -105,7 +110,7 @@ class EvalOpts(C.Structure):
                 ("migration", C.c_int), ("graph", C.c_int)]
 
 
-RESULT_STRIDE = 8
+RESULT_STRIDE = 24
 
 
 class RovSpecies(C.Structure):
@@ -177,6 +182,8 @@ SIGNATURES = {
                                       C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(EvalOpts), C.c_void_p]),
     "to_ctx_tuning": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int]),
+    "to_scene_set_penalty": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "to_scene_set_rov": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "to_gen_end_pops": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                   c_float_p]),
     "to_gen_species_model": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
@@ -264,6 +271,16 @@ class Context:
 
     def profile(self, enable: bool = True) -> None:
         self.check(self.lib.to_ctx_profile(self.handle, int(enable)), "to_ctx_profile")
+
+    # kernels bracketed by the context's event timing (to_ctx_profile)
+    KERNEL_NAMES = ("adjoint_backward", "adjoint_forward", "knn", "knn_grid", "knn_solve",
+                    "lsm_prepare", "mte_simt", "mte_sparse", "mte_tc", "pack_csc", "rasterise",
+                    "road_features", "rov_backward", "rov_exog", "rov_forward",
+                    "rov_forward_sparse", "rov_resim", "select_samples", "species_labels",
+                    "species_links", "species_patches", "surrogate_regress", "tc_pack")
+
+    def kernel_names(self):
+        return self.KERNEL_NAMES
 
     def kernel_time(self, name: str):
         ms = C.c_double(0.0)

@@ -26,6 +26,7 @@
 #include "to_internal.cuh"
 #include "to_model.cuh"
 #include "to_pop.cuh"
+#include "to_rov.cuh"
 #include "to_sparse.cuh"
 
 struct to_gen_s {
@@ -71,6 +72,19 @@ struct to_gen_s {
     int last_R = 0, last_paths = 0;
     bool last_dense = false, last_csc = false;
     bool graph_dense = false, graph_csc = false;
+    double* d_iar = nullptr;             // [RS][C] initial animals at risk
+    // MTE penalty (to_scene_set_penalty): z = inverse normal CDF of
+    // (1 - confidence); per species threshold, initial population, cost
+    double pen_z = 0.0;
+    double* d_pen = nullptr;             // [S][3]
+    // ROV of every road (to_scene_set_rov)
+    bool rov_on = false;
+    to_rov_args rov{};                   // road-independent fields + scratch
+    char* rov_buf = nullptr;
+    size_t rov_bytes = 0;
+    int* d_road_ids = nullptr;           // [max_roads]
+    double* d_rov_stats = nullptr;       // [max_roads][5]
+    float* d_rov_params = nullptr;       // [S][8] species parameters of the ROV
 };
 
 namespace {
@@ -81,19 +95,50 @@ inline uint32_t __float_as_uint_host(float f) {
     return u;
 }
 
-__global__ void k_pack_results(int n_rs, const int* __restrict__ np,
+// MTE penalty of one species (Simulator::simulateMTE, Simulator.cpp:196-214):
+// the shortfall of the lower confidence bound z*SD + mean below the
+// threshold, times the initial population and the cost per animal
+__device__ __forceinline__ double mte_penalty(double mean, double sd, double z,
+                                              const double* pen) {
+    const double lb = z * sd + mean;
+    return (double)(pen[0] > lb) * (pen[0] - lb) * pen[1] * pen[2];
+}
+
+__global__ void k_pack_results(int n_rs, int S, const int* __restrict__ np,
                                const int* __restrict__ nt,
                                const double* __restrict__ stats,
                                const int* __restrict__ nnz, int C,
+                               const double* __restrict__ iar, double pen_z,
+                               const double* __restrict__ pen,
+                               const double* __restrict__ rov_stats,
                                double* __restrict__ out) {
     int rs = blockIdx.x * blockDim.x + threadIdx.x;
     if (rs >= n_rs) return;
+    const int road = rs / S, sp = rs - road * S;
     double* o = out + (size_t)rs * TO_RESULT_STRIDE;
     o[0] = np[rs];
     o[1] = nt[rs];
     for (int q = 0; q < 5; ++q) o[2 + q] = stats[5 * (size_t)rs + q];
     // non-zeros of the highest-flow migration matrix (-1: dense path used)
     o[7] = nnz ? (double)nnz[(size_t)rs * C + C - 1] : -1.0;
+    // penalty: this species' share, then the road's sum over its species
+    double mine = 0.0, road_pen = 0.0;
+    for (int s = 0; s < S; ++s) {
+        const double* st = stats + 5 * ((size_t)road * S + s);
+        const double v = mte_penalty(st[0], st[1], pen_z, pen + 3 * s);
+        if (s == sp) mine = v;
+        road_pen += v;
+    }
+    o[8] = mine;
+    o[9] = road_pen;
+    for (int q = 0; q < 5; ++q) o[10 + q] = rov_stats ? rov_stats[5 * (size_t)road + q] : NAN;
+    o[15] = 0.0;
+    for (int c = 0; c < 8; ++c) o[16 + c] = c < C ? iar[(size_t)rs * C + c] : NAN;
+}
+
+__global__ void k_road_ids(int R, int road0, int* __restrict__ ids) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < R) ids[r] = road0 + r;
 }
 
 __global__ void k_max_int(int n, const int* __restrict__ v, int* out) {
@@ -160,6 +205,7 @@ void model_args(to_gen g, int R, const int* cell_off, const int* cells, const in
     a.mmm = g->d_mmm; a.init_pops = g->d_ip; a.caps = g->d_cp;
     a.d_flags = ctx->d_flags;
     a.n_label_types = g->n_label_types; a.label_types = g->d_label_types; a.labels = g->d_labels;
+    a.iar = g->d_iar;
 }
 
 // the model kernel writes the packed migration matrices (no dense ones)
@@ -196,14 +242,37 @@ to_status run_choice(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int cho
     return to_k::mte_simt(ctx, m, RS);
 }
 
-// The launches after the model: migration Monte Carlo, statistics, results.
+// The ROV valuation of every road (simulateROVCUDA's ALGO4 per road, as
+// to_simulate_rov_batch runs it) on the species models this generation
+// built: the packed migration matrices of every control, the roads' patch
+// counts, initial populations and capacities, all already in HBM.
+to_status rov_stage(to_ctx ctx, to_gen g, int R, int NE, int road0) {
+    to_rov_args a = g->rov;
+    a.nr = R; a.PT = R * a.P; a.G = R * a.C;
+    a.lblocks = (a.PT + 1023) / 1024;
+    a.np = g->NP; a.ne = NE;
+    a.n_patches = g->d_np; a.params = g->d_rov_params; a.init_pops = g->d_ip;
+    a.caps = g->d_cp; a.mmm = g->d_mmm; a.road_ids = g->d_road_ids;
+    a.stats = g->d_rov_stats;
+    k_road_ids<<<(R + 127) / 128, 128, 0, ctx->stream>>>(R, road0, g->d_road_ids);
+    TO_LAUNCHED(ctx);
+    // the kNN's per-query search radius starts from last year's; clear it
+    // so that every generation starts the same way
+    TO_CUDA(ctx, cudaMemsetAsync(a.kth, 0, (size_t)a.G * a.Q * sizeof(float), ctx->stream));
+    return to_k::rov_run(ctx, a, &g->csc);
+}
+
+// The launches after the model: migration Monte Carlo, statistics, the ROV
+// of every road when the scene has one, results.
 to_status tail(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice,
                double* d_results_out) {
     TO_TRY(run_choice(ctx, g, m, RS, choice));
     TO_TRY(to_k::mte_stats(ctx, m, RS, g->d_stats));
+    const int R = RS / g->S;
+    if (g->rov_on) TO_TRY(rov_stage(ctx, g, R, m.npe, m.road0));
     k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(
-        RS, g->d_np, g->d_nt, g->d_stats, choice == CH_SPARSE ? g->csc.nnz : nullptr, g->C,
-        d_results_out);
+        RS, g->S, g->d_np, g->d_nt, g->d_stats, choice == CH_SPARSE ? g->csc.nnz : nullptr, g->C,
+        g->d_iar, g->pen_z, g->d_pen, g->rov_on ? g->d_rov_stats : nullptr, d_results_out);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }
@@ -253,8 +322,8 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     const int S = g->S, RS = R * S, NP = g->NP;
     if (!cell_off) {
         // road cells from the segments, on the device
-        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off,
-                                     g->d_cells, g->max_cells, g->d_counts));
+        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->xs, g->ys, o->sem,
+                                     g->d_cell_off, g->d_cells, g->max_cells, g->d_counts));
         cell_off = g->d_cell_off;
         cells = g->d_cells;
     }
@@ -262,14 +331,17 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     model_args(g, R, cell_off, cells, seg_off, segs, o, ctx, a);
     // sparse migration asked for: the model kernel writes the packed
     // matrices itself (the tuner's dense candidates need the dense form)
-    const bool packed = (o->migration == TO_MIG_SPARSE_FP32);
+    // (the ROV stage reads the packed matrices of every control, so a scene
+    // with a ROV always takes them from the model and runs the sparse kernel)
+    const bool packed = (o->migration == TO_MIG_SPARSE_FP32) || g->rov_on;
     if (packed) csc_direct(g, a);
     TO_TRY(to_k::species_model(ctx, a, RS));
     // the widest species model decides the tile shape of the path kernel
     int* d_max = reinterpret_cast<int*>(g->d_results + (size_t)g->max_roads * S * TO_RESULT_STRIDE);
     k_max_int<<<1, 1024, 0, ctx->stream>>>(RS, g->d_np, d_max);
     TO_LAUNCHED(ctx);
-    const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32);
+    const bool try_sparse = (o->migration == TO_MIG_AUTO || o->migration == TO_MIG_SPARSE_FP32 ||
+                             g->rov_on);
     if (try_sparse) {
         if (!packed) TO_TRY(to_k::pack_csc(ctx, g->d_mmm, NP, g->C, g->d_np, RS, g->csc));
         k_min_max_int<<<1, 1024, 0, ctx->stream>>>(RS * g->C, g->csc.nnz, d_max + 1);
@@ -285,12 +357,16 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     g->csc.cap_smem = (mm[2] + 7) & ~7;
     const bool sparse_ok = try_sparse && mm[1] >= 0 &&
                            to_k::mte_sparse_smem(NE, g->csc.cap_smem) <= ctx->smem_optin;
-    if (try_sparse && !sparse_ok && o->migration == TO_MIG_SPARSE_FP32)
+    if (try_sparse && !sparse_ok && (o->migration == TO_MIG_SPARSE_FP32 || g->rov_on))
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
+    if (g->rov_on && (mm[1] < 0 ||
+                      to_k::rov_sparse_smem(NE, g->C, g->csc.cap_smem) > ctx->smem_optin))
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "the ROV forward pass does not fit %d patches",
+                            NE);
     TO_TRY(grow_end(ctx, g, (size_t)RS * o->mte_paths));
     to_mte_args m = mte_args(ctx, g, o, NE);
     int choice;
-    if (o->migration == TO_MIG_SPARSE_FP32) choice = CH_SPARSE;
+    if (o->migration == TO_MIG_SPARSE_FP32 || g->rov_on) choice = CH_SPARSE;
     else if (o->migration == TO_MIG_TC_3XTF32) choice = CH_TC;
     else if (o->migration == TO_MIG_SIMT_FP32) choice = CH_SIMT;
     else TO_TRY(tuned_choice(ctx, g, m, RS, NE, sparse_ok, NE <= 512, &choice));
@@ -299,6 +375,16 @@ to_status evaluate_direct(to_ctx ctx, to_gen g, int R, const int* cell_off,
     g->last_R = R; g->last_paths = o->mte_paths;
     g->last_dense = !packed; g->last_csc = try_sparse;
     return TO_OK;
+}
+
+// road-independent key of the scene's valuation settings (a captured
+// generation is replayed only while they are unchanged)
+uint64_t settings_key(to_gen g) {
+    uint64_t h = mix(0, g->rov_on ? (uint64_t)g->rov.P * 131 + (uint64_t)g->rov.R : 0);
+    h = mix(h, (uint64_t)(uintptr_t)g->rov_buf);
+    uint64_t zb;
+    memcpy(&zb, &g->pen_z, 8);
+    return mix(h, zb);
 }
 
 // opts.graph: replay the captured generation when the call matches it,
@@ -315,7 +401,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
                                (uint64_t)o->mte_paths, (uint64_t)o->n_years,
                                (uint64_t)__float_as_uint_host(o->dt), o->seed,
                                (uint64_t)o->road0, (uint64_t)o->sem, (uint64_t)o->migration,
-                               (uint64_t)(uintptr_t)ctx->stream};
+                               (uint64_t)(uintptr_t)ctx->stream, settings_key(g)};
     for (uint64_t f : fields) key = mix(key, f);
     if (g->exec && g->graph_key == key) {
         TO_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream));
@@ -334,6 +420,7 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     int cap = ((plan[1] + plan[1] / 4 + 64) + 7) & ~7;
     if (cap > g->csc.cap) cap = g->csc.cap;
     if ((plan[2] == CH_SPARSE && to_k::mte_sparse_smem(ne, cap) > ctx->smem_optin) ||
+        (g->rov_on && to_k::rov_sparse_smem(ne, g->C, cap) > ctx->smem_optin) ||
         plan[2] == CH_TC) {
         // no margin where it does not fit (or would resize the tensor-core
         // scratch, which cannot be allocated inside a capture)
@@ -351,8 +438,8 @@ to_status evaluate(to_ctx ctx, to_gen g, int R, const int* cell_off,
     TO_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     to_status st = TO_OK;
     if (!cell_off) {
-        st = to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off, g->d_cells,
-                                   g->max_cells, g->d_counts);
+        st = to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->xs, g->ys, o->sem,
+                                   g->d_cell_off, g->d_cells, g->max_cells, g->d_counts);
         a.cell_off = g->d_cell_off;
         a.cells = g->d_cells;
     }
@@ -484,6 +571,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     acc(R * g->n_label_types * n * 4);
     const size_t cap = (size_t)NP * 32;
     acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
+    acc(RS * C * 8);
     if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
     g->buf_bytes = bytes;
     char* p = g->buf;
@@ -516,6 +604,9 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->csc.nnz = carve<int>(p, RS * C);
     g->csc.cap = (int)cap;
     g->csc.cap_smem = 0;
+    g->d_iar = carve<double>(p, RS * C);
+    if ((e = cudaMalloc(&g->d_pen, (size_t)S * 3 * sizeof(double))) != cudaSuccess) return fail(e);
+    if ((e = cudaMemset(g->d_pen, 0, (size_t)S * 3 * sizeof(double))) != cudaSuccess) return fail(e);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
     *out = g;
     return TO_OK;
@@ -533,7 +624,187 @@ to_status to_scene_destroy(to_gen g) {
     cudaFree(g->d_label_types);
     cudaFree(g->buf);
     cudaFree(g->d_end);
+    cudaFree(g->d_pen);
+    cudaFree(g->rov_buf);
     delete g;
+    return TO_OK;
+}
+
+// Abramowitz & Stegun 26.2.23 rational approximation of the upper normal
+// quantile, as Utility::NormalCDFInverse / RationalApproximation use it
+// (include/utilities/Utility.cpp:165-193); |error| < 4.5e-4
+static double normal_cdf_inverse(double p) {
+    auto ra = [](double t) {
+        return t - ((0.010328 * t + 0.802853) * t + 2.515517) /
+                   (((0.001308 * t + 0.189269) * t + 1.432788) * t + 1.0);
+    };
+    return p < 0.5 ? -ra(std::sqrt(-2.0 * std::log(p))) : ra(std::sqrt(-2.0 * std::log(1.0 - p)));
+}
+
+to_status to_scene_set_penalty(to_ctx ctx, to_gen g, const to_penalty* pen) {
+    if (!ctx || !g || !pen || !(pen->confidence > 0.0) || !(pen->confidence < 1.0) ||
+        !pen->threshold || !pen->init_population || !pen->cost_per_animal)
+        return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    std::vector<double> h((size_t)g->S * 3);
+    for (int s = 0; s < g->S; ++s) {
+        h[3 * s] = pen->threshold[s];
+        h[3 * s + 1] = pen->init_population[s];
+        h[3 * s + 2] = pen->cost_per_animal[s];
+        for (int q = 0; q < 3; ++q)
+            if (!std::isfinite(h[3 * s + q]))
+                return to_set_error(ctx, TO_ERR_NONFINITE, "penalty of species %d", s);
+    }
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    TO_CUDA(ctx, cudaMemcpy(g->d_pen, h.data(), h.size() * sizeof(double),
+                            cudaMemcpyHostToDevice));
+    g->pen_z = normal_cdf_inverse(1.0 - pen->confidence);
+    return TO_OK;
+}
+
+to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
+    if (!ctx || !g) return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (g->exec) { cudaGraphExecDestroy(g->exec); g->exec = nullptr; }
+    g->rov_on = false;
+    if (g->rov_buf) { cudaFree(g->rov_buf); g->rov_buf = nullptr; g->rov_bytes = 0; }
+    if (!t) return TO_OK;
+    const int S = g->S, C = g->C, P = t->n_paths, Y = t->n_years, U = t->n_uncertainties;
+    const int Rr = t->dim_res, d = S + 1, NR = g->max_roads;
+    const int algo = t->algo == 0 ? 4 : t->algo;
+    if (t->n_species != S || t->n_controls != C || P < 128 || Y < 3 || Rr < 2 || U < 0 ||
+        (U > 0 && !t->uncert) || !t->flows || t->n_fuels < 0 || t->n_commodities < 0 ||
+        t->n_fuels + t->n_commodities > U || t->n_fuels > 16 || t->n_commodities > 16 ||
+        t->demand_idx >= U)
+        return TO_ERR_INVALID;
+    if (t->sem != 1 || algo != 4 || d > TO_LSM_MAXD)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED,
+                            "a generation's ROV is ALGO4 with corrected semantics, <= %d species",
+                            TO_LSM_MAXD - 1);
+    for (int f = 0; f < t->n_fuels; ++f)
+        if (!t->fuel_costs || !t->fuel_idx || t->fuel_idx[f] < 0 || t->fuel_idx[f] >= U)
+            return TO_ERR_INVALID;
+    if (t->n_commodities > 0 && (!t->ore_content || !t->ore_sd)) return TO_ERR_INVALID;
+    for (int i = 0; i < 6 * U; ++i)
+        if (!std::isfinite(t->uncert[i])) return to_set_error(ctx, TO_ERR_NONFINITE, "uncert %d", i);
+    long Ql = 1;
+    for (int j = 0; j < d; ++j) Ql *= Rr;
+    if (Ql > (1L << 22) || (long)NR * C * Ql > 0x7fffffffL)
+        return to_set_error(ctx, TO_ERR_UNSUPPORTED, "grid %ld x %d groups", Ql, NR * C);
+    const int Q = (int)Ql;
+    if ((long)NR * P > (1L << 30)) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "paths");
+    int kmax = (P > 3) ? (int)(10.0 * (std::log((double)P) + 1.0)) : 1;
+    if (kmax > P) kmax = P;
+    if (kmax > TO_KNN_KMAX) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d", kmax);
+    const size_t PT = (size_t)NR * P, G = (size_t)NR * C;
+    const size_t blk = (size_t)Rr * d + 2 * (size_t)Q;
+    const size_t nacc = (size_t)(d + 1) * (d + 2);
+    const int lblocks = (int)((PT + 1023) / 1024);
+    const size_t U1 = (size_t)(U > 0 ? U : 1);
+    size_t bytes = 0;
+    auto acc = [&](size_t b) { bytes += to_align256(b); };
+    acc(C * 4); acc(6 * U1 * 4); acc(16 * 4); acc(16 * 4); acc(16 * 4); acc(16 * 4);
+    acc(NR * 4); acc((size_t)NR * 5 * 8); acc((size_t)S * 8 * 4);
+    acc((size_t)Y * PT * 4); acc(U1 * (Y + 1) * PT * 4); acc((size_t)S * (Y + 1) * PT * 4);
+    acc((size_t)S * C * Y * PT * 4);
+    acc(G * d * P * 4); acc(G * d * P * 4); acc(G * P * 4); acc(G * 4); acc(G * 4);
+    acc((size_t)NR * d * 4); acc((size_t)NR * d * 4); acc(G * d * P * 4); acc(G * P * 4);
+    acc(G * (TO_KNN_GCELLS + 1) * 4); acc(G * sizeof(to_knn_grid)); acc(G * Q * 4);
+    acc(G * lblocks * 4); acc(G * d * 2 * 4); acc(4); acc(G * Q * nacc * 4);
+    acc(G * blk * 4);
+    acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4);
+    acc((size_t)Y * S * PT * 4);
+    acc(G * Q); acc(G * Q * 4); acc(4);
+    cudaError_t e = cudaMalloc(&g->rov_buf, bytes);
+    if (e != cudaSuccess) {
+        g->rov_buf = nullptr;
+        cudaGetLastError();
+        return to_set_error(ctx, e == cudaErrorMemoryAllocation ? TO_ERR_ALLOC : TO_ERR_CUDA,
+                            "%zu bytes of ROV scratch", bytes);
+    }
+    TO_CUDA(ctx, cudaMemset(g->rov_buf, 0, bytes));
+    g->rov_bytes = bytes;
+    char* p = g->rov_buf;
+    to_rov_args a;
+    memset(&a, 0, sizeof(a));
+    a.P = P; a.Y = Y; a.S = S; a.C = C; a.U = U; a.R = Rr; a.Q = Q;
+    a.nF = t->n_fuels; a.Cm = t->n_commodities; a.demand_idx = t->demand_idx;
+    a.sem = 1; a.road = 0; a.dt = t->dt; a.rrr = t->rrr;
+    a.unit_cost = t->unit_cost; a.unit_revenue = t->unit_revenue; a.scaling = 2.0f;
+    a.seed = t->seed; a.kmax = kmax; a.algo = 4; a.k_mult = 10;
+    a.touched = 1; a.reg_one_year = 1;
+    float* d_flows = carve<float>(p, C);
+    float* d_unc = carve<float>(p, 6 * U1);
+    float* d_fc = carve<float>(p, 16);
+    int* d_fi = carve<int>(p, 16);
+    float* d_oc = carve<float>(p, 16);
+    float* d_os = carve<float>(p, 16);
+    g->d_road_ids = carve<int>(p, NR);
+    g->d_rov_stats = carve<double>(p, (size_t)NR * 5);
+    g->d_rov_params = carve<float>(p, (size_t)S * 8);
+    a.controls = carve<int>(p, (size_t)Y * PT);
+    a.uRes = carve<float>(p, U1 * (Y + 1) * PT);
+    a.totalPops = carve<float>(p, (size_t)S * (Y + 1) * PT);
+    a.aars = carve<float>(p, (size_t)S * C * Y * PT);
+    a.xraw = carve<float>(p, G * d * P);
+    a.xn = carve<float>(p, G * d * P);
+    a.yv = carve<float>(p, G * P);
+    a.npts = carve<int>(p, G);
+    a.kc = carve<int>(p, G);
+    a.gmin = carve<float>(p, (size_t)NR * d);
+    a.gmax = carve<float>(p, (size_t)NR * d);
+    a.gsx = carve<float>(p, G * d * P);
+    a.gsi = carve<int>(p, G * P);
+    a.gcell = carve<int>(p, G * (TO_KNN_GCELLS + 1));
+    a.ggrid = carve<to_knn_grid>(p, G);
+    a.kth = carve<float>(p, G * Q);
+    a.lcnt = carve<int>(p, G * lblocks);
+    a.lkey = carve<unsigned>(p, G * d * 2);
+    a.knn_next = carve<int>(p, 1);
+    a.knn_acc = carve<float>(p, G * Q * nacc);
+    a.reg = carve<float>(p, G * blk);
+    a.condExp = carve<float>(p, (size_t)Y * PT);
+    a.optCont = carve<int>(p, (size_t)Y * PT);
+    a.unitProfits = carve<float>(p, (size_t)Y * PT);
+    a.adjPops = carve<float>(p, (size_t)Y * S * PT);
+    a.qmark = carve<unsigned char>(p, G * Q);
+    a.qlist = carve<int>(p, G * Q);
+    a.qcount = carve<int>(p, 1);
+    TO_CUDA(ctx, cudaMemcpy(d_flows, t->flows, C * sizeof(float), cudaMemcpyHostToDevice));
+    if (U > 0)
+        TO_CUDA(ctx, cudaMemcpy(d_unc, t->uncert, 6 * (size_t)U * sizeof(float),
+                                cudaMemcpyHostToDevice));
+    if (t->n_fuels > 0) {
+        TO_CUDA(ctx, cudaMemcpy(d_fc, t->fuel_costs, t->n_fuels * sizeof(float),
+                                cudaMemcpyHostToDevice));
+        TO_CUDA(ctx, cudaMemcpy(d_fi, t->fuel_idx, t->n_fuels * sizeof(int),
+                                cudaMemcpyHostToDevice));
+    }
+    if (t->n_commodities > 0) {
+        TO_CUDA(ctx, cudaMemcpy(d_oc, t->ore_content, t->n_commodities * sizeof(float),
+                                cudaMemcpyHostToDevice));
+        TO_CUDA(ctx, cudaMemcpy(d_os, t->ore_sd, t->n_commodities * sizeof(float),
+                                cudaMemcpyHostToDevice));
+    }
+    a.flows = d_flows; a.uncert = d_unc; a.fuel_costs = d_fc; a.fuel_idx = d_fi;
+    a.ore_content = d_oc; a.ore_sd = d_os;
+    // species parameters of the ROV: the template's where it gives them,
+    // else the scene's (the MTE's)
+    if (t->species) {
+        std::vector<float> prm((size_t)S * 8);
+        for (int sp = 0; sp < S; ++sp) {
+            if (!t->species[sp].params) return TO_ERR_INVALID;
+            for (int q = 0; q < 8; ++q) prm[(size_t)sp * 8 + q] = t->species[sp].params[q];
+        }
+        TO_CUDA(ctx, cudaMemcpy(g->d_rov_params, prm.data(), prm.size() * sizeof(float),
+                                cudaMemcpyHostToDevice));
+    } else {
+        TO_CUDA(ctx, cudaMemcpy(g->d_rov_params, g->d_params, (size_t)S * 8 * sizeof(float),
+                                cudaMemcpyDeviceToDevice));
+    }
+    g->rov = a;
+    g->rov_on = true;
     return TO_OK;
 }
 
@@ -622,8 +893,8 @@ to_status to_road_features_d(to_ctx ctx, to_gen g, int R, const int* seg_off,
         return TO_ERR_INVALID;
     cudaSetDevice(ctx->device);
     if (!cell_off) {
-        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->d_cell_off,
-                                     g->d_cells, g->max_cells, g->d_counts));
+        TO_TRY(to_k::rasterise_roads(ctx, R, seg_off, segs, g->W, g->H, g->xs, g->ys, TO_SEM_CORRECTED,
+                                     g->d_cell_off, g->d_cells, g->max_cells, g->d_counts));
         cell_off = g->d_cell_off;
         cells = g->d_cells;
     }

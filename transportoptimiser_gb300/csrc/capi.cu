@@ -395,7 +395,7 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
                    to_align256((size_t)NM * NM * 2) +
                    to_align256((size_t)C * NM * NM * 8) +
                    to_align256((size_t)C * NP * NP * 4) + to_align256((size_t)NP * 4) * 2 +
-                   4096;
+                   to_align256((size_t)C * 8) + 4096;
     TO_TRY(to_arena_reserve(ctx, bytes));
     int* d_hab = to_arena_take<int>(ctx, n);
     float* d_pop = to_arena_take<float>(ctx, n);
@@ -419,7 +419,8 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
     a.mmm = to_arena_take<float>(ctx, (size_t)C * NP * NP);
     a.init_pops = to_arena_take<float>(ctx, NP);
     a.caps = to_arena_take<float>(ctx, NP);
-    if (!a.caps) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
+    a.iar = out->iar ? to_arena_take<double>(ctx, C) : nullptr;
+    if (!a.caps || (out->iar && !a.iar)) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
     std::vector<float> pf(n);
     for (size_t i = 0; i < n; ++i) pf[i] = (float)in->pop_map[i];
     int G = in->G;
@@ -456,6 +457,7 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
     if (out->trans) { tr.resize((size_t)NM * NM); TO_TRY(d2h(ctx, tr.data(), a.trans, tr.size())); }
     if (out->surv) { sv.resize((size_t)C * NM * NM); TO_TRY(d2h(ctx, sv.data(), a.surv, sv.size())); }
     if (out->mmm) { mm.resize((size_t)C * NP * NP); TO_TRY(d2h(ctx, mm.data(), a.mmm, mm.size())); }
+    if (out->iar) TO_TRY(d2h(ctx, out->iar, a.iar, (size_t)C));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int i = 0; i < N; ++i)
         for (int j = 0; j < N; ++j) {

@@ -700,8 +700,7 @@ __global__ void k_knn_solve(to_rov_args a, int t) {
     }
     if (item >= a.G * a.Q) return;
     const int c = item / a.Q, qi = item - c * a.Q;
-    const size_t blk = (size_t)a.R * D + 2 * (size_t)a.Q;
-    float* yout = a.reg + ((size_t)t * a.G + c) * blk + (size_t)a.R * D;
+    float* yout = to_rov_reg_block(a, t, c) + (size_t)a.R * D;
     const int n = a.npts[c], k = a.kc[c];
     yout[qi] = (n < 3 || k <= 0)
                    ? 0.0f

@@ -805,6 +805,7 @@ k_species_links(to_model_args a) {
         const size_t at = (size_t)i * NM + (f - s_off[i]);
         const int j = dj[at];
         const double tr = wv[at] / s_sum[i];
+        wv[at] = tr;                           // kept for the animals-at-risk sums
         const int cr = cross[(size_t)i * N + j];
         if (direct) {
             // the pair's place in destination j's list (in range is
@@ -825,6 +826,31 @@ k_species_links(to_model_args a) {
             }
         }
         if (trans) trans[(size_t)i * NM + j] = tr;
+    }
+    if (a.iar) {
+        // initial animals at risk per control (SpeciesRoadPatches::
+        // computeAAR / computeInitialAAR, SpeciesRoadPatches.cpp:453-490):
+        // 1 - sum_i pop_i sum_j trans(i,j) surv_c(i,j) / sum_i pop_i, each
+        // row over its listed destinations ascending, rows ascending
+        __syncthreads();
+        for (int c = 0; c < a.C; ++c) {
+            for (int i = threadIdx.x; i < N; i += blockDim.x) {
+                const double* rowv = wv + (size_t)i * NM;
+                const uint16_t* rowj = dj + (size_t)i * NM;
+                const int n = s_off[i + 1] - s_off[i];
+                double acc = 0.0;
+                for (int q = 0; q < n; ++q)
+                    acc += rowv[q] * surv_of(c, cross[(size_t)i * N + rowj[q]]);
+                s_sum[i] = popd[i] * acc;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double tot = 0.0, init = 0.0;
+                for (int i = 0; i < N; ++i) { tot += s_sum[i]; init += popd[i]; }
+                a.iar[(size_t)rs * a.C + c] = 1.0 - tot / init;
+            }
+            __syncthreads();
+        }
     }
     if (direct) {
         // packed matrices: destination j's entries are the listed origins

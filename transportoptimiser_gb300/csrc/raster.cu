@@ -1,53 +1,127 @@
 // raster.cu - road cells of a generation of polylines on the device, and the
 // per-road features the learned surrogate reads.
 //
-// The reference builds a road's cells on the host (RoadCells::computeRoadCells,
-// include/transport/RoadCells.cpp:10-) once per road per evaluation.  Here a
-// CTA per road marks the cells of its segments in a shared-memory bitmap of
-// the grid and writes them in ascending cell order.  A segment (x1, y1) ->
-// (x2, y2) of length L is sampled at n = max(2, ceil(4 L)) + 1 points
-// s_i = i / (n - 1) (the last one exactly 1); sample i lies in cell
-// (rint(x1 + s_i (x2 - x1)), rint(y1 + s_i (y2 - y1))) when inside the grid
-// - the definition the synthetic roads use (synth.road_cells), in the same
-// double arithmetic and round-half-even.
+// The reference builds a road's cells on the host once per road per
+// evaluation (RoadCells::computeRoadCells, include/road/RoadCells.cpp:10-272):
+// each span between consecutive road points is cut at its crossings of the
+// grid lines x = k xs and y = k ys, the span's points are sorted by (x, y)
+// (ascending when the span runs towards larger x, else descending), equal
+// neighbours are dropped, and each piece between consecutive points lies in
+// the cell (ceil(mid_x / xs), ceil(mid_y / ys)) of its midpoint.  Here a CTA
+// per road has each warp take one span at a time: the lanes write the
+// span's crossings to shared memory, rank them (the same order an
+// insertion sort gives: a point's rank counts the points before it, ties
+// by position), and mark the midpoint cells of consecutive points in a
+// shared-memory bitmap of the grid; the road's cells leave in ascending
+// order.  The arithmetic is the reference's, operation for operation, in
+// double; `sem` 0 keeps its quirk for the x of a vertical-line crossing
+// (computed from row q of the crossing list, RoadCells.cpp:189-194), 1 uses
+// the crossing's own y.
 #include "to_internal.cuh"
 #include "to_model.cuh"
 
 namespace {
 
-// marks the cells of road r in the bitmap (W*H bits)
-__device__ void mark_road(int r, const int* __restrict__ seg_off, const double* __restrict__ segs,
-                          int W, int H, unsigned* bits) {
-    const int g0 = seg_off[r], g1 = seg_off[r + 1];
-    for (int g = g0; g < g1; ++g) {
-        const double x1 = segs[4 * (size_t)g], y1 = segs[4 * (size_t)g + 1];
-        const double x2 = segs[4 * (size_t)g + 2], y2 = segs[4 * (size_t)g + 3];
-        const double dx = x2 - x1, dy = y2 - y1;
-        int n = (int)ceil(4.0 * hypot(dx, dy));
-        n = (n > 2 ? n : 2) + 1;
-        const double step = 1.0 / (double)(n - 1);
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const double s = (i == n - 1) ? 1.0 : (double)i * step;
-            const double xs = x1 + s * dx, ys = y1 + s * dy;
-            const double xr = rint(xs), yr = rint(ys);
-            if (!(xr >= 0.0 && xr < (double)W && yr >= 0.0 && yr < (double)H)) continue;
-            const int c = (int)xr + (int)yr * W;
+constexpr int kRasterWarps = 4;
+constexpr int kSpanMax = 1024;         // crossings of one span
+struct SpanPt { double x, y; };
+
+__device__ __forceinline__ bool pt_less(SpanPt a, SpanPt b) {
+    return a.x < b.x || (a.x == b.x && a.y < b.y);
+}
+
+struct RasterArgs {
+    const int* seg_off;
+    const double* segs;
+    int W, H, sem;
+    double xs, ys;
+    int* flags;
+};
+
+// marks the cells of road r in the bitmap (W*H bits); scratch: per warp
+// two buffers of kSpanMax points
+__device__ void mark_road(int r, const RasterArgs& a, unsigned* bits, SpanPt* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    SpanPt* raw = scratch + (size_t)warp * 2 * kSpanMax;
+    SpanPt* srt = raw + kSpanMax;
+    const double xs = a.xs, ys = a.ys;
+    const int g0 = a.seg_off[r], g1 = a.seg_off[r + 1];
+    for (int g = g0 + warp; g < g1; g += nw) {
+        const double x0 = a.segs[4 * (size_t)g], y0 = a.segs[4 * (size_t)g + 1];
+        const double x1 = a.segs[4 * (size_t)g + 2], y1 = a.segs[4 * (size_t)g + 3];
+        const int h = (int)(x1 / xs) - (int)(x0 / xs);
+        const int v = (int)(y1 / ys) - (int)(y0 / ys);
+        const int ah = h < 0 ? -h : h, av = v < 0 ? -v : v, n = ah + av;
+        if (n > kSpanMax) {                    // longer than any span inside the grid
+            if (lane == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_CELL);
+            continue;
+        }
+        const double m = (y1 - y0) / (x1 - x0), b = y0 - x0 * m;
+        const double m2 = (x1 - x0) / (y1 - y0), b2 = x0 - y0 * m2;
+        const bool mf = isfinite(m), m2f = isfinite(m2);
+        for (int q = lane; q < ah; q += 32) {
+            double px;
+            if (h > 0) px = xs * (floor(x0 / xs) + (double)(q + 1));
+            else if (fmod(x0, xs) == 0.0) px = xs * (ceil(x0 / xs) - (double)q);
+            else px = xs * (ceil(x0 / xs) - (double)(q + 1));
+            raw[q].x = px;
+            raw[q].y = mf ? m * px + b : y0;
+        }
+        for (int q = lane; q < av; q += 32) {
+            double py;
+            if (v > 0) py = ys * (floor(y0 / ys) + (double)(q + 1));
+            else if (fmod(y0, ys) == 0.0) py = ys * (ceil(y0 / ys) - (double)q);
+            else py = ys * (ceil(y0 / ys) - (double)(q + 1));
+            raw[ah + q].y = py;
+        }
+        __syncwarp();
+        for (int q = lane; q < av; q += 32) {
+            const double src = (a.sem == 0) ? raw[q].y : raw[ah + q].y;
+            raw[ah + q].x = mf ? (src - b) / m : (m2f ? b2 + m2 * src : x0);
+        }
+        __syncwarp();
+        const bool asc = x1 >= x0;
+        for (int i = lane; i < n; i += 32) {
+            const SpanPt pi = raw[i];
+            int rank = 0;
+            for (int j = 0; j < n; ++j) {
+                const SpanPt pj = raw[j];
+                const bool before = asc ? pt_less(pj, pi) : pt_less(pi, pj);
+                const bool tie = !pt_less(pj, pi) && !pt_less(pi, pj);
+                rank += (before || (tie && j < i)) ? 1 : 0;
+            }
+            srt[rank] = pi;
+        }
+        __syncwarp();
+        for (int k = lane; k <= n; k += 32) {
+            SpanPt pa, pb;
+            if (k == 0) { pa.x = x0; pa.y = y0; } else pa = srt[k - 1];
+            if (k == n) { pb.x = x1; pb.y = y1; } else pb = srt[k];
+            if (pa.x == pb.x && pa.y == pb.y) continue;
+            const double cxd = ceil((0.5 * (pa.x + pb.x) - 0.0) / xs);
+            const double cyd = ceil((0.5 * (pa.y + pb.y) - 0.0) / ys);
+            if (!(cxd >= 0.0 && cxd < (double)a.W && cyd >= 0.0 && cyd < (double)a.H)) continue;
+            const int c = (int)cxd + (int)cyd * a.W;
             atomicOr(&bits[c >> 5], 1u << (c & 31));
         }
+        __syncwarp();
     }
 }
 
-__global__ void k_raster_count(int R, const int* __restrict__ seg_off,
-                               const double* __restrict__ segs, int W, int H,
-                               int* __restrict__ counts) {
-    extern __shared__ unsigned bits[];
+__device__ __forceinline__ SpanPt* span_scratch(unsigned* bits, int nw) {
+    return reinterpret_cast<SpanPt*>(bits + ((nw + 3) & ~3));
+}
+
+__global__ void k_raster_count(int R, RasterArgs ra, int* __restrict__ counts) {
+    extern __shared__ __align__(16) unsigned bits[];
     __shared__ int s_c;
     const int r = blockIdx.x;
+    const int W = ra.W, H = ra.H;
     const int nw = (W * H + 31) >> 5;
     for (int i = threadIdx.x; i < nw; i += blockDim.x) bits[i] = 0u;
     if (threadIdx.x == 0) s_c = 0;
     __syncthreads();
-    mark_road(r, seg_off, segs, W, H, bits);
+    mark_road(r, ra, bits, span_scratch(bits, nw));
     __syncthreads();
     int c = 0;
     for (int i = threadIdx.x; i < nw; i += blockDim.x) c += __popc(bits[i]);
@@ -85,17 +159,16 @@ __global__ void k_scan_counts(int R, const int* __restrict__ counts, int* __rest
     }
 }
 
-__global__ void k_raster_write(int R, const int* __restrict__ seg_off,
-                               const double* __restrict__ segs, int W, int H,
-                               const int* __restrict__ off, int max_cells,
+__global__ void k_raster_write(int R, RasterArgs ra, const int* __restrict__ off, int max_cells,
                                int* __restrict__ cells) {
-    extern __shared__ unsigned bits[];
+    extern __shared__ __align__(16) unsigned bits[];
     __shared__ int s_w[32];
     const int r = blockIdx.x;
+    const int W = ra.W, H = ra.H;
     const int nw = (W * H + 31) >> 5;
     for (int i = threadIdx.x; i < nw; i += blockDim.x) bits[i] = 0u;
     __syncthreads();
-    mark_road(r, seg_off, segs, W, H, bits);
+    mark_road(r, ra, bits, span_scratch(bits, nw));
     __syncthreads();
     // ascending cell order: each thread takes a contiguous run of words
     const int nt = blockDim.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -310,18 +383,23 @@ __global__ void k_road_features(int R, int W, int H, const int* __restrict__ bas
 namespace to_k {
 
 to_status rasterise_roads(to_ctx ctx, int R, const int* seg_off, const double* segs, int W, int H,
-                          int* cell_off, int* cells, int max_cells, int* counts_scratch) {
-    const size_t smem = (size_t)((W * H + 31) >> 5) * sizeof(unsigned);
+                          double xs, double ys, int sem, int* cell_off, int* cells, int max_cells,
+                          int* counts_scratch) {
+    const size_t nw = (size_t)((W * H + 31) >> 5);
+    const size_t smem = ((nw + 3) & ~size_t(3)) * sizeof(unsigned) +
+                        (size_t)kRasterWarps * 2 * kSpanMax * sizeof(SpanPt);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "grid %d x %d too large to rasterise", W, H);
+    if (!(xs > 0.0) || !(ys > 0.0)) return to_set_error(ctx, TO_ERR_INVALID, "grid spacing");
+    RasterArgs ra{seg_off, segs, W, H, sem, xs, ys, ctx->d_flags};
     TO_CUDA(ctx, cudaFuncSetAttribute(k_raster_count, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
     TO_CUDA(ctx, cudaFuncSetAttribute(k_raster_write, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
     to_prof_begin(ctx, "rasterise");
-    k_raster_count<<<R, 256, smem, ctx->stream>>>(R, seg_off, segs, W, H, counts_scratch);
+    k_raster_count<<<R, kRasterWarps * 32, smem, ctx->stream>>>(R, ra, counts_scratch);
     k_scan_counts<<<1, 1024, 0, ctx->stream>>>(R, counts_scratch, cell_off, max_cells, ctx->d_flags);
-    k_raster_write<<<R, 256, smem, ctx->stream>>>(R, seg_off, segs, W, H, cell_off, max_cells, cells);
+    k_raster_write<<<R, kRasterWarps * 32, smem, ctx->stream>>>(R, ra, cell_off, max_cells, cells);
     to_prof_end(ctx);
     ctx->launches += 3;
     TO_CUDA(ctx, cudaGetLastError());

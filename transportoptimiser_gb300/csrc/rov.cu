@@ -457,7 +457,6 @@ __global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
         a.gmin[(size_t)r * d + j] = lo;
         a.gmax[(size_t)r * d + j] = hi;
     }
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
     for (int c = 0; c < C; ++c) {
         const size_t g = (size_t)r * C + c;
         const int n = cnt[c];
@@ -469,7 +468,7 @@ __global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
         a.npts[g] = n;
         a.kc[g] = k;
         // axis values of the regression grid (createQueryPoints :1187-1190)
-        float* ax = a.reg + ((size_t)t * a.G + g) * blk;
+        float* ax = to_rov_reg_block(a, t, g);
         for (int j = 0; j < d; ++j)
             for (int di = 0; di < R; ++di)
                 ax[(size_t)j * R + di] = to_lsm_query_axis(di, mn[C][j], mx[C][j], R);
@@ -510,14 +509,13 @@ __global__ void __launch_bounds__(256) k_lsm_mark(to_rov_args a, int t) {
         for (int s = 0; s < S; ++s) state[c * S + s] = adj_pop(a, p, t, s, c);
     const int sy = a.Y + 1;
     const float prof = unit_profit(a, p, t, sy, sy);
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
     for (int c = 0; c < C; ++c) {
         bool valid = true;
         for (int s = 0; s < S; ++s)
             if (state[c * S + s] < threshold(a, s) && c > 0) { valid = false; break; }
         if (!valid) continue;
         const size_t g = (size_t)r * C + c;
-        const float* rb = a.reg + ((size_t)t * a.G + g) * blk;
+        const float* rb = to_rov_reg_block(a, t, g);
         int li[TO_LSM_MAXD];
         for (int j = 0; j < d; ++j) {
             const float v = (j < S) ? state[c * S + j] : prof;

@@ -104,8 +104,11 @@ to_status build_patches(to_ctx ctx, int W, int H, int skpx, int skpy, int xres,
 to_status line_segment_intersect(to_ctx ctx, int T, const double* d_xy1, int G,
                                  const double* d_xy2, int* d_cross);
 // raster.cu
+// RoadCells::computeRoadCells for every road (grid spacing xs, ys; sem 0
+// keeps the reference's vertical-crossing quirk)
 to_status rasterise_roads(to_ctx ctx, int R, const int* seg_off, const double* segs, int W,
-                          int H, int* cell_off, int* cells, int max_cells, int* counts_scratch);
+                          int H, double xs, double ys, int sem, int* cell_off, int* cells,
+                          int max_cells, int* counts_scratch);
 to_status road_features(to_ctx ctx, int R, int W, int H, const int* base, const float* popmap,
                         const int* seg_off, const double* segs, const int* cell_off,
                         const int* cells, float* feat);

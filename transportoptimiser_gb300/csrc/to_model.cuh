@@ -57,6 +57,7 @@ struct to_model_args {
     int n_label_types;           // T
     const int* label_types;      // [T] habitat codes
     int* labels;                 // [R][T][W*H] LabelImage numbers, 0 background
+    double* iar;                 // optional [RS][C] initial animals at risk per control
     float* init_pops;            // [RS][NP]
     float* caps;                 // [RS][NP] (padding 1.0)
     int* d_flags;

@@ -76,6 +76,9 @@ struct to_rov_args {
     unsigned char* qmark;             // [G][Q] marks of the current year (kept zero between years)
     int* qlist;                       // [G*Q] flat items g*Q + q of the marked queries
     int* qcount;                      // number of entries in qlist
+    // 1: reg holds only the current year's blocks (the regressions of year
+    // t are written and read within year t; nothing returns them)
+    int reg_one_year;
     // outputs (device)
     float* reg;                       // [Y][G][R*d + 2Q]
     float* condExp;                   // [Y][PT]
@@ -84,6 +87,13 @@ struct to_rov_args {
     float* adjPops;                   // [Y][S][PT]
     double* stats;                    // [nr][5]: value, control, SD, SE, n
 };
+
+// regression block of (year t, group g): axis values [R*d], then the Q
+// grid values, then Q standard deviations
+__host__ __device__ __forceinline__ float* to_rov_reg_block(const to_rov_args& a, int t, size_t g) {
+    const size_t blk = (size_t)a.R * (a.S + 1) + 2 * (size_t)a.Q;
+    return a.reg + ((size_t)(a.reg_one_year ? 0 : t) * a.G + g) * blk;
+}
 
 // grid query q of the current year: normalised coordinates (for kNN) and
 // the coordinates the regression centres on (createQueryPoints + host

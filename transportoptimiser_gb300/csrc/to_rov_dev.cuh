@@ -89,7 +89,6 @@ __device__ __forceinline__ void decide_interior(const to_rov_args& a, int t, int
                                                 const float* state, float& best, int& bc) {
     const int C = a.C, S = a.S, d = S + 1, R = a.R;
     const float disc = 1.0f + a.rrr * a.dt / 100.0f;
-    const size_t blk = (size_t)R * d + 2 * (size_t)a.Q;
     best = 0.0f;
     bc = 0;
     for (int c = 0; c < C; ++c) {
@@ -99,7 +98,7 @@ __device__ __forceinline__ void decide_interior(const to_rov_args& a, int t, int
         float pay = 0.0f;
         if (valid) {
             float cur = a.flows[c] * state[S * C];
-            const float* rb = a.reg + ((size_t)t * a.G + (size_t)r * C + c) * blk;
+            const float* rb = to_rov_reg_block(a, t, (size_t)r * C + c);
             float v = (a.sem == 0) ? to_lsm_interp_ref(rb, R, S, C, state)
                                    : to_lsm_interp(rb, R, S, state + c * S, state[S * C]);
             double ce = (double)(v / disc);

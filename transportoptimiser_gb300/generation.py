@@ -13,11 +13,12 @@ from .synth import Scene as SynthScene
 from .synth import road_cells
 
 
-def pack_roads(scene: SynthScene, roads) -> dict:
-    """CSR arrays (cell offsets, cells, segment offsets, segments)."""
+def pack_roads(scene: SynthScene, roads, sem: int = 1) -> dict:
+    """CSR arrays (cell offsets, cells, segment offsets, segments); the road
+    cells by RoadCells::computeRoadCells' rule (sem 0 keeps its quirk)."""
     cell_off, cells, seg_off, segs = [0], [], [0], []
     for rd in roads:
-        cs = [x + y * scene.W for (x, y) in road_cells(rd, scene.W, scene.H)]
+        cs = [x + y * scene.W for (x, y) in road_cells(rd, scene.W, scene.H, sem=sem)]
         cells.extend(cs)
         cell_off.append(len(cells))
         segs.append(np.asarray(rd.segments, np.float64).reshape(-1))
@@ -113,6 +114,30 @@ class Generation:
             self.ctx.handle, self.handle, R, C.c_void_p(d_cell_off), C.c_void_p(d_cells),
             C.c_void_p(d_seg_off), C.c_void_p(d_segs), C.byref(opts),
             C.c_void_p(d_results)), "to_evaluate_roads_d")
+
+    def set_penalty(self, confidence, threshold, init_population, cost_per_animal):
+        """MTE penalty per species (to_scene_set_penalty)."""
+        arrs = [np.ascontiguousarray(x, np.float64) for x in (threshold, init_population,
+                                                             cost_per_animal)]
+        pen = _capi.Penalty(confidence, *[ptr(a, C.c_double) for a in arrs])
+        self.ctx.check(self.ctx.lib.to_scene_set_penalty(self.ctx.handle, self.handle,
+                                                         C.byref(pen)), "to_scene_set_penalty")
+
+    def set_rov(self, problem: dict | None, species_params: bool = True):
+        """ROV valuation of every road in evaluate() (to_scene_set_rov).
+        ``problem`` is a ROV problem dict (transportoptimiser_gb300.rov) whose
+        road-independent fields apply to every road; its species' params are
+        used when species_params, else the scene's.  None switches it off."""
+        if problem is None:
+            self.ctx.check(self.ctx.lib.to_scene_set_rov(self.ctx.handle, self.handle, None),
+                           "to_scene_set_rov")
+            return
+        from .simulate_gpu import rov_ctypes
+        pr, keep = rov_ctypes(problem)
+        if not species_params:
+            pr.species = None
+        self.ctx.check(self.ctx.lib.to_scene_set_rov(self.ctx.handle, self.handle, C.byref(pr)),
+                       "to_scene_set_rov")
 
     def end_pops(self, road: int, species: int, n_paths: int) -> np.ndarray:
         """Per-path end populations of (road, species) from the last call."""

@@ -115,6 +115,8 @@ def createSpeciesModel(hab_map, pop_map, W, H, res, habitats, road_colmajor, G, 
     out.trans = ptr(big["trans"], C.c_double)
     out.surv = ptr(big["surv"], C.c_double)
     out.mmm = ptr(big["mmm"], C.c_float)
+    iar = np.zeros(Cn)
+    out.iar = ptr(iar, C.c_double)
     ctx.check(ctx.lib.to_species_model(ctx.handle, C.byref(inp), C.byref(out)),
               "to_species_model")
     N = out.n_patches
@@ -127,6 +129,7 @@ def createSpeciesModel(hab_map, pop_map, W, H, res, habitats, road_colmajor, G, 
     res_["mmm"] = big["mmm"][:Cn * N * N].reshape(Cn, N, N).copy()
     res_["init_pops"] = res_["pop"].astype(np.float32)
     res_["caps"] = res_["cap"].astype(np.float32)
+    res_["iar"] = iar
     return res_
 
 

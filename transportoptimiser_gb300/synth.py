@@ -85,17 +85,71 @@ class Scene:
         return np.where(habitable, sp.density, 0.0).astype(np.float64)
 
 
-def road_cells(road: Road, W: int, H: int) -> list:
-    """Cells a polyline passes through (sampled every 0.25 cells)."""
+def _span_points(x0, y0, x1, y1, xs, ys, sem):
+    """The grid-line crossings of one span, sorted as RoadCells sorts them."""
+    f = np.float64
+    x0, y0, x1, y1, xs, ys = f(x0), f(y0), f(x1), f(y1), f(xs), f(ys)
+    h = int(x1 / xs) - int(x0 / xs)
+    v = int(y1 / ys) - int(y0 / ys)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        m = (y1 - y0) / (x1 - x0)
+        b = y0 - x0 * m
+        m2 = (x1 - x0) / (y1 - y0)
+        b2 = x0 - y0 * m2
+    pts = []
+    for q in range(abs(h)):
+        if h > 0:
+            px = xs * (f(math.floor(x0 / xs)) + f(q + 1))
+        elif math.fmod(x0, xs) == 0.0:
+            px = xs * (f(math.ceil(x0 / xs)) - f(q))
+        else:
+            px = xs * (f(math.ceil(x0 / xs)) - f(q + 1))
+        pts.append([px, m * px + b if np.isfinite(m) else y0])
+    vy = []
+    for q in range(abs(v)):
+        if v > 0:
+            vy.append(ys * (f(math.floor(y0 / ys)) + f(q + 1)))
+        elif math.fmod(y0, ys) == 0.0:
+            vy.append(ys * (f(math.ceil(y0 / ys)) - f(q)))
+        else:
+            vy.append(ys * (f(math.ceil(y0 / ys)) - f(q + 1)))
+    ycol = [p[1] for p in pts] + vy           # column 1 of the crossing list
+    for q in range(abs(v)):
+        src = ycol[q] if sem == 0 else vy[q]
+        if np.isfinite(m):
+            px = (src - b) / m
+        elif np.isfinite(m2):
+            px = b2 + m2 * src
+        else:
+            px = x0
+        pts.append([px, vy[q]])
+    pts.sort(key=lambda p: (p[0], p[1]), reverse=not (x1 >= x0))
+    return pts
+
+
+def road_cells(road: Road, W: int, H: int, sem: int = 1, xs: float = 1.0,
+               ys: float = 1.0) -> list:
+    """Cells of a road as RoadCells::computeRoadCells (include/road/
+    RoadCells.cpp:10-272) finds them: each span is cut at its crossings of
+    the grid lines x = k xs and y = k ys (sorted by (x, y), ascending when
+    the span runs towards larger x, else descending), consecutive equal
+    points are dropped, and each piece lies in the cell (ceil(mid_x / xs),
+    ceil(mid_y / ys)) of its midpoint.  sem 0 keeps the reference's x of a
+    vertical-line crossing, computed from the y of the crossing list's row
+    q (RoadCells.cpp:189-194); sem 1 uses the crossing's own y.  Returns
+    the sorted (x, y) cells inside the grid."""
     cells = set()
     for x1, y1, x2, y2 in road.segments:
-        n = max(2, int(math.ceil(4.0 * math.hypot(x2 - x1, y2 - y1))) + 1)
-        for s in np.linspace(0.0, 1.0, n):
-            x = int(round(x1 + s * (x2 - x1)))
-            y = int(round(y1 + s * (y2 - y1)))
-            if 0 <= x < W and 0 <= y < H:
-                cells.add((x, y))
-    return sorted(cells)
+        seq = [[np.float64(x1), np.float64(y1)]] + _span_points(x1, y1, x2, y2, xs, ys, sem) + \
+              [[np.float64(x2), np.float64(y2)]]
+        for a, b in zip(seq[:-1], seq[1:]):
+            if a[0] == b[0] and a[1] == b[1]:
+                continue
+            cx = int(math.ceil((np.float64(0.5) * (a[0] + b[0]) - np.float64(0.0)) / np.float64(xs)))
+            cy = int(math.ceil((np.float64(0.5) * (a[1] + b[1]) - np.float64(0.0)) / np.float64(ys)))
+            if 0 <= cx < W and 0 <= cy < H:
+                cells.add((cx, cy))
+    return sorted(cells, key=lambda c: c[0] + c[1] * W)
 
 
 def _rng(seed: int) -> np.random.Generator:
