@@ -24,8 +24,8 @@ from transportoptimiser_gb300 import synth  # noqa: E402
 OUT = Path(__file__).resolve().parent
 
 
-def patches_case(seed: int):
-    sc = synth.mte_road(seed)
+def patches_case(seed: int, scene=None, types=(0, 1, 2)):
+    sc = scene if scene is not None else synth.mte_road(seed)
     sp, road = sc.species[0], sc.roads[0]
     hab = sc.hab_map(road)
     W = H = sc.W
@@ -34,7 +34,7 @@ def patches_case(seed: int):
     skp = (W - 1) // res
     popm = sc.pop_map(sp, hab)
     labels, nregs, area, cap, pop, cx, cy = [], [], [], [], [], [], []
-    for typ in (0, 1, 2):
+    for typ in types:
         lab, nr = po.label_image(W, H, (hab == typ).astype(np.int32), lib=po.ref())
         labels.append(lab)
         nregs.append(nr)
@@ -51,16 +51,16 @@ def patches_case(seed: int):
     xy1 = np.array([[cxa[i], cya[i], cxa[j], cya[j]] for i, j in pairs]).T.reshape(-1)
     cr = po.line_segment_intersect(xy1, len(pairs), road.colmajor(), road.G, use_ref=True)
     return dict(hab=hab, pop_map=popm, W=W, res=res, road=road.colmajor(), G=road.G,
+                types=np.array(types, np.int32),
                 labels=np.stack(labels), nregs=np.array(nregs), area=cat(area), cap=cat(cap),
                 pop=cat(pop), cx=cxa, cy=cya, pairs=np.array(pairs, np.int32), xy1=xy1,
                 pair_crossings=cr)
 
 
-def mte_case(seed: int):
-    sc = synth.mte_road(seed)
+def mte_case(seed: int, P=64, Y=30, scene=None):
+    sc = scene if scene is not None else synth.mte_road(seed)
     sp, road = sc.species[0], sc.roads[0]
-    m = po.species_model(sc, sp, road, sem=0)
-    P, Y = 64, 30
+    m = po.species_model(sc, sp, road, sem=0, max_patches=1024)
     end = po.ref_simulate_mte(P, Y, m["N"], 1.0, sp.params, m["init_pops"], m["caps"],
                               m["mmm"][2], seed, 0, 0)
     return dict(P=P, Y=Y, N=m["N"], params=sp.params, init=m["init_pops"], caps=m["caps"],
@@ -73,16 +73,16 @@ def exppv_case(seed: int):
     return dict(prm=prm, P=200, Y=40, seed=seed, values=vals, mean=mean, sd=sd)
 
 
-def rov_problem(seed: int, P=600, Y=12, R=8):
+def rov_problem(seed: int, P=600, Y=12, R=8, scene=None):
     from transportoptimiser_gb300.rov import rov_problem_from_models
-    sc = synth.mte_road(seed)
+    sc = scene if scene is not None else synth.mte_road(seed)
     m = po.species_model(sc, sc.species[0], sc.roads[0], sem=0)
     return rov_problem_from_models([m], sc, n_paths=P, n_years=Y, dim_res=R, n_processes=2,
                                    seed=seed)
 
 
-def rov_case(seed: int):
-    rp = rov_problem(seed)
+def rov_case(seed: int, **kw):
+    rp = rov_problem(seed, **kw)
     out = po.ref_simulate_rov(rp)
     sp = rp["species"][0]
     flat = {k: v for k, v in rp.items() if k != "species"}
@@ -119,6 +119,17 @@ def main():
     np.savez_compressed(OUT / "rov.npz", **rov_case(0))
     np.savez_compressed(OUT / "knn.npz", **knn_case(0))
     np.savez_compressed(OUT / "surrogate_rov.npz", **surrogate_case(0))
+    # at the benchmark shapes: the 200 x 200 generation grid (patches and
+    # crossings of its first road, 4 habitable types), the plain MTE at 2000
+    # paths x 50 years, the MTE of a generation road (~300 patches) over 50
+    # years, and the one-species ROV (the reference's multi-species ROV is
+    # not defined) at 2000 paths x 50 years with 16 bins per dimension
+    gen = synth.generation(0, n_roads=1)
+    np.savez_compressed(OUT / "patches_crossings_gen.npz",
+                        **patches_case(0, scene=gen, types=(0, 1, 2, 5)))
+    np.savez_compressed(OUT / "mte_y50.npz", **mte_case(0, P=2000, Y=50))
+    np.savez_compressed(OUT / "mte_gen.npz", **mte_case(0, P=256, Y=50, scene=gen))
+    np.savez_compressed(OUT / "rov_y50.npz", **rov_case(0, P=2000, Y=50, R=16))
     print("golden fixtures written to", OUT)
 
 

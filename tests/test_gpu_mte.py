@@ -38,9 +38,10 @@ def test_mte_simt_bit_exact_vs_oracle(ctx, sem, mig):
     assert math.isclose(st[0]["p_below"], float((e < 0.2 * m["init_pops"].astype(np.float64).sum()).mean()))
 
 
+@pytest.mark.parametrize("case", ["mte", "mte_y50", "mte_gen"])
 @pytest.mark.parametrize("mig", MIGS)
-def test_mte_matches_reference_golden(ctx, golden, mig):
-    g = golden["mte"]
+def test_mte_matches_reference_golden(ctx, golden, mig, case):
+    g = golden[case]
     m = dict(N=int(g["N"]), init_pops=g["init"], caps=g["caps"], mmm=g["mmm"][None])
     end, _ = sg.simulateMTECUDA([m], [g["params"]], int(g["P"]), int(g["Y"]), seed=int(g["seed"]),
                                 road=0, sem=0, migration=mig, control=0, ctx=ctx)

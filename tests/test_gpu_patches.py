@@ -29,14 +29,15 @@ def test_label_image_too_large_is_rejected(ctx):
         sg.labelImage(400, 400, np.ones(400 * 400, np.int32), ctx=ctx)
 
 
-def test_build_patches_matches_golden(ctx, golden):
-    g = golden["patches_crossings"]
+@pytest.mark.parametrize("case", ["patches_crossings", "patches_crossings_gen"])
+def test_build_patches_matches_golden(ctx, golden, case):
+    g = golden[case]
     W = int(g["W"]); res = int(g["res"])
     xres = res if W % res == 0 else res + 1
     skp = (W - 1) // res
     hab, popm = g["hab"], g["pop_map"]
     got = {k: [] for k in ("area", "cap", "pop", "cx", "cy")}
-    for t, typ in enumerate((0, 1, 2)):
+    for t, typ in enumerate(g["types"]):
         lab, nr = sg.labelImage(W, W, (hab == typ).astype(np.int32), ctx=ctx)
         assert np.array_equal(lab, g["labels"][t])
         r, _ = sg.buildPatches(W, W, skp, skp, xres, xres, nr, 1.0, 1.0, 1.0, 50.0, lab, popm,
@@ -47,8 +48,9 @@ def test_build_patches_matches_golden(ctx, golden):
         assert np.array_equal(np.concatenate(got[k]), g[k]), k
 
 
-def test_line_segment_intersect_matches_oracle(ctx, golden):
-    g = golden["patches_crossings"]
+@pytest.mark.parametrize("case", ["patches_crossings", "patches_crossings_gen"])
+def test_line_segment_intersect_matches_oracle(ctx, golden, case):
+    g = golden[case]
     T = len(g["pairs"])
     xy1 = g["xy1"].reshape(4, T).T
     xy2 = g["road"].reshape(4, int(g["G"])).T

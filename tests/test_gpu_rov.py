@@ -38,8 +38,9 @@ def test_rov_reference_semantics_bit_exact(ctx, golden, mig):
     _compare_exact(gpu, orc, rp["n_paths"], rp["n_years"], 1)
 
 
-def test_rov_matches_reference_golden(ctx, golden):
-    g = golden["rov"]
+@pytest.mark.parametrize("case", ["rov", "rov_y50"])
+def test_rov_matches_reference_golden(ctx, golden, case):
+    g = golden[case]
     rp = problem_from_golden(g)
     ref = ref_outputs(g)
     gpu = sg.simulateROVCUDA(rp, ctx=ctx)

@@ -15,14 +15,15 @@ from transportoptimiser_gb300 import synth
 RTOL = 1e-5
 
 
-def test_labels_patches_crossings_golden(golden):
-    g = golden["patches_crossings"]
+@pytest.mark.parametrize("case", ["patches_crossings", "patches_crossings_gen"])
+def test_labels_patches_crossings_golden(golden, case):
+    g = golden[case]
     W = int(g["W"]); res = int(g["res"])
     hab, popm = g["hab"], g["pop_map"]
     xres = res if W % res == 0 else res + 1
     skp = (W - 1) // res
     area, cx, cy, pop, cap = [], [], [], [], []
-    for t, typ in enumerate((0, 1, 2)):
+    for t, typ in enumerate(g["types"]):
         lab, nr = po.label_image(W, W, (hab == typ).astype(np.int32))
         assert nr == int(g["nregs"][t])
         assert np.array_equal(lab, g["labels"][t])
@@ -35,10 +36,13 @@ def test_labels_patches_crossings_golden(golden):
     assert np.array_equal(cr, g["pair_crossings"])
 
 
-def test_species_model_crossing_matrix_golden(golden):
-    g = golden["patches_crossings"]
-    sc = synth.mte_road(0)
-    m = po.species_model(sc, sc.species[0], sc.roads[0], sem=0)
+@pytest.mark.parametrize("case,scene", [("patches_crossings", lambda: synth.mte_road(0)),
+                                        ("patches_crossings_gen",
+                                         lambda: synth.generation(0, n_roads=1))])
+def test_species_model_crossing_matrix_golden(golden, case, scene):
+    g = golden[case]
+    sc = scene()
+    m = po.species_model(sc, sc.species[0], sc.roads[0], sem=0, max_patches=1024)
     N = m["N"]
     Cm = np.zeros((N, N), np.int32)
     for q, (i, j) in enumerate(g["pairs"]):
@@ -48,8 +52,9 @@ def test_species_model_crossing_matrix_golden(golden):
     assert np.allclose(m["trans"].sum(axis=1), 1.0, rtol=1e-12)
 
 
-def test_mte_golden(golden):
-    g = golden["mte"]
+@pytest.mark.parametrize("case", ["mte", "mte_y50", "mte_gen"])
+def test_mte_golden(golden, case):
+    g = golden[case]
     out = po.simulate_mte(int(g["P"]), int(g["Y"]), int(g["N"]), 1.0, g["params"], g["init"],
                           g["caps"], g["mmm"], int(g["seed"]), 0, 0, 0)
     np.testing.assert_allclose(out, g["end"], rtol=RTOL)
