@@ -69,6 +69,21 @@ const char* to_status_string(to_status s);
 const char* to_last_error(to_ctx ctx);
 /* number of kernels this context has launched (for accounting) */
 uint64_t to_ctx_launch_count(to_ctx ctx);
+/* Fault injection for tests of the failure paths, all on the host side or
+ * in a bounded device wait (no reference counterpart).  One-shot: the armed
+ * fault fires once, in the next call that reaches it.
+ *   TO_FAULT_ALLOC: the next scratch reservation is refused as a failed
+ *     device allocation would be (TO_ERR_ALLOC); the context stays usable.
+ *   TO_FAULT_WAIT: the next tensor-core migration kernel waits on a barrier
+ *     that nothing completes, before it issues any copy or MMA, with no time
+ *     allowed; it takes its abort path (error word, TMEM freed) and the call
+ *     returns TO_ERR_TIMEOUT; with nothing in flight the context stays
+ *     usable.  (A wait that runs out while copies or MMAs are in flight is a
+ *     different case: the context should then be destroyed.) */
+#define TO_FAULT_NONE 0
+#define TO_FAULT_ALLOC 1
+#define TO_FAULT_WAIT 2
+to_status to_ctx_inject_fault(to_ctx ctx, int fault);
 /* per-kernel CUDA-event timing: enable (clears the record), then read the
  * summed milliseconds and launch count of one kernel by name */
 to_status to_ctx_profile(to_ctx ctx, int enable);

@@ -25,8 +25,10 @@ def test_generation_of_256_roads_repeatable(ctx, mig):
     a = gen.evaluate(packed, opts)
     b = gen.evaluate(packed, opts)
     gen.close()
-    assert np.isfinite(a).all()
-    assert np.array_equal(a, b)
+    C = sc.n_controls
+    # slots 10..14 (no ROV) and the animals-at-risk slots past C are NaN
+    assert np.isfinite(a[:, :, :10]).all() and np.isfinite(a[:, :, 16:16 + C]).all()
+    assert np.array_equal(a, b, equal_nan=True)
 
 
 def test_single_road_mte_many_paths_repeatable(ctx):

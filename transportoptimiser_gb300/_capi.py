@@ -149,6 +149,7 @@ SIGNATURES = {
     "to_simulate_rov_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(RovProblem),
                                         C.POINTER(RovResult)]),
     "to_ctx_profile": (C.c_int, [C.c_void_p, C.c_int]),
+    "to_ctx_inject_fault": (C.c_int, [C.c_void_p, C.c_int]),
     "to_ctx_kernel_time": (C.c_int, [C.c_void_p, C.c_char_p, c_double_p, c_int_p]),
     "to_label_image": (C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, c_int_p, c_int_p]),
     "to_build_patches": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -259,7 +259,15 @@ to_status rov_stage(to_ctx ctx, to_gen g, int R, int NE, int road0) {
     // the kNN's per-query search radius starts from last year's; clear it
     // so that every generation starts the same way
     TO_CUDA(ctx, cudaMemsetAsync(a.kth, 0, (size_t)a.G * a.Q * sizeof(float), ctx->stream));
-    return to_k::rov_run(ctx, a, &g->csc);
+    to_csc csc = g->csc;
+    if (csc.uent) {
+        // every control's packed columns in one list per destination; at most
+        // as many entries as the widest packed matrix (nested patterns)
+        csc.ucap_smem = csc.cap_smem;
+        if (to_k::rov_union_smem(NE, g->C, csc.ucap_smem) > ctx->smem_optin) csc.uent = nullptr;
+        else TO_TRY(to_k::union_csc(ctx, g->NP, g->C, g->d_np, R * g->S, csc));
+    }
+    return to_k::rov_run(ctx, a, &csc);
 }
 
 // The launches after the model: migration Monte Carlo, statistics, the ROV
@@ -572,6 +580,12 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     const size_t cap = (size_t)NP * 32;
     acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
     acc(RS * C * 8);
+    // union form of each road-species' C <= 3 matrices (the ROV forward
+    // pass's form): the species models' patterns are nested - control c's
+    // entries are a subset of the lowest-hazard control's - so a union
+    // holds no more entries than that control's packed matrix
+    const size_t ucap = C <= 3 ? cap : 0;
+    if (C <= 3) { acc(RS * ucap * 16); acc(RS * (NP + 1) * 4); acc(RS * 4); }
     if ((e = cudaMalloc(&g->buf, bytes)) != cudaSuccess) return fail(e);
     g->buf_bytes = bytes;
     char* p = g->buf;
@@ -605,6 +619,14 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->csc.cap = (int)cap;
     g->csc.cap_smem = 0;
     g->d_iar = carve<double>(p, RS * C);
+    g->csc.uent = nullptr; g->csc.uptr = nullptr; g->csc.unnz = nullptr;
+    g->csc.ucap = 0; g->csc.ucap_smem = 0;
+    if (C <= 3) {
+        g->csc.uent = carve<int4>(p, RS * ucap);
+        g->csc.uptr = carve<int>(p, RS * (NP + 1));
+        g->csc.unnz = carve<int>(p, RS);
+        g->csc.ucap = (int)ucap;
+    }
     if ((e = cudaMalloc(&g->d_pen, (size_t)S * 3 * sizeof(double))) != cudaSuccess) return fail(e);
     if ((e = cudaMemset(g->d_pen, 0, (size_t)S * 3 * sizeof(double))) != cudaSuccess) return fail(e);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
@@ -733,7 +755,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     a.sem = 1; a.road = 0; a.dt = t->dt; a.rrr = t->rrr;
     a.unit_cost = t->unit_cost; a.unit_revenue = t->unit_revenue; a.scaling = 2.0f;
     a.seed = t->seed; a.kmax = kmax; a.algo = 4; a.k_mult = 10;
-    a.touched = 1; a.reg_one_year = 1;
+    a.touched = 1; a.reg_one_year = 1; a.flags = ctx->d_flags;
     float* d_flows = carve<float>(p, C);
     float* d_unc = carve<float>(p, 6 * U1);
     float* d_fc = carve<float>(p, 16);

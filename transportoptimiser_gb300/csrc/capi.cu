@@ -34,6 +34,11 @@ to_status to_check_cuda(to_ctx ctx, cudaError_t e, const char* what) {
 
 to_status to_arena_reserve(to_ctx ctx, size_t bytes) {
     ctx->arena_off = 0;
+    if (ctx->fault == TO_FAULT_ALLOC) {
+        // test hook: this reservation is refused as a failed allocation would be
+        ctx->fault = TO_FAULT_NONE;
+        return to_set_error(ctx, TO_ERR_ALLOC, "scratch of %zu bytes refused (injected)", bytes);
+    }
     if (bytes <= ctx->arena_cap) return TO_OK;
     if (ctx->arena) {
         TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -42,7 +47,13 @@ to_status to_arena_reserve(to_ctx ctx, size_t bytes) {
         ctx->arena_cap = 0;
     }
     size_t cap = bytes + bytes / 4 + (1 << 20);
-    TO_CUDA(ctx, cudaMalloc(&ctx->arena, cap));
+    const cudaError_t e = cudaMalloc(&ctx->arena, cap);
+    if (e != cudaSuccess) {
+        ctx->arena = nullptr;
+        cudaGetLastError();
+        return to_set_error(ctx, e == cudaErrorMemoryAllocation ? TO_ERR_ALLOC : TO_ERR_CUDA,
+                            "scratch of %zu bytes: %s", cap, cudaGetErrorString(e));
+    }
     ctx->arena_cap = cap;
     return TO_OK;
 }
@@ -125,6 +136,12 @@ const char* to_status_string(to_status s) {
 }
 
 const char* to_last_error(to_ctx ctx) { return ctx ? ctx->err : ""; }
+
+to_status to_ctx_inject_fault(to_ctx ctx, int fault) {
+    if (!ctx || fault < TO_FAULT_NONE || fault > TO_FAULT_WAIT) return TO_ERR_INVALID;
+    ctx->fault = fault;
+    return TO_OK;
+}
 
 to_status to_ctx_profile(to_ctx ctx, int enable) {
     if (!ctx) return TO_ERR_INVALID;

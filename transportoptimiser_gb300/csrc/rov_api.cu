@@ -156,6 +156,9 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     acc((size_t)Y * PT * 4); acc((size_t)Y * S * PT * 4); acc((size_t)NR * 5 * 8);
     acc((size_t)RS * C * (NP + 1) * 4); acc((size_t)RS * C * cap * 2); acc((size_t)RS * C * cap * 4);
     acc((size_t)RS * C * 4);
+    // union form of each road-species' C <= 3 matrices
+    const int ucap = C <= 3 ? (C * cap < NP * NP ? C * cap : NP * NP) : 0;
+    if (C <= 3) { acc((size_t)RS * ucap * 16); acc((size_t)RS * (NP + 1) * 4); acc((size_t)RS * 4); }
     if (algo == 6) { acc((size_t)Y * S * NP * P * 4); acc((size_t)Y * S * P * 4); }
     // regressions fitted only where the backward pass reads them, unless
     // the caller asks for the surfaces (corrected semantics, ALGO4)
@@ -172,7 +175,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     a.nF = pr->n_fuels; a.Cm = pr->n_commodities; a.demand_idx = pr->demand_idx;
     a.sem = pr->sem; a.road = pr->road; a.dt = pr->dt; a.rrr = pr->rrr;
     a.unit_cost = pr->unit_cost; a.unit_revenue = pr->unit_revenue; a.scaling = 2.0f;
-    a.seed = pr->seed; a.np = NP; a.ne = NP; a.kmax = kmax;
+    a.seed = pr->seed; a.np = NP; a.ne = NP; a.kmax = kmax; a.flags = ctx->d_flags;
     a.algo = algo; a.k_mult = algo == 6 ? 3 : 10;
     float* d_mmm = to_arena_take<float>(ctx, mmm.size());
     float* d_ip = to_arena_take<float>(ctx, ip.size());
@@ -221,6 +224,14 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     csc.nnz = to_arena_take<int>(ctx, (size_t)RS * C);
     csc.cap = cap;
     csc.cap_smem = 0;
+    csc.uent = nullptr; csc.uptr = nullptr; csc.unnz = nullptr; csc.ucap = 0; csc.ucap_smem = 0;
+    if (C <= 3) {
+        csc.uent = to_arena_take<int4>(ctx, (size_t)RS * ucap);
+        csc.uptr = to_arena_take<int>(ctx, (size_t)RS * (NP + 1));
+        csc.unnz = to_arena_take<int>(ctx, (size_t)RS);
+        csc.ucap = ucap;
+        if (!csc.unnz) return to_set_error(ctx, TO_ERR_ALLOC, "arena sizing");
+    }
     if (algo == 6) {
         a.popsY = to_arena_take<float>(ctx, (size_t)Y * S * NP * P);
         a.gmY = to_arena_take<float>(ctx, (size_t)Y * S * P);
@@ -260,6 +271,22 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
         for (int v : nz) { if (v < 0) ok = false; mx = v > mx ? v : mx; }
         csc.cap_smem = (mx + 7) & ~7;
         sparse = ok && to_k::rov_sparse_smem(NP, C, csc.cap_smem) <= ctx->smem_optin;
+        if (ok && csc.uent) {
+            // one list per destination for all controls (the forward pass's form)
+            TO_TRY(to_k::union_csc(ctx, NP, C, d_np, RS, csc));
+            std::vector<int> un((size_t)RS);
+            TO_CUDA(ctx, cudaMemcpyAsync(un.data(), csc.unnz, un.size() * sizeof(int),
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+            TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+            int um = 0;
+            bool uok = true;
+            for (int v : un) { if (v < 0) uok = false; um = v > um ? v : um; }
+            csc.ucap_smem = (um + 7) & ~7;
+            if (!uok || to_k::rov_union_smem(NP, C, csc.ucap_smem) > ctx->smem_optin)
+                csc.uent = nullptr;                   // the per-control form then
+            else
+                sparse = true;
+        }
         if (!sparse && (pr->migration == TO_MIG_SPARSE_FP32 || algo == 6 || NR > 1))
             return to_set_error(ctx, TO_ERR_UNSUPPORTED, "matrices too dense for the sparse form");
     }

@@ -262,6 +262,272 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 }
 
 // ---------------------------------------------------------------------------
+// Union of the C <= 3 controls' packed columns of one (road, species): one
+// CTA; a thread per destination merges its C ascending origin lists (count,
+// CTA scan, write).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int union_step(const int* b, const int* e, const uint16_t* const* ix,
+                                          int C, int* pos) {
+    int lo = 0x7fffffff;
+    for (int c = 0; c < C; ++c)
+        if (pos[c] < e[c] && (int)ix[c][pos[c]] < lo) lo = ix[c][pos[c]];
+    return lo;
+}
+
+__global__ void __launch_bounds__(256)
+k_union_csc(int NP, int C, const int* __restrict__ n_patches, to_csc csc) {
+    const int rs = blockIdx.x;
+    const int N = n_patches[rs];
+    __shared__ int s_tmp[32];
+    int* up = csc.uptr + (size_t)rs * (NP + 1);
+    const uint16_t* ix[3];
+    const float* vv[3];
+    bool ok = true;
+    for (int c = 0; c < C; ++c) {
+        const size_t mtx = (size_t)rs * C + c;
+        ix[c] = csc.idx + mtx * csc.cap;
+        vv[c] = csc.val + mtx * csc.cap;
+        ok = ok && csc.nnz[mtx] >= 0;
+    }
+    if (!ok) {                                    // a control above its capacity
+        if (threadIdx.x == 0) csc.unnz[rs] = -1;
+        return;
+    }
+    // pass 1: union size of each column; a thread takes a run of columns
+    const int chunk = (NP + (int)blockDim.x - 1) / (int)blockDim.x;
+    const int k0 = (int)threadIdx.x * chunk, k1 = min(NP, k0 + chunk);
+    int cnt = 0;
+    for (int k = k0; k < k1; ++k) {
+        int b[3], e[3], pos[3];
+        for (int c = 0; c < C; ++c) {
+            const int* p = csc.ptr + ((size_t)rs * C + c) * (NP + 1);
+            b[c] = pos[c] = k < N ? p[k] : 0;
+            e[c] = k < N ? p[k + 1] : 0;
+        }
+        int n = 0;
+        for (;;) {
+            const int lo = union_step(b, e, ix, C, pos);
+            if (lo == 0x7fffffff) break;
+            for (int c = 0; c < C; ++c) if (pos[c] < e[c] && (int)ix[c][pos[c]] == lo) ++pos[c];
+            ++n;
+        }
+        up[k] = n;
+        cnt += n;
+    }
+    // CTA exclusive scan of the per-thread totals
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    int base = 0, total = 0;
+    for (int w = 0; w < nw; ++w) { if (w < warp) base += s_tmp[w]; total += s_tmp[w]; }
+    base += x - cnt;
+    for (int k = k0; k < k1; ++k) { const int n = up[k]; up[k] = base; base += n; }
+    if (threadIdx.x == 0) {
+        up[NP] = total;
+        csc.unnz[rs] = total <= csc.ucap ? total : -1;
+    }
+    if (total > csc.ucap) return;
+    // pass 2: the entries
+    int4* out = csc.uent + (size_t)rs * csc.ucap;
+    for (int k = k0; k < k1; ++k) {
+        int b[3], e[3], pos[3];
+        for (int c = 0; c < C; ++c) {
+            const int* p = csc.ptr + ((size_t)rs * C + c) * (NP + 1);
+            b[c] = pos[c] = k < N ? p[k] : 0;
+            e[c] = k < N ? p[k + 1] : 0;
+        }
+        int q = up[k];
+        for (;;) {
+            const int lo = union_step(b, e, ix, C, pos);
+            if (lo == 0x7fffffff) break;
+            float v[3] = {0.0f, 0.0f, 0.0f};
+            for (int c = 0; c < C; ++c)
+                if (pos[c] < e[c] && (int)ix[c][pos[c]] == lo) { v[c] = vv[c][pos[c]]; ++pos[c]; }
+            out[q++] = make_int4(lo, __float_as_int(v[0]), __float_as_int(v[1]),
+                                 __float_as_int(v[2]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// ROV forward paths on the union columns (C <= 3 controls) - grid (ceil(P/32),
+// roads).  As k_rov_forward_sparse, but each non-zero of destination k is
+// one 16-byte shared load {row byte offset, value of control 0, 1, 2} that
+// serves every control's migration (three FMA chains, each in ascending
+// origin order with exact zero terms where a control has no entry), and the
+// year's three growth-mean draws per path are spread over the CTA.
+// ---------------------------------------------------------------------------
+template <int MAXG>
+__global__ void __launch_bounds__(1024, 1)
+k_rov_forward_union(to_rov_args a, to_csc csc) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int NE = a.ne, NG = NE >> 2, NP = a.np, C = a.C, Y = a.Y, P = a.P;
+    const size_t PT = (size_t)a.PT;
+    const int rd = blockIdx.y;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int path = blockIdx.x * kLanes + lane;
+    const size_t gp = (size_t)rd * P + path;
+    int4* ue = reinterpret_cast<int4*>(sm_raw);                    // [ucap_smem]
+    float* cur = reinterpret_cast<float*>(ue + csc.ucap_smem);     // [NE][32]
+    float* part = cur + (size_t)NE * kLanes;                       // [C+1][NG][32]
+    float* capv = part + (size_t)(C + 1) * NG * kLanes;            // [NE]
+    float* gm = capv + NE;                                         // [32]
+    float* tot = gm + kLanes;                                      // [32]
+    float* ntot = tot + kLanes;                                    // [32]
+    float* xs = ntot + kLanes;                                     // [3][32]
+    int* ctl = reinterpret_cast<int*>(xs + 3 * kLanes);            // [32]
+    int* uptr = ctl + kLanes;                                      // [NE+1]
+    const uint32_t road = (uint32_t)a.road_ids[rd];
+
+    for (int s = 0; s < a.S; ++s) {
+        const int rs = rd * a.S + s;
+        const int N = a.n_patches[rs];
+        const int N4 = (N + 3) & ~3;
+        const int NGr = N4 >> 2;
+        const float* sp = a.params + 8 * s;
+        const float* ip = a.init_pops + (size_t)rs * NP;
+        const int nu = csc.unnz[rs];
+        if (nu < 0 || nu > csc.ucap_smem || N > NE) {
+            // outside the shape this launch was planned for: flag, no result
+            if (threadIdx.x == 0 && a.flags) atomicExch(a.flags, TO_DEVERR_PLAN);
+            if (warp == 0 && path < P)
+                for (int t = 0; t <= Y; ++t)
+                    a.totalPops[((size_t)s * (Y + 1) + t) * PT + gp] = NAN;
+            continue;
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
+            const int k = q / kLanes;
+            cur[q] = (k < N) ? ip[k] : 0.0f;
+        }
+        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)rs * NP + k];
+        for (int k = threadIdx.x; k <= NE; k += blockDim.x)
+            uptr[k] = csc.uptr[(size_t)rs * (NP + 1) + (k <= NP ? k : NP)];
+        for (int e = threadIdx.x; e < nu; e += blockDim.x) {
+            int4 v = csc.uent[(size_t)rs * csc.ucap + e];
+            v.x *= kLanes * (int)sizeof(float);                    // origin -> row byte offset
+            ue[e] = v;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            float tt = 0.0f;
+            for (int grp = 0; grp < NGr; ++grp) {
+                const float* v = cur + (size_t)grp * 4 * kLanes + lane;
+                tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
+            }
+            tot[lane] = tt;
+            gm[lane] = sp[0];
+            if (path < P) a.totalPops[((size_t)s * (Y + 1)) * PT + gp] = tt;
+        }
+        const float jp = (a.sem == 0) ? sp[5] : sp[6];
+        const float s5 = sp[5] * sp[5];
+        for (int t = 0; t < Y; ++t) {
+            // the growth mean's three draws per path, one thread each
+            for (int q = threadIdx.x; q < 3 * kLanes; q += blockDim.x) {
+                const int which = q >> 5, i = q & 31;
+                const uint32_t pth = (uint32_t)(blockIdx.x * kLanes + i);
+                float v;
+                if (which == 0) {
+                    v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road, pth, t, s) < jp) ? 1.0f : 0.0f;
+                } else if (which == 1) {
+                    v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road, pth, t, s) * sp[2];
+                } else {
+                    const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road, pth, t, s);
+                    const float jsz = (a.sem == 0) ? (zj * s5 - s5 / 2.0f) : (zj * sp[5] - s5 / 2.0f);
+                    v = to_expf(jsz) - 1.0f;
+                }
+                xs[q] = v;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                const float g = gm[lane];
+                const float jump = xs[lane], brown = xs[kLanes + lane], em1 = xs[2 * kLanes + lane];
+                const float gn = g + sp[4] * (sp[1] - g) * a.dt + g * brown + em1 * g * jump;
+                gm[lane] = gn;
+                ctl[lane] = (path < P) ? a.controls[(size_t)t * PT + gp] : 0;
+                if (a.gmY && path < P) a.gmY[((size_t)t * a.S + s) * P + path] = gn;
+            }
+            __syncthreads();
+            if (a.popsY) {
+                for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
+                    const int pth = blockIdx.x * kLanes + (q & (kLanes - 1));
+                    if (pth < P)
+                        a.popsY[(((size_t)t * a.S + s) * NE + (q >> 5)) * P + pth] = cur[q];
+                }
+            }
+            const float g = gm[lane];
+            const int my_c = ctl[lane];
+            const unsigned char* curb = reinterpret_cast<const unsigned char*>(cur) + lane * 4;
+            float nv[MAXG][4];
+#pragma unroll
+            for (int gi = 0; gi < MAXG; ++gi) {
+                const int grp = warp + gi * W;
+                if (grp < NGr) {
+                    float z[4];
+                    to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
+                               (uint32_t)((s * N4) >> 2) + grp, z);
+                    float m0[4], m1[4], m2[4], np4[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int k = grp * 4 + j;
+                        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+                        const int e1 = uptr[k + 1];
+#pragma unroll 2
+                        for (int e = uptr[k]; e < e1; ++e) {
+                            const int4 en = ue[e];
+                            const float x = *reinterpret_cast<const float*>(curb + en.x);
+                            a0 = fmaf(x, __int_as_float(en.y), a0);
+                            a1 = fmaf(x, __int_as_float(en.z), a1);
+                            a2 = fmaf(x, __int_as_float(en.w), a2);
+                        }
+                        m0[j] = a0; m1[j] = a1; m2[j] = a2;
+                        const float mv = (my_c == 0) ? a0 : ((my_c == 1) ? a1 : a2);
+                        const float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
+                        const float cpk = capv[k];
+                        const float v = (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
+                                                     : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
+                        nv[gi][j] = v;
+                        np4[j] = v;
+                    }
+                    part[((size_t)0 * NG + grp) * kLanes + lane] = grouped4(m0[0], m0[1], m0[2], m0[3]);
+                    if (C > 1)
+                        part[((size_t)1 * NG + grp) * kLanes + lane] = grouped4(m1[0], m1[1], m1[2], m1[3]);
+                    if (C > 2)
+                        part[((size_t)2 * NG + grp) * kLanes + lane] = grouped4(m2[0], m2[1], m2[2], m2[3]);
+                    part[((size_t)C * NG + grp) * kLanes + lane] = grouped4(np4[0], np4[1], np4[2], np4[3]);
+                }
+            }
+            __syncthreads();
+            for (int c = warp; c <= C; c += W) {
+                float tt = 0.0f;
+                for (int grp = 0; grp < NGr; ++grp)
+                    tt = tt + part[((size_t)c * NG + grp) * kLanes + lane];
+                if (path < P) {
+                    if (c < C) a.aars[(((size_t)s * C + c) * Y + t) * PT + gp] = tt / tot[lane];
+                    else a.totalPops[((size_t)s * (Y + 1) + t + 1) * PT + gp] = tt;
+                }
+                if (c == C) ntot[lane] = tt;
+            }
+            __syncthreads();
+            if (warp == 0) tot[lane] = ntot[lane];
+#pragma unroll
+            for (int gi = 0; gi < MAXG; ++gi) {
+                const int grp = warp + gi * W;
+                if (grp < NGr) {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // ROV forward paths (forwardPathKernel :789-956) - grid ceil(P/32)
 // ---------------------------------------------------------------------------
 template <int CMAX, int MAXG>
@@ -662,7 +928,49 @@ size_t rov_sparse_smem(int NE, int C, int cap_smem) {
            (size_t)C * (NE + 1) * 4 + (size_t)C * cap_smem * 6 + 16;
 }
 
+size_t rov_union_smem(int NE, int C, int ucap_smem) {
+    if (NE > 32 * kMaxG * 4 || C > 3) return ~size_t(0);
+    const int NG = NE / 4;
+    return (size_t)ucap_smem * 16 +
+           (size_t)(NE * kLanes + (C + 1) * NG * kLanes + NE + 7 * kLanes) * 4 +
+           (size_t)(NE + 1) * 4 + 16;
+}
+
+to_status union_csc(to_ctx ctx, int NP, int C, const int* n_patches, int n_rs, to_csc& csc) {
+    if (C > 3 || !csc.uent || !csc.uptr || !csc.unnz)
+        return to_set_error(ctx, TO_ERR_INVALID, "union form: %d controls", C);
+    k_union_csc<<<n_rs, 256, 0, ctx->stream>>>(NP, C, n_patches, csc);
+    TO_LAUNCHED(ctx);
+    return TO_OK;
+}
+
 to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc) {
+    if (csc.uent && a.C <= 3) {
+        const size_t smem = rov_union_smem(a.ne, a.C, csc.ucap_smem);
+        if (smem > ctx->smem_optin)
+            return to_set_error(ctx, TO_ERR_UNSUPPORTED, "union ROV needs %zu B", smem);
+        const dim3 blocks((a.P + kLanes - 1) / kLanes, a.nr);
+        const int NG = a.ne / 4;
+        to_prof_begin(ctx, "rov_forward_sparse");
+        if (NG <= 32 * 3) {
+            // at most three groups a warp (<= 384 patches): fewer live values
+            // between the year's barriers than four
+            const int warps = (NG + 2) / 3 > 4 ? (NG + 2) / 3 : 4;
+            TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_union<3>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_rov_forward_union<3><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
+        } else {
+            const int warps = warps_for(a.ne, 4);
+            if ((NG + warps - 1) / warps > kMaxG)
+                return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", a.ne);
+            TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_union<kMaxG>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_rov_forward_union<kMaxG><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
+        }
+        to_prof_end(ctx);
+        TO_LAUNCHED(ctx);
+        return TO_OK;
+    }
     size_t smem = rov_sparse_smem(a.ne, a.C, csc.cap_smem);
     if (smem > ctx->smem_optin)
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "sparse ROV needs %zu B", smem);

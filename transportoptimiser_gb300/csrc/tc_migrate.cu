@@ -148,8 +148,15 @@ k_mte_tc(to_mte_args a, TcShape sh, const float* __restrict__ packed, int* __res
     const uint32_t id = to_tc::idesc(2, 128, TP);
     bool ok = true;
     uint32_t gi_base = 0;          // chunk counter across years (ring phases)
+    if (a.fault_wait) {
+        // test hook: a wait that nothing completes, before any copy or MMA
+        // is issued, with no time allowed - the abort path below runs
+        // (error word, TMEM freed) with nothing in flight
+        const bool w = to_tc::mbar_wait_limit(&done, 0u, 0ull);
+        if (__syncthreads_or(!w)) ok = false;
+    }
 
-    for (int t = 0; t < a.n_years; ++t) {
+    for (int t = 0; t < a.n_years && ok; ++t) {
         // growth-rate mean (SimulateGPU.cu:691-701), one thread per path
         for (int q = tid; q < TP; q += 128) {
             const uint32_t path = (uint32_t)(path0 + q);
@@ -323,6 +330,7 @@ namespace to_k {
 to_status mte_tc(to_ctx ctx, to_mte_args a, int n_rs) {
     int maxN = a.npe > 0 ? a.npe : a.npad;
     if (!a.flags) a.flags = ctx->d_flags;
+    if (ctx->fault == TO_FAULT_WAIT) { a.fault_wait = 1; ctx->fault = TO_FAULT_NONE; }
     TcShape sh;
     if (!pick_shape(maxN, ctx->smem_optin, sh))
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "tensor-core migration: %d patches", maxN);

@@ -49,6 +49,7 @@ struct to_ctx_s {
     };
     std::vector<tune_entry> tune;
     char err[512] = {0};
+    int fault = 0;              // to_ctx_inject_fault: armed one-shot fault
 };
 
 // device-side error codes written to ctx->d_flags[0]

@@ -19,6 +19,9 @@ struct to_mte_args {
     const float* params;         // [S][8]
     float* end_pops;             // [RS][P]
     int* flags;                  // device error word (plan checks), may be null
+    int fault_wait;              // test hook (to_ctx_inject_fault): the tensor-core
+                                 // kernel's first wait, on a barrier nothing arrives
+                                 // at, runs out at once
 };
 
 namespace to_k {

@@ -79,6 +79,7 @@ struct to_rov_args {
     // 1: reg holds only the current year's blocks (the regressions of year
     // t are written and read within year t; nothing returns them)
     int reg_one_year;
+    int* flags;                       // device error word (plan checks), may be null
     // outputs (device)
     float* reg;                       // [Y][G][R*d + 2Q]
     float* condExp;                   // [Y][PT]

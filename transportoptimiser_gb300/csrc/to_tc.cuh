@@ -64,7 +64,9 @@ __device__ __forceinline__ void mbar_init(void* mbar, uint32_t count) {
 
 // Wait for phase `parity` of the mbarrier to complete.  Bounded: gives up
 // after about 0.2 s of global time and returns false.
-__device__ __forceinline__ bool mbar_wait(void* mbar, uint32_t parity) {
+// bounded wait on a phase of an mbarrier: gives up after limit_ns of global
+// time (or 2^24 polls) and returns false
+__device__ __forceinline__ bool mbar_wait_limit(void* mbar, uint32_t parity, uint64_t limit_ns) {
     const uint32_t addr = smem_u32(mbar);
     uint64_t t0;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
@@ -76,9 +78,12 @@ __device__ __forceinline__ bool mbar_wait(void* mbar, uint32_t parity) {
         if (done) return true;
         uint64_t t1;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
-        if (t1 - t0 > 200000000ull) return false;
+        if (t1 - t0 > limit_ns) return false;
     }
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(void* mbar, uint32_t parity) {
+    return mbar_wait_limit(mbar, parity, 200000000ull);
 }
 
 // generic-proxy smem writes -> visible to the tensor core (async proxy)
