@@ -300,14 +300,18 @@ def surrogate_leg(args, gen, scene, P, ctx):
                                   seed=88)
     pred, _ = ens.predict(Xt, ctx)
     err = np.abs(pred[:, 0] - Yt[:, 0]) / Yt[:, 0]
-    opts = gen.opts(P, YEARS, seed=5)
+    opts = gen.opts(P, YEARS, seed=5, sem=SEM)
     pop = args.roads
     out = {}
-    for name, e, tol in (("screened_tol10", ens, 0.10), ("screened_tol20", ens, 0.20),
-                         ("plain_mc", None, 0.0)):
+    # config 4's own rule (Monte Carlo where the predicted error is above 1%,
+    # and on the top 10%), then wider tolerances, then Monte Carlo throughout
+    for name, e, tol, top in (("rule_1pct_top10", ens, 0.01, 0.10),
+                              ("screened_tol10", ens, 0.10, 0.25),
+                              ("screened_tol20", ens, 0.20, 0.25),
+                              ("plain_mc", None, 0.0, 0.25)):
         tm = {}
         _, best, n_mc, secs = sga.run_ga(gen, scene, args.ga_generations, pop, opts,
-                                         np.random.default_rng(7), e, tol, timings=tm)
+                                         np.random.default_rng(7), e, tol, top=top, timings=tm)
         designs = args.ga_generations * pop
         out[name] = {"designs_per_s": designs / secs, "mc_valuations": n_mc,
                      "designs": designs, "best_fitness_mc": best, "seconds": secs,
@@ -318,8 +322,12 @@ def surrogate_leg(args, gen, scene, P, ctx):
             "final_loss": float(ens.members[0].loss_curve[-1]),
             "heldout_median_rel_err_mean_end_ratio": float(np.median(err)),
             "ga": out, "ga_generations": args.ga_generations, "ga_population": pop,
-            "screen_rule": "MC on the top 25% by predicted fitness plus the members' spread, "
-                           "and where the members disagree by > tol",
+            "screen_rule": "MC on the top fraction (10% for rule_1pct_top10, else 25%) by "
+                           "predicted fitness plus the members' spread, and where the members "
+                           "disagree by > tol (1%, 10%, 20%)",
+            "features": list(sga.FEATURES),
+            "designs_per_s_ratio_rule_1pct_vs_mc":
+                out["rule_1pct_top10"]["designs_per_s"] / out["plain_mc"]["designs_per_s"],
             "designs_per_s_ratio_screened_tol10_vs_mc":
                 out["screened_tol10"]["designs_per_s"] / out["plain_mc"]["designs_per_s"],
             "designs_per_s_ratio_screened_tol20_vs_mc":
@@ -708,6 +716,7 @@ def main():
                          "unit": "designs/s", "ms_per_step": mte_only_ms,
                          "note": "the same generation valued by MTE alone"},
             "kernel_ms_per_step": {k: round(v[0], 4) for k, v in split.items()},
+            "rov_grid_share_fitted": float(res[:, 0, 15].mean()),
             "roofline": roofline,
             "surrogate": surrogate,
             "rov_one_road": rov_adj["rov"] if rov_adj else None,

@@ -473,7 +473,8 @@ int to_ctx_tuning(to_ctx ctx, char* buf, int len);
  *   (to_scene_set_rov; else NaN): value, optimal first-period control, the
  *   reference's SD statistic, Monte Carlo standard error, paths behind the
  *   value,
- *   15 reserved (0),
+ *   15 the share of the ROV's regression grid its backward pass read, and so
+ *   fitted, over its years and controls (0 without a ROV),
  *   16..23 initial animals at risk of control c = 0..7
  *   (SpeciesRoadPatches::computeInitialAAR, SpeciesRoadPatches.cpp:453-490;
  *   NaN past n_controls) */

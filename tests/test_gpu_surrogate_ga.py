@@ -64,11 +64,13 @@ def test_surrogate_gain_over_local_linear_and_plain_ga(ctx):
     Xt, Yt = sga.generate_dataset(gen, sc, 512, paths=1024, rng=np.random.default_rng(12), seed=5)
     pred, _ = ens.predict(Xt, ctx)
     err_mlp = np.median(np.abs(pred[:, 0] - Yt[:, 0]) / Yt[:, 0])
-    # the method without it: the reference's local-linear surrogate of one
-    # aggregate predictor (animals within 3 cells of the road, its IAR)
-    om, _ = sg.buildSurrogateMTECUDA(X[:, 9].astype(np.float64), Y[:, 0].astype(np.float64),
+    # the method without it: the reference's local-linear surrogate of the
+    # end population against the initial animals at risk (buildSurrogateMTECUDA
+    # looks a species up by its IAR), here their mean over species at full flow
+    iar, iar_t = X[:, 11:14].mean(1), Xt[:, 11:14].mean(1)
+    om, _ = sg.buildSurrogateMTECUDA(iar.astype(np.float64), Y[:, 0].astype(np.float64),
                                      np.zeros(len(X)), 32, ctx=ctx)
-    ll = np.interp(Xt[:, 9], om[:32], om[32:])
+    ll = np.interp(iar_t, om[:32], om[32:])
     err_ll = np.median(np.abs(ll - Yt[:, 0]) / Yt[:, 0])
     assert err_mlp < err_ll, (err_mlp, err_ll)
     # ranking, which the screening relies on: recall of the true top 10% of
@@ -87,7 +89,7 @@ def test_surrogate_gain_over_local_linear_and_plain_ga(ctx):
     # predicted fitness and on designs whose members disagree by more than
     # the tolerance, 10% or 20%) against Monte Carlo on every design: fewer
     # Monte Carlo valuations for the same outcome
-    opts = gen.opts(128, 50, seed=9)
+    opts = gen.opts(128, 50, seed=9, sem=1)
     for tol, max_frac in ((0.10, 0.75), (0.20, 0.6)):
         fs, fp, ns, npl = [], [], 0, 0
         for seed in (3, 4, 5, 6, 7, 8):

@@ -15,10 +15,17 @@ class FakeGen:
 
     ctx = None
 
+    class scene:
+        n_controls = 3
+
     def __init__(self, n_species=3, scale=1.0):
         self.S = n_species
         self.scale = scale
         self.evaluated = []
+
+    @staticmethod
+    def opts(paths, years=50, **kw):
+        return ("opts", paths, years)
 
     @staticmethod
     def _key(packed, r):
@@ -37,9 +44,11 @@ class FakeGen:
     def evaluate_segments(self, packed, opts):
         R = len(packed["seg_off"]) - 1
         out = np.zeros((R, self.S, RESULT_STRIDE))
+        model_only = isinstance(opts, tuple) and opts[2] == 0   # the species-model pass
         for r in range(R):
             v = self._key(packed, r)
-            self.evaluated.append(v)
+            if not model_only:
+                self.evaluated.append(v)
             v *= self.scale
             out[r, :, 6] = 100.0               # initial population
             out[r, :, 2] = 100.0 * (1.0 + v)   # end population: ratio 1 + v

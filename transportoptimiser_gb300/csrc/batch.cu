@@ -111,6 +111,7 @@ __global__ void k_pack_results(int n_rs, int S, const int* __restrict__ np,
                                const double* __restrict__ iar, double pen_z,
                                const double* __restrict__ pen,
                                const double* __restrict__ rov_stats,
+                               const unsigned* __restrict__ qroad, double q_all,
                                double* __restrict__ out) {
     int rs = blockIdx.x * blockDim.x + threadIdx.x;
     if (rs >= n_rs) return;
@@ -132,7 +133,9 @@ __global__ void k_pack_results(int n_rs, int S, const int* __restrict__ np,
     o[8] = mine;
     o[9] = road_pen;
     for (int q = 0; q < 5; ++q) o[10 + q] = rov_stats ? rov_stats[5 * (size_t)road + q] : NAN;
-    o[15] = 0.0;
+    // share of the regression grid the road's backward pass read (and so
+    // fitted), over its years and controls
+    o[15] = (rov_stats && qroad && q_all > 0.0) ? (double)qroad[road] / q_all : 0.0;
     for (int c = 0; c < 8; ++c) o[16 + c] = c < C ? iar[(size_t)rs * C + c] : NAN;
 }
 
@@ -280,7 +283,9 @@ to_status tail(to_ctx ctx, to_gen g, const to_mte_args& m, int RS, int choice,
     if (g->rov_on) TO_TRY(rov_stage(ctx, g, R, m.npe, m.road0));
     k_pack_results<<<(RS + 127) / 128, 128, 0, ctx->stream>>>(
         RS, g->S, g->d_np, g->d_nt, g->d_stats, choice == CH_SPARSE ? g->csc.nnz : nullptr, g->C,
-        g->d_iar, g->pen_z, g->d_pen, g->rov_on ? g->d_rov_stats : nullptr, d_results_out);
+        g->d_iar, g->pen_z, g->d_pen, g->rov_on ? g->d_rov_stats : nullptr,
+        g->rov_on ? g->rov.qroad : nullptr,
+        g->rov_on ? (double)(g->rov.Y - 2) * g->rov.C * g->rov.Q : 0.0, d_results_out);
     TO_LAUNCHED(ctx);
     return TO_OK;
 }
@@ -737,7 +742,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     acc(G * blk * 4);
     acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4);
     acc((size_t)Y * S * PT * 4);
-    acc(G * Q); acc(G * Q * 4); acc(4);
+    acc(G * Q); acc(G * Q * 4); acc(4); acc((size_t)NR * 4);
     cudaError_t e = cudaMalloc(&g->rov_buf, bytes);
     if (e != cudaSuccess) {
         g->rov_buf = nullptr;
@@ -793,6 +798,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     a.qmark = carve<unsigned char>(p, G * Q);
     a.qlist = carve<int>(p, G * Q);
     a.qcount = carve<int>(p, 1);
+    a.qroad = carve<unsigned>(p, NR);
     TO_CUDA(ctx, cudaMemcpy(d_flows, t->flows, C * sizeof(float), cudaMemcpyHostToDevice));
     if (U > 0)
         TO_CUDA(ctx, cudaMemcpy(d_unc, t->uncert, 6 * (size_t)U * sizeof(float),

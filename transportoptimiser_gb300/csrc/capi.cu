@@ -83,7 +83,7 @@ void to_prof_end(to_ctx ctx) {
     ctx->n_prof++;
 }
 
-static to_status check_device_flags(to_ctx ctx) {
+to_status to_check_device_flags(to_ctx ctx) {
     int f = 0;
     TO_TRY(to_read_device_flags(ctx, &f));
     if (f != TO_DEVERR_NONE) {
@@ -278,7 +278,7 @@ to_status to_label_image(to_ctx ctx, int W, int H, const int* input,
     int nr = 0;
     TO_TRY(d2h(ctx, &nr, d_nr, 1));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    TO_TRY(check_device_flags(ctx));
+    TO_TRY(to_check_device_flags(ctx));
     if (n_regions) *n_regions = nr;
     return TO_OK;
 }
@@ -321,7 +321,7 @@ to_status to_build_patches(to_ctx ctx, int W, int H, int skpx, int skpy,
     int end = 0;
     TO_TRY(d2h(ctx, &end, d_cnt, 1));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    TO_TRY(check_device_flags(ctx));
+    TO_TRY(to_check_device_flags(ctx));
     std::vector<double> o((size_t)5 * (end > start ? end - start : 0));
     if (end > start) {
         TO_CUDA(ctx, cudaMemcpy(o.data(), d_out + (size_t)5 * start,
@@ -458,7 +458,7 @@ to_status to_species_model(to_ctx ctx, const to_species_in* in,
     TO_TRY(d2h(ctx, &N, d_np, 1));
     TO_TRY(d2h(ctx, &nt, d_nt, 1));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    TO_TRY(check_device_flags(ctx));
+    TO_TRY(to_check_device_flags(ctx));
     out->n_patches = N;
     out->n_transitions = nt;
     TO_TRY(d2h(ctx, out->area, a.area, N));
@@ -588,6 +588,8 @@ to_status to_simulate_mte(to_ctx ctx, const to_mte_problem* prob,
     TO_TRY(d2h(ctx, ef.data(), d_end, ef.size()));
     TO_TRY(d2h(ctx, st.data(), d_stats, st.size()));
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // a bounded wait that ran out (tensor-core kernel) or a plan check
+    TO_TRY(to_check_device_flags(ctx));
     if (end_pops)
         for (size_t i = 0; i < ef.size(); ++i) end_pops[i] = (double)ef[i];
     if (stats)

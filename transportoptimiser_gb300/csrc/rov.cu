@@ -552,6 +552,12 @@ __global__ void __launch_bounds__(1024) k_lsm_list(to_rov_args a) {
         a.qlist[s_base + s_w[warp] + __popc(b & ((1u << lane) - 1u))] = (int)i;
         a.qmark[i] = 0;
     }
+    if (a.qroad && b) {
+        // queries fitted per road (a warp's 32 items mostly share one road)
+        const int road = (int)(i / ((size_t)a.Q * a.C));
+        const unsigned same = __match_any_sync(0xffffffffu, road);
+        if (on && lane == __ffs(same & b) - 1) atomicAdd(&a.qroad[road], (unsigned)__popc(same & b));
+    }
 }
 
 }  // namespace
@@ -757,6 +763,7 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
         return to_set_error(ctx, TO_ERR_INVALID, "touched-query mode: sem 1, ALGO4, scratch");
     if (a.touched)
         TO_CUDA(ctx, cudaMemsetAsync(a.qmark, 0, (size_t)a.G * a.Q, ctx->stream));
+    if (a.qroad) TO_CUDA(ctx, cudaMemsetAsync(a.qroad, 0, (size_t)a.nr * sizeof(unsigned), ctx->stream));
     k_rov_terminal<<<pblocks, tpb, 0, ctx->stream>>>(a);
     TO_LAUNCHED(ctx);
     if (a.lblocks != (a.PT + kLsmChunk - 1) / kLsmChunk || (a.nr > 1 && a.P < kLsmMinPaths))

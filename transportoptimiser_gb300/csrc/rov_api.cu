@@ -293,6 +293,8 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     TO_TRY(to_k::rov_run(ctx, a, sparse ? &csc : nullptr));
     std::vector<double> st((size_t)NR * 5);
     TO_TRY(down(ctx, st.data(), a.stats, (size_t)NR * 5));
+    TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    TO_TRY(to_check_device_flags(ctx));
     // road-major device arrays -> each road's [Y][P] (or [Y][S][P]) output
     std::vector<float> f;
     std::vector<int> iv;

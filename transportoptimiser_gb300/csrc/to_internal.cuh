@@ -88,6 +88,9 @@ static inline T* to_arena_take(to_ctx ctx, size_t count) {
 static inline size_t to_align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 to_status to_read_device_flags(to_ctx ctx, int* flag);
+// reads and clears the device error word; TO_ERR_TIMEOUT for a bounded wait
+// that ran out, TO_ERR_UNSUPPORTED for the other device checks
+to_status to_check_device_flags(to_ctx ctx);
 
 // Bracket a launch with events when profiling is on.
 void to_prof_begin(to_ctx ctx, const char* name);

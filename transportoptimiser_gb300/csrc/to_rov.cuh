@@ -76,6 +76,7 @@ struct to_rov_args {
     unsigned char* qmark;             // [G][Q] marks of the current year (kept zero between years)
     int* qlist;                       // [G*Q] flat items g*Q + q of the marked queries
     int* qcount;                      // number of entries in qlist
+    unsigned* qroad;                  // [nr] queries fitted per road over the years (may be null)
     // 1: reg holds only the current year's blocks (the regressions of year
     // t are written and read within year t; nothing returns them)
     int reg_one_year;

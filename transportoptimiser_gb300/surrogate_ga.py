@@ -16,7 +16,12 @@ Per road the surrogate predicts:
     0 mean over species of E[end population] / initial population
     1 mean over species of P(end < 0.2 initial)
     2 min over species of E[end population] / initial population
-from the 16 device-computed features of to_road_features.
+from 16 inputs (FEATURES): road length, segments and cells, the shares of
+the road's cells on each habitat, the animals on and near the road (device
+features, to_road_features), and what the reference's own surrogates look
+up - each species' initial animals at risk (SpeciesRoadPatches::
+computeInitialAAR) at full flow, their mean at half flow, and the animals
+left off the road - from a species-model pass with no Monte Carlo.
 """
 from __future__ import annotations
 
@@ -29,6 +34,31 @@ from .generation import Generation, pack_segments
 from .mlp import MLPSurrogate
 
 OUTPUTS = ("mean_end_ratio", "p_below", "min_end_ratio")
+FEATURES = ("length / W", "segments / 64", "road cells / W", "share of road cells on code 2",
+            "on code 3", "on code 5", "share of species 0's animals on road cells",
+            "within 3 cells", "within 6 cells", "within 12 cells", "sinuosity / 10",
+            "initial animals at risk, species 0, full flow", "species 1, full flow",
+            "species 2, full flow", "mean over species, half flow",
+            "initial animals, mean over species / 10^5")
+# the device features kept (to_road_features slots)
+_GEOM = (0, 1, 2, 5, 6, 7, 8, 9, 10, 11, 15)
+SEM = 1
+
+
+def road_features(gen: Generation, packed: dict) -> np.ndarray:
+    """[R][16] surrogate inputs (FEATURES) of the roads in `packed`
+    (segments): device features plus one species-model pass per road."""
+    f = gen.features(packed)
+    res = gen.evaluate_segments(packed, gen.opts(32, 0, sem=SEM))
+    C = gen.scene.n_controls
+    S = res.shape[1]
+    iar_full = res[:, :, 16 + C - 1]
+    cols = [f[:, i] for i in _GEOM]
+    for s in range(3):
+        cols.append(iar_full[:, s] if s < S else iar_full.mean(1))
+    cols.append(res[:, :, 16 + C // 2].mean(1))
+    cols.append(res[:, :, 6].mean(1) / 1e5)
+    return np.stack(cols, 1).astype(np.float32)
 
 
 def targets(results: np.ndarray) -> np.ndarray:
@@ -84,9 +114,9 @@ def generate_dataset(gen: Generation, scene, n_samples: int, paths: int, rng,
     while done < n_samples:
         m = min(batch, n_samples - done)
         packed = pack_segments(random_roads(scene, m, rng))
-        X.append(gen.features(packed))
+        X.append(road_features(gen, packed))
         Y.append(targets(gen.evaluate_segments(packed, gen.opts(paths, years, seed=seed,
-                                                                road0=done))))
+                                                                road0=done, sem=SEM))))
         done += m
     return np.concatenate(X), np.concatenate(Y).astype(np.float32)
 
@@ -114,7 +144,7 @@ def screened_values(gen: Generation, ens: Ensemble, roads, opts, tol=0.10, top=0
     """Values of a generation with surrogate screening.  Returns (y [R][3],
     fitness [R], mask of the designs re-valued by Monte Carlo, features)."""
     packed = pack_segments(roads)
-    feats = gen.features(packed)
+    feats = road_features(gen, packed)
     y, spread = ens.predict(feats, gen.ctx)
     # optimistic: the predicted fitness plus the members' relative spread
     # on the fitness term, so uncertain designs get a chance
@@ -146,7 +176,7 @@ def run_ga(gen: Generation, scene, generations: int, pop: int, opts, rng, ens: E
         tv = time.perf_counter()
         if ens is None:
             packed = pack_segments(roads)
-            feats = gen.features(packed)
+            feats = road_features(gen, packed)
             y = targets(gen.evaluate_segments(packed, opts))
             fit = fitness(y, feats)
             mc = np.ones(len(roads), bool)
