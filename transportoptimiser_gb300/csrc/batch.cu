@@ -737,6 +737,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     acc((size_t)S * C * Y * PT * 4);
     acc(G * d * P * 4); acc(G * d * P * 4); acc(G * P * 4); acc(G * 4); acc(G * 4);
     acc((size_t)NR * d * 4); acc((size_t)NR * d * 4); acc(G * d * P * 4); acc(G * P * 4);
+    acc((size_t)NR * d * Rr * 4);
     acc(G * (TO_KNN_GCELLS + 1) * 4); acc(G * sizeof(to_knn_grid)); acc(G * Q * 4);
     acc(G * lblocks * 4); acc(G * d * 2 * 4); acc(4); acc(G * Q * nacc * 4);
     acc(G * blk * 4);
@@ -781,6 +782,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     a.kc = carve<int>(p, G);
     a.gmin = carve<float>(p, (size_t)NR * d);
     a.gmax = carve<float>(p, (size_t)NR * d);
+    a.qax = carve<float>(p, (size_t)NR * d * Rr);
     a.gsx = carve<float>(p, G * d * P);
     a.gsi = carve<int>(p, G * P);
     a.gcell = carve<int>(p, G * (TO_KNN_GCELLS + 1));

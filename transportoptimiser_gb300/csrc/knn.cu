@@ -51,9 +51,61 @@ __device__ __forceinline__ float sqdist(const float* ref, int stride, int i, int
     return s;
 }
 
+// bitonic sort of up to 128 entries held in registers, four a lane
+// (element e = 4 lane + i): strides 1 and 2 pair a lane's own registers,
+// larger strides pair lanes through shuffles.  The entries are distinct
+// (the point index is in the low word), so any sorting network gives the
+// same order.
+__device__ __forceinline__ void warp_sort_reg128(WarpScratch& ws, int cnt) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long v[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int e = lane * 4 + i;
+        v[i] = e < cnt ? ws.sel[e] : ~0ull;
+    }
+#pragma unroll
+    for (int size = 2; size <= 128; size <<= 1) {
+#pragma unroll
+        for (int s2 = size >> 1; s2 > 0; s2 >>= 1) {
+            if (s2 >= 4) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int e = lane * 4 + i;
+                    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v[i], s2 >> 2);
+                    const bool take_min = ((e & s2) == 0) == ((e & size) == 0);
+                    const bool less = v[i] < w;
+                    v[i] = (take_min == less) ? v[i] : w;
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int j = i ^ s2;
+                    if (j > i) {
+                        const bool up = (((lane * 4 + i) & size) == 0);
+                        if ((v[i] > v[j]) == up) {
+                            const unsigned long long t = v[i];
+                            v[i] = v[j];
+                            v[j] = t;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) ws.sel[lane * 4 + i] = v[i];
+    __syncwarp();
+}
+
 // bitonic sort of ws.sel[0..cnt), padded to a power of two; every lane
 // owns compare-exchange pairs, so no lane idles
 __device__ void warp_sort_sel(WarpScratch& ws, int cnt) {
+    if (cnt <= 128) {
+        warp_sort_reg128(ws, cnt);
+        return;
+    }
     const int lane = threadIdx.x & 31;
     int kp = 1;
     while (kp < cnt) kp <<= 1;
@@ -174,8 +226,10 @@ __device__ __forceinline__ bool next_threshold(int cnt, int k, float target, flo
                                                float& T, float& lo, float& hi) {
     if (cnt < k) lo = T; else hi = T;
     float nt;
+    // the threshold only steers the search (every key <= T is kept and the
+    // selection is exact), so the fast power is enough here
     if (cnt == 0) nt = (T > 0.0f) ? T * 16.0f : 1e-30f;
-    else nt = T * powf(target / (float)cnt, expo);
+    else nt = T * __powf(target / (float)cnt, expo);
     if ((lo >= 0.0f && !(nt > lo)) || (hi >= 0.0f && !(nt < hi))) {
         if (lo >= 0.0f && hi >= 0.0f) nt = sqrtf(fmaxf(lo, 1e-38f) * hi);
         else if (hi < 0.0f) nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
@@ -474,6 +528,13 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
             }
         }
         if (!g.ok) for (int j = 0; j < TO_LSM_MAXD; ++j) { g.lo[j] = g.hi[j] = 0.0f; }
+        // a query's first threshold when it has no k-th distance from the
+        // year before: the squared width of the widest cell
+        float T0 = 0.0f;
+        for (int j = 0; j < d; ++j)
+            if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
+        if (!(T0 > 0.0f) && n > 0 && k > 0) T0 = powf((float)k / (float)n, 2.0f / (float)d);
+        g.T0 = T0;
         s_g = g;
         a.ggrid[c] = g;
     }
@@ -561,9 +622,10 @@ __device__ bool reg_select(const float (&key)[kRegKeys], int k, int dim, float T
     int cnt = -1;
     for (int iter = 0; iter < 64; ++iter) {
         if (!(T < INFINITY) || !(T >= 0.0f)) return false;
-        cnt = 0;
+        unsigned mine = 0;
 #pragma unroll
-        for (int u = 0; u < kRegKeys; ++u) cnt += __popc(__ballot_sync(kFull, key[u] <= T));
+        for (int u = 0; u < kRegKeys; ++u) mine += (key[u] <= T) ? 1u : 0u;
+        cnt = (int)__reduce_add_sync(kFull, mine);
         if (cnt >= k && cnt <= cap) break;
         if (!next_threshold(cnt, k, target, expo, T, lo, hi)) return false;
     }
@@ -597,23 +659,23 @@ k_knn_rov(to_rov_args a, int t) {
     // (group, query) items, group g = road*C + control: every grid query, or
     // the year's list of the queries the backward pass reads
     const int items = a.touched ? *a.qcount : a.G * Q;
+    const bool qpow2 = (Q & (Q - 1)) == 0;
+    const int qshift = qpow2 ? __ffs(Q) - 1 : 0;
     for (;;) {
         int item = 0;
         if (lane == 0) item = atomicAdd(a.knn_next, 1);
         item = __shfl_sync(kFull, item, 0);
         if (item >= items) break;
         if (a.touched) item = a.qlist[item];
-        const int c = item / Q, qi = item - c * Q;
+        const int c = qpow2 ? (item >> qshift) : item / Q;
+        const int qi = item - c * Q;
         const int n = a.npts[c], k = a.kc[c];
         if (n < 3 || k <= 0) continue;           // k_knn_solve writes 0
         const to_knn_grid g = a.ggrid[c];
         const float* xs = a.xn + (size_t)c * D * P;
         const float* y = a.yv + (size_t)c * P;
         const float* xr = a.xraw + (size_t)c * D * P;
-        float T0 = 0.0f;
-        for (int j = 0; j < D; ++j)
-            if (g.inv[j] > 0.0f) T0 = fmaxf(T0, 1.0f / (g.inv[j] * g.inv[j]));
-        if (!(T0 > 0.0f)) T0 = powf((float)k / (float)n, 2.0f / (float)D);
+        const float T0 = g.T0;
         float* kth_prev = a.kth + (size_t)c * Q;
         const float kp = kth_prev[qi];
         float T = kp > 0.0f ? kp * kSeedGrow : T0;
@@ -692,12 +754,19 @@ k_knn_rov(to_rov_args a, int t) {
 // one regression system per thread: the intercept at grid query qi of
 // group c (0 where the group has too few points)
 template <int D>
+__device__ __forceinline__ void knn_solve_one(const to_rov_args& a, int t, int item);
+
+// grid-stride over the year's items (all queries, or the fitted list)
+template <int D>
 __global__ void k_knn_solve(to_rov_args a, int t) {
-    int item = blockIdx.x * blockDim.x + threadIdx.x;
-    if (a.touched) {
-        if (item >= *a.qcount) return;
-        item = a.qlist[item];
-    }
+    const int total = a.touched ? *a.qcount : a.G * a.Q;
+    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total;
+         it += gridDim.x * blockDim.x)
+        knn_solve_one<D>(a, t, a.touched ? a.qlist[it] : it);
+}
+
+template <int D>
+__device__ __forceinline__ void knn_solve_one(const to_rov_args& a, int t, int item) {
     if (item >= a.G * a.Q) return;
     const int c = item / a.Q, qi = item - c * a.Q;
     float* yout = to_rov_reg_block(a, t, c) + (size_t)a.R * D;
@@ -753,7 +822,9 @@ to_status launch_knn_rov(to_ctx ctx, const to_rov_args& a, int t) {
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     to_prof_begin(ctx, "knn_solve");
-    k_knn_solve<D><<<(items + 127) / 128, 128, 0, ctx->stream>>>(a, t);
+    const int sblocks = (items + 127) / 128;
+    const int smax = (ctx->sm_count > 0 ? ctx->sm_count : 152) * 16;
+    k_knn_solve<D><<<sblocks < smax ? sblocks : smax, 128, 0, ctx->stream>>>(a, t);
     to_prof_end(ctx);
     TO_LAUNCHED(ctx);
     return TO_OK;

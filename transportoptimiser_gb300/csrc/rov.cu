@@ -456,6 +456,10 @@ __global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
         mn[C][j] = lo; mx[C][j] = hi;
         a.gmin[(size_t)r * d + j] = lo;
         a.gmax[(size_t)r * d + j] = hi;
+        if (a.qax)
+            for (int di = 0; di < R; ++di)
+                a.qax[((size_t)r * d + j) * R + di] =
+                    to_lsm_normalise(to_lsm_query_axis(di, lo, hi, R), lo, hi, j == S, a.scaling);
     }
     for (int c = 0; c < C; ++c) {
         const size_t g = (size_t)r * C + c;

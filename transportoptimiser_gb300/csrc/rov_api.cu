@@ -147,6 +147,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     acc((size_t)S * (Y + 1) * PT * 4); acc((size_t)S * C * Y * PT * 4);
     acc((size_t)G * d * P * 4); acc((size_t)G * d * P * 4); acc((size_t)G * P * 4);
     acc(G * 4); acc(G * 4); acc((size_t)NR * d * 4); acc((size_t)NR * d * 4);
+    acc((size_t)NR * d * R * 4);
     acc((size_t)G * d * P * 4); acc((size_t)G * P * 4);
     acc((size_t)G * (TO_KNN_GCELLS + 1) * 4); acc((size_t)G * sizeof(to_knn_grid));
     acc((size_t)G * Q * 4);
@@ -201,6 +202,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     a.kc = to_arena_take<int>(ctx, G);
     a.gmin = to_arena_take<float>(ctx, (size_t)NR * d);
     a.gmax = to_arena_take<float>(ctx, (size_t)NR * d);
+    a.qax = to_arena_take<float>(ctx, (size_t)NR * d * R);
     a.gsx = to_arena_take<float>(ctx, (size_t)G * d * P);
     a.gsi = to_arena_take<int>(ctx, (size_t)G * P);
     a.gcell = to_arena_take<int>(ctx, (size_t)G * (TO_KNN_GCELLS + 1));

@@ -190,6 +190,17 @@ TO_HD void to_box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Logistic growth step of a patch population after migration, corrected     */
+/* semantics: m (1 + gr (c - m) / c) with the division by the capacity done   */
+/* as a multiplication by its reciprocal rc = 1 / c, computed once per patch. */
+/* (The reference's arithmetic, kept in sem 0, divides every step; the two    */
+/* differ by at most a rounding.)                                             */
+/* ------------------------------------------------------------------------ */
+TO_HD float to_logistic_rc(float m, float gr, float c, float rc) {
+    return m * (1.0f + gr * (c - m) * rc);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Stream layout.  A stream value is addressed by (stream, path, year,        */
 /* lane-group, lane).  One Philox call yields 4 words -> 4 uniforms or 4      */
 /* normals (two Box-Muller pairs).                                            */

@@ -15,6 +15,7 @@ struct to_knn_grid {
     float lo[TO_LSM_MAXD], hi[TO_LSM_MAXD], inv[TO_LSM_MAXD], w[TO_LSM_MAXD];
     int G[TO_LSM_MAXD];
     int ok;
+    float T0;                 // first squared-distance threshold of a query
 };
 
 // A batch of nr roads with the same dimensions: path arrays are road-major
@@ -54,6 +55,7 @@ struct to_rov_args {
     int* kc;                          // [G]
     float* gmin;                      // [nr][d]
     float* gmax;                      // [nr][d]
+    float* qax;                       // [nr][d][R] normalised grid axes of the year (may be null)
     float* gsx;                       // [G][d][P] points in cell order
     int* gsi;                         // [G][P] their original indices
     int* gcell;                       // [G][TO_KNN_GCELLS + 1] cell starts
@@ -106,15 +108,27 @@ __device__ __forceinline__ void to_rov_query(const to_rov_args& a, int road, int
     const int R = a.R;
     const float* lo = a.gmin + (size_t)road * D;
     const float* hi = a.gmax + (size_t)road * D;
+    const float* ax = a.qax ? a.qax + (size_t)road * D * R : nullptr;
+    const bool pow2 = (R & (R - 1)) == 0;
+    const int lr = pow2 ? __ffs(R) - 1 : 0;           // log2 R
     int rem = q;
     int div = a.Q / R;
 #pragma unroll
     for (int j = 0; j < D; ++j) {
-        int di = rem / div;
-        rem -= di * div;
-        div /= R;
-        float raw = to_lsm_query_axis(di, lo[j], hi[j], R);
-        float nv = to_lsm_normalise(raw, lo[j], hi[j], j == a.S, a.scaling);
+        int di;
+        if (pow2) {
+            // q's base-R digit of dimension j (dimension 0 most significant)
+            di = (q >> (lr * (D - 1 - j))) & (R - 1);
+        } else {
+            di = rem / div;
+            rem -= di * div;
+            div /= R;
+        }
+        // the year's normalised axis values, computed once per road
+        // (k_lsm_stats) with the same operations
+        const float nv = ax ? ax[j * R + di]
+                            : to_lsm_normalise(to_lsm_query_axis(di, lo[j], hi[j], R), lo[j],
+                                               hi[j], j == a.S, a.scaling);
         qn[j] = nv;
         xq[j] = (a.sem == 0) ? to_lsm_unit_axis(di, R) : nv;
     }
