@@ -70,21 +70,28 @@ TO_HD void to_lsm_acc_add(int dim, float* acc, float z, float y, const float* xv
             A[(i + 1) * m + (j + 1)] = fmaf(dx[j] * dx[i], z, A[(i + 1) * m + (j + 1)]);
 }
 
-/* FP64 Cholesky of the (symmetric) normal equations; a direction whose
- * pivot falls below 1e-6 of its diagonal is dropped (its coefficient set to
- * zero).  Returns the intercept (the regression value at the query). */
+/* FP64 Cholesky of the (symmetric) normal equations, with the unknowns
+ * ordered slopes first and the intercept last: the intercept is then the
+ * last forward-substitution value over its pivot, with no back
+ * substitution; each pivot is divided once (its reciprocal multiplies its
+ * column).  A direction whose pivot falls below 1e-6 of its diagonal is
+ * dropped (its coefficient set to zero).  Returns the intercept (the
+ * regression value at the query), 0 when its own direction is dropped. */
 TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
     int m = dim + 1;
     double A[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
     double L[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
-    double b[TO_LSM_MAXD + 1], z[TO_LSM_MAXD + 1], x[TO_LSM_MAXD + 1];
+    double b[TO_LSM_MAXD + 1], z[TO_LSM_MAXD + 1], inv[TO_LSM_MAXD + 1];
     int keep[TO_LSM_MAXD + 1];
+    /* unknown p of the solve is term (p + 1) % m of the accumulated sums
+     * (term 0 is the intercept) */
     for (int i = 0; i < m; ++i) {
-        b[i] = (double)acc[i];
-        for (int j = 0; j < m; ++j) {
-            int a = i <= j ? i : j, c = i <= j ? j : i;
+        const int oi = (i + 1) % m;
+        b[i] = (double)acc[oi];
+        for (int j = 0; j <= i; ++j) {
+            const int oj = (j + 1) % m;
+            const int a = oi <= oj ? oi : oj, c = oi <= oj ? oj : oi;
             A[i * m + j] = (double)acc[m + a * m + c];
-            L[i * m + j] = 0.0;
         }
     }
     for (int j = 0; j < m; ++j) {
@@ -93,13 +100,14 @@ TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
             if (keep[k]) s = s - L[j * m + k] * L[j * m + k];
         if (!(s > 1e-6 * A[j * m + j]) || !(s > 0.0)) { keep[j] = 0; continue; }
         keep[j] = 1;
-        double r = sqrt(s);
+        const double r = sqrt(s);
+        inv[j] = 1.0 / r;
         L[j * m + j] = r;
         for (int i = j + 1; i < m; ++i) {
             double v = A[i * m + j];
             for (int k = 0; k < j; ++k)
                 if (keep[k]) v = v - L[i * m + k] * L[j * m + k];
-            L[i * m + j] = v / r;
+            L[i * m + j] = v * inv[j];
         }
     }
     for (int i = 0; i < m; ++i) {
@@ -107,16 +115,9 @@ TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
         double v = b[i];
         for (int k = 0; k < i; ++k)
             if (keep[k]) v = v - L[i * m + k] * z[k];
-        z[i] = v / L[i * m + i];
+        z[i] = v * inv[i];
     }
-    for (int i = m - 1; i >= 0; --i) {
-        if (!keep[i]) { x[i] = 0.0; continue; }
-        double v = z[i];
-        for (int k = i + 1; k < m; ++k)
-            if (keep[k]) v = v - L[k * m + i] * x[k];
-        x[i] = v / L[i * m + i];
-    }
-    return keep[0] ? (float)x[0] : 0.0f;
+    return keep[m - 1] ? (float)(z[m - 1] * inv[m - 1]) : 0.0f;
 }
 
 /* float -> int the way the reference's assignment truncates, with the GPU's
