@@ -672,8 +672,13 @@ def main():
     mte_ms = split.get("mte_sparse", (0.0, 0))[0]
     mte_flops = 2.0 * P * float((Ns.astype(np.float64) ** 2).sum()) * YEARS
     mte_useful = 2.0 * P * float(nnz.sum()) * YEARS if (nnz >= 0).all() else None
-    roofline = roofline_line(top, split, P, P_rov, R_dim, Ns, mte_flops, mte_useful, bf16_peak,
-                             hbm_peak, peak_kind, args.roads, S)
+    # units of work of the two issue-bound kernels in this step
+    Q_rov = R_dim ** (S + 1)
+    units = {"rov_forward_sparse": args.roads * math.ceil(P_rov / 32) * S * YEARS,
+             "knn": float(res[:, 0, 15].sum()) * (YEARS - 2) * len(scene.flows) * Q_rov}
+    clock_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    roofline = roofline_line(top, split, units, clock_mhz, mte_flops, mte_useful, bf16_peak,
+                             hbm_peak, peak_kind)
 
     rov_adj = rov_adjoint_leg(ctx) if rank == 0 and args.rov_leg else None
     rov_gen = rov_generation_leg(ctx) if rank == 0 and args.rov_leg else None
@@ -734,25 +739,59 @@ def main():
     return 0
 
 
-def roofline_line(top, split, P, P_rov, R_dim, Ns, mte_flops, mte_useful, bf16_peak, hbm_peak,
-                  peak_kind, roads, S):
-    """Roofline of the step's dominant kernel.  The ROV's kNN + regression
-    kernel is bound by instruction issue (ncu: issue slots, not DRAM or a
-    tensor pipe); its algorithmic unit is the grid query (k neighbours, the
-    local normal equations).  The MTE migration kernel is reported against
-    the dense-contraction count of the benchmark spec (2 P N^2 Y per road and
-    species) next to its useful, non-zero FLOPs."""
+# Per unit of work, from ncu captures of the bench's own step at 64 roads
+# (profiles/k_rov_forward_union_k_knn_rov_generation.md): warp instructions
+# executed (smsp__inst_executed.sum) and DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum) divided by the units that launch processed.
+#   k_rov_forward_union: unit = one 32-path tile of a road, one species, one year
+#   k_knn_rov: unit = one fitted regression query (k nearest points and the
+#              local normal equations)
+ROOF = {
+    "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": None,
+                           "bytes_per_unit": None,
+                           "unit": "(32-path tile, species, year)"},
+    "knn": {"kernel": "k_knn_rov", "inst_per_unit": None, "bytes_per_unit": None,
+            "unit": "fitted regression query"},
+}
+SMS, SCHEDULERS = 152, 4
+
+
+def roofline_line(top, split, units, clock_mhz, mte_flops, mte_useful, bf16_peak, hbm_peak,
+                  peak_kind):
+    """Roofline of the step's dominant kernel.  The ROV's forward pass and
+    its kNN + regression kernel are both bound by instruction issue: their
+    data stay in shared memory and L1/L2 (DRAM idle), and the migration
+    matrices are 2.3-5% non-zero (a dense tensor-core contraction would do
+    20-40x the work).  `achieved` is warp instructions per second (ncu's
+    count per unit of work x the units this step processed / the kernel's
+    CUDA-event time), `peak` the issue slots per second of 152 SMs x 4
+    schedulers at the SM clock sampled during the timed steps."""
     name, (ms, n) = top
-    out = {"kernel": "k_" + name, "kernel_ms": ms, "launches_per_step": n}
+    ref = ROOF.get(name)
+    out = {"kernel": ref["kernel"] if ref else "k_" + name, "kernel_ms": ms,
+           "launches_per_step": n, "bound": "issue", "unit": "Gwarp-inst/s",
+           "peak_kind": "issue slots: %d SMs x %d schedulers x %.0f MHz (sampled)"
+                        % (SMS, SCHEDULERS, clock_mhz)}
+    peak = SMS * SCHEDULERS * clock_mhz * 1e6 / 1e9
+    if ref and ref["inst_per_unit"] and ms > 0 and units.get(name):
+        u = units[name]
+        ach = ref["inst_per_unit"] * u / (ms / 1e3) / 1e9
+        traffic = ref["bytes_per_unit"] * u / max(n, 1)
+        out.update({"achieved": ach, "peak": peak, "frac": ach / peak,
+                    "traffic": traffic, "traffic_unit": "bytes per launch",
+                    "units_per_step": u, "unit_of_work": ref["unit"],
+                    "inst_per_unit": ref["inst_per_unit"],
+                    "dram_frac": (traffic * max(n, 1) / (ms / 1e3) / 1e9) / hbm_peak})
+    else:
+        out.update({"achieved": None, "peak": peak, "frac": None, "traffic": None})
     mte_ms = split.get("mte_sparse", (0.0, 0))[0]
     out["mte_sparse"] = {"ms": mte_ms, "dense_equiv_tflops": (mte_flops / (mte_ms / 1e3) / 1e12)
                          if mte_ms > 0 else None,
                          "useful_tflops": (mte_useful / (mte_ms / 1e3) / 1e12)
                          if (mte_ms > 0 and mte_useful) else None,
                          "frac_of_bf16_peak": (mte_flops / (mte_ms / 1e3) / 1e12 / bf16_peak)
-                         if mte_ms > 0 else None}
-    out.update({"bound": "issue", "unit": "Ginst/s", "achieved": None, "peak": None,
-                "frac": None, "traffic": None, "peak_kind": peak_kind})
+                         if mte_ms > 0 else None,
+                         "bf16_peak_kind": peak_kind}
     return out
 
 

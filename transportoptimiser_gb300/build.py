@@ -81,7 +81,7 @@ def build_oracle(force: bool = False) -> Path:
     deps = srcs + [ORACLE_DIR / "oracle.h", ORACLE_DIR / "oracle_rov.h", ORACLE_DIR / "oracle_mlp.h",
                    ORACLE_DIR / "oracle_adjoint.h", ORACLE_DIR / "oracle_interp.h",
                    ORACLE_DIR / "oracle_sample.h",
-                   CSRC / "to_math.h", CSRC / "to_lsm_math.h"]
+                   CSRC / "to_math.h", CSRC / "to_math_tables.h", CSRC / "to_lsm_math.h"]
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
     if force or _stale(ORACLE_LIB, deps):
         cc = shutil.which("gcc") or "cc"

@@ -19,7 +19,13 @@
  *     a two-part ln2, then the degree-7 Taylor polynomial of e^r on |r|<=ln2/2.
  *   - to_sincospif: quadrant reduction y = q/2 + r (exact), then the Taylor
  *     series of sin(pi r), cos(pi r) on |r| <= 1/4.
- *   - Box-Muller normals and open/half-open uniforms from Philox words.
+ *   - Box-Muller normals and open/half-open uniforms from Philox words, with
+ *     a table-assisted log (a 128-entry table of reciprocals and their logs
+ *     reduces the mantissa to within 1/200 of 1, then a degree-4 series of
+ *     log1p) and sine/cosine (a 128-entry table of sin/cos of 2 pi j/128,
+ *     then the angle-addition formulas with degree-5 / degree-4 series for
+ *     the remainder, below 2 pi/128); the tables (to_math_tables.h) are
+ *     written by make_math_tables.py.
  *
  * The reference draws its streams from cuRAND XORWOW seeded with
  * srand(time(NULL)) (include/gpuCode/SimulateGPU.cu:3186-3214, 3732-3751,
@@ -36,6 +42,18 @@
 #else
 #define TO_HD static inline
 #endif
+
+#include "to_math_tables.h"
+
+typedef struct { float a, b; } to_f2;
+/* the tables, once in device memory and once on the host, from the same
+   literals */
+#if defined(__CUDACC__)
+static __device__ const to_f2 to_log_tab_d[128] = TO_LOG_TABLE_INIT;
+static __device__ const to_f2 to_sc_tab_d[128] = TO_SINCOS_TABLE_INIT;
+#endif
+static const to_f2 to_log_tab_h[128] = TO_LOG_TABLE_INIT;
+static const to_f2 to_sc_tab_h[128] = TO_SINCOS_TABLE_INIT;
 
 /* ------------------------------------------------------------------------ */
 /* bit casts                                                                 */
@@ -178,13 +196,68 @@ TO_HD void to_sincospif(float y, float* sp, float* cp) {
     *sp = so; *cp = co;
 }
 
-/* Box-Muller: two open uniforms -> two standard normals */
+/* ------------------------------------------------------------------------ */
+/* log of the open uniform to_u01_open(x), table-assisted: with u = 2^e m,    */
+/* m in [1, 2), entry i = the top 7 bits of m's fraction gives R ~ 1/m and    */
+/* G = -log R (entries whose interval lies above sqrt 2 read m as m/2 with    */
+/* e + 1: their G carries -log 2), t = m R - 1 (|t| < 1/200, one rounding),   */
+/* log u = e log 2 + G + log1p t, log1p t = t - t^2/2 + t^3/3 - t^4/4.         */
+/* ------------------------------------------------------------------------ */
+TO_HD to_f2 to_log_entry(int i) {
+#if defined(__CUDA_ARCH__)
+    return to_log_tab_d[i];
+#else
+    return to_log_tab_h[i];
+#endif
+}
+
+TO_HD to_f2 to_sincos_entry(int j) {
+#if defined(__CUDA_ARCH__)
+    return to_sc_tab_d[j];
+#else
+    return to_sc_tab_h[j];
+#endif
+}
+
+TO_HD float to_log_u01(uint32_t x) {
+    const uint32_t b = to_f2u(to_u01_open(x));
+    const int i = (int)((b >> 16) & 127u);
+    const to_f2 rg = to_log_entry(i);
+    const int e = (int)(b >> 23) - 127 + (i >= TO_LOG_SPLIT ? 1 : 0);
+    const float m = to_u2f((b & 0x007FFFFFu) | 0x3F800000u);
+    const float t = fmaf(m, rg.a, -1.0f);
+    float q = fmaf(t, -0.25f, 0x1.555556p-2f /* 1/3 */);
+    q = fmaf(t, q, -0.5f);
+    q = q * t;
+    const float lg = rg.b + fmaf(q, t, t);
+    const float fe = (float)e;
+    /* ln2 = hi + lo, hi has 24 bits */
+    return fmaf(fe, 0x1.62e430p-1f, fmaf(fe, -0x1.05c610p-29f, lg));
+}
+
+/* sin and cos of 2 pi to_u01(x): the angle's top 7 bits pick the table entry
+   (sin a, cos a), a = 2 pi j / 128; the remaining 17 bits give the remainder
+   r < 2 pi / 128, whose sine r - r^3/6 + r^5/120 and cosine 1 - r^2/2 + r^4/24
+   combine with the entry by the angle-addition formulas */
+TO_HD void to_sincos2pi_u01(uint32_t x, float* sp, float* cp) {
+    const int j = (int)(x >> 25);
+    const float r = (float)((x >> 8) & 0x1FFFFu) * 0x1.921fb6p-22f;   /* 2 pi 2^-24 */
+    const float r2 = r * r;
+    float s = fmaf(r2, 0x1.111112p-7f /* 1/120 */, -0x1.555556p-3f /* -1/6 */);
+    s = fmaf(r2 * r, s, r);
+    float c = fmaf(r2, 0x1.555556p-5f /* 1/24 */, -0.5f);
+    c = fmaf(r2, c, 1.0f);
+    const to_f2 sc = to_sincos_entry(j);
+    *sp = fmaf(sc.a, c, sc.b * s);
+    *cp = fmaf(sc.b, c, -(sc.a * s));
+}
+
+/* Box-Muller: two Philox words -> two standard normals, radius from the
+   open uniform of the first, angle from the half-open uniform of the second */
 TO_HD void to_box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
-    float u1 = to_u01_open(a);
-    float u2 = to_u01(b);
-    float rad = sqrtf(-2.0f * to_logf(u1));
+    float rad = sqrtf(-2.0f * to_log_u01(a));
     float sn, cs;
-    to_sincospif(2.0f * u2, &sn, &cs);
+    to_sincos2pi_u01(b, &sn, &cs);
     *z0 = rad * cs;
     *z1 = rad * sn;
 }
