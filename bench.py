@@ -577,6 +577,13 @@ def main():
         if args.profile_only:
             step_device()
             torch.cuda.synchronize()
+            r = d_res.cpu().numpy().reshape(args.roads, S, RESULT_STRIDE)
+            C = len(scene.flows)
+            print(json.dumps({"profile_step": {
+                "roads": args.roads, "rov_paths": P_rov, "mte_paths": P, "species": S,
+                "years": YEARS, "fitted_queries": float(r[:, 0, 15].sum()) * (YEARS - 2) * C *
+                R_dim ** (S + 1),
+                "forward_units": args.roads * math.ceil(P_rov / 32) * S * YEARS}}), flush=True)
             return 0
         if world > 1:
             torch.distributed.barrier()
@@ -739,18 +746,24 @@ def main():
     return 0
 
 
-# Per unit of work, from ncu captures of the bench's own step at 64 roads
-# (profiles/k_rov_forward_union_k_knn_rov_generation.md): warp instructions
-# executed (smsp__inst_executed.sum) and DRAM bytes (dram__bytes_read.sum +
-# dram__bytes_write.sum) divided by the units that launch processed.
+# Per unit of work, from one ncu capture of this bench's own replayed step at
+# 64 roads (640 ROV paths a road, 192,000 forward units, 5,955,452 fitted
+# queries over the step's 48 kNN launches):
+#   ncu --metrics smsp__inst_executed.sum,dram__bytes_read.sum,
+#       dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
+#       -k "regex:k_knn_rov|k_rov_forward_union" -s 98 -c 49 --csv
+#       python bench.py --profile-only --roads 64 --no-rov-leg
+#       --surrogate-samples 0 --no-cpu-baseline --warmup 1
+# warp instructions executed and DRAM bytes (read + write) divided by the
+# units that step processed.
 #   k_rov_forward_union: unit = one 32-path tile of a road, one species, one year
 #   k_knn_rov: unit = one fitted regression query (k nearest points and the
 #              local normal equations)
 ROOF = {
-    "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": None,
-                           "bytes_per_unit": None,
+    "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": 53793.0,
+                           "bytes_per_unit": 288.0,
                            "unit": "(32-path tile, species, year)"},
-    "knn": {"kernel": "k_knn_rov", "inst_per_unit": None, "bytes_per_unit": None,
+    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 2426.6, "bytes_per_unit": 107.6,
             "unit": "fitted regression query"},
 }
 SMS, SCHEDULERS = 152, 4
@@ -766,24 +779,31 @@ def roofline_line(top, split, units, clock_mhz, mte_flops, mte_useful, bf16_peak
     count per unit of work x the units this step processed / the kernel's
     CUDA-event time), `peak` the issue slots per second of 152 SMs x 4
     schedulers at the SM clock sampled during the timed steps."""
-    name, (ms, n) = top
-    ref = ROOF.get(name)
-    out = {"kernel": ref["kernel"] if ref else "k_" + name, "kernel_ms": ms,
-           "launches_per_step": n, "bound": "issue", "unit": "Gwarp-inst/s",
-           "peak_kind": "issue slots: %d SMs x %d schedulers x %.0f MHz (sampled)"
-                        % (SMS, SCHEDULERS, clock_mhz)}
     peak = SMS * SCHEDULERS * clock_mhz * 1e6 / 1e9
-    if ref and ref["inst_per_unit"] and ms > 0 and units.get(name):
-        u = units[name]
-        ach = ref["inst_per_unit"] * u / (ms / 1e3) / 1e9
-        traffic = ref["bytes_per_unit"] * u / max(n, 1)
-        out.update({"achieved": ach, "peak": peak, "frac": ach / peak,
-                    "traffic": traffic, "traffic_unit": "bytes per launch",
-                    "units_per_step": u, "unit_of_work": ref["unit"],
-                    "inst_per_unit": ref["inst_per_unit"],
-                    "dram_frac": (traffic * max(n, 1) / (ms / 1e3) / 1e9) / hbm_peak})
-    else:
-        out.update({"achieved": None, "peak": peak, "frac": None, "traffic": None})
+
+    def issue_line(name, ms, n):
+        ref = ROOF.get(name)
+        line = {"kernel": ref["kernel"] if ref else "k_" + name, "kernel_ms": ms,
+                "launches_per_step": n, "bound": "issue", "unit": "Gwarp-inst/s",
+                "peak_kind": "issue slots: %d SMs x %d schedulers x %.0f MHz (sampled)"
+                             % (SMS, SCHEDULERS, clock_mhz)}
+        if ref and ref["inst_per_unit"] and ms > 0 and units.get(name):
+            u = units[name]
+            ach = ref["inst_per_unit"] * u / (ms / 1e3) / 1e9
+            traffic = ref["bytes_per_unit"] * u / max(n, 1)
+            line.update({"achieved": ach, "peak": peak, "frac": ach / peak,
+                         "traffic": traffic, "traffic_unit": "bytes per launch",
+                         "units_per_step": u, "unit_of_work": ref["unit"],
+                         "inst_per_unit": ref["inst_per_unit"],
+                         "dram_frac": (traffic * max(n, 1) / (ms / 1e3) / 1e9) / hbm_peak})
+        else:
+            line.update({"achieved": None, "peak": peak, "frac": None, "traffic": None})
+        return line
+
+    name, (ms, n) = top
+    out = issue_line(name, ms, n)
+    # the other issue-bound kernel of the step
+    out["others"] = [issue_line(k, *split[k]) for k in ROOF if k != name and k in split]
     mte_ms = split.get("mte_sparse", (0.0, 0))[0]
     out["mte_sparse"] = {"ms": mte_ms, "dense_equiv_tflops": (mte_flops / (mte_ms / 1e3) / 1e12)
                          if mte_ms > 0 else None,

@@ -101,7 +101,7 @@ __device__ __forceinline__ void warp_sort_reg128(WarpScratch& ws, int cnt) {
 
 // bitonic sort of ws.sel[0..cnt), padded to a power of two; every lane
 // owns compare-exchange pairs, so no lane idles
-__device__ void warp_sort_sel(WarpScratch& ws, int cnt) {
+__device__ __noinline__ void warp_sort_sel(WarpScratch& ws, int cnt) {
     if (cnt <= 128) {
         warp_sort_reg128(ws, cnt);
         return;
@@ -249,7 +249,7 @@ __device__ __forceinline__ float sel_key(const WarpScratch& ws, int i) {
 // lo_n and hi_n of them have key <= T, then compact those to the front in
 // their stored order (in place: a write never passes the read position).
 // Returns false, changing nothing, when ties make the window unreachable.
-__device__ bool narrow_stored(WarpScratch& ws, int& cnt, float& T, int lo_n, int hi_n,
+__device__ __noinline__ bool narrow_stored(WarpScratch& ws, int& cnt, float& T, int lo_n, int hi_n,
                               float expo) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;

@@ -356,32 +356,43 @@ k_union_csc(int NP, int C, const int* __restrict__ n_patches, to_csc csc) {
 
 // ---------------------------------------------------------------------------
 // ROV forward paths on the union columns (C <= 3 controls) - grid (ceil(P/32),
-// roads).  As k_rov_forward_sparse, but each non-zero of destination k is
-// one 16-byte shared load {row byte offset, value of control 0, 1, 2} that
-// serves every control's migration (three FMA chains, each in ascending
-// origin order with exact zero terms where a control has no entry), and the
-// year's three growth-mean draws per path are spread over the CTA.
+// roads), up to 32 warps.  As k_rov_forward_sparse, but
+//  * each non-zero of destination k is one 16-byte shared load {row byte
+//    offset, value of control 0, 1, 2} that serves every control's
+//    migration (three FMA chains, each in ascending origin order with exact
+//    zero terms where a control has no entry);
+//  * a warp takes the year's groups of four destinations from a shared
+//    counter, widest group first, and writes the new populations to the
+//    second buffer, so that no warp waits at the year's barrier for a fixed
+//    share of wide columns;
+//  * the growth mean's three draws per path are drawn for kGmChunk years at
+//    a time by the whole CTA, and every warp carries the lane's growth mean
+//    forward itself (same expression, same bits) - two barriers a year.
+// The values equal k_rov_forward_sparse's bit for bit: every group's
+// arithmetic and every sum's order is unchanged, only who computes it.
 // ---------------------------------------------------------------------------
-template <int MAXG>
+constexpr int kGmChunk = 16;
+
 __global__ void __launch_bounds__(1024, 1)
 k_rov_forward_union(to_rov_args a, to_csc csc) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    const int NE = a.ne, NG = NE >> 2, NP = a.np, C = a.C, Y = a.Y, P = a.P;
+    const int NE = a.ne, NG = NE >> 2, C = a.C, Y = a.Y, P = a.P;
     const size_t PT = (size_t)a.PT;
     const int rd = blockIdx.y;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int path = blockIdx.x * kLanes + lane;
     const size_t gp = (size_t)rd * P + path;
     int4* ue = reinterpret_cast<int4*>(sm_raw);                    // [ucap_smem]
-    float* cur = reinterpret_cast<float*>(ue + csc.ucap_smem);     // [NE][32]
-    float* part = cur + (size_t)NE * kLanes;                       // [C+1][NG][32]
+    float* bufA = reinterpret_cast<float*>(ue + csc.ucap_smem);    // [NE][32]
+    float* bufB = bufA + (size_t)NE * kLanes;                      // [NE][32]
+    float* part = bufB + (size_t)NE * kLanes;                      // [C+1][NG][32]
     float* capv = part + (size_t)(C + 1) * NG * kLanes;            // [NE]
-    float* gm = capv + NE;                                         // [32]
-    float* tot = gm + kLanes;                                      // [32]
+    float* xs = capv + NE;                                         // [kGmChunk][3][32]
+    float* tot = xs + kGmChunk * 3 * kLanes;                       // [32]
     float* ntot = tot + kLanes;                                    // [32]
-    float* xs = ntot + kLanes;                                     // [3][32]
-    int* ctl = reinterpret_cast<int*>(xs + 3 * kLanes);            // [32]
-    int* uptr = ctl + kLanes;                                      // [NE+1]
+    int* uptr = reinterpret_cast<int*>(ntot + kLanes);             // [NE+1]
+    int* order = uptr + NE + 1;                                    // [NG]
+    int* grab = order + NG;                                        // [2]
     const uint32_t road = (uint32_t)a.road_ids[rd];
 
     for (int s = 0; s < a.S; ++s) {
@@ -390,7 +401,7 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
         const int N4 = (N + 3) & ~3;
         const int NGr = N4 >> 2;
         const float* sp = a.params + 8 * s;
-        const float* ip = a.init_pops + (size_t)rs * NP;
+        const float* ip = a.init_pops + (size_t)rs * a.np;
         const int nu = csc.unnz[rs];
         if (nu < 0 || nu > csc.ucap_smem || N > NE) {
             // outside the shape this launch was planned for: flag, no result
@@ -401,19 +412,33 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
             continue;
         }
         __syncthreads();
+        float* cur = bufA;
+        float* nxt = bufB;
         for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
             const int k = q / kLanes;
             cur[q] = (k < N) ? ip[k] : 0.0f;
+            nxt[q] = 0.0f;
         }
-        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)rs * NP + k];
+        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)rs * a.np + k];
         for (int k = threadIdx.x; k <= NE; k += blockDim.x)
-            uptr[k] = csc.uptr[(size_t)rs * (NP + 1) + (k <= NP ? k : NP)];
+            uptr[k] = csc.uptr[(size_t)rs * (a.np + 1) + (k <= a.np ? k : a.np)];
         for (int e = threadIdx.x; e < nu; e += blockDim.x) {
             int4 v = csc.uent[(size_t)rs * csc.ucap + e];
             v.x *= kLanes * (int)sizeof(float);                    // origin -> row byte offset
             ue[e] = v;
         }
+        if (threadIdx.x < 2) grab[threadIdx.x] = 0;
         __syncthreads();
+        // the groups in descending order of entries (ties: lower group first)
+        for (int gq = threadIdx.x; gq < NGr; gq += blockDim.x) {
+            const int w = uptr[4 * gq + 4] - uptr[4 * gq];
+            int rank = 0;
+            for (int u = 0; u < NGr; ++u) {
+                const int wu = uptr[4 * u + 4] - uptr[4 * u];
+                rank += (wu > w) || (wu == w && u < gq);
+            }
+            order[rank] = gq;
+        }
         if (warp == 0) {
             float tt = 0.0f;
             for (int grp = 0; grp < NGr; ++grp) {
@@ -421,38 +446,43 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
                 tt = tt + grouped4(v[0], v[kLanes], v[2 * kLanes], v[3 * kLanes]);
             }
             tot[lane] = tt;
-            gm[lane] = sp[0];
             if (path < P) a.totalPops[((size_t)s * (Y + 1)) * PT + gp] = tt;
         }
         const float jp = (a.sem == 0) ? sp[5] : sp[6];
         const float s5 = sp[5] * sp[5];
+        float g = sp[0];                                           // this lane's growth mean
         for (int t = 0; t < Y; ++t) {
-            // the growth mean's three draws per path, one thread each
-            for (int q = threadIdx.x; q < 3 * kLanes; q += blockDim.x) {
-                const int which = q >> 5, i = q & 31;
-                const uint32_t pth = (uint32_t)(blockIdx.x * kLanes + i);
-                float v;
-                if (which == 0) {
-                    v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road, pth, t, s) < jp) ? 1.0f : 0.0f;
-                } else if (which == 1) {
-                    v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road, pth, t, s) * sp[2];
-                } else {
-                    const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road, pth, t, s);
-                    const float jsz = (a.sem == 0) ? (zj * s5 - s5 / 2.0f) : (zj * sp[5] - s5 / 2.0f);
-                    v = to_expf(jsz) - 1.0f;
+            if (t % kGmChunk == 0) {
+                // the next years' growth-mean draws, one thread each
+                const int nc = min(kGmChunk, Y - t);
+                for (int q = threadIdx.x; q < nc * 3 * kLanes; q += blockDim.x) {
+                    const int yy = q / (3 * kLanes), r = q - yy * 3 * kLanes;
+                    const int which = r >> 5, i = r & 31;
+                    const uint32_t pth = (uint32_t)(blockIdx.x * kLanes + i);
+                    const int ty = t + yy;
+                    float v;
+                    if (which == 0) {
+                        v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road, pth, ty, s) < jp) ? 1.0f
+                                                                                             : 0.0f;
+                    } else if (which == 1) {
+                        v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road, pth, ty, s) * sp[2];
+                    } else {
+                        const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road, pth, ty, s);
+                        const float jsz = (a.sem == 0) ? (zj * s5 - s5 / 2.0f)
+                                                       : (zj * sp[5] - s5 / 2.0f);
+                        v = to_expf(jsz) - 1.0f;
+                    }
+                    xs[q] = v;
                 }
-                xs[q] = v;
+                __syncthreads();
             }
-            __syncthreads();
-            if (warp == 0) {
-                const float g = gm[lane];
-                const float jump = xs[lane], brown = xs[kLanes + lane], em1 = xs[2 * kLanes + lane];
-                const float gn = g + sp[4] * (sp[1] - g) * a.dt + g * brown + em1 * g * jump;
-                gm[lane] = gn;
-                ctl[lane] = (path < P) ? a.controls[(size_t)t * PT + gp] : 0;
-                if (a.gmY && path < P) a.gmY[((size_t)t * a.S + s) * P + path] = gn;
+            {
+                const float* xt = xs + (t % kGmChunk) * 3 * kLanes;
+                const float jump = xt[lane], brown = xt[kLanes + lane], em1 = xt[2 * kLanes + lane];
+                g = g + sp[4] * (sp[1] - g) * a.dt + g * brown + em1 * g * jump;
             }
-            __syncthreads();
+            if (warp == 0 && a.gmY && path < P) a.gmY[((size_t)t * a.S + s) * P + path] = g;
+            const int my_c = (path < P) ? a.controls[(size_t)t * PT + gp] : 0;
             if (a.popsY) {
                 for (int q = threadIdx.x; q < NE * kLanes; q += blockDim.x) {
                     const int pth = blockIdx.x * kLanes + (q & (kLanes - 1));
@@ -460,48 +490,49 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
                         a.popsY[(((size_t)t * a.S + s) * NE + (q >> 5)) * P + pth] = cur[q];
                 }
             }
-            const float g = gm[lane];
-            const int my_c = ctl[lane];
             const unsigned char* curb = reinterpret_cast<const unsigned char*>(cur) + lane * 4;
-            float nv[MAXG][4];
+            int* gc = grab + (t & 1);
+            for (;;) {
+                int i = 0;
+                if (lane == 0) i = atomicAdd(gc, 1);
+                i = __shfl_sync(0xffffffffu, i, 0);
+                if (i >= NGr) break;
+                const int grp = order[i];
+                float z[4];
+                to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
+                           (uint32_t)((s * N4) >> 2) + grp, z);
+                float m0[4], m1[4], m2[4], np4[4];
 #pragma unroll
-            for (int gi = 0; gi < MAXG; ++gi) {
-                const int grp = warp + gi * W;
-                if (grp < NGr) {
-                    float z[4];
-                    to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
-                               (uint32_t)((s * N4) >> 2) + grp, z);
-                    float m0[4], m1[4], m2[4], np4[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const int k = grp * 4 + j;
-                        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-                        const int e1 = uptr[k + 1];
+                for (int j = 0; j < 4; ++j) {
+                    const int k = grp * 4 + j;
+                    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+                    const int e1 = uptr[k + 1];
 #pragma unroll 2
-                        for (int e = uptr[k]; e < e1; ++e) {
-                            const int4 en = ue[e];
-                            const float x = *reinterpret_cast<const float*>(curb + en.x);
-                            a0 = fmaf(x, __int_as_float(en.y), a0);
-                            a1 = fmaf(x, __int_as_float(en.z), a1);
-                            a2 = fmaf(x, __int_as_float(en.w), a2);
-                        }
-                        m0[j] = a0; m1[j] = a1; m2[j] = a2;
-                        const float mv = (my_c == 0) ? a0 : ((my_c == 1) ? a1 : a2);
-                        const float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
-                        const float cpk = capv[k];
-                        const float v = (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
-                                                     : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
-                        nv[gi][j] = v;
-                        np4[j] = v;
+                    for (int e = uptr[k]; e < e1; ++e) {
+                        const int4 en = ue[e];
+                        const float x = *reinterpret_cast<const float*>(curb + en.x);
+                        a0 = fmaf(x, __int_as_float(en.y), a0);
+                        a1 = fmaf(x, __int_as_float(en.z), a1);
+                        a2 = fmaf(x, __int_as_float(en.w), a2);
                     }
-                    part[((size_t)0 * NG + grp) * kLanes + lane] = grouped4(m0[0], m0[1], m0[2], m0[3]);
-                    if (C > 1)
-                        part[((size_t)1 * NG + grp) * kLanes + lane] = grouped4(m1[0], m1[1], m1[2], m1[3]);
-                    if (C > 2)
-                        part[((size_t)2 * NG + grp) * kLanes + lane] = grouped4(m2[0], m2[1], m2[2], m2[3]);
-                    part[((size_t)C * NG + grp) * kLanes + lane] = grouped4(np4[0], np4[1], np4[2], np4[3]);
+                    m0[j] = a0; m1[j] = a1; m2[j] = a2;
+                    const float mv = (my_c == 0) ? a0 : ((my_c == 1) ? a1 : a2);
+                    const float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
+                    const float cpk = capv[k];
+                    const float v = (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
+                                                 : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
+                    nxt[k * kLanes + lane] = v;
+                    np4[j] = v;
                 }
+                part[((size_t)0 * NG + grp) * kLanes + lane] = grouped4(m0[0], m0[1], m0[2], m0[3]);
+                if (C > 1)
+                    part[((size_t)1 * NG + grp) * kLanes + lane] = grouped4(m1[0], m1[1], m1[2], m1[3]);
+                if (C > 2)
+                    part[((size_t)2 * NG + grp) * kLanes + lane] = grouped4(m2[0], m2[1], m2[2], m2[3]);
+                part[((size_t)C * NG + grp) * kLanes + lane] = grouped4(np4[0], np4[1], np4[2], np4[3]);
             }
+            // last used in the year before; two barriers before the next year
+            if (threadIdx.x == 0) grab[(t + 1) & 1] = 0;
             __syncthreads();
             for (int c = warp; c <= C; c += W) {
                 float tt = 0.0f;
@@ -515,14 +546,9 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
             }
             __syncthreads();
             if (warp == 0) tot[lane] = ntot[lane];
-#pragma unroll
-            for (int gi = 0; gi < MAXG; ++gi) {
-                const int grp = warp + gi * W;
-                if (grp < NGr) {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) cur[(grp * 4 + j) * kLanes + lane] = nv[gi][j];
-                }
-            }
+            float* tmp = cur;
+            cur = nxt;
+            nxt = tmp;
         }
     }
 }
@@ -932,8 +958,9 @@ size_t rov_union_smem(int NE, int C, int ucap_smem) {
     if (NE > 32 * kMaxG * 4 || C > 3) return ~size_t(0);
     const int NG = NE / 4;
     return (size_t)ucap_smem * 16 +
-           (size_t)(NE * kLanes + (C + 1) * NG * kLanes + NE + 7 * kLanes) * 4 +
-           (size_t)(NE + 1) * 4 + 16;
+           (size_t)(2 * NE * kLanes + (C + 1) * NG * kLanes + NE + kGmChunk * 3 * kLanes +
+                    2 * kLanes) * 4 +
+           (size_t)(NE + 1 + NG + 2) * 4 + 16;
 }
 
 to_status union_csc(to_ctx ctx, int NP, int C, const int* n_patches, int n_rs, to_csc& csc) {
@@ -951,22 +978,11 @@ to_status rov_forward_sparse(to_ctx ctx, const to_rov_args& a, to_csc csc) {
             return to_set_error(ctx, TO_ERR_UNSUPPORTED, "union ROV needs %zu B", smem);
         const dim3 blocks((a.P + kLanes - 1) / kLanes, a.nr);
         const int NG = a.ne / 4;
+        const int warps = NG < 32 ? (NG > 4 ? NG : 4) : 32;
         to_prof_begin(ctx, "rov_forward_sparse");
-        if (NG <= 32 * 3) {
-            // at most three groups a warp (<= 384 patches): fewer live values
-            // between the year's barriers than four
-            const int warps = (NG + 2) / 3 > 4 ? (NG + 2) / 3 : 4;
-            TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_union<3>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_rov_forward_union<3><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
-        } else {
-            const int warps = warps_for(a.ne, 4);
-            if ((NG + warps - 1) / warps > kMaxG)
-                return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", a.ne);
-            TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_union<kMaxG>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_rov_forward_union<kMaxG><<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
-        }
+        TO_CUDA(ctx, cudaFuncSetAttribute(k_rov_forward_union,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_rov_forward_union<<<blocks, warps * 32, smem, ctx->stream>>>(a, csc);
         to_prof_end(ctx);
         TO_LAUNCHED(ctx);
         return TO_OK;
