@@ -28,6 +28,7 @@ void vexp(const float* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = 
 void vsc(const float* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i) to_sincospif(x[i], &s[i], &c[i]); }
 void vlogu(const uint32_t* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = to_log_u01(x[i]); }
 void vsc2(const uint32_t* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i) to_sincos2pi_u01(x[i], &s[i], &c[i]); }
+void vdiv(const float* a, const float* b, float* q, int n) { for (int i = 0; i < n; ++i) q[i] = to_div_rcp(a[i], b[i], 1.0f / b[i]); }
 """
 
 
@@ -108,3 +109,30 @@ def test_box_muller_log_and_sincos_accuracy(tmp_path_factory):
     ang = 2.0 * math.pi * (x >> 8).astype(np.float64) * 2.0 ** -24
     assert np.max(np.abs(s - np.sin(ang))) < 2.5e-7
     assert np.max(np.abs(c - np.cos(ang))) < 2.5e-7
+
+
+def test_division_from_reciprocal_is_correctly_rounded(tmp_path_factory):
+    """to_div_rcp (Markstein's quotient from the rounded reciprocal) against
+    IEEE float division, bit for bit: random significands over the growth
+    step's ranges and well beyond them, and divisors with all-ones, all-zero
+    and single-bit significands."""
+    h = _helper(tmp_path_factory)
+    fp = C.POINTER(C.c_float)
+    rng = np.random.default_rng(7)
+    n = 1 << 22
+
+    def floats(emin, emax, m):
+        sig = rng.integers(0, 1 << 23, m, dtype=np.uint32)
+        exp = rng.integers(127 + emin, 127 + emax + 1, m, dtype=np.uint32)
+        sign = rng.integers(0, 2, m, dtype=np.uint32) << 31
+        return (sign | (exp << 23) | sig).view(np.float32)
+
+    a = np.concatenate([floats(-30, 30, n), (rng.standard_normal(n) * 1e4).astype(np.float32)])
+    b = np.concatenate([np.abs(floats(-30, 30, n)), rng.uniform(1.0, 1e5, n).astype(np.float32)])
+    special = np.array([0x3F7FFFFF, 0x3F800000, 0x3F800001, 0x42C80000, 0x4B7FFFFF, 0x3FFFFFFF],
+                       np.uint32).view(np.float32)
+    b[:len(special) * 1000] = np.repeat(special, 1000)
+    q = np.zeros_like(a)
+    h.vdiv(a.ctypes.data_as(fp), b.ctypes.data_as(fp), q.ctypes.data_as(fp), len(a))
+    want = a / b
+    assert np.array_equal(q.view(np.uint32), want.view(np.uint32))

@@ -386,8 +386,8 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
     float* bufA = reinterpret_cast<float*>(ue + csc.ucap_smem);    // [NE][32]
     float* bufB = bufA + (size_t)NE * kLanes;                      // [NE][32]
     float* part = bufB + (size_t)NE * kLanes;                      // [C+1][NG][32]
-    float* capv = part + (size_t)(C + 1) * NG * kLanes;            // [NE]
-    float* xs = capv + NE;                                         // [kGmChunk][3][32]
+    float2* capr = reinterpret_cast<float2*>(part + (size_t)(C + 1) * NG * kLanes);  // [NE]
+    float* xs = reinterpret_cast<float*>(capr + NE);               // [kGmChunk][3][32]
     float* tot = xs + kGmChunk * 3 * kLanes;                       // [32]
     float* ntot = tot + kLanes;                                    // [32]
     int* uptr = reinterpret_cast<int*>(ntot + kLanes);             // [NE+1]
@@ -419,7 +419,10 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
             cur[q] = (k < N) ? ip[k] : 0.0f;
             nxt[q] = 0.0f;
         }
-        for (int k = threadIdx.x; k < NE; k += blockDim.x) capv[k] = a.caps[(size_t)rs * a.np + k];
+        for (int k = threadIdx.x; k < NE; k += blockDim.x) {
+            const float cp = a.caps[(size_t)rs * a.np + k];
+            capr[k] = make_float2(cp, 1.0f / cp);          // capacity, its reciprocal
+        }
         for (int k = threadIdx.x; k <= NE; k += blockDim.x)
             uptr[k] = csc.uptr[(size_t)rs * (a.np + 1) + (k <= a.np ? k : a.np)];
         for (int e = threadIdx.x; e < nu; e += blockDim.x) {
@@ -518,9 +521,12 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
                     m0[j] = a0; m1[j] = a1; m2[j] = a2;
                     const float mv = (my_c == 0) ? a0 : ((my_c == 1) ? a1 : a2);
                     const float gr = (a.sem == 0) ? g + z[j] * sp[7] : fmaf(sp[7] * z[j], g, g);
-                    const float cpk = capv[k];
-                    const float v = (a.sem == 0) ? mv * (1.0f + gr * (cpk - mv) / cpk / 100.0f)
-                                                 : fmaxf(mv * (1.0f + gr * (cpk - mv) / cpk), 0.0f);
+                    const float2 cr = capr[k];
+                    // the divisions as to_div_rcp: the same bits
+                    const float v = (a.sem == 0)
+                        ? mv * (1.0f + to_div_rcp(to_div_rcp(gr * (cr.x - mv), cr.x, cr.y), 100.0f,
+                                                  0.01f))
+                        : fmaxf(mv * (1.0f + to_div_rcp(gr * (cr.x - mv), cr.x, cr.y)), 0.0f);
                     nxt[k * kLanes + lane] = v;
                     np4[j] = v;
                 }
@@ -958,7 +964,7 @@ size_t rov_union_smem(int NE, int C, int ucap_smem) {
     if (NE > 32 * kMaxG * 4 || C > 3) return ~size_t(0);
     const int NG = NE / 4;
     return (size_t)ucap_smem * 16 +
-           (size_t)(2 * NE * kLanes + (C + 1) * NG * kLanes + NE + kGmChunk * 3 * kLanes +
+           (size_t)(2 * NE * kLanes + (C + 1) * NG * kLanes + 2 * NE + kGmChunk * 3 * kLanes +
                     2 * kLanes) * 4 +
            (size_t)(NE + 1 + NG + 2) * 4 + 16;
 }

@@ -263,14 +263,17 @@ TO_HD void to_box_muller(uint32_t a, uint32_t b, float* z0, float* z1) {
 }
 
 /* ------------------------------------------------------------------------ */
-/* Logistic growth step of a patch population after migration, corrected     */
-/* semantics: m (1 + gr (c - m) / c) with the division by the capacity done   */
-/* as a multiplication by its reciprocal rc = 1 / c, computed once per patch. */
-/* (The reference's arithmetic, kept in sem 0, divides every step; the two    */
-/* differ by at most a rounding.)                                             */
+/* a / b rounded to nearest, from rb = 1 / b rounded to nearest (computed    */
+/* once per divisor): q = RN(a rb); the remainder a - b q is exact in one    */
+/* FMA; RN(q + (a - b q) rb) is the correctly rounded quotient whenever no   */
+/* step over- or underflows (P. Markstein, "Computation of elementary        */
+/* functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1), */
+/* 1990).  The same value as the division a / b, bit for bit.                */
 /* ------------------------------------------------------------------------ */
-TO_HD float to_logistic_rc(float m, float gr, float c, float rc) {
-    return m * (1.0f + gr * (c - m) * rc);
+TO_HD float to_div_rcp(float a, float b, float rb) {
+    const float q = a * rb;
+    const float r = fmaf(-q, b, a);
+    return fmaf(r, rb, q);
 }
 
 /* ------------------------------------------------------------------------ */

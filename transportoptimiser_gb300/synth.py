@@ -221,5 +221,54 @@ def generation(seed: int = 0, n_roads: int = 256, W: int = 200, tile: int = 30,
            for _ in range(n_species)]
     sc = Scene(W=W, H=W, res=res, base_map=base, species=spp, n_controls=3,
                flows=flows, seed=seed)
-    sc.roads = [random_road(W, W, int(rng.integers(8, 65)), rng) for _ in range(n_roads)]
+    # roads of 20-400 patch crossings each: a draw outside is redrawn
+    lab = patch_labels(base, W, W, res)
+    sc.roads = []
+    while len(sc.roads) < n_roads:
+        rd = random_road(W, W, int(rng.integers(8, 65)), rng)
+        if 20 <= patch_crossings(rd, lab, W, W) <= 400:
+            sc.roads.append(rd)
     return sc
+
+
+def type_components(base: np.ndarray, W: int, H: int) -> np.ndarray:
+    """[H][W] labels of the 4-connected regions of equal habitat code (the
+    smallest cell index of the region), by min-label propagation."""
+    g = base.reshape(H, W)
+    lab = np.arange(W * H, dtype=np.int64).reshape(H, W)
+    pairs = [((slice(None), slice(1, None)), (slice(None), slice(None, -1))),
+             ((slice(None), slice(None, -1)), (slice(None), slice(1, None))),
+             ((slice(1, None), slice(None)), (slice(None, -1), slice(None))),
+             ((slice(None, -1), slice(None)), (slice(1, None), slice(None)))]
+    while True:
+        new = lab.copy()
+        for a, b in pairs:
+            same = g[a] == g[b]
+            new[a] = np.where(same, np.minimum(new[a], lab[b]), new[a])
+        if np.array_equal(new, lab):
+            return lab
+        lab = new
+
+
+def patch_labels(base: np.ndarray, W: int, H: int, block: int) -> np.ndarray:
+    """[H][W] patch ids as the species models cut them: a region of equal
+    habitat code within one block x block square of cells."""
+    lab = type_components(base, W, H)
+    yy, xx = np.mgrid[0:H, 0:W]
+    nb = ((W + block - 1) // block) * ((H + block - 1) // block)
+    return lab * nb + (yy // block) * ((W + block - 1) // block) + xx // block
+
+
+def patch_crossings(road: Road, lab: np.ndarray, W: int, H: int) -> int:
+    """How often the road's path passes from one patch into another (ids
+    from patch_labels), sampled at quarter-cell steps."""
+    xs, ys = [], []
+    for x1, y1, x2, y2 in road.segments:
+        n = max(2, int(math.hypot(x2 - x1, y2 - y1) * 4))
+        t = np.linspace(0.0, 1.0, n)
+        xs.append(x1 + t * (x2 - x1))
+        ys.append(y1 + t * (y2 - y1))
+    x = np.clip(np.concatenate(xs).astype(np.int64), 0, W - 1)
+    y = np.clip(np.concatenate(ys).astype(np.int64), 0, H - 1)
+    seq = lab[y, x]
+    return int((seq[1:] != seq[:-1]).sum())
