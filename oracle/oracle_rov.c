@@ -83,14 +83,14 @@ void or_knn(const float* ref, int n, const float* query, int Q, int dim, int k,
 /* xraw(i, j): x of neighbour i in dimension j as the kernel reads it.       */
 /* lanes = 1: neighbours summed in order (surrogate builders).  lanes = 32:  */
 /* neighbour kk goes to partial sum kk % 32, and the 32 partial sums are     */
-/* combined by the butterfly s[l] = s[l] + s[l ^ o], o = 16, 8, 4, 2, 1,     */
-/* which is the order the device's warp shuffle reduction adds them in.     */
+/* added in lane order, ((s0 + s1) + s2) + ... + s31, as the device's        */
+/* shared-memory reduction adds them.                                       */
 /* ------------------------------------------------------------------------ */
 static float local_linear(int dim, int k, int Q, int qi, const float* dist,
                           const int* ind, const float* y, const float* xbuf,
                           int n, int pointmajor, const float* xq, int lanes) {
     enum { ACC = TO_LSM_MAXD + 1 + (TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1) };
-    float acc[32][ACC], tmp[32][ACC];
+    float acc[32][ACC];
     const int na = (dim + 1) + (dim + 1) * (dim + 1);
     for (int l = 0; l < lanes; ++l) to_lsm_acc_init(dim, acc[l]);
     float h = dist[(size_t)(k - 1) * Q + qi];
@@ -102,10 +102,10 @@ static float local_linear(int dim, int k, int Q, int qi, const float* dist,
             xv[j] = pointmajor ? xbuf[(size_t)i * dim + j] : xbuf[(size_t)j * n + i];
         to_lsm_acc_add(dim, acc[kk % lanes], to_lsm_weight(d, h), y[i], xv, xq);
     }
-    for (int o = lanes / 2; o > 0; o >>= 1) {
-        for (int l = 0; l < lanes; ++l)
-            for (int e = 0; e < na; ++e) tmp[l][e] = acc[l][e] + acc[l ^ o][e];
-        memcpy(acc, tmp, sizeof(float) * ACC * (size_t)lanes);
+    for (int e = 0; e < na; ++e) {
+        float s = acc[0][e];
+        for (int l = 1; l < lanes; ++l) s = s + acc[l][e];
+        acc[0][e] = s;
     }
     return to_lsm_solve_intercept(dim, acc[0]);
 }

@@ -593,11 +593,16 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 // query) items from a counter, so no warp waits on another: items differ a
 // lot in cost (queries outside the point cloud need wide radii).  A query's
 // threshold starts from its k-th distance of the year before, times
-// kSeedGrow.  After the selection every lane accumulates the normal
-// equations of neighbours lane, lane+32, ...; the butterfly sum leaves the
-// same totals in every lane, and lane 0 stores them.  k_knn_solve then
-// solves one system per thread (FP64 Cholesky, to_lsm_math.h).
+// kSeedGrow (kSeedGrowReg where the keys are in registers).  After the
+// selection every lane accumulates the normal equations of neighbours lane,
+// lane+32, ...; the 32 partials of each sum are added in lane order through
+// shared memory, and the item's sums are stored at its list position.
+// k_knn_solve then solves one system per thread (FP64 square-root-free
+// Cholesky, to_lsm_math.h).
 constexpr float kSeedGrow = 1.4f;
+// the register search re-counts cheaply: a tighter first threshold (about
+// 1.44 k keys qualify in four dimensions against 1.96 k)
+constexpr float kSeedGrowReg = 1.2f;
 // groups of at most this many points skip the threshold search
 constexpr int kBrute = 128;
 // groups of at most this many points keep every key in registers (12 per
@@ -645,6 +650,10 @@ __device__ bool reg_select(const float (&key)[kRegKeys], int k, int dim, float T
 
 template <int D>
 __host__ __device__ constexpr int knn_acc_len() { return (D + 1) + (D + 1) * (D + 1); }
+// the sums a regression keeps: (D + 1) right-hand sides, then the upper
+// triangle i <= j of the (D + 1)^2 matrix in row order
+template <int D>
+__host__ __device__ constexpr int knn_sums() { return (D + 1) + (D + 1) * (D + 2) / 2; }
 
 size_t knn_rov_smem() { return sizeof(WarpScratch) * kWarps; }
 
@@ -653,6 +662,7 @@ __global__ void __launch_bounds__(kWarps * 32, 4)
 k_knn_rov(to_rov_args a, int t) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     constexpr int M = D + 1, NA = knn_acc_len<D>();
+    constexpr int NS = knn_sums<D>();
     const int P = a.P, Q = a.Q;
     const int lane = threadIdx.x & 31;
     WarpScratch& ws = reinterpret_cast<WarpScratch*>(sm_raw)[threadIdx.x >> 5];
@@ -662,11 +672,11 @@ k_knn_rov(to_rov_args a, int t) {
     const bool qpow2 = (Q & (Q - 1)) == 0;
     const int qshift = qpow2 ? __ffs(Q) - 1 : 0;
     for (;;) {
-        int item = 0;
-        if (lane == 0) item = atomicAdd(a.knn_next, 1);
-        item = __shfl_sync(kFull, item, 0);
-        if (item >= items) break;
-        if (a.touched) item = a.qlist[item];
+        int li = 0;                               // position in the year's list
+        if (lane == 0) li = atomicAdd(a.knn_next, 1);
+        li = __shfl_sync(kFull, li, 0);
+        if (li >= items) break;
+        const int item = a.touched ? a.qlist[li] : li;
         const int c = qpow2 ? (item >> qshift) : item / Q;
         const int qi = item - c * Q;
         const int n = a.npts[c], k = a.kc[c];
@@ -697,7 +707,7 @@ k_knn_rov(to_rov_args a, int t) {
                 const int i = lane + 32 * u;
                 key[u] = (i < n) ? sqdist(xs, P, i, D, qn) : INFINITY;
             }
-            ok = reg_select(key, k, D, T, ws);
+            ok = reg_select(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
         } else if (g.ok) {
             GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
                            a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
@@ -732,48 +742,75 @@ k_knn_rov(to_rov_args a, int t) {
             }
             to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
         }
-        float* sa = a.knn_acc + (size_t)item * NA;
+        // the item's NS sums, at its list position
+        float* sa = a.knn_acc + (size_t)li * NS;
+        // the normal-equation sums: every lane's partials into shared memory
+        // (sum e in row e, lane in column, rows 33 wide), then lane e adds
+        // row e's 32 partials in lane order
+        static_assert(NS * 33 * sizeof(float) <= sizeof(WarpScratch), "reduction rows");
+        float* red = reinterpret_cast<float*>(&ws);
+        __syncwarp();
+        {
+            int e = 0;
 #pragma unroll
-        for (int e = 0; e < M; ++e) {
-            float x = acc[e];
-            for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
-            if (lane == 0) sa[e] = x;
+            for (int i = 0; i < M; ++i) red[(e++) * 33 + lane] = acc[i];
+#pragma unroll
+            for (int i = 0; i < M; ++i)
+#pragma unroll
+                for (int j = i; j < M; ++j) red[(e++) * 33 + lane] = acc[M + i * M + j];
         }
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-#pragma unroll
-            for (int j = i; j < M; ++j) {
-                float x = acc[M + i * M + j];
-                for (int o = 16; o > 0; o >>= 1) x = x + __shfl_xor_sync(kFull, x, o);
-                if (lane == 0) sa[M + i * M + j] = x;
-            }
+        __syncwarp();
+        if (lane < NS) {
+            float x = red[lane * 33];
+#pragma unroll 8
+            for (int l = 1; l < 32; ++l) x = x + red[lane * 33 + l];
+            sa[lane] = x;
+        }
         __syncwarp();
     }
 }
 
-// one regression system per thread: the intercept at grid query qi of
-// group c (0 where the group has too few points)
+// One regression system per thread over the year's list, 128 at a time: a
+// chunk's sums (NS a system, consecutive list positions) are copied to
+// shared memory word by word with consecutive threads on consecutive words
+// (rows padded to an odd stride), then each thread lays its own out as the
+// solver reads them and writes the intercept at grid query qi of group c
+// (0 where the group has too few points).
 template <int D>
-__device__ __forceinline__ void knn_solve_one(const to_rov_args& a, int t, int item);
-
-// grid-stride over the year's items (all queries, or the fitted list)
-template <int D>
-__global__ void k_knn_solve(to_rov_args a, int t) {
+__global__ void __launch_bounds__(128) k_knn_solve(to_rov_args a, int t) {
+    constexpr int M = D + 1, NS = knn_sums<D>(), NSP = NS | 1;
+    __shared__ float s[128 * NSP];
     const int total = a.touched ? *a.qcount : a.G * a.Q;
-    for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total;
-         it += gridDim.x * blockDim.x)
-        knn_solve_one<D>(a, t, a.touched ? a.qlist[it] : it);
-}
-
-template <int D>
-__device__ __forceinline__ void knn_solve_one(const to_rov_args& a, int t, int item) {
-    if (item >= a.G * a.Q) return;
-    const int c = item / a.Q, qi = item - c * a.Q;
-    float* yout = to_rov_reg_block(a, t, c) + (size_t)a.R * D;
-    const int n = a.npts[c], k = a.kc[c];
-    yout[qi] = (n < 3 || k <= 0)
-                   ? 0.0f
-                   : to_lsm_solve_intercept(D, a.knn_acc + (size_t)item * knn_acc_len<D>());
+    for (int base = blockIdx.x * 128; base < total; base += gridDim.x * 128) {
+        const int cnt = min(128, total - base);
+        __syncthreads();
+        const float* src = a.knn_acc + (size_t)base * NS;
+        for (int q = threadIdx.x; q < cnt * NS; q += 128) {
+            const int i = q / NS;
+            s[i * NSP + (q - i * NS)] = src[q];
+        }
+        __syncthreads();
+        if ((int)threadIdx.x >= cnt) continue;
+        const int li = base + threadIdx.x;
+        const int item = a.touched ? a.qlist[li] : li;
+        if (item >= a.G * a.Q) continue;
+        const int c = item / a.Q, qi = item - c * a.Q;
+        const int n = a.npts[c], k = a.kc[c];
+        float y = 0.0f;
+        if (n >= 3 && k > 0) {
+            float acc[knn_acc_len<D>()];
+            const float* si = s + threadIdx.x * NSP;
+            int e = 0;
+#pragma unroll
+            for (int i = 0; i < M; ++i) acc[i] = si[e++];
+#pragma unroll
+            for (int i = 0; i < M; ++i)
+#pragma unroll
+                for (int j = i; j < M; ++j) acc[M + i * M + j] = si[e++];
+            y = to_lsm_solve_intercept(D, acc);
+        }
+        (to_rov_reg_block(a, t, c) + (size_t)a.R * D)[qi] = y;
+    }
 }
 
 // generic: explicit dim-major queries

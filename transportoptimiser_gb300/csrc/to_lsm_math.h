@@ -11,8 +11,9 @@
  *   Gaussian kernel weights,  multiLocLinReg         :2982-3033
  *   normal equations
  *   solve                     solveLinearSystem      :129-190 (FP32 Gaussian
- *                             elimination; here FP64 Cholesky, with near-
- *                             singular directions dropped)
+ *                             elimination; here FP64 square-root-free
+ *                             Cholesky, with near-singular directions
+ *                             dropped)
  *   interpolation of the      backwardInduction      :2564-2703
  *   regression grid
  */
@@ -70,54 +71,76 @@ TO_HD void to_lsm_acc_add(int dim, float* acc, float z, float y, const float* xv
             A[(i + 1) * m + (j + 1)] = fmaf(dx[j] * dx[i], z, A[(i + 1) * m + (j + 1)]);
 }
 
-/* FP64 Cholesky of the (symmetric) normal equations, with the unknowns
- * ordered slopes first and the intercept last: the intercept is then the
- * last forward-substitution value over its pivot, with no back
- * substitution; each pivot is divided once (its reciprocal multiplies its
- * column).  A direction whose pivot falls below 1e-6 of its diagonal is
- * dropped (its coefficient set to zero).  Returns the intercept (the
- * regression value at the query), 0 when its own direction is dropped. */
+/* 1 / x for x > 0 in double: the float reciprocal of x refined by two
+ * Newton-Raphson steps y <- y + y (1 - x y), each with the residual in one
+ * FMA (relative error about 2^-23, then 2^-46, then within an ulp).  x out
+ * of float range takes the division. */
+TO_HD double to_rcp64(double x) {
+    const float xf = (float)x;
+    if (!(xf > 1e-37f && xf < 1e37f)) return 1.0 / x;
+    double y = (double)(1.0f / xf);
+    y = fma(y, fma(-x, y, 1.0), y);
+    y = fma(y, fma(-x, y, 1.0), y);
+    return y;
+}
+
+/* FP64 square-root-free Cholesky (L D L^T) of the (symmetric) normal
+ * equations, with the unknowns ordered slopes first and the intercept
+ * last: with L unit lower triangular, L y = b and the intercept is
+ * y[m-1] / d[m-1], with no back substitution.  Each pivot's reciprocal
+ * (to_rcp64) scales its column.  A direction whose pivot falls below 1e-6
+ * of its diagonal is dropped (its coefficient set to zero).  Returns the
+ * intercept (the regression value at the query), 0 when its own direction
+ * is dropped. */
 TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
     int m = dim + 1;
     double A[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
-    double L[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
-    double b[TO_LSM_MAXD + 1], z[TO_LSM_MAXD + 1], inv[TO_LSM_MAXD + 1];
+    double L[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];   /* L[i][j], i > j */
+    double U[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];   /* L[i][j] d[j] */
+    double b[TO_LSM_MAXD + 1], y[TO_LSM_MAXD + 1], inv[TO_LSM_MAXD + 1];
     int keep[TO_LSM_MAXD + 1];
     /* unknown p of the solve is term (p + 1) % m of the accumulated sums
      * (term 0 is the intercept) */
+    TO_UNROLL
     for (int i = 0; i < m; ++i) {
         const int oi = (i + 1) % m;
         b[i] = (double)acc[oi];
+        TO_UNROLL
         for (int j = 0; j <= i; ++j) {
             const int oj = (j + 1) % m;
             const int a = oi <= oj ? oi : oj, c = oi <= oj ? oj : oi;
             A[i * m + j] = (double)acc[m + a * m + c];
         }
     }
+    TO_UNROLL
     for (int j = 0; j < m; ++j) {
         double s = A[j * m + j];
+        TO_UNROLL
         for (int k = 0; k < j; ++k)
-            if (keep[k]) s = s - L[j * m + k] * L[j * m + k];
+            if (keep[k]) s = s - L[j * m + k] * U[j * m + k];
         if (!(s > 1e-6 * A[j * m + j]) || !(s > 0.0)) { keep[j] = 0; continue; }
         keep[j] = 1;
-        const double r = sqrt(s);
-        inv[j] = 1.0 / r;
-        L[j * m + j] = r;
+        inv[j] = to_rcp64(s);
+        TO_UNROLL
         for (int i = j + 1; i < m; ++i) {
             double v = A[i * m + j];
+            TO_UNROLL
             for (int k = 0; k < j; ++k)
-                if (keep[k]) v = v - L[i * m + k] * L[j * m + k];
+                if (keep[k]) v = v - L[i * m + k] * U[j * m + k];
+            U[i * m + j] = v;
             L[i * m + j] = v * inv[j];
         }
     }
+    TO_UNROLL
     for (int i = 0; i < m; ++i) {
-        if (!keep[i]) { z[i] = 0.0; continue; }
+        if (!keep[i]) { y[i] = 0.0; continue; }
         double v = b[i];
+        TO_UNROLL
         for (int k = 0; k < i; ++k)
-            if (keep[k]) v = v - L[i * m + k] * z[k];
-        z[i] = v * inv[i];
+            if (keep[k]) v = v - L[i * m + k] * y[k];
+        y[i] = v;
     }
-    return keep[m - 1] ? (float)(z[m - 1] * inv[m - 1]) : 0.0f;
+    return keep[m - 1] ? (float)(y[m - 1] * inv[m - 1]) : 0.0f;
 }
 
 /* float -> int the way the reference's assignment truncates, with the GPU's

@@ -39,8 +39,11 @@
 
 #if defined(__CUDACC__)
 #define TO_HD __host__ __device__ __forceinline__
+/* full unrolling of a loop whose trip count is known where it is inlined */
+#define TO_UNROLL _Pragma("unroll")
 #else
 #define TO_HD static inline
+#define TO_UNROLL
 #endif
 
 #include "to_math_tables.h"
