@@ -56,6 +56,7 @@ struct to_gen_s {
     uint16_t* d_tdest;
     float *d_mmm, *d_ip, *d_cp;
     float* d_end = nullptr;              // grown on demand [RS][P]
+    int* d_mte_order = nullptr;          // [RS] the MTE's launch order (k_mte_order)
     size_t end_cap = 0;
     double* d_stats;                     // [RS][5]
     double* d_results;                   // [RS][8]
@@ -236,6 +237,7 @@ to_mte_args mte_args(to_ctx ctx, to_gen g, const to_eval_opts* o, int NE) {
     m.npad = g->NP; m.npe = NE; m.n_patches = g->d_np; m.mmm = g->d_mmm;
     m.init_pops = g->d_ip; m.caps = g->d_cp; m.params = g->d_params;
     m.end_pops = g->d_end; m.flags = ctx->d_flags;
+    m.order_buf = g->d_mte_order;
     return m;
 }
 
@@ -585,6 +587,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     const size_t cap = (size_t)NP * 32;
     acc(RS * C * (NP + 1) * 4); acc(RS * C * cap * 2); acc(RS * C * cap * 4); acc(RS * C * 4);
     acc(RS * C * 8);
+    acc(RS * 4);                               // the MTE's launch order
     // union form of each road-species' C <= 3 matrices (the ROV forward
     // pass's form): the species models' patterns are nested - control c's
     // entries are a subset of the lowest-hazard control's - so a union
@@ -624,6 +627,7 @@ to_status to_scene_create(to_ctx ctx, const to_scene* sc, to_gen* out) {
     g->csc.cap = (int)cap;
     g->csc.cap_smem = 0;
     g->d_iar = carve<double>(p, RS * C);
+    g->d_mte_order = carve<int>(p, RS);
     g->csc.uent = nullptr; g->csc.uptr = nullptr; g->csc.unnz = nullptr;
     g->csc.ucap = 0; g->csc.ucap_smem = 0;
     if (C <= 3) {

@@ -96,11 +96,18 @@ __device__ __forceinline__ float grouped4(float a, float b, float c, float d) {
 }
 
 // ---------------------------------------------------------------------------
-// MTE (mteKernel :595-717) - grid (ceil(P/32), RS).  Warp w owns groups
-// w, w+W, ... (at most MAXG); the next year's populations wait in registers
-// until every warp has read this year's, so one shared buffer suffices.
+// MTE (mteKernel :595-717) - grid (ceil(P/PW), RS), the (road, species) of
+// grid row y taken from a.order when it is set (widest first, k_mte_order).
+// A warp's groups of four destinations are dealt in snake order over the
+// groups sorted by entries (warp w takes ranks w, 2W-1-w, 2W+w), at most
+// MAXG a warp; the next year's populations wait in registers until every
+// warp has read this year's, so one shared buffer suffices.  The growth
+// mean's draws are made kGmChunk years at a time by the whole CTA, and
+// every warp carries its lanes' growth means itself.  The values do not
+// depend on which warp computes a group.
 // ---------------------------------------------------------------------------
 constexpr int kMaxG = 4;
+constexpr int kGmChunk = 16;
 
 template <int MAXG, int PPL>
 __global__ void __launch_bounds__(1024, 1)
@@ -110,7 +117,7 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     constexpr int PW = kLanes * PPL;                           // paths per CTA
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int NE = a.npe, NG = NE >> 2, NP = a.npad;
-    const int rs = a.rs0 + blockIdx.y;
+    const int rs = a.rs0 + (a.order ? a.order[blockIdx.y] : (int)blockIdx.y);
     const int road = rs / a.S, sp = rs - road * a.S;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int mtx = rs * a.C + a.c_use;
@@ -125,10 +132,10 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
     int2* cent = reinterpret_cast<int2*>(sm_raw);              // [cap_smem] (row byte offset, value)
     float* cur = reinterpret_cast<float*>(cent + csc.cap_smem);// [NE][PW]
     float* part = cur + (size_t)NE * PW;                       // [NG][PW]
-    float* capv = part + (size_t)NG * PW;                      // [NE]
-    float* gm = capv + NE;                                     // [PW]
-    float* xs = gm + PW;                                       // [3][PW] year's draws
-    int* cptr = reinterpret_cast<int*>(xs + 3 * PW);           // [NE+1]
+    float2* capr = reinterpret_cast<float2*>(part + (size_t)NG * PW);  // [NE] capacity, 1/capacity
+    float* xs = reinterpret_cast<float*>(capr + NE);           // [kGmChunk][3][PW] draws
+    int* cptr = reinterpret_cast<int*>(xs + kGmChunk * 3 * PW);// [NE+1]
+    int* order = cptr + NE + 1;                                // [NG] groups, widest first
 
     const int N = a.n_patches[rs];
     const int N4 = (N + 3) & ~3;
@@ -149,8 +156,10 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
         int k = q / PW;
         cur[q] = (k < N) ? ip[k] : 0.0f;
     }
-    for (int k = threadIdx.x; k < NE; k += blockDim.x)
-        capv[k] = a.caps[(size_t)rs * NP + k];
+    for (int k = threadIdx.x; k < NE; k += blockDim.x) {
+        const float cp = a.caps[(size_t)rs * NP + k];
+        capr[k] = make_float2(cp, 1.0f / cp);
+    }
     for (int k = threadIdx.x; k <= NE; k += blockDim.x)
         cptr[k] = csc.ptr[(size_t)mtx * (NP + 1) + (k <= NP ? k : NP)];
     for (int e = threadIdx.x; e < nnz; e += blockDim.x) {
@@ -158,49 +167,65 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
         cent[e] = make_int2(l * PW * (int)sizeof(float),
                             __float_as_int(csc.val[(size_t)mtx * csc.cap + e]));
     }
-    for (int i = threadIdx.x; i < PW; i += blockDim.x) gm[i] = p0;
     __syncthreads();
+    for (int gq = threadIdx.x; gq < NGr; gq += blockDim.x) {
+        const int w = cptr[4 * gq + 4] - cptr[4 * gq];
+        int rank = 0;
+        for (int u = 0; u < NGr; ++u) {
+            const int wu = cptr[4 * u + 4] - cptr[4 * u];
+            rank += (wu > w) || (wu == w && u < gq);
+        }
+        order[rank] = gq;
+    }
+    float g[PPL];
+#pragma unroll
+    for (int i = 0; i < PPL; ++i) g[i] = p0;
 
     for (int t = 0; t < a.n_years; ++t) {
-        // the growth mean's three draws per path, one thread each: jump
-        // indicator, Brownian term, jump factor minus one
-        for (int q = threadIdx.x; q < 3 * PW; q += blockDim.x) {
-            const int which = q / PW, i = q - which * PW;
-            const uint32_t path = (uint32_t)(blockIdx.x * PW + i);
-            float v;
-            if (which == 0) {
-                v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road_id, path, t, sp) < p6) ? 1.0f : 0.0f;
-            } else if (which == 1) {
-                v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road_id, path, t, sp) * p2;
-            } else {
-                const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road_id, path, t, sp);
-                const float jsz = (a.sem == 0) ? (zj * sj2 - sj2 / 2.0f) : (zj * p5 - sj2 / 2.0f);
-                v = to_expf(jsz) - 1.0f;
+        if (t % kGmChunk == 0) {
+            // the next years' growth-mean draws, one thread each: jump
+            // indicator, Brownian term, jump factor minus one
+            const int nc = min(kGmChunk, a.n_years - t);
+            for (int q = threadIdx.x; q < nc * 3 * PW; q += blockDim.x) {
+                const int yy = q / (3 * PW), r = q - yy * 3 * PW;
+                const int which = r / PW, i = r - which * PW;
+                const uint32_t path = (uint32_t)(blockIdx.x * PW + i);
+                const int ty = t + yy;
+                float v;
+                if (which == 0) {
+                    v = (to_uniform1(a.seed, TO_STREAM_SP_JUMP, road_id, path, ty, sp) < p6) ? 1.0f
+                                                                                              : 0.0f;
+                } else if (which == 1) {
+                    v = to_normal1(a.seed, TO_STREAM_SP_BROWNIAN, road_id, path, ty, sp) * p2;
+                } else {
+                    const float zj = to_normal1(a.seed, TO_STREAM_SP_JUMPSIZE, road_id, path, ty, sp);
+                    const float jsz = (a.sem == 0) ? (zj * sj2 - sj2 / 2.0f) : (zj * p5 - sj2 / 2.0f);
+                    v = to_expf(jsz) - 1.0f;
+                }
+                xs[q] = v;
             }
-            xs[q] = v;
+            __syncthreads();
         }
-        __syncthreads();
-        for (int i = threadIdx.x; i < PW; i += blockDim.x) {
-            const float jump = xs[i], brown = xs[PW + i], em1 = xs[2 * PW + i];
-            const float g = gm[i];
-            gm[i] = g + p4 * (p1 - g) * a.dt + g * brown + em1 * g * jump;
-        }
-        __syncthreads();
-        float g[PPL];
+        const float* xt = xs + (t % kGmChunk) * 3 * PW;
 #pragma unroll
-        for (int i = 0; i < PPL; ++i) g[i] = gm[lane + kLanes * i];
+        for (int i = 0; i < PPL; ++i) {
+            const int pi = lane + kLanes * i;
+            const float jump = xt[pi], brown = xt[PW + pi], em1 = xt[2 * PW + pi];
+            g[i] = g[i] + p4 * (p1 - g[i]) * a.dt + g[i] * brown + em1 * g[i] * jump;
+        }
         const bool last = (t == a.n_years - 1);
         float nv[MAXG][4][PPL];
 #pragma unroll
         for (int gi = 0; gi < MAXG; ++gi) {
-            const int grp = warp + gi * W;
-            if (grp < NGr) {
+            const int slot = gi * W + ((gi & 1) ? W - 1 - warp : warp);
+            if (slot < NGr) {
+                const int grp = order[slot];
                 float z[PPL][4];
 #pragma unroll
                 for (int i = 0; i < PPL; ++i)
                     to_normal4(a.seed, TO_STREAM_GROWTH, road_id, (uint32_t)(path0 + kLanes * i), t,
                                (uint32_t)((sp * N4) >> 2) + grp, z[i]);
-                float m4[4][PPL];
+                float msum[PPL];            // grouped4 of the migrated values, in order
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int k = grp * 4 + j;
@@ -216,26 +241,27 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 #pragma unroll
                         for (int i = 0; i < PPL; ++i) acc[i] = fmaf(row[kLanes * i], v, acc[i]);
                     }
-                    const float c = capv[k];
+                    const float2 cr = capr[k];
 #pragma unroll
                     for (int i = 0; i < PPL; ++i) {
-                        m4[j][i] = acc[i];
+                        msum[i] = (j == 0) ? acc[i] : msum[i] + acc[i];
                         float gr = fmaf(p7 * z[i][j], g[i], g[i]);
-                        nv[gi][j][i] = acc[i] * (1.0f + gr * (c - acc[i]) / c);
+                        // the division as to_div_rcp: the same bits
+                        nv[gi][j][i] = acc[i] * (1.0f + to_div_rcp(gr * (cr.x - acc[i]), cr.x, cr.y));
                     }
                 }
                 if (last)
 #pragma unroll
                     for (int i = 0; i < PPL; ++i)
-                        part[grp * PW + lane + kLanes * i] =
-                            grouped4(m4[0][i], m4[1][i], m4[2][i], m4[3][i]);
+                        part[grp * PW + lane + kLanes * i] = msum[i];
             }
         }
         __syncthreads();
 #pragma unroll
         for (int gi = 0; gi < MAXG; ++gi) {
-            const int grp = warp + gi * W;
-            if (grp < NGr) {
+            const int slot = gi * W + ((gi & 1) ? W - 1 - warp : warp);
+            if (slot < NGr) {
+                const int grp = order[slot];
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -243,8 +269,8 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
                         cur[(grp * 4 + j) * PW + lane + kLanes * i] = nv[gi][j][i];
             }
         }
+        __syncthreads();
     }
-    __syncthreads();
     for (int i = threadIdx.x; i < PW; i += blockDim.x) {
         const int path = blockIdx.x * PW + i;
         if (path >= a.n_paths) continue;
@@ -258,6 +284,22 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
             }
         }
         a.end_pops[(size_t)rs * a.n_paths + path] = e;
+    }
+}
+
+// The launch order of the MTE's (road, species): by descending packed
+// entries of the used control (ties by index), so the widest models start
+// first and the last wave holds the narrow ones.  One CTA.
+__global__ void __launch_bounds__(1024) k_mte_order(int n_rs, int rs0, int C, int c_use,
+                                                    const int* __restrict__ nnz, int* order) {
+    for (int i = threadIdx.x; i < n_rs; i += blockDim.x) {
+        const int w = nnz[(size_t)(rs0 + i) * C + c_use];
+        int rank = 0;
+        for (int j = 0; j < n_rs; ++j) {
+            const int wj = nnz[(size_t)(rs0 + j) * C + c_use];
+            rank += (wj > w) || (wj == w && j < i);
+        }
+        order[rank] = i;
     }
 }
 
@@ -371,8 +413,6 @@ k_union_csc(int NP, int C, const int* __restrict__ n_patches, to_csc csc) {
 // The values equal k_rov_forward_sparse's bit for bit: every group's
 // arithmetic and every sum's order is unchanged, only who computes it.
 // ---------------------------------------------------------------------------
-constexpr int kGmChunk = 16;
-
 __global__ void __launch_bounds__(1024, 1)
 k_rov_forward_union(to_rov_args a, to_csc csc) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
@@ -902,8 +942,8 @@ size_t mte_sparse_smem_ppl(int NE, int cap_smem, int ppl) {
     const int maxg = ppl == 1 ? kMaxG : 3;      // 32 warps of maxg groups of four
     if (NE > 32 * maxg * 4) return ~size_t(0);
     const int NG = NE / 4, PW = kLanes * ppl;
-    return (size_t)cap_smem * 8 + (size_t)(NE * PW + NG * PW + NE + 4 * PW) * 4 +
-           (size_t)(NE + 1) * 4 + 16;
+    return (size_t)cap_smem * 8 + (size_t)(NE * PW + NG * PW + 2 * NE + kGmChunk * 3 * PW) * 4 +
+           (size_t)(NE + 1 + NG) * 4 + 16;
 }
 
 size_t mte_sparse_smem(int NE, int cap_smem) { return mte_sparse_smem_ppl(NE, cap_smem, 1); }
@@ -935,6 +975,11 @@ to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
         return to_set_error(ctx, TO_ERR_UNSUPPORTED, "patches %d", NE);
     const int PW = kLanes * ppl;
     dim3 grid((a.n_paths + PW - 1) / PW, n_rs);
+    if (a.order_buf && n_rs > 1) {
+        k_mte_order<<<1, 1024, 0, ctx->stream>>>(n_rs, a.rs0, a.C, a.c_use, csc.nnz, a.order_buf);
+        TO_LAUNCHED(ctx);
+        a.order = a.order_buf;
+    }
     to_prof_begin(ctx, "mte_sparse");
     if (ppl == 2) {
         // 32 warps of at most three groups (NE <= 384): a shorter chain of

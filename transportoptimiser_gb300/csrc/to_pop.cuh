@@ -19,6 +19,9 @@ struct to_mte_args {
     const float* params;         // [S][8]
     float* end_pops;             // [RS][P]
     int* flags;                  // device error word (plan checks), may be null
+    const int* order;            // [n_rs] launch order of the (road, species), or null
+    int* order_buf;              // scratch for it ([n_rs] ints), or null: the
+                                 // sparse launcher then orders widest first
     int fault_wait;              // test hook (to_ctx_inject_fault): the tensor-core
                                  // kernel's first wait, on a barrier nothing arrives
                                  // at, runs out at once
