@@ -233,6 +233,7 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
 #pragma unroll
                     for (int i = 0; i < PPL; ++i) acc[i] = 0.0f;
                     const int e1 = cptr[k + 1];
+#pragma unroll 2
                     for (int e = cptr[k]; e < e1; ++e) {
                         const int2 ce = cent[e];
                         const float* row = reinterpret_cast<const float*>(
@@ -550,7 +551,7 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
                     const int k = grp * 4 + j;
                     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
                     const int e1 = uptr[k + 1];
-#pragma unroll 2
+#pragma unroll 4
                     for (int e = uptr[k]; e < e1; ++e) {
                         const int4 en = ue[e];
                         const float x = *reinterpret_cast<const float*>(curb + en.x);
