@@ -81,10 +81,11 @@ void or_knn(const float* ref, int n, const float* query, int Q, int dim, int k,
 /* ------------------------------------------------------------------------ */
 /* multiLocLinReg at one query (SimulateGPU.cu:2942-3052).                   */
 /* xraw(i, j): x of neighbour i in dimension j as the kernel reads it.       */
-/* lanes = 1: neighbours summed in order (surrogate builders).  lanes = 32:  */
-/* neighbour kk goes to partial sum kk % 32, and the 32 partial sums are     */
-/* added in lane order, ((s0 + s1) + s2) + ... + s31, as the device's        */
-/* shared-memory reduction adds them.                                       */
+/* lanes = 1: neighbours summed in distance order (surrogate builders).     */
+/* lanes = 32: the k nearest in ascending point index, neighbour m of that  */
+/* order to partial sum m % 32, and the 32 partial sums added in lane      */
+/* order, ((s0 + s1) + s2) + ... + s31, as the device gathers and reduces  */
+/* them.                                                                   */
 /* ------------------------------------------------------------------------ */
 static float local_linear(int dim, int k, int Q, int qi, const float* dist,
                           const int* ind, const float* y, const float* xbuf,
@@ -94,14 +95,26 @@ static float local_linear(int dim, int k, int Q, int qi, const float* dist,
     const int na = (dim + 1) + (dim + 1) * (dim + 1);
     for (int l = 0; l < lanes; ++l) to_lsm_acc_init(dim, acc[l]);
     float h = dist[(size_t)(k - 1) * Q + qi];
-    for (int kk = 0; kk < k; ++kk) {
+    /* the order of the sum: lanes = 1 by distance, lanes = 32 by ascending
+     * point index */
+    int* ord = (int*)malloc(sizeof(int) * (size_t)k);
+    for (int m = 0; m < k; ++m) {
+        int v = m, j = m;
+        const int key = ind[(size_t)m * Q + qi];
+        if (lanes > 1)
+            for (; j > 0 && ind[(size_t)ord[j - 1] * Q + qi] > key; --j) ord[j] = ord[j - 1];
+        ord[j] = v;
+    }
+    for (int m = 0; m < k; ++m) {
+        const int kk = ord[m];
         float d = dist[(size_t)kk * Q + qi];
         int i = ind[(size_t)kk * Q + qi] - 1;
         float xv[TO_LSM_MAXD];
         for (int j = 0; j < dim; ++j)
             xv[j] = pointmajor ? xbuf[(size_t)i * dim + j] : xbuf[(size_t)j * n + i];
-        to_lsm_acc_add(dim, acc[kk % lanes], to_lsm_weight(d, h), y[i], xv, xq);
+        to_lsm_acc_add(dim, acc[m % lanes], to_lsm_weight(d, h), y[i], xv, xq);
     }
+    free(ord);
     for (int e = 0; e < na; ++e) {
         float s = acc[0][e];
         for (int l = 1; l < lanes; ++l) s = s + acc[l][e];

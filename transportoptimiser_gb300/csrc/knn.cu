@@ -9,10 +9,11 @@
 // squared-distance threshold T by ballot compaction; T adapts until between
 // k and the store size qualify, then the survivors are narrowed to the power
 // of two above k and bitonic-sorted by (squared distance, index): exactly
-// the set and order the reference's stable insertion sort returns.  Small
-// point sets are handled whole (all keys sorted, or the threshold searched
-// on keys held in registers).  When exact ties keep the count out of the
-// window, a 4 x 8-bit radix select on the same keys takes over.
+// the set the reference's stable insertion sort returns.  Groups of at most
+// 384 points keep every key in registers and search a threshold with
+// exactly k keys at or below it (ties at the k-th place broken by index),
+// with no sort.  When exact ties keep the count out of the window, a
+// 4 x 8-bit radix select on the same keys takes over.
 //
 // For the ROV the points of each control are first binned into a uniform
 // cell grid (k_knn_grid, a counting sort), so a threshold pass visits only
@@ -20,9 +21,10 @@
 // are contiguous in the sorted order - instead of all n points.  The ranges
 // are widened by a small tolerance, so no point with key <= T is missed.
 // The local linear regression runs in the same warp right after the
-// selection: lane l accumulates neighbours l, l+32, ... and the partial
-// normal equations are summed by an xor butterfly (the oracle does the same).
-// Nothing of size P x Q is written.
+// selection, over the k nearest in ascending point index: lane l
+// accumulates neighbours l, l+32, ... of that order, and each normal-
+// equation sum adds the 32 lane partials in lane order (the oracle does the
+// same).  Nothing of size P x Q is written.
 #include "to_internal.cuh"
 #include "to_lsm_math.h"
 #include "to_rov.cuh"
@@ -603,49 +605,108 @@ constexpr float kSeedGrow = 1.4f;
 // the register search re-counts cheaply: a tighter first threshold (about
 // 1.44 k keys qualify in four dimensions against 1.96 k)
 constexpr float kSeedGrowReg = 1.2f;
-// groups of at most this many points skip the threshold search
-constexpr int kBrute = 128;
 // groups of at most this many points keep every key in registers (12 per
 // lane) and search the threshold on them, without the cell grid
 constexpr int kRegKeys = 12;
 constexpr int kReg = 32 * kRegKeys;
 
-// Threshold selection on keys held in registers (lane l holds points l,
-// l+32, ...): T moves until between k and cap keys qualify, then they are
-// compacted into ws.sel and sorted by (key, index).  Every key <= T is
-// kept, so the k nearest come out exact.  False when ties keep the count
-// out of the window.
-__device__ bool reg_select(const float (&key)[kRegKeys], int k, int dim, float T,
-                          WarpScratch& ws) {
+// One step of the exact search for a threshold with exactly k keys at or
+// below it: interpolate (count ~ T^(dim/2)); where that leaves the bracket,
+// halve the bracket's bit patterns (keys are >= 0, so their bits order as
+// the values).  False when the bracket holds no float strictly inside it:
+// equal keys then straddle the k-th place.
+__device__ __forceinline__ bool exact_step(int cnt, int k, float expo, float& T, float& lo,
+                                           float& hi) {
+    if (cnt < k) lo = T; else hi = T;
+    float nt = (cnt == 0) ? ((T > 0.0f) ? T * 16.0f : 1e-30f)
+                          : T * __powf((float)k / (float)cnt, expo);
+    const bool has_lo = lo >= 0.0f, has_hi = hi >= 0.0f;
+    if ((has_lo && !(nt > lo)) || (has_hi && !(nt < hi)) || !(nt < INFINITY)) {
+        if (has_lo && has_hi) {
+            const unsigned ul = __float_as_uint(lo), uh = __float_as_uint(hi);
+            if (uh - ul < 2u) return false;
+            nt = __uint_as_float(ul + (uh - ul) / 2u);
+        } else if (!has_hi) {
+            nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
+        } else {
+            nt = T * 0.25f;
+        }
+    }
+    T = nt;
+    return true;
+}
+
+// The k nearest of keys held in registers (lane l holds points l, l+32,
+// ...): the threshold moves until exactly k keys are at or below it; where
+// equal keys straddle the k-th place, every key below the tied value is
+// taken and then the lowest-index keys at it - the k smallest by (key,
+// index).  The k points go to ws.sel in ascending point index (the order
+// the regression sums them in).  Returns the k-th smallest key, or -1 when
+// the threshold leaves the finite range (the caller falls back).
+__device__ float reg_select_exact(const float (&key)[kRegKeys], int k, int dim, float T,
+                                  WarpScratch& ws) {
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    int cap = 32;
-    while (cap < k) cap <<= 1;
     const float expo = 2.0f / (float)dim;
-    const float target = 0.5f * (float)(k + cap);
     float lo = -1.0f, hi = -1.0f;
-    int cnt = -1;
-    for (int iter = 0; iter < 64; ++iter) {
-        if (!(T < INFINITY) || !(T >= 0.0f)) return false;
+    bool tie = false;
+    for (int iter = 0;; ++iter) {
+        if (iter == 200 || !(T < INFINITY) || !(T >= 0.0f)) return -1.0f;
         unsigned mine = 0;
 #pragma unroll
         for (int u = 0; u < kRegKeys; ++u) mine += (key[u] <= T) ? 1u : 0u;
-        cnt = (int)__reduce_add_sync(kFull, mine);
-        if (cnt >= k && cnt <= cap) break;
-        if (!next_threshold(cnt, k, target, expo, T, lo, hi)) return false;
+        const int cnt = (int)__reduce_add_sync(kFull, mine);
+        if (cnt == k) break;
+        if (!exact_step(cnt, k, expo, T, lo, hi)) { tie = true; break; }
     }
-    if (cnt < k || cnt > cap) return false;
-    int pos = 0;
+    // tie: lo and hi are adjacent floats, fewer than k keys <= lo and more
+    // than k <= hi, so the keys in between all equal hi
+    int need = 0;
+    if (tie) {
+        unsigned below = 0;
+#pragma unroll
+        for (int u = 0; u < kRegKeys; ++u) below += (key[u] < hi) ? 1u : 0u;
+        need = k - (int)__reduce_add_sync(kFull, below);
+    }
+    int pos = 0, eqs = 0;
+    unsigned top = 0;
 #pragma unroll
     for (int u = 0; u < kRegKeys; ++u) {
-        const bool le = key[u] <= T;
-        const unsigned m = __ballot_sync(kFull, le);
-        if (le) ws.sel[pos + __popc(m & lt_mask)] = pack_sel(key[u], lane + 32 * u);
+        bool take;
+        if (!tie) {
+            take = key[u] <= T;
+        } else {
+            const bool eq = key[u] == hi;
+            const unsigned me = __ballot_sync(kFull, eq);
+            take = key[u] < hi || (eq && eqs + __popc(me & lt_mask) < need);
+            eqs += __popc(me);
+        }
+        const unsigned m = __ballot_sync(kFull, take);
+        if (take) {
+            ws.sel[pos + __popc(m & lt_mask)] = pack_sel(key[u], lane + 32 * u);
+            top = max(top, __float_as_uint(key[u]));
+        }
         pos += __popc(m);
     }
     __syncwarp();
-    warp_sort_sel(ws, cnt);
-    return true;
+    return __uint_as_float(__reduce_max_sync(kFull, top));
+}
+
+// ws.sel[0..k) from (key, index) order into ascending index order: the
+// words swapped, one sort, swapped back
+__device__ __noinline__ void to_index_order(WarpScratch& ws, int k) {
+    const int lane = threadIdx.x & 31;
+    for (int i = lane; i < k; i += 32) {
+        const unsigned long long v = ws.sel[i];
+        ws.sel[i] = (v << 32) | (v >> 32);
+    }
+    __syncwarp();
+    warp_sort_sel(ws, k);
+    for (int i = lane; i < k; i += 32) {
+        const unsigned long long v = ws.sel[i];
+        ws.sel[i] = (v << 32) | (v >> 32);
+    }
+    __syncwarp();
 }
 
 template <int D>
@@ -691,33 +752,37 @@ k_knn_rov(to_rov_args a, int t) {
         float T = kp > 0.0f ? kp * kSeedGrow : T0;
         float qn[D], xq[D];
         to_rov_query<D>(a, c / a.C, qi, qn, xq);
-        bool ok = false;
-        if (n <= kBrute) {
-            // few points (small batches of paths): every point's key, one
-            // sort by (key, index) - the same k nearest in the same order
-            for (int i = lane; i < kBrute; i += 32)
-                ws.sel[i] = (i < n) ? pack_sel(sqdist(xs, P, i, D, qn), i) : ~0ull;
-            __syncwarp();
-            warp_sort_sel(ws, n);
-            ok = true;
-        } else if (n <= kReg) {
+        // the k nearest into ws.sel in ascending point index; kth = the k-th
+        // smallest distance (squared)
+        float kth = -1.0f;
+        if (n <= kReg) {
             float key[kRegKeys];
 #pragma unroll
             for (int u = 0; u < kRegKeys; ++u) {
                 const int i = lane + 32 * u;
                 key[u] = (i < n) ? sqdist(xs, P, i, D, qn) : INFINITY;
             }
-            ok = reg_select(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
-        } else if (g.ok) {
-            GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
-                           a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
-            ok = threshold_select(k, D, T, ws, gp);
+            kth = reg_select_exact(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
         } else {
-            ScanPass sp{xs, P, n, D, qn, &ws};
-            ok = threshold_select(k, D, T, ws, sp);
+            bool ok;
+            if (g.ok) {
+                GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
+                               a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
+                ok = threshold_select(k, D, T, ws, gp);
+            } else {
+                ScanPass sp{xs, P, n, D, qn, &ws};
+                ok = threshold_select(k, D, T, ws, sp);
+            }
+            if (ok) {
+                kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+                to_index_order(ws, k);
+            }
         }
-        if (!ok) warp_select(xs, P, n, D, qn, k, ws);
-        const float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+        if (kth < 0.0f) {                         // exact radix selection
+            warp_select(xs, P, n, D, qn, k, ws);
+            kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+            to_index_order(ws, k);
+        }
         if (lane == 0) kth_prev[qi] = kth;
         // lane-strided local linear regression
         float acc[NA];

@@ -409,45 +409,60 @@ __global__ void __launch_bounds__(kLsmChunk) k_lsm_scatter(to_rov_args a, int t)
     }
 }
 
-// one thread per road: group totals, the reference's min/max rules, the
-// road's combined range, k and the regression grid axes
-__global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+// a warp per road, lanes over its (control, dimension, bin) items: group
+// totals, the reference's min/max rules, the road's combined range, k and
+// the regression grid axes
+constexpr int kStatsWarps = 4;
+
+__global__ void __launch_bounds__(kStatsWarps * 32) k_lsm_stats(to_rov_args a, int t, int nb) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int r = blockIdx.x * kStatsWarps + w;
     if (r >= a.nr) return;
+    __shared__ int s_cnt[kStatsWarps][TO_ROV_MAXC];
+    __shared__ float s_mn[kStatsWarps][TO_ROV_MAXC + 1][TO_LSM_MAXD];
+    __shared__ float s_mx[kStatsWarps][TO_ROV_MAXC + 1][TO_LSM_MAXD];
     const int P = a.P, S = a.S, C = a.C, d = S + 1, R = a.R;
     const int bfirst = (int)(((size_t)r * P) / kLsmChunk);
     const int blast = (int)(((size_t)r * P + P - 1) / kLsmChunk);
-    int cnt[TO_ROV_MAXC];
-    float mn[TO_ROV_MAXC + 1][TO_LSM_MAXD], mx[TO_ROV_MAXC + 1][TO_LSM_MAXD];
-    for (int c = 0; c < C; ++c) {
+    int* cnt = s_cnt[w];
+    float (*mn)[TO_LSM_MAXD] = s_mn[w];
+    float (*mx)[TO_LSM_MAXD] = s_mx[w];
+    for (int c = lane; c < C; c += 32) {
         const size_t g = (size_t)r * C + c;
         int n = 0;
         for (int b = bfirst; b <= blast; ++b) n += a.lcnt[g * nb + b];
         cnt[c] = n;
     }
-    for (int c = 0; c < C; ++c) {
+    __syncwarp();
+    // each control's own ranges (control 0, and any with more than d + 1
+    // points), then the others take control 0's
+    for (int q = lane; q < C * d; q += 32) {
+        const int c = q / d, j = q - c * d;
         const size_t g = (size_t)r * C + c;
-        const bool own = (c == 0) || (cnt[c] > d + 1);
-        for (int j = 0; j < d; ++j) {
-            if (own && cnt[c] > 0) {
-                float lo = lsm_unkey(a.lkey[2 * (g * d + j)]);
-                float hi = lsm_unkey(a.lkey[2 * (g * d + j) + 1]);
-                // the reference scans from the first point with
-                // "if (xmin > x) ... else if (xmax < x)": plain min and
-                // max, except that a first value of -0/+0 keeps its sign
-                // when it is the extreme
-                const float first = a.xraw[(g * d + j) * P];
-                if (lo == first) lo = first;
-                if (hi == first) hi = first;
-                mn[c][j] = lo; mx[c][j] = hi;
-            } else if (own) {
-                mn[c][j] = 0.0f; mx[c][j] = 0.0f;
-            } else {
-                mn[c][j] = mn[0][j]; mx[c][j] = mx[0][j];
-            }
+        if (!((c == 0) || (cnt[c] > d + 1))) continue;
+        if (cnt[c] > 0) {
+            float lo = lsm_unkey(a.lkey[2 * (g * d + j)]);
+            float hi = lsm_unkey(a.lkey[2 * (g * d + j) + 1]);
+            // the reference scans from the first point with
+            // "if (xmin > x) ... else if (xmax < x)": plain min and max,
+            // except that a first value of -0/+0 keeps its sign when it is
+            // the extreme
+            const float first = a.xraw[(g * d + j) * P];
+            if (lo == first) lo = first;
+            if (hi == first) hi = first;
+            mn[c][j] = lo; mx[c][j] = hi;
+        } else {
+            mn[c][j] = 0.0f; mx[c][j] = 0.0f;
         }
     }
-    for (int j = 0; j < d; ++j) {
+    __syncwarp();
+    for (int q = lane; q < C * d; q += 32) {
+        const int c = q / d, j = q - c * d;
+        if ((c == 0) || (cnt[c] > d + 1)) continue;
+        mn[c][j] = mn[0][j]; mx[c][j] = mx[0][j];
+    }
+    __syncwarp();
+    for (int j = lane; j < d; j += 32) {
         float lo = mn[0][j], hi = mx[0][j];
         for (int c = 1; c < C; ++c) {
             if (lo > mn[c][j]) lo = mn[c][j];
@@ -456,12 +471,16 @@ __global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
         mn[C][j] = lo; mx[C][j] = hi;
         a.gmin[(size_t)r * d + j] = lo;
         a.gmax[(size_t)r * d + j] = hi;
-        if (a.qax)
-            for (int di = 0; di < R; ++di)
-                a.qax[((size_t)r * d + j) * R + di] =
-                    to_lsm_normalise(to_lsm_query_axis(di, lo, hi, R), lo, hi, j == S, a.scaling);
     }
-    for (int c = 0; c < C; ++c) {
+    __syncwarp();
+    if (a.qax)
+        for (int q = lane; q < d * R; q += 32) {
+            const int j = q / R, di = q - j * R;
+            const float lo = mn[C][j], hi = mx[C][j];
+            a.qax[((size_t)r * d + j) * R + di] =
+                to_lsm_normalise(to_lsm_query_axis(di, lo, hi, R), lo, hi, j == S, a.scaling);
+        }
+    for (int c = lane; c < C; c += 32) {
         const size_t g = (size_t)r * C + c;
         const int n = cnt[c];
         int k = 0;
@@ -471,11 +490,12 @@ __global__ void k_lsm_stats(to_rov_args a, int t, int nb) {
         }
         a.npts[g] = n;
         a.kc[g] = k;
-        // axis values of the regression grid (createQueryPoints :1187-1190)
-        float* ax = to_rov_reg_block(a, t, g);
-        for (int j = 0; j < d; ++j)
-            for (int di = 0; di < R; ++di)
-                ax[(size_t)j * R + di] = to_lsm_query_axis(di, mn[C][j], mx[C][j], R);
+    }
+    // axis values of the regression grid (createQueryPoints :1187-1190)
+    for (int q = lane; q < C * d * R; q += 32) {
+        const int c = q / (d * R), jr = q - c * d * R, j = jr / R, di = jr - j * R;
+        float* ax = to_rov_reg_block(a, t, (size_t)r * C + c);
+        ax[(size_t)j * R + di] = to_lsm_query_axis(di, mn[C][j], mx[C][j], R);
     }
 }
 
@@ -780,7 +800,8 @@ to_status rov_backward(to_ctx ctx, const to_rov_args& a, int pblocks, int tpb,
         TO_LAUNCHED(ctx);
         k_lsm_scatter<<<a.lblocks, kLsmChunk, 0, ctx->stream>>>(a, t);
         TO_LAUNCHED(ctx);
-        k_lsm_stats<<<(a.nr + 127) / 128, 128, 0, ctx->stream>>>(a, t, a.lblocks);
+        k_lsm_stats<<<(a.nr + kStatsWarps - 1) / kStatsWarps, kStatsWarps * 32, 0, ctx->stream>>>(
+            a, t, a.lblocks);
         TO_LAUNCHED(ctx);
         k_lsm_norm<<<fblocks, 256, 0, ctx->stream>>>(a);
         TO_LAUNCHED(ctx);
