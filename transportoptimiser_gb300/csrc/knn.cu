@@ -602,9 +602,9 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 // k_knn_solve then solves one system per thread (FP64 square-root-free
 // Cholesky, to_lsm_math.h).
 constexpr float kSeedGrow = 1.4f;
-// the register search re-counts cheaply: a tighter first threshold (about
-// 1.44 k keys qualify in four dimensions against 1.96 k)
-constexpr float kSeedGrowReg = 1.2f;
+// the register search re-counts cheaply: it starts from last year's k-th
+// distance itself (about k keys qualify)
+constexpr float kSeedGrowReg = 1.0f;
 // groups of at most this many points keep every key in registers (12 per
 // lane) and search the threshold on them, without the cell grid
 constexpr int kRegKeys = 12;
