@@ -51,6 +51,11 @@ ROV_DIM_RES = 8
 ROV_SEED = 17
 SEM = 1
 REF_SECONDS = 90          # the reference arm's sample window
+# N* of the bench scene (synth.generation(0), 256 roads): the largest per-road
+# N* of the 2000-path MTE and 5000-path ROV pilots, as this arm's pilots
+# compute it on the GPU.  The reference arm values the same workload at these
+# path counts (its CPU cannot run the pilots of all 256 roads in its window).
+SCENE_N_STAR = (64, 768)
 YEARS = 50
 
 
@@ -255,7 +260,13 @@ def run_reference(args):
     b.build_oracle()
     scene = synth.generation(0, n_roads=args.roads)
     habs = [scene.hab_map(rd) for rd in scene.roads]       # rasterised outside the timing
-    P_mte, P_rov = reference_n_star(scene, habs, [0, 1], args.rov_dim_res)
+    if args.roads == N_ROADS:
+        P_mte, P_rov = SCENE_N_STAR
+        nstar = "N* of the GPU arm's pilots for this scene (SCENE_N_STAR)"
+    else:
+        P_mte, P_rov = reference_n_star(scene, habs, [0, 1], args.rov_dim_res)
+        nstar = ("N* from CPU pilots (MTE %d paths, ROV %d paths) on 2 roads"
+                 % (PILOT_PATHS, ROV_PILOT_PATHS // 4))
     for _ in range(args.warmup):
         oracle_road(scene, 0, scene.roads[0], habs[0], 64, 0, args.rov_dim_res)
     value, cores, n = oracle_generation(scene, habs, P_mte, P_rov, args.rov_dim_res,
@@ -268,10 +279,13 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "mte_paths": P_mte, "rov_paths": P_rov,
-                       "semantics": "corrected", "note": "the steps share one continuous "
-                       "sample; N* from CPU pilots (MTE %d paths, ROV %d paths) on 2 roads"
-                       % (PILOT_PATHS, ROV_PILOT_PATHS // 4)},
+            "config": {"workload": WORKLOAD, "roads": args.roads,
+                       "species": len(scene.species),
+                       "mte_paths_per_road": P_mte, "rov_paths_per_road": P_rov,
+                       "pilot_paths": {"mte": PILOT_PATHS, "rov": ROV_PILOT_PATHS},
+                       "years": YEARS, "rov_bins_per_dim": args.rov_dim_res,
+                       "semantics": "corrected",
+                       "note": "the steps share one continuous sample; " + nstar},
             "cpu_baseline": {"value": value, "unit": "designs/s", "cores": cores,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "designs/s", "h2d_bytes_per_step": 0,
@@ -714,6 +728,7 @@ def main():
                        "mte_paths_per_road": P, "rov_paths_per_road": P_rov,
                        "pilot_paths": {"mte": PILOT_PATHS, "rov": ROV_PILOT_PATHS},
                        "years": YEARS, "rov_bins_per_dim": R_dim, "semantics": "corrected",
+                       "n_star_as_reference_arm": (P, P_rov) == SCENE_N_STAR,
                        "patches_min_max": [int(Ns.min()), int(Ns.max())],
                        "graph": "whole generation (species models, MTE, ROV, results) "
                                 "captured once, replayed per step",
@@ -747,7 +762,7 @@ def main():
 
 
 # Per unit of work, from one ncu capture of this bench's own replayed step at
-# 64 roads (640 ROV paths a road, 192,000 forward units, 5,955,452 fitted
+# 64 roads (640 ROV paths a road, 192,000 forward units, 6,180,003 fitted
 # queries over the step's 48 kNN launches):
 #   ncu --metrics smsp__inst_executed.sum,dram__bytes_read.sum,
 #       dram__bytes_write.sum,gpu__time_duration.sum --clock-control none
@@ -760,10 +775,10 @@ def main():
 #   k_knn_rov: unit = one fitted regression query (k nearest points and the
 #              local normal equations)
 ROOF = {
-    "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": 53793.0,
-                           "bytes_per_unit": 288.0,
+    "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": 48086.0,
+                           "bytes_per_unit": 281.9,
                            "unit": "(32-path tile, species, year)"},
-    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 2426.6, "bytes_per_unit": 107.6,
+    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 1857.0, "bytes_per_unit": 22.8,
             "unit": "fitted regression query"},
 }
 SMS, SCHEDULERS = 152, 4
