@@ -7,13 +7,15 @@
 //
 // A warp handles one query at a time.  It gathers every point within a
 // squared-distance threshold T by ballot compaction; T adapts until between
-// k and the store size qualify, then the survivors are narrowed to the power
-// of two above k and bitonic-sorted by (squared distance, index): exactly
-// the set the reference's stable insertion sort returns.  Groups of at most
-// 384 points keep every key in registers and search a threshold with
-// exactly k keys at or below it (ties at the k-th place broken by index),
-// with no sort.  When exact ties keep the count out of the window, a
-// 4 x 8-bit radix select on the same keys takes over.
+// k and the store size qualify, then a threshold with exactly k of them at
+// or below it is searched among the stored keys (ties at the k-th place
+// broken by index): exactly the set the reference's stable insertion sort
+// returns.  The kNN entry point then sorts them by (squared distance,
+// index), as the reference returns them; the ROV sorts them by index.
+// Groups of at most 384 points keep every key in registers and search the
+// exact-k threshold on them, and their compaction already yields index
+// order, with no sort.  When the search fails (ties keep the count out of
+// the window), a 4 x 8-bit radix select on the same keys takes over.
 //
 // For the ROV the points of each control are first binned into a uniform
 // cell grid (k_knn_grid, a counting sort), so a threshold pass visits only
@@ -242,6 +244,32 @@ __device__ __forceinline__ bool next_threshold(int cnt, int k, float target, flo
     return true;
 }
 
+// One step of the exact search for a threshold with exactly k keys at or
+// below it: interpolate (count ~ T^(dim/2)); where that leaves the bracket,
+// halve the bracket's bit patterns (keys are >= 0, so their bits order as
+// the values).  False when the bracket holds no float strictly inside it:
+// equal keys then straddle the k-th place.
+__device__ __forceinline__ bool exact_step(int cnt, int k, float expo, float& T, float& lo,
+                                           float& hi) {
+    if (cnt < k) lo = T; else hi = T;
+    float nt = (cnt == 0) ? ((T > 0.0f) ? T * 16.0f : 1e-30f)
+                          : T * __powf((float)k / (float)cnt, expo);
+    const bool has_lo = lo >= 0.0f, has_hi = hi >= 0.0f;
+    if ((has_lo && !(nt > lo)) || (has_hi && !(nt < hi)) || !(nt < INFINITY)) {
+        if (has_lo && has_hi) {
+            const unsigned ul = __float_as_uint(lo), uh = __float_as_uint(hi);
+            if (uh - ul < 2u) return false;
+            nt = __uint_as_float(ul + (uh - ul) / 2u);
+        } else if (!has_hi) {
+            nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
+        } else {
+            nt = T * 0.25f;
+        }
+    }
+    T = nt;
+    return true;
+}
+
 __device__ __forceinline__ float sel_key(const WarpScratch& ws, int i) {
     // high word of the packed (key, index) entry
     return __uint_as_float(reinterpret_cast<const unsigned*>(ws.sel)[2 * i + 1]);
@@ -282,8 +310,64 @@ __device__ __noinline__ bool narrow_stored(WarpScratch& ws, int& cnt, float& T, 
     return true;
 }
 
+// The k nearest among the cnt stored candidates (all with key <= T): a
+// threshold with exactly k stored keys at or below it (exact_step), the
+// survivors moved to the front in stored order (in place: a write never
+// passes the read position); where equal keys straddle the k-th place,
+// every key below the tied value and then the tied ones of lowest index.
+// Returns the k-th smallest key, or -1 when the search fails.
+__device__ __noinline__ float narrow_exact(WarpScratch& ws, int cnt, float T, int k, float expo) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    float lo = -1.0f, hi = -1.0f;
+    bool tie = false;
+    int c2 = cnt;
+    for (int iter = 0; c2 != k; ++iter) {
+        if (iter == 200) return -1.0f;
+        if (!exact_step(c2, k, expo, T, lo, hi)) { tie = true; break; }
+        unsigned cl = 0;
+        for (int i = lane; i < cnt; i += 32) cl += (sel_key(ws, i) <= T) ? 1u : 0u;
+        c2 = (int)__reduce_add_sync(kFull, cl);
+    }
+    unsigned thr = 0xFFFFFFFFu;          // the largest index taken at the tied key
+    if (tie) {
+        unsigned below = 0;
+        for (int i = lane; i < cnt; i += 32) below += (sel_key(ws, i) < hi) ? 1u : 0u;
+        const int need = k - (int)__reduce_add_sync(kFull, below);
+        for (int r = 0; r < need; ++r) {
+            unsigned m = 0xFFFFFFFFu;
+            for (int i = lane; i < cnt; i += 32) {
+                const unsigned long long v = ws.sel[i];
+                const unsigned idx = (unsigned)v;
+                if (sel_key(ws, i) == hi && (r == 0 || idx > thr)) m = min(m, idx);
+            }
+            thr = __reduce_min_sync(kFull, m);
+        }
+    }
+    int pos0 = 0;
+    unsigned top = 0;
+    for (int base = 0; base < cnt; base += 32) {
+        const int i = base + lane;
+        const unsigned long long v = (i < cnt) ? ws.sel[i] : ~0ull;
+        const float kv = __uint_as_float((unsigned)(v >> 32));
+        const bool take = (i < cnt) && (tie ? (kv < hi || (kv == hi && (unsigned)v <= thr))
+                                             : kv <= T);
+        const unsigned m = __ballot_sync(kFull, take);
+        if (take) {
+            ws.sel[pos0 + __popc(m & lt_mask)] = v;
+            top = max(top, __float_as_uint(kv));
+        }
+        pos0 += __popc(m);
+    }
+    __syncwarp();
+    return __uint_as_float(__reduce_max_sync(kFull, top));
+}
+
+// Threshold passes until between k and kStore points qualify, then the
+// exact k nearest among them (narrow_exact, stored order).  Returns the
+// k-th smallest key, or -1 when the window or the search fails.
 template <class Pass>
-__device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass pass) {
+__device__ float threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass pass) {
     float lo = -1.0f, hi = -1.0f;        // bracket: count(lo) < k, count(hi) > window
     const float expo = 2.0f / (float)dim;
     const float target = sqrtf((float)k * (float)kStore);
@@ -295,20 +379,8 @@ __device__ bool threshold_select(int k, int dim, float& T, WarpScratch& ws, Pass
         if (!next_threshold(cnt, k, target, expo, T, lo, hi)) { cnt = -1; break; }
     }
     __syncwarp();
-    if (cnt < k || cnt > kStore) return false;
-    int cap = 32;
-    while (cap < k) cap <<= 1;
-    if (cnt > cap) {
-        float T2 = T;
-        if (!narrow_stored(ws, cnt, T2, k, cap, expo) && cnt > TO_KNN_KMAX &&
-            !narrow_stored(ws, cnt, T2, k, TO_KNN_KMAX, expo))
-            return false;
-    }
-    warp_sort_sel(ws, cnt);
-    // next query starts from a threshold a little above this k-th distance
-    float kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
-    T = (kth > 0.0f) ? kth * 1.3f : 1e-30f;
-    return true;
+    if (cnt < k || cnt > kStore) return -1.0f;
+    return narrow_exact(ws, cnt, T, k, expo);
 }
 
 // full scan over n points in index order (dim-major, given stride)
@@ -610,32 +682,6 @@ constexpr float kSeedGrowReg = 1.0f;
 constexpr int kRegKeys = 12;
 constexpr int kReg = 32 * kRegKeys;
 
-// One step of the exact search for a threshold with exactly k keys at or
-// below it: interpolate (count ~ T^(dim/2)); where that leaves the bracket,
-// halve the bracket's bit patterns (keys are >= 0, so their bits order as
-// the values).  False when the bracket holds no float strictly inside it:
-// equal keys then straddle the k-th place.
-__device__ __forceinline__ bool exact_step(int cnt, int k, float expo, float& T, float& lo,
-                                           float& hi) {
-    if (cnt < k) lo = T; else hi = T;
-    float nt = (cnt == 0) ? ((T > 0.0f) ? T * 16.0f : 1e-30f)
-                          : T * __powf((float)k / (float)cnt, expo);
-    const bool has_lo = lo >= 0.0f, has_hi = hi >= 0.0f;
-    if ((has_lo && !(nt > lo)) || (has_hi && !(nt < hi)) || !(nt < INFINITY)) {
-        if (has_lo && has_hi) {
-            const unsigned ul = __float_as_uint(lo), uh = __float_as_uint(hi);
-            if (uh - ul < 2u) return false;
-            nt = __uint_as_float(ul + (uh - ul) / 2u);
-        } else if (!has_hi) {
-            nt = (T > 0.0f) ? T * 4.0f : 1e-30f;
-        } else {
-            nt = T * 0.25f;
-        }
-    }
-    T = nt;
-    return true;
-}
-
 // The k nearest of keys held in registers (lane l holds points l, l+32,
 // ...): the threshold moves until exactly k keys are at or below it; where
 // equal keys straddle the k-th place, every key below the tied value is
@@ -764,19 +810,15 @@ k_knn_rov(to_rov_args a, int t) {
             }
             kth = reg_select_exact(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
         } else {
-            bool ok;
             if (g.ok) {
                 GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
                                a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
-                ok = threshold_select(k, D, T, ws, gp);
+                kth = threshold_select(k, D, T, ws, gp);
             } else {
                 ScanPass sp{xs, P, n, D, qn, &ws};
-                ok = threshold_select(k, D, T, ws, sp);
+                kth = threshold_select(k, D, T, ws, sp);
             }
-            if (ok) {
-                kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
-                to_index_order(ws, k);
-            }
+            if (kth >= 0.0f) to_index_order(ws, k);
         }
         if (kth < 0.0f) {                         // exact radix selection
             warp_select(xs, P, n, D, qn, k, ws);
@@ -899,7 +941,9 @@ k_knn_generic(const float* ref_g, int n, const float* query, int Q, int dim, int
     WarpScratch& ws = wsa[warp];
     float T = powf((float)k / (float)n, 2.0f / (float)dim);
     ScanPass sp{ref, n, n, dim, q, &ws};
-    if (!threshold_select(k, dim, T, ws, sp)) warp_select(ref, n, n, dim, q, k, ws);
+    // the k nearest, then sorted by (distance, index) as the reference returns them
+    if (threshold_select(k, dim, T, ws, sp) >= 0.0f) warp_sort_sel(ws, k);
+    else warp_select(ref, n, n, dim, q, k, ws);
     for (int kk = lane; kk < k; kk += 32) {
         unsigned long long v = ws.sel[kk];
         dist[(size_t)kk * Q + qi] = sqrtf(__uint_as_float((unsigned)(v >> 32)));
