@@ -12,7 +12,7 @@
 // broken by index): exactly the set the reference's stable insertion sort
 // returns.  The kNN entry point then sorts them by (squared distance,
 // index), as the reference returns them; the ROV sorts them by index.
-// Groups of at most 384 points keep every key in registers and search the
+// Groups of at most 320 points keep every key in registers and search the
 // exact-k threshold on them, and their compaction already yields index
 // order, with no sort.  When the search fails (ties keep the count out of
 // the window), a 4 x 8-bit radix select on the same keys takes over.
@@ -677,9 +677,11 @@ constexpr float kSeedGrow = 1.4f;
 // the register search re-counts cheaply: it starts from last year's k-th
 // distance itself (about k keys qualify)
 constexpr float kSeedGrowReg = 1.0f;
-// groups of at most this many points keep every key in registers (12 per
-// lane) and search the threshold on them, without the cell grid
-constexpr int kRegKeys = 12;
+// groups of at most this many points keep every key in registers (10 per
+// lane: the generation's groups hold about P/C = 256 points; fewer slots
+// send the larger groups to the cell grid, more cost every query the
+// empty slots) and search the threshold on them, without the cell grid
+constexpr int kRegKeys = 10;
 constexpr int kReg = 32 * kRegKeys;
 
 // The k nearest of keys held in registers (lane l holds points l, l+32,
