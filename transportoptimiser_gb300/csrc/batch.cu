@@ -730,7 +730,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     if (kmax > TO_KNN_KMAX) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d", kmax);
     const size_t PT = (size_t)NR * P, G = (size_t)NR * C;
     const size_t blk = (size_t)Rr * d + 2 * (size_t)Q;
-    const size_t nacc = (size_t)(d + 1) * (d + 2);
+    const size_t nacc = (size_t)(d + 1) * (d + 4) / 2;   // sums a query (doubles)
     const int lblocks = (int)((PT + 1023) / 1024);
     const size_t U1 = (size_t)(U > 0 ? U : 1);
     size_t bytes = 0;
@@ -743,7 +743,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     acc((size_t)NR * d * 4); acc((size_t)NR * d * 4); acc(G * d * P * 4); acc(G * P * 4);
     acc((size_t)NR * d * Rr * 4);
     acc(G * (TO_KNN_GCELLS + 1) * 4); acc(G * sizeof(to_knn_grid)); acc(G * Q * 4);
-    acc(G * lblocks * 4); acc(G * d * 2 * 4); acc(4); acc(G * Q * nacc * 4);
+    acc(G * lblocks * 4); acc(G * d * 2 * 4); acc(4); acc(G * Q * nacc * 8);
     acc(G * blk * 4);
     acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4);
     acc((size_t)Y * S * PT * 4);
@@ -795,7 +795,7 @@ to_status to_scene_set_rov(to_ctx ctx, to_gen g, const to_rov_problem* t) {
     a.lcnt = carve<int>(p, G * lblocks);
     a.lkey = carve<unsigned>(p, G * d * 2);
     a.knn_next = carve<int>(p, 1);
-    a.knn_acc = carve<float>(p, G * Q * nacc);
+    a.knn_acc = carve<double>(p, G * Q * nacc);
     a.reg = carve<float>(p, G * blk);
     a.condExp = carve<float>(p, (size_t)Y * PT);
     a.optCont = carve<int>(p, (size_t)Y * PT);

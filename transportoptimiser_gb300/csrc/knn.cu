@@ -852,7 +852,7 @@ k_knn_rov(to_rov_args a, int t) {
             to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
         }
         // the item's NS sums, at its list position
-        float* sa = a.knn_acc + (size_t)li * NS;
+        double* sa = a.knn_acc + (size_t)li * NS;
         // the normal-equation sums: every lane's partials into shared memory
         // (sum e in row e, lane in column, rows 33 wide), then lane e adds
         // row e's 32 partials in lane order
@@ -873,27 +873,27 @@ k_knn_rov(to_rov_args a, int t) {
             float x = red[lane * 33];
 #pragma unroll 8
             for (int l = 1; l < 32; ++l) x = x + red[lane * 33 + l];
-            sa[lane] = x;
+            sa[lane] = (double)x;                // exact; spares the solve a conversion
         }
         __syncwarp();
     }
 }
 
 // One regression system per thread over the year's list, 128 at a time: a
-// chunk's sums (NS a system, consecutive list positions) are copied to
-// shared memory word by word with consecutive threads on consecutive words
-// (rows padded to an odd stride), then each thread lays its own out as the
-// solver reads them and writes the intercept at grid query qi of group c
-// (0 where the group has too few points).
+// chunk's sums (NS doubles a system, consecutive list positions) are copied
+// to shared memory word by word with consecutive threads on consecutive
+// words (rows padded to an odd stride), then each thread solves its own and
+// writes the intercept at grid query qi of group c (0 where the group has
+// too few points).
 template <int D>
 __global__ void __launch_bounds__(128) k_knn_solve(to_rov_args a, int t) {
-    constexpr int M = D + 1, NS = knn_sums<D>(), NSP = NS | 1;
-    __shared__ float s[128 * NSP];
+    constexpr int NS = knn_sums<D>(), NSP = NS | 1;
+    __shared__ double s[128 * NSP];
     const int total = a.touched ? *a.qcount : a.G * a.Q;
     for (int base = blockIdx.x * 128; base < total; base += gridDim.x * 128) {
         const int cnt = min(128, total - base);
         __syncthreads();
-        const float* src = a.knn_acc + (size_t)base * NS;
+        const double* src = a.knn_acc + (size_t)base * NS;
         for (int q = threadIdx.x; q < cnt * NS; q += 128) {
             const int i = q / NS;
             s[i * NSP + (q - i * NS)] = src[q];
@@ -905,19 +905,7 @@ __global__ void __launch_bounds__(128) k_knn_solve(to_rov_args a, int t) {
         if (item >= a.G * a.Q) continue;
         const int c = item / a.Q, qi = item - c * a.Q;
         const int n = a.npts[c], k = a.kc[c];
-        float y = 0.0f;
-        if (n >= 3 && k > 0) {
-            float acc[knn_acc_len<D>()];
-            const float* si = s + threadIdx.x * NSP;
-            int e = 0;
-#pragma unroll
-            for (int i = 0; i < M; ++i) acc[i] = si[e++];
-#pragma unroll
-            for (int i = 0; i < M; ++i)
-#pragma unroll
-                for (int j = i; j < M; ++j) acc[M + i * M + j] = si[e++];
-            y = to_lsm_solve_intercept(D, acc);
-        }
+        const float y = (n >= 3 && k > 0) ? to_lsm_solve_compact(D, s + threadIdx.x * NSP) : 0.0f;
         (to_rov_reg_block(a, t, c) + (size_t)a.R * D)[qi] = y;
     }
 }

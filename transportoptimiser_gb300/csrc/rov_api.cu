@@ -136,7 +136,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     if (kmax > TO_KNN_KMAX) return to_set_error(ctx, TO_ERR_UNSUPPORTED, "k %d", kmax);
     const size_t blk = (size_t)R * d + 2 * (size_t)Q;
     const int lblocks = (PT + 1023) / 1024;
-    const size_t nacc = (size_t)(d + 1) * (d + 2);
+    const size_t nacc = (size_t)(d + 1) * (d + 4) / 2;   // sums a query (doubles)
     const int cap = NP * 64 < NP * NP ? NP * 64 : NP * NP;
     size_t bytes = 0;
     auto acc = [&](size_t b) { bytes += to_align256(b); };
@@ -152,7 +152,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     acc((size_t)G * (TO_KNN_GCELLS + 1) * 4); acc((size_t)G * sizeof(to_knn_grid));
     acc((size_t)G * Q * 4);
     acc((size_t)G * lblocks * 4); acc((size_t)G * d * 2 * 4);
-    acc(4); acc((size_t)G * Q * nacc * 4);
+    acc(4); acc((size_t)G * Q * nacc * 8);
     acc((size_t)Y * G * blk * 4); acc((size_t)Y * PT * 4); acc((size_t)Y * PT * 4);
     acc((size_t)Y * PT * 4); acc((size_t)Y * S * PT * 4); acc((size_t)NR * 5 * 8);
     acc((size_t)RS * C * (NP + 1) * 4); acc((size_t)RS * C * cap * 2); acc((size_t)RS * C * cap * 4);
@@ -212,7 +212,7 @@ to_status to_simulate_rov_batch(to_ctx ctx, int n_roads, const to_rov_problem* p
     a.lkey = to_arena_take<unsigned>(ctx, (size_t)G * d * 2);
     a.lblocks = lblocks;
     a.knn_next = to_arena_take<int>(ctx, 1);
-    a.knn_acc = to_arena_take<float>(ctx, (size_t)G * Q * nacc);
+    a.knn_acc = to_arena_take<double>(ctx, (size_t)G * Q * nacc);
     a.reg = to_arena_take<float>(ctx, (size_t)Y * G * blk);
     a.condExp = to_arena_take<float>(ctx, (size_t)Y * PT);
     a.optCont = to_arena_take<int>(ctx, (size_t)Y * PT);

@@ -91,8 +91,9 @@ TO_HD double to_rcp64(double x) {
  * (to_rcp64) scales its column.  A direction whose pivot falls below 1e-6
  * of its diagonal is dropped (its coefficient set to zero).  Returns the
  * intercept (the regression value at the query), 0 when its own direction
- * is dropped. */
-TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
+ * is dropped.  sums: the right-hand sides B (m values), then the upper
+ * triangle i <= j of the matrix A in row order. */
+TO_HD float to_lsm_solve_compact(int dim, const double* sums) {
     int m = dim + 1;
     double A[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];
     double L[(TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 1)];   /* L[i][j], i > j */
@@ -104,12 +105,12 @@ TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
     TO_UNROLL
     for (int i = 0; i < m; ++i) {
         const int oi = (i + 1) % m;
-        b[i] = (double)acc[oi];
+        b[i] = sums[oi];
         TO_UNROLL
         for (int j = 0; j <= i; ++j) {
             const int oj = (j + 1) % m;
             const int a = oi <= oj ? oi : oj, c = oi <= oj ? oj : oi;
-            A[i * m + j] = (double)acc[m + a * m + c];
+            A[i * m + j] = sums[m + a * m - a * (a - 1) / 2 + (c - a)];
         }
     }
     TO_UNROLL
@@ -141,6 +142,22 @@ TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
         y[i] = v;
     }
     return keep[m - 1] ? (float)(y[m - 1] * inv[m - 1]) : 0.0f;
+}
+
+/* The same from the accumulator layout acc = [B (m) | A (m x m)]: its
+ * sums in the compact order (B, then the upper triangle of A in row
+ * order), exactly as doubles. */
+TO_HD float to_lsm_solve_intercept(int dim, const float* acc) {
+    const int m = dim + 1;
+    double sums[(TO_LSM_MAXD + 1) + (TO_LSM_MAXD + 1) * (TO_LSM_MAXD + 2) / 2];
+    int e = 0;
+    TO_UNROLL
+    for (int i = 0; i < m; ++i) sums[e++] = (double)acc[i];
+    TO_UNROLL
+    for (int i = 0; i < m; ++i)
+        TO_UNROLL
+        for (int j = i; j < m; ++j) sums[e++] = (double)acc[m + i * m + j];
+    return to_lsm_solve_compact(dim, sums);
 }
 
 /* float -> int the way the reference's assignment truncates, with the GPU's

@@ -69,7 +69,7 @@ struct to_rov_args {
     float* popsY;                     // ALGO6: [Y][S][ne][P] patch populations, start of year
     float* gmY;                       // ALGO6: [Y][S][P] mean growth rate of the year
     int* knn_next;                    // work counter of the kNN kernel
-    float* knn_acc;                   // [G][Q][(d+1)(d+2)] normal equations per query
+    double* knn_acc;                  // [G*Q][(d+1)(d+4)/2] normal-equation sums per listed query
     int kmax;
     // touched-query mode (corrected semantics, ALGO4, surfaces not
     // returned): a year's regressions are fitted only at the grid queries
