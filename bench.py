@@ -776,9 +776,9 @@ def main():
 #              local normal equations)
 ROOF = {
     "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": 48086.0,
-                           "bytes_per_unit": 281.9,
+                           "bytes_per_unit": 283.0,
                            "unit": "(32-path tile, species, year)"},
-    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 1857.0, "bytes_per_unit": 22.8,
+    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 1670.5, "bytes_per_unit": 22.8,
             "unit": "fitted regression query"},
 }
 SMS, SCHEDULERS = 152, 4

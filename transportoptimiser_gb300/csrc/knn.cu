@@ -780,102 +780,109 @@ k_knn_rov(to_rov_args a, int t) {
     const int items = a.touched ? *a.qcount : a.G * Q;
     const bool qpow2 = (Q & (Q - 1)) == 0;
     const int qshift = qpow2 ? __ffs(Q) - 1 : 0;
+    // two positions of the year's list a request (half the round trips to
+    // the counter) where the list holds at least two items a warp; one
+    // where it is short (a single road), so that no warp waits idle
+    const int take = (items >= 2 * (int)gridDim.x * kWarps) ? 2 : 1;
     for (;;) {
-        int li = 0;                               // position in the year's list
-        if (lane == 0) li = atomicAdd(a.knn_next, 1);
-        li = __shfl_sync(kFull, li, 0);
-        if (li >= items) break;
-        const int item = a.touched ? a.qlist[li] : li;
-        const int c = qpow2 ? (item >> qshift) : item / Q;
-        const int qi = item - c * Q;
-        const int n = a.npts[c], k = a.kc[c];
-        if (n < 3 || k <= 0) continue;           // k_knn_solve writes 0
-        const to_knn_grid g = a.ggrid[c];
-        const float* xs = a.xn + (size_t)c * D * P;
-        const float* y = a.yv + (size_t)c * P;
-        const float* xr = a.xraw + (size_t)c * D * P;
-        const float T0 = g.T0;
-        float* kth_prev = a.kth + (size_t)c * Q;
-        const float kp = kth_prev[qi];
-        float T = kp > 0.0f ? kp * kSeedGrow : T0;
-        float qn[D], xq[D];
-        to_rov_query<D>(a, c / a.C, qi, qn, xq);
-        // the k nearest into ws.sel in ascending point index; kth = the k-th
-        // smallest distance (squared)
-        float kth = -1.0f;
-        if (n <= kReg) {
-            float key[kRegKeys];
+        int l0 = 0;
+        if (lane == 0) l0 = atomicAdd(a.knn_next, take);
+        l0 = __shfl_sync(kFull, l0, 0);
+        if (l0 >= items) break;
+        for (int li = l0; li < l0 + take && li < items; ++li) {
+            const int item = a.touched ? a.qlist[li] : li;
+            const int c = qpow2 ? (item >> qshift) : item / Q;
+            const int qi = item - c * Q;
+            const int n = a.npts[c], k = a.kc[c];
+            if (n < 3 || k <= 0) continue;           // k_knn_solve writes 0
+            const float* xs = a.xn + (size_t)c * D * P;
+            const float* y = a.yv + (size_t)c * P;
+            const float* xr = a.xraw + (size_t)c * D * P;
+            const float T0 = a.ggrid[c].T0;
+            float* kth_prev = a.kth + (size_t)c * Q;
+            const float kp = kth_prev[qi];
+            float T = kp > 0.0f ? kp * kSeedGrow : T0;
+            float qn[D], xq[D];
+            to_rov_query<D>(a, c / a.C, qi, qn, xq);
+            // the k nearest into ws.sel in ascending point index; kth = the k-th
+            // smallest distance (squared)
+            float kth = -1.0f;
+            if (n <= kReg) {
+                float key[kRegKeys];
 #pragma unroll
-            for (int u = 0; u < kRegKeys; ++u) {
-                const int i = lane + 32 * u;
-                key[u] = (i < n) ? sqdist(xs, P, i, D, qn) : INFINITY;
-            }
-            kth = reg_select_exact(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
-        } else {
-            if (g.ok) {
-                GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
-                               a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
-                kth = threshold_select(k, D, T, ws, gp);
-            } else {
-                ScanPass sp{xs, P, n, D, qn, &ws};
-                kth = threshold_select(k, D, T, ws, sp);
-            }
-            if (kth >= 0.0f) to_index_order(ws, k);
-        }
-        if (kth < 0.0f) {                         // exact radix selection
-            warp_select(xs, P, n, D, qn, k, ws);
-            kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
-            to_index_order(ws, k);
-        }
-        if (lane == 0) kth_prev[qi] = kth;
-        // lane-strided local linear regression
-        float acc[NA];
-        to_lsm_acc_init(D, acc);
-        const float h = sqrtf(kth);
-        for (int kk = lane; kk < k; kk += 32) {
-            const unsigned long long v = ws.sel[kk];
-            const int i = (int)(v & 0xFFFFFFFFu);
-            const float dd = sqrtf(__uint_as_float((unsigned)(v >> 32)));
-            float xv[D];
-#pragma unroll
-            for (int j = 0; j < D; ++j) {
-                if (a.sem == 0) {
-                    // the reference reads its dim-major buffer (stride n)
-                    // point-major (multiLocLinReg, SimulateGPU.cu:3002)
-                    int f = i * D + j;
-                    int jj = f / n, m = f - jj * n;
-                    xv[j] = xr[(size_t)jj * P + m];
-                } else {
-                    xv[j] = xs[(size_t)j * P + i];
+                for (int u = 0; u < kRegKeys; ++u) {
+                    const int i = lane + 32 * u;
+                    key[u] = (i < n) ? sqdist(xs, P, i, D, qn) : INFINITY;
                 }
+                kth = reg_select_exact(key, k, D, kp > 0.0f ? kp * kSeedGrowReg : T0, ws);
+            } else {
+                if (a.ggrid[c].ok) {
+                    // the cell grid, copied only where it is used
+                    const to_knn_grid g = a.ggrid[c];
+                    GridPass<D> gp{&g, a.gsx + (size_t)c * D * P, a.gsi + (size_t)c * P,
+                                   a.gcell + (size_t)c * (TO_KNN_GCELLS + 1), P, qn, &ws, k};
+                    kth = threshold_select(k, D, T, ws, gp);
+                } else {
+                    ScanPass sp{xs, P, n, D, qn, &ws};
+                    kth = threshold_select(k, D, T, ws, sp);
+                }
+                if (kth >= 0.0f) to_index_order(ws, k);
             }
-            to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
-        }
-        // the item's NS sums, at its list position
-        double* sa = a.knn_acc + (size_t)li * NS;
-        // the normal-equation sums: every lane's partials into shared memory
-        // (sum e in row e, lane in column, rows 33 wide), then lane e adds
-        // row e's 32 partials in lane order
-        static_assert(NS * 33 * sizeof(float) <= sizeof(WarpScratch), "reduction rows");
-        float* red = reinterpret_cast<float*>(&ws);
-        __syncwarp();
-        {
-            int e = 0;
+            if (kth < 0.0f) {                         // exact radix selection
+                warp_select(xs, P, n, D, qn, k, ws);
+                kth = __uint_as_float((unsigned)(ws.sel[k - 1] >> 32));
+                to_index_order(ws, k);
+            }
+            if (lane == 0) kth_prev[qi] = kth;
+            // lane-strided local linear regression
+            float acc[NA];
+            to_lsm_acc_init(D, acc);
+            const float h = sqrtf(kth);
+            for (int kk = lane; kk < k; kk += 32) {
+                const unsigned long long v = ws.sel[kk];
+                const int i = (int)(v & 0xFFFFFFFFu);
+                const float dd = sqrtf(__uint_as_float((unsigned)(v >> 32)));
+                float xv[D];
 #pragma unroll
-            for (int i = 0; i < M; ++i) red[(e++) * 33 + lane] = acc[i];
+                for (int j = 0; j < D; ++j) {
+                    if (a.sem == 0) {
+                        // the reference reads its dim-major buffer (stride n)
+                        // point-major (multiLocLinReg, SimulateGPU.cu:3002)
+                        int f = i * D + j;
+                        int jj = f / n, m = f - jj * n;
+                        xv[j] = xr[(size_t)jj * P + m];
+                    } else {
+                        xv[j] = xs[(size_t)j * P + i];
+                    }
+                }
+                to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
+            }
+            // the item's NS sums, at its list position
+            double* sa = a.knn_acc + (size_t)li * NS;
+            // the normal-equation sums: every lane's partials into shared memory
+            // (sum e in row e, lane in column, rows 33 wide), then lane e adds
+            // row e's 32 partials in lane order
+            static_assert(NS * 33 * sizeof(float) <= sizeof(WarpScratch), "reduction rows");
+            float* red = reinterpret_cast<float*>(&ws);
+            __syncwarp();
+            {
+                int e = 0;
 #pragma unroll
-            for (int i = 0; i < M; ++i)
+                for (int i = 0; i < M; ++i) red[(e++) * 33 + lane] = acc[i];
 #pragma unroll
-                for (int j = i; j < M; ++j) red[(e++) * 33 + lane] = acc[M + i * M + j];
-        }
-        __syncwarp();
-        if (lane < NS) {
-            float x = red[lane * 33];
+                for (int i = 0; i < M; ++i)
+#pragma unroll
+                    for (int j = i; j < M; ++j) red[(e++) * 33 + lane] = acc[M + i * M + j];
+            }
+            __syncwarp();
+            if (lane < NS) {
+                float x = red[lane * 33];
 #pragma unroll 8
-            for (int l = 1; l < 32; ++l) x = x + red[lane * 33 + l];
-            sa[lane] = (double)x;                // exact; spares the solve a conversion
+                for (int l = 1; l < 32; ++l) x = x + red[lane * 33 + l];
+                sa[lane] = (double)x;                // exact; spares the solve a conversion
+            }
+            __syncwarp();
         }
-        __syncwarp();
     }
 }
 
