@@ -501,16 +501,7 @@ struct GridPass {
             if (lane == 31) row_off[32] = total;
             __syncwarp();
             int my = 0;                     // row of this lane's point
-            for (int base = 0; base < total; base += 32) {
-                const int f = base + lane;
-                const bool in = f < total;
-                float key = INFINITY;
-                int i = 0;
-                if (in) {
-                    while (f >= row_off[my + 1]) ++my;
-                    i = row_beg[my] + (f - row_off[my]);
-                    key = sqdist(gs, stride, i, D, q);
-                }
+            auto take = [&](float key, bool in, int gidx) {
                 bool le = in && key <= T;
                 unsigned m = __ballot_sync(kFull, le);
                 if (!over && cnt + __popc(m) > kStore) {
@@ -522,8 +513,28 @@ struct GridPass {
                     }
                 }
                 const int pos = cnt + __popc(m & lt_mask);
-                if (le && pos < kStore) ws->sel[pos] = pack_sel(key, gi[i]);
+                if (le && pos < kStore) ws->sel[pos] = pack_sel(key, gidx);
                 cnt += __popc(m);
+            };
+            // two chunks of 32 points an iteration: every coordinate and
+            // index load is issued before the first key is compared
+            for (int base = 0; base < total; base += 64) {
+                const int fa = base + lane, fb = fa + 32;
+                const bool ina = fa < total, inb = fb < total;
+                int ia = 0, ib = 0;
+                if (ina) {
+                    while (fa >= row_off[my + 1]) ++my;
+                    ia = row_beg[my] + (fa - row_off[my]);
+                }
+                if (inb) {
+                    while (fb >= row_off[my + 1]) ++my;
+                    ib = row_beg[my] + (fb - row_off[my]);
+                }
+                const int ga = ina ? gi[ia] : 0, gb = inb ? gi[ib] : 0;
+                const float ka = ina ? sqdist(gs, stride, ia, D, q) : INFINITY;
+                const float kb = inb ? sqdist(gs, stride, ib, D, q) : INFINITY;
+                take(ka, ina, ga);
+                take(kb, inb, gb);
             }
             if (over && cnt > 4 * kStore) return cnt;   // far above the window
             __syncwarp();
