@@ -1,9 +1,10 @@
 #!/usr/bin/env python3
 """Road designs valued per second at +-1% Monte Carlo standard error.
 
-Workload (the batched GA generation): 256 roads (8-64 control points) on a
-200 x 200 habitat grid with 5 habitat types (201-368 patches per species
-model) and 3 species, 50 yearly steps (synthetic, seeded).  A "step" values
+Workload (the batched GA generation): 256 roads (8-64 control points, 20-400
+patch crossings) on a 200 x 200 habitat grid with 5 habitat types (200-345
+patches per species model) and 3 species, 50 yearly steps (synthetic,
+seeded).  A "step" values
 every road of the generation in both of the reference's modes: the
 species-road model (patches, crossings, transition and survival matrices,
 initial animals at risk), the MTE population Monte Carlo at N*_mte paths and
@@ -21,6 +22,7 @@ largest over roads is used for the batch).
              the habitat maps rasterised beforehand, and its GPU-kernel share
     --impl reference - the CPU restatement of the reference (oracle/) on all
              host cores, one road per core, bounded sample of the same work
+             at the same N* (SCENE_N_STAR)
 
 One JSON line on stdout (rank 0).
 """

@@ -680,10 +680,11 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
 // threshold starts from its k-th distance of the year before, times
 // kSeedGrow (kSeedGrowReg where the keys are in registers).  After the
 // selection every lane accumulates the normal equations of neighbours lane,
-// lane+32, ...; the 32 partials of each sum are added in lane order through
-// shared memory, and the item's sums are stored at its list position.
-// k_knn_solve then solves one system per thread (FP64 square-root-free
-// Cholesky, to_lsm_math.h).
+// lane+32, ... of the k nearest in ascending point index; the 32 partials
+// of each sum are added in lane order through shared memory, and the
+// item's sums are stored as doubles at its list position.  k_knn_solve
+// then solves one system per thread (FP64 square-root-free Cholesky,
+// to_lsm_math.h).
 constexpr float kSeedGrow = 1.4f;
 // the register search re-counts cheaply: it starts from last year's k-th
 // distance itself (about k keys qualify)
