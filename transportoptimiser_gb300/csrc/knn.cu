@@ -543,6 +543,13 @@ struct GridPass {
     }
 };
 
+// groups of at most this many points keep every key in registers (10 per
+// lane: the generation's groups hold about P/C = 256 points; fewer slots
+// send the larger groups to the cell grid, more cost every query the
+// empty slots) and search the threshold on them, without the cell grid
+constexpr int kRegKeys = 10;
+constexpr int kReg = 32 * kRegKeys;
+
 // Per regression group (road, control): bounding box of the normalised
 // points, a cell grid of about 32n/k cells (at most TO_KNN_GCELLS; a few
 // points per cell, since rows are set up 32 at a time and cost little), and
@@ -624,7 +631,8 @@ __global__ void __launch_bounds__(1024) k_knn_grid(to_rov_args a) {
         a.ggrid[c] = g;
     }
     __syncthreads();
-    if (!s_g.ok) return;
+    // groups the register search takes need only the box (T0), not the cells
+    if (!s_g.ok || n <= kReg) return;
     int ncell = 1;
     for (int j = 0; j < d; ++j) ncell *= s_g.G[j];
     for (int i = tid; i < ncell; i += blockDim.x) s_cnt[i] = 0;
@@ -689,12 +697,6 @@ constexpr float kSeedGrow = 1.4f;
 // the register search re-counts cheaply: it starts from last year's k-th
 // distance itself (about k keys qualify)
 constexpr float kSeedGrowReg = 1.0f;
-// groups of at most this many points keep every key in registers (10 per
-// lane: the generation's groups hold about P/C = 256 points; fewer slots
-// send the larger groups to the cell grid, more cost every query the
-// empty slots) and search the threshold on them, without the cell grid
-constexpr int kRegKeys = 10;
-constexpr int kReg = 32 * kRegKeys;
 
 // The k nearest of keys held in registers (lane l holds points l, l+32,
 // ...): the threshold moves until exactly k keys are at or below it; where
