@@ -226,15 +226,18 @@ k_mte_sparse(to_mte_args a, to_csc csc) {
                     to_normal4(a.seed, TO_STREAM_GROWTH, road_id, (uint32_t)(path0 + kLanes * i), t,
                                (uint32_t)((sp * N4) >> 2) + grp, z[i]);
                 float msum[PPL];            // grouped4 of the migrated values, in order
+                // the group's column pointers: one 16-byte load and one word
+                const int4 c4 = reinterpret_cast<const int4*>(cptr)[grp];
+                const int cb[5] = {c4.x, c4.y, c4.z, c4.w, cptr[grp * 4 + 4]};
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int k = grp * 4 + j;
                     float acc[PPL];
 #pragma unroll
                     for (int i = 0; i < PPL; ++i) acc[i] = 0.0f;
-                    const int e1 = cptr[k + 1];
+                    const int e1 = cb[j + 1];
 #pragma unroll 2
-                    for (int e = cptr[k]; e < e1; ++e) {
+                    for (int e = cb[j]; e < e1; ++e) {
                         const int2 ce = cent[e];
                         const float* row = reinterpret_cast<const float*>(
                             reinterpret_cast<const unsigned char*>(cur) + ce.x) + lane;
@@ -546,13 +549,16 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
                 to_normal4(a.seed, TO_STREAM_GROWTH, road, path, t,
                            (uint32_t)((s * N4) >> 2) + grp, z);
                 float m0[4], m1[4], m2[4], np4[4];
+                // the group's column pointers: one 16-byte load and one word
+                const int4 u4 = reinterpret_cast<const int4*>(uptr)[grp];
+                const int ub[5] = {u4.x, u4.y, u4.z, u4.w, uptr[grp * 4 + 4]};
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const int k = grp * 4 + j;
                     float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-                    const int e1 = uptr[k + 1];
+                    const int e1 = ub[j + 1];
 #pragma unroll 4
-                    for (int e = uptr[k]; e < e1; ++e) {
+                    for (int e = ub[j]; e < e1; ++e) {
                         const int4 en = ue[e];
                         const float x = *reinterpret_cast<const float*>(curb + en.x);
                         a0 = fmaf(x, __int_as_float(en.y), a0);
@@ -583,6 +589,7 @@ k_rov_forward_union(to_rov_args a, to_csc csc) {
             __syncthreads();
             for (int c = warp; c <= C; c += W) {
                 float tt = 0.0f;
+#pragma unroll 8
                 for (int grp = 0; grp < NGr; ++grp)
                     tt = tt + part[((size_t)c * NG + grp) * kLanes + lane];
                 if (path < P) {
@@ -967,6 +974,8 @@ to_status mte_sparse(to_ctx ctx, to_mte_args a, int n_rs, to_csc csc) {
     if (a.npe <= 0) a.npe = a.npad;
     if (!a.flags) a.flags = ctx->d_flags;
     const int NE = a.npe;
+    if (csc.cap_smem & 1)       // the 8-byte entries must leave the column pointers 16-byte aligned
+        return to_set_error(ctx, TO_ERR_INVALID, "packed capacity %d is odd", csc.cap_smem);
     const int ppl = (a.n_paths > kLanes) ? mte_ppl(NE, csc.cap_smem, ctx->smem_optin) : 1;
     size_t smem = mte_sparse_smem_ppl(NE, csc.cap_smem, ppl);
     if (smem > ctx->smem_optin)
