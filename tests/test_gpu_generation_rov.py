@@ -147,3 +147,31 @@ def test_mte_penalty(ctx):
         assert all(math.isclose(res[r, s, 9], tot, rel_tol=1e-12) for s in range(3))
     assert (res[:, :, 8] > 0).any() and (res[:, :, 8] == 0).any()
     gen.close()
+
+
+def test_generation_rov_at_the_bench_shape(ctx):
+    """The benchmark's ROV shape: 768 paths, 50 years, 8 bins per state
+    dimension, 3 species (about 256 points per regression group, so every
+    query takes the exact-k search on keys held in registers; the
+    benchmark's step meets ties at the k-th place there).  Two roads of the
+    benchmark scene against the batched entry point (decisions and values)
+    and the oracle (continuation values bit for bit)."""
+    sc = synth.generation(0, n_roads=8)
+    P, Y, R, road0 = 768, 50, 8, 0
+    gen = Generation(sc, max_roads=8, max_patches=512, ctx=ctx)
+    packed = pack_roads(sc, sc.roads)
+    gen.evaluate(packed, gen.opts(64, Y, seed=0, road0=road0, sem=1, migration=MIG_SPARSE_FP32))
+    gen.set_rov(_template(gen, sc, P, Y, R, seed=17, road0=road0))
+    res = gen.evaluate(packed, gen.opts(64, Y, seed=0, road0=road0, sem=1, migration=MIG_AUTO,
+                                        graph=True))
+    for r in (0, 5):
+        models = [gen.species_model(r, s) for s in range(3)]
+        prob = rov_problem_from_models(models, sc, n_paths=P, n_years=Y, dim_res=R, sem=1,
+                                       n_processes=3, demand=True, seed=17, road=road0 + r)
+        ref = sg.simulateROVCUDA_batch([prob], want=("cond_exp",), ctx=ctx)[0]
+        assert res[r, 0, 10] == ref["stats"][0]
+        assert res[r, 0, 11] == ref["stats"][1]
+        orc = po.simulate_rov(prob, threads=16)
+        assert np.array_equal(ref["cond_exp"].astype(np.float32), orc["cond_exp"])
+        assert math.isclose(res[r, 0, 10], orc["stats"][0], rel_tol=1e-7)
+    gen.close()
