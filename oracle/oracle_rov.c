@@ -20,9 +20,12 @@
  *   buildSurrogateMTECUDA / ROVCUDA     SimulateGPU.cu:5533-5917
  *
  * The normal equations are accumulated in FP32 as in the reference and
- * solved by FP64 Cholesky (the reference: FP32 Gaussian elimination); the
- * kNN selection is "k smallest by (squared distance, index)", which is what
- * the reference's stable insertion sort returns.
+ * solved by FP64 square-root-free Cholesky (the reference: FP32 Gaussian
+ * elimination); the kNN selection is "k smallest by (squared distance,
+ * index)", which is what the reference's stable insertion sort returns.
+ * The ROV regressions sum the k nearest in ascending point index over 32
+ * lane partials added in lane order (the device's order; the reference
+ * sums them one by one in distance order).
  */
 #include "oracle_rov.h"
 #include "oracle.h"
