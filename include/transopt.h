@@ -64,6 +64,9 @@ to_status to_ctx_create(int device, to_ctx* ctx);
 to_status to_ctx_destroy(to_ctx ctx);
 /* enqueue `_d` work on a caller stream (cudaStream_t passed as void*) */
 to_status to_ctx_set_stream(to_ctx ctx, void* stream);
+/* wait for the context's stream; then report (and clear) what enqueued `_d`
+ * work flagged on the device: TO_ERR_UNSUPPORTED (a generation outgrew its
+ * captured plan, capacities exceeded) or TO_ERR_TIMEOUT (a bounded wait) */
 to_status to_ctx_synchronize(to_ctx ctx);
 const char* to_status_string(to_status s);
 const char* to_last_error(to_ctx ctx);

@@ -89,3 +89,53 @@ def test_graph_replay_matches_direct_and_replans(ctx):
     out = gen.evaluate(packed_b, gen.opts(64, 30, seed=7, graph=True))  # violates, re-plans
     np.testing.assert_array_equal(out, gen.evaluate(packed_b, gen.opts(64, 30, seed=7)))
     gen.close()
+
+
+def test_device_form_reports_an_outgrown_plan_at_synchronize(ctx):
+    """to_evaluate_roads_d replays the captured graph without reading anything
+    back: roads beyond the plan captured on the first generation raise the
+    device flag, which to_ctx_synchronize reports (TO_ERR_UNSUPPORTED) and
+    clears."""
+    import torch
+    from transportoptimiser_gb300._capi import RESULT_STRIDE, TransOptError
+    sc = synth.generation(3, n_roads=48)
+    gen = Generation(sc, max_roads=16, max_patches=512, ctx=ctx)
+    nmax = []
+    for r0 in range(0, 48, 16):
+        res = gen.evaluate(pack_roads(sc, sc.roads[r0:r0 + 16]), gen.opts(32, 5, seed=1))
+        nmax += list(res[:, :, 0].max(axis=1))
+    order = np.argsort(nmax)
+    small = pack_roads(sc, [sc.roads[i] for i in order[:16]])
+    big = pack_roads(sc, [sc.roads[i] for i in order[-16:]])
+    assert max(nmax) > sorted(nmax)[15] + 16, "need a generation beyond the plan margin"
+    S = len(sc.species)
+    # one set of device buffers for both generations: the graph is keyed on
+    # their addresses, so the second call replays the first one's plan
+    dev = {k: torch.zeros(max(small[k].size, big[k].size),
+                          dtype=torch.from_numpy(small[k]).dtype, device="cuda")
+           for k in small}
+    d_res = torch.zeros(16 * S * RESULT_STRIDE, dtype=torch.float64, device="cuda")
+    opts = gen.opts(64, 30, seed=7, graph=True)
+
+    def run_device(packed):
+        for k, v in packed.items():
+            dev[k][:v.size].copy_(torch.from_numpy(v))
+        torch.cuda.synchronize()
+        gen.evaluate_device(16, dev["cell_off"].data_ptr(), dev["cells"].data_ptr(),
+                            dev["seg_off"].data_ptr(), dev["segs"].data_ptr(), opts,
+                            d_res.data_ptr())
+
+    run_device(small)                              # plans and captures
+    ctx.synchronize()
+    np.testing.assert_array_equal(d_res.cpu().numpy().reshape(16, S, RESULT_STRIDE),
+                                  gen.evaluate(small, gen.opts(64, 30, seed=7)))
+    run_device(big)                                # replays the small roads' plan
+    with pytest.raises(TransOptError) as e:
+        ctx.synchronize()
+    assert e.value.status == 6                     # TO_ERR_UNSUPPORTED
+    assert "plan" in str(e.value)
+    ctx.synchronize()                              # the flag was cleared
+    # the host form re-plans by itself and agrees with the direct path
+    out = gen.evaluate(big, gen.opts(64, 30, seed=7, graph=True))
+    np.testing.assert_array_equal(out, gen.evaluate(big, gen.opts(64, 30, seed=7)))
+    gen.close()

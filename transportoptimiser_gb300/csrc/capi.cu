@@ -96,6 +96,7 @@ to_status to_check_device_flags(to_ctx ctx) {
                          : f == TO_DEVERR_PATCHES ? "patch capacity exceeded"
                          : f == TO_DEVERR_SPIN ? "bounded wait expired"
                          : f == TO_DEVERR_CELL ? "road cell outside the grid"
+                         : f == TO_DEVERR_PLAN ? "roads outgrew the captured plan"
                          : "device check failed";
         return to_set_error(ctx, f == TO_DEVERR_SPIN ? TO_ERR_TIMEOUT
                                                       : TO_ERR_UNSUPPORTED,
@@ -258,8 +259,11 @@ int to_ctx_tuning(to_ctx ctx, char* buf, int len) {
 
 to_status to_ctx_synchronize(to_ctx ctx) {
     if (!ctx) return TO_ERR_INVALID;
+    cudaSetDevice(ctx->device);
     TO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return TO_OK;
+    // what the enqueued `_d` work reported on the device (a plan outgrown, a
+    // bounded wait run out), read and cleared
+    return to_check_device_flags(ctx);
 }
 
 // ---- LabelImage ------------------------------------------------------------
