@@ -90,15 +90,12 @@ def build_oracle(force: bool = False) -> Path:
     return ORACLE_LIB
 
 
-def reference_dir() -> Path:
-    """Where the reference tree is mounted (TO_REFERENCE_DIR, the same
-    variable oracle/build_ref.sh reads)."""
-    return Path(os.environ.get("TO_REFERENCE_DIR", "/root/reference"))
-
-
 def build_reference_pin() -> None:
+    """oracle/_ref from the reference tree: the recipe (oracle/build_ref.sh)
+    knows where the tree is mounted (TO_REFERENCE_DIR) and skips the build
+    where it is absent."""
     script = ORACLE_DIR / "build_ref.sh"
-    if reference_dir().exists() and script.exists():
+    if script.exists():
         _run(["sh", str(script)])
 
 
