@@ -18,7 +18,7 @@ KAT = [
 
 HELPER = r"""
 #include <stdint.h>
-#include "to_math.h"
+#include "to_lsm_math.h"
 void kat(const uint32_t* c, const uint32_t* k, uint32_t* o) {
   to_u32x4 r = to_philox4x32_10(c[0], c[1], c[2], c[3], k[0], k[1]);
   for (int i = 0; i < 4; ++i) o[i] = r.v[i];
@@ -29,6 +29,9 @@ void vsc(const float* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i
 void vlogu(const uint32_t* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = to_log_u01(x[i]); }
 void vsc2(const uint32_t* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i) to_sincos2pi_u01(x[i], &s[i], &c[i]); }
 void vdiv(const float* a, const float* b, float* q, int n) { for (int i = 0; i < n; ++i) q[i] = to_div_rcp(a[i], b[i], 1.0f / b[i]); }
+void vw(const float* d, const float* h, float* w0, float* w1, int n) {
+  for (int i = 0; i < n; ++i) { w0[i] = to_lsm_weight(d[i], h[i]); w1[i] = to_lsm_weight_within(d[i], h[i], 1.0f / h[i]); }
+}
 """
 
 
@@ -136,3 +139,35 @@ def test_division_from_reciprocal_is_correctly_rounded(tmp_path_factory):
     h.vdiv(a.ctypes.data_as(fp), b.ctypes.data_as(fp), q.ctypes.data_as(fp), len(a))
     want = a / b
     assert np.array_equal(q.view(np.uint32), want.view(np.uint32))
+
+
+def test_kernel_weight_within_the_bandwidth_equals_the_general_form(tmp_path_factory):
+    """to_lsm_weight_within (the kNN kernel's form: reciprocal of the
+    bandwidth once per query, the exponential on [-1/2, 0]) gives the bits of
+    to_lsm_weight (the oracle's form) for every distance 0 <= d <= h: the
+    kernel's case, d and h square roots of float squared distances with h the
+    largest, over the whole float range of such keys, and the edges d = 0,
+    d = h and d one ulp below h."""
+    h = _helper(tmp_path_factory)
+    fp = C.POINTER(C.c_float)
+    rng = np.random.default_rng(11)
+    n = 1 << 21
+    # squared distances: log-uniform over the positive floats a key can take
+    kmax = np.exp(rng.uniform(np.log(1e-44), np.log(1e30), n)).astype(np.float32)
+    kmax = np.maximum(kmax, np.float32(1.4e-45))
+    key = (kmax * rng.uniform(0.0, 1.0, n).astype(np.float32)).astype(np.float32)
+    hh = np.sqrt(kmax).astype(np.float32)
+    dd = np.sqrt(np.minimum(key, kmax)).astype(np.float32)
+    m = n // 8
+    dd[:m] = 0.0
+    dd[m:2 * m] = hh[m:2 * m]
+    dd[2 * m:3 * m] = np.nextafter(hh[2 * m:3 * m], np.float32(0.0))
+    # the bench's scale: normalised coordinates, bandwidths 1e-3 .. 1
+    hh[3 * m:4 * m] = rng.uniform(1e-3, 1.0, m).astype(np.float32)
+    dd[3 * m:4 * m] = (hh[3 * m:4 * m] * rng.uniform(0.0, 1.0, m)).astype(np.float32)
+    assert np.all(dd <= hh) and np.all(hh > 0)
+    w0 = np.zeros(n, np.float32)
+    w1 = np.zeros(n, np.float32)
+    h.vw(dd.ctypes.data_as(fp), hh.ctypes.data_as(fp), w0.ctypes.data_as(fp),
+         w1.ctypes.data_as(fp), n)
+    assert np.array_equal(w0.view(np.uint32), w1.view(np.uint32))

@@ -851,7 +851,7 @@ k_knn_rov(to_rov_args a, int t) {
             // lane-strided local linear regression
             float acc[NA];
             to_lsm_acc_init(D, acc);
-            const float h = sqrtf(kth);
+            const float h = sqrtf(kth), rh = 1.0f / h;
             for (int kk = lane; kk < k; kk += 32) {
                 const unsigned long long v = ws.sel[kk];
                 const int i = (int)(v & 0xFFFFFFFFu);
@@ -869,7 +869,8 @@ k_knn_rov(to_rov_args a, int t) {
                         xv[j] = xs[(size_t)j * P + i];
                     }
                 }
-                to_lsm_acc_add(D, acc, to_lsm_weight(dd, h), y[i], xv, xq);
+                // dd <= h: every neighbour lies within the k-th distance
+                to_lsm_acc_add(D, acc, to_lsm_weight_within(dd, h, rh), y[i], xv, xq);
             }
             // the item's NS sums, at its list position
             double* sa = a.knn_acc + (size_t)li * NS;

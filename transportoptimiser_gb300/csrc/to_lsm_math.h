@@ -49,6 +49,29 @@ TO_HD float to_lsm_weight(float d, float h) {
     return to_expf(w) * 0.3989422804f;
 }
 
+/* to_lsm_weight(d, h) for a neighbour within the bandwidth, 0 <= d <= h,
+ * with rh = 1 / h computed once per query: the same bits.  t = d / h by
+ * to_div_rcp (correctly rounded: t <= 1, and the remainder d - h q is a
+ * multiple of about 2^-46 d, far above the float underflow for any float
+ * distance d > 0).  w = -t^2 / 2 then lies in [-1/2, 0], where to_expf's
+ * range checks never fire and its k = rint(w / ln 2) is 0 or -1: its
+ * scaling (p 2^(k/2)) 2^(k - k/2) is p 2^k. */
+TO_HD float to_lsm_weight_within(float d, float h, float rh) {
+    const float t = to_div_rcp(d, h, rh);
+    const float w = ((-t) * t) / 2.0f;
+    const float k = rintf(w * 0x1.715476p+0f);
+    float r = fmaf(-k, 0x1.62e430p-1f, w);
+    r = fmaf(-k, -0x1.05c610p-29f, r);
+    float p = fmaf(r, 0x1.a01a02p-13f, 0x1.6c16c2p-10f);
+    p = fmaf(r, p, 0x1.111112p-7f);
+    p = fmaf(r, p, 0x1.555556p-5f);
+    p = fmaf(r, p, 0x1.555556p-3f);
+    p = fmaf(r, p, 0.5f);
+    p = fmaf(r, p, 1.0f);
+    p = fmaf(r, p, 1.0f);
+    return (p * to_pow2i((int)k)) * 0.3989422804f;
+}
+
 /* acc = [B (m) | A (m x m row-major)], m = dim + 1; only i <= j of A */
 TO_HD void to_lsm_acc_init(int dim, float* acc) {
     int m = dim + 1;
