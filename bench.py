@@ -780,7 +780,7 @@ ROOF = {
     "rov_forward_sparse": {"kernel": "k_rov_forward_union", "inst_per_unit": 46845.0,
                            "bytes_per_unit": 280.0,
                            "unit": "(32-path tile, species, year)"},
-    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 1677.1, "bytes_per_unit": 22.8,
+    "knn": {"kernel": "k_knn_rov", "inst_per_unit": 1588.3, "bytes_per_unit": 22.8,
             "unit": "fitted regression query"},
 }
 SMS, SCHEDULERS = 152, 4
