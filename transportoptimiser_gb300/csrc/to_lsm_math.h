@@ -114,7 +114,9 @@ TO_HD double to_rcp64(double x) {
  * (to_rcp64) scales its column.  A direction whose pivot falls below 1e-6
  * of its diagonal is dropped (its coefficient set to zero).  Returns the
  * intercept (the regression value at the query), 0 when its own direction
- * is dropped.  sums: the right-hand sides B (m values), then the upper
+ * is dropped.  Every update s - l u is one fused multiply-add (half the
+ * FP64 operations of a multiply and a subtraction; the FP64 pipe bounds
+ * the solve).  sums: the right-hand sides B (m values), then the upper
  * triangle i <= j of the matrix A in row order. */
 TO_HD float to_lsm_solve_compact(int dim, const double* sums) {
     int m = dim + 1;
@@ -141,7 +143,7 @@ TO_HD float to_lsm_solve_compact(int dim, const double* sums) {
         double s = A[j * m + j];
         TO_UNROLL
         for (int k = 0; k < j; ++k)
-            if (keep[k]) s = s - L[j * m + k] * U[j * m + k];
+            if (keep[k]) s = fma(-L[j * m + k], U[j * m + k], s);
         if (!(s > 1e-6 * A[j * m + j]) || !(s > 0.0)) { keep[j] = 0; continue; }
         keep[j] = 1;
         inv[j] = to_rcp64(s);
@@ -150,7 +152,7 @@ TO_HD float to_lsm_solve_compact(int dim, const double* sums) {
             double v = A[i * m + j];
             TO_UNROLL
             for (int k = 0; k < j; ++k)
-                if (keep[k]) v = v - L[i * m + k] * U[j * m + k];
+                if (keep[k]) v = fma(-L[i * m + k], U[j * m + k], v);
             U[i * m + j] = v;
             L[i * m + j] = v * inv[j];
         }
@@ -161,7 +163,7 @@ TO_HD float to_lsm_solve_compact(int dim, const double* sums) {
         double v = b[i];
         TO_UNROLL
         for (int k = 0; k < i; ++k)
-            if (keep[k]) v = v - L[i * m + k] * y[k];
+            if (keep[k]) v = fma(-L[i * m + k], y[k], v);
         y[i] = v;
     }
     return keep[m - 1] ? (float)(y[m - 1] * inv[m - 1]) : 0.0f;
