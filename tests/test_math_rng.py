@@ -29,6 +29,7 @@ void vsc(const float* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i
 void vlogu(const uint32_t* x, float* y, int n) { for (int i = 0; i < n; ++i) y[i] = to_log_u01(x[i]); }
 void vsc2(const uint32_t* x, float* s, float* c, int n) { for (int i = 0; i < n; ++i) to_sincos2pi_u01(x[i], &s[i], &c[i]); }
 void vdiv(const float* a, const float* b, float* q, int n) { for (int i = 0; i < n; ++i) q[i] = to_div_rcp(a[i], b[i], 1.0f / b[i]); }
+float vsolve(int dim, const double* sums) { return to_lsm_solve_compact(dim, sums); }
 void vw(const float* d, const float* h, float* w0, float* w1, int n) {
   for (int i = 0; i < n; ++i) { w0[i] = to_lsm_weight(d[i], h[i]); w1[i] = to_lsm_weight_within(d[i], h[i], 1.0f / h[i]); }
 }
@@ -171,3 +172,42 @@ def test_kernel_weight_within_the_bandwidth_equals_the_general_form(tmp_path_fac
     h.vw(dd.ctypes.data_as(fp), hh.ctypes.data_as(fp), w0.ctypes.data_as(fp),
          w1.ctypes.data_as(fp), n)
     assert np.array_equal(w0.view(np.uint32), w1.view(np.uint32))
+
+
+def _compact_sums(dx, y, z):
+    """The normal-equation sums of a weighted local linear fit in the solve's
+    compact order: B (sum y w_i z, w = [1, dx]), then the upper triangle of
+    A (sum w_i w_j z) row by row."""
+    w = np.concatenate([np.ones((len(y), 1)), dx], axis=1)
+    m = w.shape[1]
+    B = (w * (y * z)[:, None]).sum(0)
+    A = (w * z[:, None]).T @ w
+    return np.concatenate([B, [A[i, j] for i in range(m) for j in range(i, m)]])
+
+
+def test_regression_solve_matches_weighted_least_squares(tmp_path_factory):
+    """to_lsm_solve_compact (FP64 square-root-free Cholesky, intercept last,
+    every update one fused multiply-add) returns the intercept of the
+    weighted least-squares fit, against numpy's float64 solution, for local
+    fits of 3 and 4 state dimensions; a state dimension constant over the
+    neighbours is dropped and the fit of the others returned."""
+    h = _helper(tmp_path_factory)
+    h.vsolve.restype = C.c_float
+    h.vsolve.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    rng = np.random.default_rng(5)
+    for case in range(400):
+        d = 3 + case % 2
+        n = 65
+        dx = rng.normal(0.0, 0.1, (n, d))
+        coef = rng.normal(0.0, 1.0, d + 1)
+        y = coef[0] + dx @ coef[1:] + rng.normal(0.0, 0.05, n)
+        z = np.exp(-rng.uniform(0.0, 0.5, n)) * 0.3989422804
+        if case % 5 == 4:
+            dx[:, case % d] = 0.0          # a direction the neighbours do not span
+        sums = _compact_sums(dx, y, z)
+        got = h.vsolve(d, sums.ctypes.data_as(C.POINTER(C.c_double)))
+        keep = [j for j in range(d) if np.any(dx[:, j] != 0.0)]
+        w = np.concatenate([np.ones((n, 1)), dx[:, keep]], axis=1)
+        sw = np.sqrt(z)
+        want = np.linalg.lstsq(w * sw[:, None], y * sw, rcond=None)[0][0]
+        assert abs(got - want) <= 1e-6 * max(1.0, abs(want)), (case, got, want)
